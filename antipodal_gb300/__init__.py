@@ -1,0 +1,308 @@
+"""GB300-native batch generalized winding numbers, with the antipodal library's batch API.
+
+This Python module mirrors the reference's C++ entry points (same names, argument order and meaning) over the
+C ABI of libantipodal_gb300.so, so tests and benchmarks read like the reference's own:
+
+    disp = CudaDispatcher()                                   # a Dispatcher that runs on one GPU
+    isect = CudaIntersector(disp, vertices, indices)          # an Intersector backed by a device LBVH
+    eval_gwnr_mesh_batch(disp, isect, positions, out, x0, boundary)
+
+Arrays may be numpy arrays (host memory) or torch tensors (host or CUDA); shapes follow the reference value
+types: positions (n, 3), boundary (s, 7) = [pos0, pos1, weight], vertices (v, 3), indices (3 f,) int32.
+Every call runs the CUDA kernels; if the extension is not built, or no GPU is present, calls raise -- there is
+no CPU fallback.  (The CPU oracle used by the tests lives in oracle/, outside this package.)
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import FRAC_EXACT, FRAC_MIXED, Stats
+
+__all__ = [
+    "GwnError", "CudaDispatcher", "CudaIntersector", "eval_gwnr_mesh_batch_fractional",
+    "eval_gwnr_mesh_batch_integer", "eval_gwnr_mesh_batch", "build_boundary_segments", "library",
+]
+
+
+class GwnError(RuntimeError):
+    """A non-zero status from the C ABI; ``status`` holds the code, the message the library's detail."""
+
+    def __init__(self, status: int, where: str, detail: str):
+        super().__init__(f"{where}: {_lib.STATUS.get(status, 'error')} ({status}): {detail}")
+        self.status = status
+
+
+def library():
+    return _lib.load()
+
+
+def _check(status: int, where: str):
+    if status != _lib.AGWN_OK:
+        detail = library().agwn_last_error_message()
+        raise GwnError(status, where, detail.decode() if detail else "")
+
+
+# --------------------------------------------------------------------------------------------------------------
+# array plumbing
+# --------------------------------------------------------------------------------------------------------------
+def _is_torch(a) -> bool:
+    return type(a).__module__.startswith("torch")
+
+
+def _dtype_of(a):
+    if _is_torch(a):
+        import torch
+        return {torch.float64: np.float64, torch.float32: np.float32, torch.int32: np.int32}.get(a.dtype)
+    return np.asarray(a).dtype.type
+
+
+class _View:
+    """Pointer + element count of a contiguous array; keeps any temporary copy alive."""
+
+    def __init__(self, a, dtype, cols: int | None, name: str, writable: bool = False):
+        if _is_torch(a):
+            if not a.is_contiguous():
+                raise ValueError(f"{name}: tensor must be contiguous")
+            if _dtype_of(a) is not dtype:
+                raise TypeError(f"{name}: expected {np.dtype(dtype).name}, got {a.dtype}")
+            self.keep = a
+            self.ptr = a.data_ptr()
+            numel = a.numel()
+        else:
+            if writable:
+                if not isinstance(a, np.ndarray) or a.dtype != dtype or not a.flags.c_contiguous:
+                    raise TypeError(f"{name}: output must be a C-contiguous {np.dtype(dtype).name} numpy array")
+                arr = a
+            else:
+                arr = np.ascontiguousarray(a, dtype=dtype)
+            self.keep = arr
+            self.ptr = arr.ctypes.data if arr.size else None
+            numel = arr.size
+        if cols and numel % cols:
+            raise ValueError(f"{name}: size {numel} is not a multiple of {cols}")
+        self.n = numel // cols if cols else numel
+
+
+def _vec3(x0, dtype):
+    v = np.ascontiguousarray(np.asarray(x0.cpu() if _is_torch(x0) else x0, dtype=dtype).reshape(3))
+    return v, v.ctypes.data
+
+
+def _float_kind(positions):
+    dt = _dtype_of(positions)
+    if dt not in (np.float64, np.float32):
+        raise TypeError("positions must be float64 or float32")
+    return dt, ("f64" if dt is np.float64 else "f32")
+
+
+# --------------------------------------------------------------------------------------------------------------
+# Dispatcher / Intersector
+# --------------------------------------------------------------------------------------------------------------
+class CudaDispatcher:
+    """The reference's Dispatcher role (src/antipodal/dispatcher/dispatcher.hh:3-36) on one GPU.
+
+    Holds a device, a stream and scratch memory, plus the fractional-term options:
+    ``precision`` "exact" (the reference's arithmetic, the default) or "mixed" (FP32 pairs with TwoSum
+    accumulation and FP64 near / ill-conditioned / branch-cut pairs; double inputs), ``tau`` (mixed mode
+    near-pair ratio), ``term_err`` (mixed mode per-pair FP32 error bound, radians),
+    ``queries_per_thread``, ``block`` and ``seg_tile`` (kernel shape), ``timing`` (CUDA-event kernel timing).
+    Like PoolDispatcher it runs one job at a time.  ``parallel_for`` is not provided: arbitrary host callables
+    have no device form here, and the library has no CPU fallback.
+    """
+
+    def __init__(self, device: int = 0, stream=None, precision: str = "exact", tau: float = 8.0,
+                 term_err: float = 2e-8, queries_per_thread: int = 4, block: int = 256, seg_tile: int = 512,
+                 timing: bool = False):
+        lib = library()
+        handle = None
+        if stream is not None:
+            handle = stream if isinstance(stream, int) else stream.cuda_stream  # torch.cuda.Stream
+            if handle == 0:
+                handle = 1  # cudaStreamLegacy: the legacy default stream (NULL would mean "create one")
+        h = C.c_void_p()
+        _check(lib.agwn_context_create(device, handle, C.byref(h)), "agwn_context_create")
+        self._h = h
+        self.device = device
+        self.set_precision(precision)
+        self.set_option(_lib.OPT_MIXED_TAU, tau)
+        self.set_option(_lib.OPT_MIXED_TERM_ERR, term_err)
+        self.set_option(_lib.OPT_QUERIES_PER_THREAD, queries_per_thread)
+        self.set_option(_lib.OPT_FRAC_BLOCK, block)
+        self.set_option(_lib.OPT_SEG_TILE, seg_tile)
+        self.set_option(_lib.OPT_TIMING, 1 if timing else 0)
+
+    @property
+    def handle(self):
+        if self._h is None:
+            raise RuntimeError("dispatcher is closed")
+        return self._h
+
+    def set_option(self, option: int, value: float):
+        _check(library().agwn_context_set_option(self.handle, option, float(value)), "agwn_context_set_option")
+
+    def get_option(self, option: int) -> float:
+        v = C.c_double()
+        _check(library().agwn_context_get_option(self.handle, option, C.byref(v)), "agwn_context_get_option")
+        return v.value
+
+    def set_precision(self, precision: str):
+        mode = {"exact": FRAC_EXACT, "mixed": FRAC_MIXED}[precision]
+        self.set_option(_lib.OPT_FRAC_MODE, mode)
+        self.precision = precision
+
+    def synchronize(self):
+        _check(library().agwn_context_synchronize(self.handle), "agwn_context_synchronize")
+
+    def stats(self, reset: bool = False) -> dict:
+        s = Stats()
+        _check(library().agwn_context_get_stats(self.handle, C.byref(s), int(reset)), "agwn_context_get_stats")
+        names = ["fractional", "integer", "robust", "parametric", "other"]
+        return {"kernel_ms": dict(zip(names, list(s.kernel_ms))), "launches": dict(zip(names, list(s.launches))),
+                "fp64_pairs": s.fp64_pairs, "pairs": s.pairs}
+
+    def probe_fp32_peak(self) -> float:
+        """Measured FP32 FMA throughput of this GPU, TFLOP/s."""
+        v = C.c_double()
+        _check(library().agwn_probe_fp32_peak(self.handle, C.byref(v)), "agwn_probe_fp32_peak")
+        return v.value
+
+    def parallel_for(self, begin, end, f):  # noqa: D401 - concept member, deliberately unavailable
+        raise TypeError("CudaDispatcher runs the library's GWN kernels only; generic host callables are not "
+                        "executed (no CPU fallback)")
+
+    def close(self):
+        if getattr(self, "_h", None) is not None:
+            library().agwn_context_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class CudaIntersector:
+    """The reference's Intersector role (src/antipodal/intersector/intersector.hh:3-40) over a device LBVH.
+
+    Counts equal NaiveIntersector<T>'s (intersector.hh:55-100) bit for bit.  Unlike NaiveIntersector it copies
+    the mesh to the device, so the caller's arrays need not outlive it.
+    """
+
+    def __init__(self, dispatcher: CudaDispatcher, vertices, indices):
+        dt = _dtype_of(vertices)
+        if dt not in (np.float64, np.float32):
+            raise TypeError("vertices must be float64 or float32")
+        self.dtype = dt
+        self.kind = "f64" if dt is np.float64 else "f32"
+        v = _View(vertices, dt, 3, "vertices")
+        i = _View(indices, np.int32, None, "indices")
+        if i.n % 3:
+            raise ValueError("indices: length must be a multiple of 3")
+        h = C.c_void_p()
+        fn = getattr(library(), f"agwn_bvh_create_{self.kind}")
+        _check(fn(dispatcher.handle, v.ptr, v.n, i.ptr, i.n, C.byref(h)), "agwn_bvh_create")
+        self._h = h
+        self.n_triangles = i.n // 3
+
+    @property
+    def handle(self):
+        if self._h is None:
+            raise RuntimeError("intersector is closed")
+        return self._h
+
+    def info(self) -> dict:
+        n = C.c_int64()
+        d = C.c_int32()
+        _check(library().agwn_bvh_info(self.handle, C.byref(n), C.byref(d)), "agwn_bvh_info")
+        return {"triangles": n.value, "depth": d.value}
+
+    def close(self):
+        if getattr(self, "_h", None) is not None:
+            library().agwn_bvh_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# --------------------------------------------------------------------------------------------------------------
+# batch functions (src/antipodal/gwn_mesh.hh)
+# --------------------------------------------------------------------------------------------------------------
+def eval_gwnr_mesh_batch_fractional(dispatcher: CudaDispatcher, positions, out_wnrs, x0, boundary):
+    """gwn_mesh.hh:67-83: out_wnrs[i] = fractional GWN at positions[i]."""
+    dt, kind = _float_kind(positions)
+    p = _View(positions, dt, 3, "positions")
+    o = _View(out_wnrs, dt, None, "out_wnrs", writable=True)
+    if p.n != o.n:
+        raise ValueError("positions and out_wnrs must have the same size")
+    b = _View(boundary, dt, 7, "boundary")
+    _, xp = x = _vec3(x0, dt)
+    fn = getattr(library(), f"agwn_mesh_batch_fractional_{kind}")
+    _check(fn(dispatcher.handle, p.ptr, p.n, o.ptr, xp, b.ptr, b.n), "eval_gwnr_mesh_batch_fractional")
+    del x
+
+
+def eval_gwnr_mesh_batch_integer(dispatcher: CudaDispatcher, intersector: CudaIntersector, positions, out_counts,
+                                 x0):
+    """gwn_mesh.hh:127-143: out_counts[i] = signed ray crossings along (positions[i], x0)."""
+    dt, kind = _float_kind(positions)
+    p = _View(positions, dt, 3, "positions")
+    o = _View(out_counts, np.int32, None, "out_counts", writable=True)
+    if p.n != o.n:
+        raise ValueError("positions and out_counts must have the same size")
+    _, xp = x = _vec3(x0, dt)
+    fn = getattr(library(), f"agwn_mesh_batch_integer_{kind}")
+    _check(fn(dispatcher.handle, intersector.handle, p.ptr, p.n, o.ptr, xp), "eval_gwnr_mesh_batch_integer")
+    del x
+
+
+def eval_gwnr_mesh_batch(dispatcher: CudaDispatcher, intersector: CudaIntersector | None, positions, out_wnrs, x0,
+                         boundary):
+    """gwn_mesh.hh:201-219: out_wnrs[i] = fractional + integer GWN, fused per query.  ``intersector`` None
+    means no integer term (an all-boundary evaluation)."""
+    dt, kind = _float_kind(positions)
+    p = _View(positions, dt, 3, "positions")
+    o = _View(out_wnrs, dt, None, "out_wnrs", writable=True)
+    if p.n != o.n:
+        raise ValueError("positions and out_wnrs must have the same size")
+    b = _View(boundary, dt, 7, "boundary")
+    _, xp = x = _vec3(x0, dt)
+    fn = getattr(library(), f"agwn_mesh_batch_{kind}")
+    ih = intersector.handle if intersector is not None else None
+    _check(fn(dispatcher.handle, ih, p.ptr, p.n, o.ptr, xp, b.ptr, b.n), "eval_gwnr_mesh_batch")
+    del x
+
+
+def eval_gwnr_mesh_batch_integer_bruteforce(dispatcher: CudaDispatcher, vertices, indices, positions, out_counts,
+                                            x0):
+    """Every query against every triangle (no hierarchy); double precision only."""
+    p = _View(positions, np.float64, 3, "positions")
+    o = _View(out_counts, np.int32, None, "out_counts", writable=True)
+    v = _View(vertices, np.float64, 3, "vertices")
+    i = _View(indices, np.int32, None, "indices")
+    _, xp = x = _vec3(x0, np.float64)
+    _check(library().agwn_mesh_batch_integer_bruteforce_f64(dispatcher.handle, v.ptr, v.n, i.ptr, i.n, p.ptr, p.n,
+                                                            o.ptr, xp), "bruteforce")
+    del x
+
+
+def build_boundary_segments(vertices, indices) -> np.ndarray:
+    """Open boundary as (s, 7) [pos0, pos1, weight] rows, the rule of build_boundary_segments
+    (src/antipodal/math/common.hh:123-174), ordered by (lo, hi) vertex index.  Host-side (numpy)."""
+    from .synth import boundary_segments
+    v = np.asarray(vertices)
+    return boundary_segments(v, np.asarray(indices, np.int32)).astype(v.dtype)

@@ -1,0 +1,82 @@
+"""ctypes declarations of libantipodal_gb300.so (the C ABI in include/antipodal_gb300.h)."""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libantipodal_gb300.so")
+
+_P = C.c_void_p
+_I64 = C.c_int64
+_I = C.c_int
+_D = C.c_double
+_PP = C.POINTER(C.c_void_p)
+
+AGWN_OK = 0
+STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA runtime error", 3: "out of device memory",
+          4: "BVH traversal stack exhausted", 5: "device wait timed out", 6: "unsupported", 7: "no CUDA device"}
+
+OPT_FRAC_MODE, OPT_MIXED_TAU, OPT_QUERIES_PER_THREAD, OPT_FRAC_BLOCK, OPT_TIMING, OPT_SEG_TILE, \
+    OPT_MIXED_TERM_ERR = range(7)
+FRAC_EXACT, FRAC_MIXED = 0, 1
+K_FRACTIONAL, K_INTEGER, K_ROBUST, K_PARAMETRIC, K_OTHER, K_COUNT = range(6)
+
+
+class Stats(C.Structure):
+    _fields_ = [("kernel_ms", C.c_double * K_COUNT), ("launches", C.c_int64 * K_COUNT),
+                ("fp64_pairs", C.c_int64), ("pairs", C.c_int64)]
+
+
+# name -> (restype, argtypes)
+SIGNATURES = {
+    "agwn_status_string": (C.c_char_p, [_I]),
+    "agwn_last_error_message": (C.c_char_p, []),
+    "agwn_abi_version": (_I, []),
+    "agwn_context_create": (_I, [_I, _P, _PP]),
+    "agwn_context_destroy": (_I, [_P]),
+    "agwn_context_synchronize": (_I, [_P]),
+    "agwn_context_set_option": (_I, [_P, _I, _D]),
+    "agwn_context_get_option": (_I, [_P, _I, C.POINTER(_D)]),
+    "agwn_context_get_stats": (_I, [_P, C.POINTER(Stats), _I]),
+    "agwn_mesh_batch_fractional_f64": (_I, [_P, _P, _I64, _P, _P, _P, _I64]),
+    "agwn_mesh_batch_fractional_f32": (_I, [_P, _P, _I64, _P, _P, _P, _I64]),
+    "agwn_bvh_create_f64": (_I, [_P, _P, _I64, _P, _I64, _PP]),
+    "agwn_bvh_create_f32": (_I, [_P, _P, _I64, _P, _I64, _PP]),
+    "agwn_bvh_destroy": (_I, [_P]),
+    "agwn_bvh_info": (_I, [_P, C.POINTER(_I64), C.POINTER(C.c_int32)]),
+    "agwn_mesh_batch_integer_f64": (_I, [_P, _P, _P, _I64, _P, _P]),
+    "agwn_mesh_batch_integer_f32": (_I, [_P, _P, _P, _I64, _P, _P]),
+    "agwn_mesh_batch_f64": (_I, [_P, _P, _P, _I64, _P, _P, _P, _I64]),
+    "agwn_mesh_batch_f32": (_I, [_P, _P, _P, _I64, _P, _P, _P, _I64]),
+    "agwn_mesh_batch_integer_bruteforce_f64": (_I, [_P, _P, _I64, _P, _I64, _P, _I64, _P, _P]),
+    "agwn_probe_fp32_peak": (_I, [_P, C.POINTER(_D)]),
+}
+
+_lock = threading.Lock()
+_lib = None
+
+
+def load(path: str | None = None) -> C.CDLL:
+    """Loads the library once; raises if it has not been built (there is no CPU fallback)."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        p = path or LIB_PATH
+        if not os.path.exists(p):
+            raise RuntimeError(
+                f"{p} is missing: build the CUDA extension first (python -c 'import __graft_entry__ as g; g.build()')")
+        lib = C.CDLL(p)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(lib, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = lib
+        return lib
+
+
+def declared_symbols() -> list[str]:
+    return list(SIGNATURES)

@@ -1,0 +1,215 @@
+// Shared internals of libantipodal_gb300: error reporting, the context (stream, scratch arena, options,
+// timing), host/device pointer handling and small device helpers.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+
+#include "../../include/antipodal_gb300.h"
+
+namespace agwn
+{
+// ---- errors --------------------------------------------------------------------------------------------------
+void set_message(const char* fmt, ...);
+int fail(int status, const char* fmt, ...);
+void clear_message();
+
+#define AGWN_TRY_CUDA(expr)                                                                                        \
+    do                                                                                                             \
+    {                                                                                                              \
+        cudaError_t agwn_e_ = (expr);                                                                              \
+        if (agwn_e_ != cudaSuccess)                                                                                \
+            return ::agwn::fail(agwn_e_ == cudaErrorMemoryAllocation ? AGWN_ERR_NOMEM : AGWN_ERR_CUDA,             \
+                                "%s failed: %s (%s:%d)", #expr, cudaGetErrorString(agwn_e_), __FILE__, __LINE__); \
+    } while (0)
+
+#define AGWN_TRY(expr)                                                                                             \
+    do                                                                                                             \
+    {                                                                                                              \
+        int agwn_s_ = (expr);                                                                                      \
+        if (agwn_s_ != AGWN_OK)                                                                                    \
+            return agwn_s_;                                                                                        \
+    } while (0)
+
+#define AGWN_CHECK_ARG(cond, ...)                                                                                  \
+    do                                                                                                             \
+    {                                                                                                              \
+        if (!(cond))                                                                                               \
+            return ::agwn::fail(AGWN_ERR_INVALID, __VA_ARGS__);                                                    \
+    } while (0)
+
+// Device-side error flags, one word each, set with atomicOr by kernels and read by the host at synchronisation.
+enum flag_slot
+{
+    FLAG_STACK = 0,   // traversal stack exhausted
+    FLAG_TIMEOUT = 1, // bounded wait ran out
+    FLAG_COUNT = 8
+};
+
+// ---- device scratch ----------------------------------------------------------------------------------------
+// A grow-only device buffer.  Slots are reused across calls of one context.
+struct DevBuf
+{
+    void* ptr = nullptr;
+    size_t cap = 0;
+    int reserve(size_t bytes);
+    void release();
+};
+
+enum scratch_slot
+{
+    S_QUERIES = 0,
+    S_OUT = 1,
+    S_COUNTS = 2,
+    S_SEGS = 3,
+    S_SEGS_RAW = 4,
+    S_FRAME = 5,
+    S_MISC0 = 6,
+    S_MISC1 = 7,
+    S_MISC2 = 8,
+    S_MISC3 = 9,
+    S_COUNT = 10
+};
+
+struct Context
+{
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int* d_flags = nullptr;        // FLAG_COUNT ints
+    int* h_flags = nullptr;        // pinned mirror
+    long long* d_counters = nullptr; // [0] fp64 pairs, [1] pairs
+    DevBuf scratch[S_COUNT];
+    int sm_count = 0;
+
+    // options
+    int frac_mode = AGWN_FRAC_EXACT;
+    double mixed_tau = 8.0;
+    double mixed_term_err = 2e-8;
+    int queries_per_thread = 4;
+    int frac_block = 256;
+    int seg_tile = 512;
+    int timing = 0;
+
+    // statistics
+    double kernel_ms[AGWN_K_COUNT] = {};
+    long long launches[AGWN_K_COUNT] = {};
+    static constexpr int kMaxPending = 64;
+    cudaEvent_t ev_begin[kMaxPending] = {};
+    cudaEvent_t ev_end[kMaxPending] = {};
+    int pending_class[kMaxPending] = {};
+    int n_pending = 0;
+
+    int scratch_reserve(int slot, size_t bytes, void** out);
+    // Brackets a launch with timing events when AGWN_OPT_TIMING is on; always counts the launch.
+    int launch_begin(int kclass);
+    int launch_end(int kclass);
+    int drain_timing(); // folds finished events into kernel_ms (synchronises the stream)
+    int check_flags();  // synchronises and reports device flags
+};
+
+// ---- host/device pointers ----------------------------------------------------------------------------------
+bool is_device_pointer(const void* p);
+
+// Makes `count` elements of `src` readable by the device: returns src itself for device memory, else copies
+// it into scratch `slot` on the context's stream.
+int stage_in(Context& ctx, const void* src, size_t bytes, int slot, const void** dev);
+// Output staging: returns `dst` for device memory, else scratch `slot`; `*host` tells whether a copy back is due.
+int stage_out(Context& ctx, void* dst, size_t bytes, int slot, void** dev, bool* host);
+
+// ---- launch geometry ---------------------------------------------------------------------------------------
+inline int div_up(int64_t a, int64_t b)
+{
+    return int((a + b - 1) / b);
+}
+} // namespace agwn
+
+struct agwn_context : agwn::Context
+{
+};
+
+// ---- device helpers ----------------------------------------------------------------------------------------
+namespace agwn
+{
+// Unfused IEEE arithmetic.  Each operation rounds once, like the reference's default (FMA-free) CPU build, so a
+// formula written with these reproduces the CPU's values exactly.  The intrinsics are never contracted.
+struct rd
+{
+    double v;
+    rd() = default;
+    __device__ __forceinline__ constexpr rd(double x) : v(x) {}
+    __device__ __forceinline__ friend rd operator+(rd a, rd b) { return rd(__dadd_rn(a.v, b.v)); }
+    __device__ __forceinline__ friend rd operator-(rd a, rd b) { return rd(__dsub_rn(a.v, b.v)); }
+    __device__ __forceinline__ friend rd operator*(rd a, rd b) { return rd(__dmul_rn(a.v, b.v)); }
+    __device__ __forceinline__ friend rd operator/(rd a, rd b) { return rd(__ddiv_rn(a.v, b.v)); }
+    __device__ __forceinline__ friend rd operator-(rd a) { return rd(-a.v); }
+};
+struct rf
+{
+    float v;
+    rf() = default;
+    __device__ __forceinline__ constexpr rf(float x) : v(x) {}
+    __device__ __forceinline__ friend rf operator+(rf a, rf b) { return rf(__fadd_rn(a.v, b.v)); }
+    __device__ __forceinline__ friend rf operator-(rf a, rf b) { return rf(__fsub_rn(a.v, b.v)); }
+    __device__ __forceinline__ friend rf operator*(rf a, rf b) { return rf(__fmul_rn(a.v, b.v)); }
+    __device__ __forceinline__ friend rf operator/(rf a, rf b) { return rf(__fdiv_rn(a.v, b.v)); }
+    __device__ __forceinline__ friend rf operator-(rf a) { return rf(-a.v); }
+};
+template <class T>
+struct exact_of;
+template <>
+struct exact_of<double>
+{
+    using type = rd;
+};
+template <>
+struct exact_of<float>
+{
+    using type = rf;
+};
+
+__device__ __forceinline__ rd ex_sqrt(rd a)
+{
+    return rd(__dsqrt_rn(a.v));
+}
+__device__ __forceinline__ rf ex_sqrt(rf a)
+{
+    return rf(__fsqrt_rn(a.v));
+}
+__device__ __forceinline__ double ex_atan2(rd y, rd x)
+{
+    return atan2(y.v, x.v);
+}
+__device__ __forceinline__ float ex_atan2(rf y, rf x)
+{
+    return atan2f(y.v, x.v);
+}
+
+template <class S>
+struct ev3
+{
+    S x, y, z;
+};
+template <class S>
+__device__ __forceinline__ ev3<S> operator-(ev3<S> a, ev3<S> b)
+{
+    return {a.x - b.x, a.y - b.y, a.z - b.z};
+}
+template <class S>
+__device__ __forceinline__ S edot(ev3<S> a, ev3<S> b)
+{
+    return a.x * b.x + a.y * b.y + a.z * b.z;
+}
+template <class S>
+__device__ __forceinline__ ev3<S> ecross(ev3<S> a, ev3<S> b)
+{
+    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+
+// Bounded spin limits: every device-side wait gives up after this many polls and raises FLAG_TIMEOUT.
+constexpr long long kSpinLimit = 1ll << 22;
+} // namespace agwn

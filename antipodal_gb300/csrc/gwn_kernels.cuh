@@ -1,0 +1,33 @@
+// Declarations shared by the translation units of libantipodal_gb300.
+#pragma once
+
+#include "agwn_internal.cuh"
+
+namespace agwn
+{
+// Device state of a CudaIntersector: triangles in hierarchy order and a linear BVH (see lbvh.cu).
+struct Bvh
+{
+    int device = 0;
+    int scalar_bytes = 8;       // 8: double geometry, 4: float geometry
+    int64_t n_tri = 0;
+    int32_t depth = 0;
+    void* tri = nullptr;        // n_tri x 9 scalars (a, b, c) in leaf order
+    void* nodes = nullptr;      // (n_tri - 1) x BvhNode
+    float* root_box = nullptr;  // 6 floats; used when n_tri == 1
+    double scene_scale = 1.0;   // max |coordinate| of the geometry, for the traversal tolerance
+};
+
+// Fractional term of the mesh GWN for `n` device-resident queries; adds `counts[i]` (if non-null).
+template <class T>
+int fractional_run(Context& ctx, const T* d_pos, int64_t n, T* d_out, const int32_t* d_counts, const T* x0_host,
+                   const T* d_seg_raw, int64_t n_seg);
+
+// Integer term over a BVH for `n` device-resident queries.
+template <class T>
+int integer_run(Context& ctx, const Bvh& bvh, const T* d_pos, int64_t n, int32_t* d_counts, const T* dir_host);
+} // namespace agwn
+
+struct agwn_bvh : agwn::Bvh
+{
+};

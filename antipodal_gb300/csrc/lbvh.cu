@@ -1,0 +1,823 @@
+// Integer (ray-crossing) term of the mesh GWN over a linear BVH built on the device, and the CudaIntersector
+// C ABI.
+//
+// Counting rule: NaiveIntersector::signed_intersection_count (src/antipodal/intersector/intersector.hh:61-100):
+// Moller-Trumbore against (p, dir), t >= 0, sign of (e1 x e2) . dir, with its early rejections.  The test is
+// written with unfused, correctly rounded operations (rd/rf), so every candidate triangle gets exactly the CPU's
+// decision -- including the double count of a ray through an edge shared by two triangles.
+//
+// The hierarchy only culls.  Boxes are rounded outward to float and, at traversal time, grown by a tolerance
+// far above the float rounding of the ray origin and of the slab arithmetic, so a triangle that the exact test
+// would count is never culled: counts equal the linear scan's.
+//
+// Build (all on the device): triangle boxes and centroids -> 30-bit Morton codes -> stable LSD radix sort of
+// (code, triangle) in four 8-bit passes -> Karras (2012) hierarchy over the sorted codes (ties broken by
+// position) -> bottom-up boxes with one atomic visit counter per node.  Leaves hold one triangle each; the
+// triangles are copied into leaf order so a leaf's vertices are one contiguous 9-scalar record.
+
+#include "agwn_internal.cuh"
+#include "gwn_kernels.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+namespace agwn
+{
+namespace
+{
+// Internal node: boxes of both children, so one 64-byte fetch decides both.  lo_l.w / lo_r.w hold the child
+// codes as int bits: >= 0 an internal node, < 0 the leaf ~code.
+struct alignas(16) BvhNode
+{
+    float4 lo_l, hi_l, lo_r, hi_r;
+};
+
+constexpr int kStackDepth = 64;
+
+__device__ __forceinline__ unsigned expand_bits(unsigned v)
+{
+    v = (v * 0x00010001u) & 0xFF0000FFu;
+    v = (v * 0x00000101u) & 0x0F00F00Fu;
+    v = (v * 0x00000011u) & 0xC30C30C3u;
+    v = (v * 0x00000005u) & 0x49249249u;
+    return v;
+}
+
+__device__ __forceinline__ unsigned float_flip(float f)
+{
+    unsigned const u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float float_unflip(unsigned u)
+{
+    return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
+}
+
+template <class T>
+__device__ __forceinline__ float to_float_down(T v)
+{
+    if constexpr (sizeof(T) == 8)
+        return __double2float_rd(v);
+    else
+        return v;
+}
+template <class T>
+__device__ __forceinline__ float to_float_up(T v)
+{
+    if constexpr (sizeof(T) == 8)
+        return __double2float_ru(v);
+    else
+        return v;
+}
+
+// Per triangle: outward-rounded float box, centroid; scene centroid bounds (flipped-uint atomics) and the largest
+// coordinate magnitude.  Raises flags[FLAG_COUNT - 1] on an out-of-range index.
+template <class T>
+__global__ void k_tri_boxes(const T* __restrict__ verts, int64_t nv, const int32_t* __restrict__ idx, int64_t n_tri,
+                            float* __restrict__ box, float* __restrict__ cen, unsigned* __restrict__ cbounds,
+                            unsigned* __restrict__ scale_bits, int* flags)
+{
+    float cmn[3] = {INFINITY, INFINITY, INFINITY}, cmx[3] = {-INFINITY, -INFINITY, -INFINITY};
+    float amax = 0.f;
+    for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; t < n_tri; t += int64_t(gridDim.x) * blockDim.x)
+    {
+        int32_t const i0 = idx[3 * t], i1 = idx[3 * t + 1], i2 = idx[3 * t + 2];
+        if (i0 < 0 || i1 < 0 || i2 < 0 || i0 >= nv || i1 >= nv || i2 >= nv)
+        {
+            atomicOr(flags + FLAG_COUNT - 1, 1);
+            continue;
+        }
+        T const* a = verts + 3 * int64_t(i0);
+        T const* b = verts + 3 * int64_t(i1);
+        T const* c = verts + 3 * int64_t(i2);
+        for (int k = 0; k < 3; ++k)
+        {
+            T const mn = min(a[k], min(b[k], c[k]));
+            T const mx = max(a[k], max(b[k], c[k]));
+            float const lo = to_float_down(mn), hi = to_float_up(mx);
+            box[6 * t + k] = lo;
+            box[6 * t + 3 + k] = hi;
+            float const ce = 0.5f * (lo + hi);
+            cen[3 * t + k] = ce;
+            cmn[k] = fminf(cmn[k], ce);
+            cmx[k] = fmaxf(cmx[k], ce);
+            amax = fmaxf(amax, fmaxf(fabsf(lo), fabsf(hi)));
+        }
+    }
+    for (int k = 0; k < 3; ++k)
+    {
+        for (int o = 16; o > 0; o >>= 1)
+        {
+            cmn[k] = fminf(cmn[k], __shfl_xor_sync(0xffffffffu, cmn[k], o));
+            cmx[k] = fmaxf(cmx[k], __shfl_xor_sync(0xffffffffu, cmx[k], o));
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1)
+        amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, o));
+    if ((threadIdx.x & 31) == 0)
+    {
+        for (int k = 0; k < 3; ++k)
+        {
+            atomicMin(cbounds + k, float_flip(cmn[k]));
+            atomicMax(cbounds + 3 + k, float_flip(cmx[k]));
+        }
+        atomicMax(scale_bits, __float_as_uint(amax)); // non-negative floats order like their bits
+    }
+}
+
+__global__ void k_morton(const float* __restrict__ cen, int64_t n_tri, const unsigned* __restrict__ cbounds,
+                         unsigned* __restrict__ keys, unsigned* __restrict__ vals)
+{
+    float lo[3], ext[3];
+    for (int k = 0; k < 3; ++k)
+    {
+        lo[k] = float_unflip(cbounds[k]);
+        float const hi = float_unflip(cbounds[3 + k]);
+        ext[k] = hi - lo[k];
+    }
+    for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; t < n_tri; t += int64_t(gridDim.x) * blockDim.x)
+    {
+        unsigned m[3];
+        for (int k = 0; k < 3; ++k)
+        {
+            float const u = ext[k] > 0.f ? (cen[3 * t + k] - lo[k]) / ext[k] : 0.5f;
+            m[k] = unsigned(fminf(fmaxf(u * 1024.f, 0.f), 1023.f));
+        }
+        keys[t] = (expand_bits(m[0]) << 2) | (expand_bits(m[1]) << 1) | expand_bits(m[2]);
+        vals[t] = unsigned(t);
+    }
+}
+
+// ---- stable LSD radix sort, 8 bits per pass -----------------------------------------------------------------
+constexpr int kRsBlock = 256;
+constexpr int kRsIpt = 8;
+constexpr int kRsTile = kRsBlock * kRsIpt;
+
+__global__ void __launch_bounds__(kRsBlock) k_rs_hist(const unsigned* __restrict__ keys, int64_t n, int shift,
+                                                      unsigned* __restrict__ hist, int n_blocks)
+{
+    __shared__ unsigned cnt[256];
+    cnt[threadIdx.x] = 0;
+    __syncthreads();
+    int64_t const base = int64_t(blockIdx.x) * kRsTile;
+    for (int r = 0; r < kRsIpt; ++r)
+    {
+        int64_t const i = base + r * kRsBlock + threadIdx.x;
+        if (i < n)
+            atomicAdd(&cnt[(keys[i] >> shift) & 255u], 1u);
+    }
+    __syncthreads();
+    hist[int64_t(threadIdx.x) * n_blocks + blockIdx.x] = cnt[threadIdx.x];
+}
+
+// Exclusive scan of m counters in one block of 1024 threads.
+__global__ void __launch_bounds__(1024) k_rs_scan(unsigned* __restrict__ hist, int64_t m)
+{
+    __shared__ unsigned part[1024];
+    int64_t const per = (m + 1023) / 1024;
+    int64_t const b = per * threadIdx.x;
+    int64_t const e = min(b + per, m);
+    unsigned s = 0;
+    for (int64_t i = b; i < e; ++i)
+        s += hist[i];
+    part[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1)
+    {
+        unsigned const v = threadIdx.x >= unsigned(o) ? part[threadIdx.x - o] : 0u;
+        __syncthreads();
+        part[threadIdx.x] += v;
+        __syncthreads();
+    }
+    unsigned run = threadIdx.x ? part[threadIdx.x - 1] : 0u;
+    for (int64_t i = b; i < e; ++i)
+    {
+        unsigned const v = hist[i];
+        hist[i] = run;
+        run += v;
+    }
+}
+
+__global__ void __launch_bounds__(kRsBlock) k_rs_scatter(const unsigned* __restrict__ kin,
+                                                         const unsigned* __restrict__ vin, int64_t n, int shift,
+                                                         const unsigned* __restrict__ hist, int n_blocks,
+                                                         unsigned* __restrict__ kout, unsigned* __restrict__ vout)
+{
+    constexpr int W = kRsBlock / 32;
+    __shared__ unsigned base[256];
+    __shared__ unsigned wcnt[W][256];
+    base[threadIdx.x] = hist[int64_t(threadIdx.x) * n_blocks + blockIdx.x];
+    for (int w = 0; w < W; ++w)
+        wcnt[w][threadIdx.x] = 0;
+    __syncthreads();
+    int const lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned const lt = (1u << lane) - 1u;
+    int64_t const tile0 = int64_t(blockIdx.x) * kRsTile;
+    for (int r = 0; r < kRsIpt; ++r)
+    {
+        int64_t const i = tile0 + r * kRsBlock + threadIdx.x;
+        bool const valid = i < n;
+        unsigned const key = valid ? kin[i] : 0u;
+        unsigned const val = valid ? vin[i] : 0u;
+        unsigned const d = valid ? ((key >> shift) & 255u) : 256u;
+        unsigned const peers = __match_any_sync(0xffffffffu, d);
+        unsigned const rank = __popc(peers & lt);
+        bool const leader = (peers & lt) == 0;
+        if (valid && leader)
+            wcnt[warp][d] = __popc(peers);
+        __syncthreads();
+        if (valid)
+        {
+            unsigned pos = base[d] + rank;
+            for (int w = 0; w < warp; ++w)
+                pos += wcnt[w][d];
+            kout[pos] = key;
+            vout[pos] = val;
+        }
+        __syncthreads();
+        if (valid && leader)
+        {
+            atomicAdd(&base[d], unsigned(__popc(peers))); // several warps may hold the same digit
+            wcnt[warp][d] = 0;
+        }
+        __syncthreads();
+    }
+}
+
+// ---- Karras hierarchy ---------------------------------------------------------------------------------------
+__device__ __forceinline__ int delta(const unsigned* keys, int n, int i, int j)
+{
+    if (j < 0 || j >= n)
+        return -1;
+    unsigned const a = keys[i], b = keys[j];
+    if (a == b)
+        return 32 + __clz(unsigned(i) ^ unsigned(j));
+    return __clz(a ^ b);
+}
+
+__global__ void k_karras(const unsigned* __restrict__ keys, int n, int* __restrict__ left, int* __restrict__ right,
+                         int* __restrict__ parent_node, int* __restrict__ parent_leaf)
+{
+    int const i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n - 1)
+        return;
+    int const d = (delta(keys, n, i, i + 1) - delta(keys, n, i, i - 1)) >= 0 ? 1 : -1;
+    int const dmin = delta(keys, n, i, i - d);
+    int lmax = 2;
+    while (delta(keys, n, i, i + lmax * d) > dmin)
+        lmax *= 2;
+    int l = 0;
+    for (int t = lmax / 2; t >= 1; t /= 2)
+        if (delta(keys, n, i, i + (l + t) * d) > dmin)
+            l += t;
+    int const j = i + l * d;
+    int const dnode = delta(keys, n, i, j);
+    int s = 0;
+    for (int div = 2;; div *= 2)
+    {
+        int const t = (l + div - 1) / div;
+        if (delta(keys, n, i, i + (s + t) * d) > dnode)
+            s += t;
+        if (t <= 1)
+            break;
+    }
+    int const gamma = i + s * d + min(d, 0);
+    int const lo = min(i, j), hi = max(i, j);
+    int const lc = (lo == gamma) ? ~gamma : gamma;
+    int const rc = (hi == gamma + 1) ? ~(gamma + 1) : gamma + 1;
+    left[i] = lc;
+    right[i] = rc;
+    if (lc < 0)
+        parent_leaf[~lc] = i;
+    else
+        parent_node[lc] = i;
+    if (rc < 0)
+        parent_leaf[~rc] = i;
+    else
+        parent_node[rc] = i;
+    if (i == 0)
+        parent_node[0] = -1;
+}
+
+// Leaf setup: copy each sorted triangle's vertices into leaf order and its box into leaf slots.
+template <class T>
+__global__ void k_leaves(const T* __restrict__ verts, const int32_t* __restrict__ idx,
+                         const unsigned* __restrict__ order, const float* __restrict__ box, int64_t n_tri,
+                         T* __restrict__ tri, float* __restrict__ leaf_box)
+{
+    for (int64_t l = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; l < n_tri; l += int64_t(gridDim.x) * blockDim.x)
+    {
+        unsigned const t = order[l];
+        for (int v = 0; v < 3; ++v)
+        {
+            T const* p = verts + 3 * int64_t(idx[3 * int64_t(t) + v]);
+            for (int k = 0; k < 3; ++k)
+                tri[9 * l + 3 * v + k] = p[k];
+        }
+        for (int k = 0; k < 6; ++k)
+            leaf_box[6 * l + k] = box[6 * int64_t(t) + k];
+    }
+}
+
+__global__ void k_refit(int n, const int* __restrict__ left, const int* __restrict__ right,
+                        const int* __restrict__ parent_node, const int* __restrict__ parent_leaf,
+                        const float* __restrict__ leaf_box, float* node_box, int* visit, BvhNode* __restrict__ nodes)
+{
+    int const l = blockIdx.x * blockDim.x + threadIdx.x;
+    if (l >= n)
+        return;
+    int node = parent_leaf[l];
+    while (node >= 0)
+    {
+        __threadfence();
+        if (atomicAdd(&visit[node], 1) == 0)
+            return; // the sibling subtree is not finished; its last thread continues upward
+        float b[2][6];
+        int const ch[2] = {left[node], right[node]};
+        for (int c = 0; c < 2; ++c)
+        {
+            const float* src = ch[c] < 0 ? leaf_box + 6 * int64_t(~ch[c]) : node_box + 6 * int64_t(ch[c]);
+            for (int k = 0; k < 6; ++k)
+                b[c][k] = __ldcg(src + k);
+        }
+        BvhNode nd;
+        nd.lo_l = make_float4(b[0][0], b[0][1], b[0][2], __int_as_float(ch[0]));
+        nd.hi_l = make_float4(b[0][3], b[0][4], b[0][5], 0.f);
+        nd.lo_r = make_float4(b[1][0], b[1][1], b[1][2], __int_as_float(ch[1]));
+        nd.hi_r = make_float4(b[1][3], b[1][4], b[1][5], 0.f);
+        nodes[node] = nd;
+        for (int k = 0; k < 3; ++k)
+        {
+            __stcg(node_box + 6 * int64_t(node) + k, fminf(b[0][k], b[1][k]));
+            __stcg(node_box + 6 * int64_t(node) + 3 + k, fmaxf(b[0][3 + k], b[1][3 + k]));
+        }
+        node = parent_node[node];
+    }
+}
+
+__global__ void k_depth(int n, const int* __restrict__ parent_node, const int* __restrict__ parent_leaf, int* depth)
+{
+    int const l = blockIdx.x * blockDim.x + threadIdx.x;
+    if (l >= n)
+        return;
+    int d = 1;
+    int node = parent_leaf[l];
+    while (node >= 0 && d <= n)
+    {
+        ++d;
+        node = parent_node[node];
+    }
+    atomicMax(depth, d); // d > n only for a broken parent chain
+}
+
+// ---- traversal ----------------------------------------------------------------------------------------------
+// Moller-Trumbore sign with NaiveIntersector's arithmetic and early rejections, in unfused precision S.
+template <class S>
+__device__ __forceinline__ int mt_sign(ev3<S> p, ev3<S> dir, ev3<S> a, ev3<S> b, ev3<S> c)
+{
+    ev3<S> const e1 = b - a;
+    ev3<S> const e2 = c - a;
+    ev3<S> const h = ecross(dir, e2);
+    S const det = edot(e1, h);
+    if (det.v == 0)
+        return 0;
+    S const inv = S(1) / det;
+    ev3<S> const s = p - a;
+    S const u = inv * edot(s, h);
+    if (u.v < 0 || u.v > 1)
+        return 0;
+    ev3<S> const q = ecross(s, e1);
+    S const v = inv * edot(dir, q);
+    if (v.v < 0 || (u + v).v > 1)
+        return 0;
+    S const t = inv * edot(e2, q);
+    if (t.v < 0)
+        return 0;
+    ev3<S> const ng = ecross(e1, e2);
+    return edot(ng, dir).v > 0 ? 1 : -1;
+}
+
+template <class T>
+__device__ __forceinline__ int leaf_test(const T* __restrict__ tri, int leaf, ev3<typename exact_of<T>::type> p,
+                                         ev3<typename exact_of<T>::type> dir)
+{
+    using S = typename exact_of<T>::type;
+    const T* r = tri + 9 * int64_t(leaf);
+    ev3<S> const a{S(r[0]), S(r[1]), S(r[2])};
+    ev3<S> const b{S(r[3]), S(r[4]), S(r[5])};
+    ev3<S> const c{S(r[6]), S(r[7]), S(r[8])};
+    return mt_sign(p, dir, a, b, c);
+}
+
+__device__ __forceinline__ bool slab(float4 lo, float4 hi, float ox, float oy, float oz, float ix, float iy, float iz,
+                                     float tol)
+{
+    float const tx0 = (lo.x - tol - ox) * ix, tx1 = (hi.x + tol - ox) * ix;
+    float const ty0 = (lo.y - tol - oy) * iy, ty1 = (hi.y + tol - oy) * iy;
+    float const tz0 = (lo.z - tol - oz) * iz, tz1 = (hi.z + tol - oz) * iz;
+    float const tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fminf(tz0, tz1));
+    float const tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fmaxf(tz0, tz1));
+    return tn <= tf && tf >= 0.f;
+}
+
+__device__ __forceinline__ float safe_inv(float d)
+{
+    float const dd = fabsf(d) < 1e-30f ? copysignf(1e-30f, d) : d;
+    return 1.0f / dd;
+}
+
+template <class T>
+__global__ void __launch_bounds__(128) k_traverse(const BvhNode* __restrict__ nodes, const T* __restrict__ tri,
+                                                  int64_t n_tri, float scene_scale, const T* __restrict__ pos,
+                                                  int64_t n, int32_t* __restrict__ counts, T dx, T dy, T dz,
+                                                  int* flags)
+{
+    using S = typename exact_of<T>::type;
+    ev3<S> const dir{S(dx), S(dy), S(dz)};
+    float const ix = safe_inv(float(dx)), iy = safe_inv(float(dy)), iz = safe_inv(float(dz));
+    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+    {
+        T const px = pos[3 * i], py = pos[3 * i + 1], pz = pos[3 * i + 2];
+        ev3<S> const p{S(px), S(py), S(pz)};
+        int sum = 0;
+        if (n_tri == 1)
+        {
+            sum = leaf_test<T>(tri, 0, p, dir);
+        }
+        else if (n_tri > 1)
+        {
+            float const ox = float(px), oy = float(py), oz = float(pz);
+            float const qmax = fmaxf(fmaxf(fabsf(ox), fabsf(oy)), fabsf(oz));
+            float const tol = (qmax + scene_scale) * 3.0517578e-5f + 1e-30f; // 2^-15 of the coordinate scale
+            int stack[kStackDepth];
+            int sp = 0;
+            int node = 0;
+            while (true)
+            {
+                BvhNode const nd = nodes[node];
+                int const lc = __float_as_int(nd.lo_l.w), rc = __float_as_int(nd.lo_r.w);
+                bool const hl = slab(nd.lo_l, nd.hi_l, ox, oy, oz, ix, iy, iz, tol);
+                bool const hr = slab(nd.lo_r, nd.hi_r, ox, oy, oz, ix, iy, iz, tol);
+                int next = -1;
+                if (hl)
+                {
+                    if (lc < 0)
+                        sum += leaf_test<T>(tri, ~lc, p, dir);
+                    else
+                        next = lc;
+                }
+                if (hr)
+                {
+                    if (rc < 0)
+                        sum += leaf_test<T>(tri, ~rc, p, dir);
+                    else if (next < 0)
+                        next = rc;
+                    else
+                    {
+                        if (sp == kStackDepth)
+                        {
+                            atomicOr(flags + FLAG_STACK, 1);
+                            break;
+                        }
+                        stack[sp++] = rc;
+                    }
+                }
+                if (next >= 0)
+                    node = next;
+                else if (sp > 0)
+                    node = stack[--sp];
+                else
+                    break;
+            }
+        }
+        counts[i] = sum;
+    }
+}
+
+template <class T>
+__global__ void __launch_bounds__(128) k_bruteforce(const T* __restrict__ verts, const int32_t* __restrict__ idx,
+                                                    int64_t n_tri, const T* __restrict__ pos, int64_t n,
+                                                    int32_t* __restrict__ counts, T dx, T dy, T dz)
+{
+    using S = typename exact_of<T>::type;
+    ev3<S> const dir{S(dx), S(dy), S(dz)};
+    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+    {
+        ev3<S> const p{S(pos[3 * i]), S(pos[3 * i + 1]), S(pos[3 * i + 2])};
+        int sum = 0;
+        for (int64_t t = 0; t < n_tri; ++t)
+        {
+            T const* a = verts + 3 * int64_t(idx[3 * t]);
+            T const* b = verts + 3 * int64_t(idx[3 * t + 1]);
+            T const* c = verts + 3 * int64_t(idx[3 * t + 2]);
+            sum += mt_sign(p, dir, ev3<S>{S(a[0]), S(a[1]), S(a[2])}, ev3<S>{S(b[0]), S(b[1]), S(b[2])},
+                           ev3<S>{S(c[0]), S(c[1]), S(c[2])});
+        }
+        counts[i] = sum;
+    }
+}
+
+// RAII device buffer for build temporaries.
+struct Tmp
+{
+    void* p = nullptr;
+    ~Tmp()
+    {
+        if (p)
+            cudaFree(p);
+    }
+    int alloc(size_t bytes)
+    {
+        cudaError_t const e = cudaMalloc(&p, bytes ? bytes : 1);
+        if (e != cudaSuccess)
+        {
+            cudaGetLastError();
+            p = nullptr;
+            return fail(e == cudaErrorMemoryAllocation ? AGWN_ERR_NOMEM : AGWN_ERR_CUDA, "cudaMalloc(%zu): %s", bytes,
+                        cudaGetErrorString(e));
+        }
+        return AGWN_OK;
+    }
+    template <class U>
+    U* as() const
+    {
+        return static_cast<U*>(p);
+    }
+};
+
+void bvh_free(Bvh* b)
+{
+    if (!b)
+        return;
+    if (b->tri)
+        cudaFree(b->tri);
+    if (b->nodes)
+        cudaFree(b->nodes);
+    b->tri = nullptr;
+    b->nodes = nullptr;
+}
+
+template <class T>
+int bvh_build(Context& ctx, const T* vertices, int64_t nv, const int32_t* indices, int64_t n_idx, Bvh* out)
+{
+    AGWN_CHECK_ARG(nv >= 0 && n_idx >= 0 && n_idx % 3 == 0, "index count must be a non-negative multiple of 3");
+    AGWN_CHECK_ARG(n_idx / 3 < (int64_t(1) << 31) - 1, "too many triangles");
+    AGWN_CHECK_ARG(n_idx == 0 || (vertices && indices && nv > 0), "null vertices/indices");
+    int64_t const n_tri = n_idx / 3;
+    out->scalar_bytes = int(sizeof(T));
+    out->n_tri = n_tri;
+    out->device = ctx.device;
+    if (n_tri == 0)
+        return AGWN_OK;
+    cudaStream_t const st = ctx.stream;
+    const void* dv = nullptr;
+    const void* di = nullptr;
+    AGWN_TRY(stage_in(ctx, vertices, sizeof(T) * 3 * nv, S_MISC0, &dv));
+    AGWN_TRY(stage_in(ctx, indices, sizeof(int32_t) * n_idx, S_MISC1, &di));
+    const T* V = static_cast<const T*>(dv);
+    const int32_t* I = static_cast<const int32_t*>(di);
+
+    Tmp box, cen, misc, keys0, vals0, keys1, vals1, hist, left, right, pnode, pleaf, nbox, visit, leafbox;
+    AGWN_TRY(box.alloc(sizeof(float) * 6 * n_tri));
+    AGWN_TRY(cen.alloc(sizeof(float) * 3 * n_tri));
+    AGWN_TRY(misc.alloc(sizeof(unsigned) * 16));
+    AGWN_TRY(keys0.alloc(sizeof(unsigned) * n_tri));
+    AGWN_TRY(vals0.alloc(sizeof(unsigned) * n_tri));
+    AGWN_TRY(keys1.alloc(sizeof(unsigned) * n_tri));
+    AGWN_TRY(vals1.alloc(sizeof(unsigned) * n_tri));
+    int const n_rs_blocks = div_up(n_tri, kRsTile);
+    AGWN_TRY(hist.alloc(sizeof(unsigned) * 256 * n_rs_blocks));
+    AGWN_TRY(left.alloc(sizeof(int) * n_tri));
+    AGWN_TRY(right.alloc(sizeof(int) * n_tri));
+    AGWN_TRY(pnode.alloc(sizeof(int) * n_tri));
+    AGWN_TRY(pleaf.alloc(sizeof(int) * n_tri));
+    AGWN_TRY(nbox.alloc(sizeof(float) * 6 * n_tri));
+    AGWN_TRY(visit.alloc(sizeof(int) * n_tri));
+    AGWN_TRY(leafbox.alloc(sizeof(float) * 6 * n_tri));
+
+    unsigned init[8];
+    for (int k = 0; k < 3; ++k)
+    {
+        init[k] = 0xFFFFFFFFu; // min of flipped floats
+        init[3 + k] = 0u;      // max of flipped floats
+    }
+    init[6] = 0u; // scale bits
+    init[7] = 0u; // depth
+    AGWN_TRY_CUDA(cudaMemcpyAsync(misc.p, init, sizeof(init), cudaMemcpyHostToDevice, st));
+    AGWN_TRY_CUDA(cudaMemsetAsync(ctx.d_flags + FLAG_COUNT - 1, 0, sizeof(int), st));
+    int const g = std::min(div_up(n_tri, 256), 8 * ctx.sm_count);
+    AGWN_TRY(ctx.launch_begin(AGWN_K_OTHER));
+    k_tri_boxes<T><<<g, 256, 0, st>>>(V, nv, I, n_tri, box.as<float>(), cen.as<float>(), misc.as<unsigned>(),
+                                      misc.as<unsigned>() + 6, ctx.d_flags);
+    AGWN_TRY(ctx.launch_end(AGWN_K_OTHER));
+    int bad = 0;
+    AGWN_TRY_CUDA(cudaMemcpyAsync(&bad, ctx.d_flags + FLAG_COUNT - 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+    AGWN_TRY_CUDA(cudaStreamSynchronize(st));
+    if (bad)
+    {
+        AGWN_TRY_CUDA(cudaMemsetAsync(ctx.d_flags + FLAG_COUNT - 1, 0, sizeof(int), st));
+        return fail(AGWN_ERR_INVALID, "triangle index out of range [0, %lld)", (long long)nv);
+    }
+    AGWN_TRY(ctx.launch_begin(AGWN_K_OTHER));
+    k_morton<<<g, 256, 0, st>>>(cen.as<float>(), n_tri, misc.as<unsigned>(), keys0.as<unsigned>(),
+                                vals0.as<unsigned>());
+    AGWN_TRY(ctx.launch_end(AGWN_K_OTHER));
+    // four stable passes; the result lands back in keys0/vals0
+    unsigned *ka = keys0.as<unsigned>(), *va = vals0.as<unsigned>(), *kb = keys1.as<unsigned>(),
+             *vb = vals1.as<unsigned>();
+    for (int pass = 0; pass < 4; ++pass)
+    {
+        int const shift = 8 * pass;
+        AGWN_TRY(ctx.launch_begin(AGWN_K_OTHER));
+        k_rs_hist<<<n_rs_blocks, kRsBlock, 0, st>>>(ka, n_tri, shift, hist.as<unsigned>(), n_rs_blocks);
+        k_rs_scan<<<1, 1024, 0, st>>>(hist.as<unsigned>(), int64_t(256) * n_rs_blocks);
+        k_rs_scatter<<<n_rs_blocks, kRsBlock, 0, st>>>(ka, va, n_tri, shift, hist.as<unsigned>(), n_rs_blocks, kb, vb);
+        AGWN_TRY(ctx.launch_end(AGWN_K_OTHER));
+        std::swap(ka, kb);
+        std::swap(va, vb);
+    }
+    T* tri = nullptr;
+    AGWN_TRY_CUDA(cudaMalloc(&tri, sizeof(T) * 9 * n_tri));
+    out->tri = tri;
+    AGWN_TRY(ctx.launch_begin(AGWN_K_OTHER));
+    k_leaves<T><<<g, 256, 0, st>>>(V, I, va, box.as<float>(), n_tri, tri, leafbox.as<float>());
+    AGWN_TRY(ctx.launch_end(AGWN_K_OTHER));
+    if (n_tri > 1)
+    {
+        BvhNode* nodes = nullptr;
+        AGWN_TRY_CUDA(cudaMalloc(&nodes, sizeof(BvhNode) * (n_tri - 1)));
+        out->nodes = nodes;
+        AGWN_TRY_CUDA(cudaMemsetAsync(visit.p, 0, sizeof(int) * n_tri, st));
+        int const gb = div_up(n_tri, 256);
+        AGWN_TRY(ctx.launch_begin(AGWN_K_OTHER));
+        k_karras<<<gb, 256, 0, st>>>(ka, int(n_tri), left.as<int>(), right.as<int>(), pnode.as<int>(),
+                                     pleaf.as<int>());
+        k_refit<<<gb, 256, 0, st>>>(int(n_tri), left.as<int>(), right.as<int>(), pnode.as<int>(), pleaf.as<int>(),
+                                    leafbox.as<float>(), nbox.as<float>(), visit.as<int>(), nodes);
+        k_depth<<<gb, 256, 0, st>>>(int(n_tri), pnode.as<int>(), pleaf.as<int>(),
+                                    reinterpret_cast<int*>(misc.as<unsigned>() + 7));
+        AGWN_TRY(ctx.launch_end(AGWN_K_OTHER));
+    }
+    unsigned back[8];
+    AGWN_TRY_CUDA(cudaMemcpyAsync(back, misc.p, sizeof(back), cudaMemcpyDeviceToHost, st));
+    AGWN_TRY_CUDA(cudaStreamSynchronize(st));
+    float scale;
+    std::memcpy(&scale, &back[6], sizeof(float));
+    out->scene_scale = scale;
+    out->depth = n_tri > 1 ? int32_t(back[7]) : 1;
+    if (out->depth > n_tri)
+        return fail(AGWN_ERR_CUDA, "BVH build produced a broken hierarchy (depth %d for %lld triangles)", out->depth,
+                    (long long)n_tri);
+    if (out->depth >= kStackDepth)
+        set_message("BVH depth %d is at or above the traversal stack depth %d", out->depth, kStackDepth);
+    return AGWN_OK;
+}
+} // namespace
+
+template <class T>
+int integer_run(Context& ctx, const Bvh& bvh, const T* d_pos, int64_t n, int32_t* d_counts, const T* dir_host)
+{
+    if (n == 0)
+        return AGWN_OK;
+    int const block = 128;
+    int const grid = int(std::min<int64_t>(div_up(n, block), int64_t(ctx.sm_count) * 16));
+    AGWN_TRY(ctx.launch_begin(AGWN_K_INTEGER));
+    k_traverse<T><<<grid, block, 0, ctx.stream>>>(static_cast<const BvhNode*>(bvh.nodes), static_cast<const T*>(bvh.tri),
+                                                  bvh.n_tri, float(bvh.scene_scale), d_pos, n, d_counts, dir_host[0],
+                                                  dir_host[1], dir_host[2], ctx.d_flags);
+    return ctx.launch_end(AGWN_K_INTEGER);
+}
+
+template int integer_run<double>(Context&, const Bvh&, const double*, int64_t, int32_t*, const double*);
+template int integer_run<float>(Context&, const Bvh&, const float*, int64_t, int32_t*, const float*);
+
+namespace
+{
+template <class T>
+int bvh_create(agwn_context* ctx, const T* vertices, int64_t nv, const int32_t* indices, int64_t n_idx, agwn_bvh** out)
+{
+    AGWN_CHECK_ARG(ctx && out, "null context/out");
+    *out = nullptr;
+    clear_message();
+    AGWN_TRY_CUDA(cudaSetDevice(ctx->device));
+    auto* b = new agwn_bvh{};
+    int const s = bvh_build<T>(*ctx, vertices, nv, indices, n_idx, b);
+    if (s != AGWN_OK)
+    {
+        bvh_free(b);
+        delete b;
+        return s;
+    }
+    *out = b;
+    return AGWN_OK;
+}
+
+template <class T>
+int batch_integer(agwn_context* ctx, const agwn_bvh* bvh, const T* positions, int64_t n, int32_t* out, const T* dir)
+{
+    AGWN_CHECK_ARG(ctx && bvh && dir, "null context/intersector/dir");
+    AGWN_CHECK_ARG(n >= 0, "negative size");
+    AGWN_CHECK_ARG(n == 0 || (positions && out), "null positions/out");
+    AGWN_CHECK_ARG(bvh->scalar_bytes == int(sizeof(T)), "intersector precision does not match the queries");
+    clear_message();
+    AGWN_TRY_CUDA(cudaSetDevice(ctx->device));
+    if (n == 0)
+        return AGWN_OK;
+    const void* dpos = nullptr;
+    void* dout = nullptr;
+    bool host_out = false;
+    AGWN_TRY(stage_in(*ctx, positions, sizeof(T) * 3 * n, S_QUERIES, &dpos));
+    AGWN_TRY(stage_out(*ctx, out, sizeof(int32_t) * n, S_COUNTS, &dout, &host_out));
+    if (bvh->n_tri == 0)
+        AGWN_TRY_CUDA(cudaMemsetAsync(dout, 0, sizeof(int32_t) * n, ctx->stream));
+    else
+        AGWN_TRY(integer_run<T>(*ctx, *bvh, static_cast<const T*>(dpos), n, static_cast<int32_t*>(dout), dir));
+    if (host_out)
+    {
+        AGWN_TRY_CUDA(cudaMemcpyAsync(out, dout, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, ctx->stream));
+        return ctx->check_flags();
+    }
+    if (dpos != positions)
+        return ctx->check_flags();
+    return AGWN_OK;
+}
+} // namespace
+} // namespace agwn
+
+using namespace agwn;
+
+extern "C"
+{
+int agwn_bvh_create_f64(agwn_context* ctx, const double* vertices, int64_t n_vertices, const int32_t* indices,
+                        int64_t n_indices, agwn_bvh** out)
+{
+    return bvh_create<double>(ctx, vertices, n_vertices, indices, n_indices, out);
+}
+int agwn_bvh_create_f32(agwn_context* ctx, const float* vertices, int64_t n_vertices, const int32_t* indices,
+                        int64_t n_indices, agwn_bvh** out)
+{
+    return bvh_create<float>(ctx, vertices, n_vertices, indices, n_indices, out);
+}
+int agwn_bvh_destroy(agwn_bvh* bvh)
+{
+    if (!bvh)
+        return AGWN_OK;
+    cudaSetDevice(bvh->device);
+    cudaDeviceSynchronize();
+    bvh_free(bvh);
+    delete bvh;
+    return AGWN_OK;
+}
+int agwn_bvh_info(const agwn_bvh* bvh, int64_t* n_triangles, int32_t* depth)
+{
+    AGWN_CHECK_ARG(bvh, "null intersector");
+    if (n_triangles)
+        *n_triangles = bvh->n_tri;
+    if (depth)
+        *depth = bvh->depth;
+    return AGWN_OK;
+}
+int agwn_mesh_batch_integer_f64(agwn_context* ctx, const agwn_bvh* bvh, const double* positions, int64_t n,
+                                int32_t* out_counts, const double* dir)
+{
+    return batch_integer<double>(ctx, bvh, positions, n, out_counts, dir);
+}
+int agwn_mesh_batch_integer_f32(agwn_context* ctx, const agwn_bvh* bvh, const float* positions, int64_t n,
+                                int32_t* out_counts, const float* dir)
+{
+    return batch_integer<float>(ctx, bvh, positions, n, out_counts, dir);
+}
+int agwn_mesh_batch_integer_bruteforce_f64(agwn_context* ctx, const double* vertices, int64_t n_vertices,
+                                           const int32_t* indices, int64_t n_indices, const double* positions,
+                                           int64_t n, int32_t* out_counts, const double* dir)
+{
+    AGWN_CHECK_ARG(ctx && dir, "null context/dir");
+    AGWN_CHECK_ARG(n >= 0 && n_vertices >= 0 && n_indices >= 0 && n_indices % 3 == 0, "bad sizes");
+    AGWN_CHECK_ARG(n == 0 || (positions && out_counts), "null positions/out");
+    clear_message();
+    AGWN_TRY_CUDA(cudaSetDevice(ctx->device));
+    if (n == 0)
+        return AGWN_OK;
+    const void *dv = nullptr, *di = nullptr, *dpos = nullptr;
+    void* dout = nullptr;
+    bool host_out = false;
+    AGWN_TRY(stage_in(*ctx, vertices, sizeof(double) * 3 * n_vertices, S_MISC0, &dv));
+    AGWN_TRY(stage_in(*ctx, indices, sizeof(int32_t) * n_indices, S_MISC1, &di));
+    AGWN_TRY(stage_in(*ctx, positions, sizeof(double) * 3 * n, S_QUERIES, &dpos));
+    AGWN_TRY(stage_out(*ctx, out_counts, sizeof(int32_t) * n, S_COUNTS, &dout, &host_out));
+    // indices are trusted here as in NaiveIntersector; validate them on the host when they live there
+    if (!is_device_pointer(indices))
+        for (int64_t i = 0; i < n_indices; ++i)
+            AGWN_CHECK_ARG(indices[i] >= 0 && indices[i] < n_vertices, "triangle index out of range");
+    int const grid = int(std::min<int64_t>(div_up(n, 128), int64_t(ctx->sm_count) * 16));
+    AGWN_TRY(ctx->launch_begin(AGWN_K_INTEGER));
+    k_bruteforce<double><<<grid, 128, 0, ctx->stream>>>(static_cast<const double*>(dv), static_cast<const int32_t*>(di),
+                                                        n_indices / 3, static_cast<const double*>(dpos), n,
+                                                        static_cast<int32_t*>(dout), dir[0], dir[1], dir[2]);
+    AGWN_TRY(ctx->launch_end(AGWN_K_INTEGER));
+    if (host_out)
+        AGWN_TRY_CUDA(cudaMemcpyAsync(out_counts, dout, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    return ctx->check_flags();
+}
+} // extern "C"

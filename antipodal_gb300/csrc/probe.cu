@@ -1,0 +1,68 @@
+// Throughput probe: the FP32 FMA rate this GPU sustains at its current clocks, the denominator of the
+// fractional kernel's compute roofline (the kernel is bound by the FP32 pipe, not by HBM or tensor cores).
+
+#include "agwn_internal.cuh"
+
+namespace agwn
+{
+namespace
+{
+constexpr int kChains = 8;
+
+// Each thread runs kChains independent FMA chains for `iters` steps.  The result is stored only if it equals a
+// value that cannot occur, so the chains are kept but nothing is written.
+__global__ void __launch_bounds__(256) k_ffma(int iters, float a, float b, float* sink)
+{
+    float v[kChains];
+#pragma unroll
+    for (int c = 0; c < kChains; ++c)
+        v[c] = a + float(threadIdx.x + c);
+    for (int i = 0; i < iters; ++i)
+    {
+#pragma unroll
+        for (int c = 0; c < kChains; ++c)
+            v[c] = fmaf(v[c], a, b);
+    }
+    float s = 0.f;
+#pragma unroll
+    for (int c = 0; c < kChains; ++c)
+        s += v[c];
+    if (s == -1.2345e-30f)
+        sink[0] = s;
+}
+} // namespace
+} // namespace agwn
+
+using namespace agwn;
+
+extern "C" int agwn_probe_fp32_peak(agwn_context* ctx, double* tflops)
+{
+    AGWN_CHECK_ARG(ctx && tflops, "null argument");
+    AGWN_TRY_CUDA(cudaSetDevice(ctx->device));
+    float* sink = nullptr;
+    AGWN_TRY(ctx->scratch_reserve(S_MISC3, sizeof(float), reinterpret_cast<void**>(&sink)));
+    int per_sm = 0;
+    AGWN_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_ffma, 256, 0));
+    int const grid = ctx->sm_count * per_sm * 4;
+    int const iters = 1 << 14;
+    cudaEvent_t e0, e1;
+    AGWN_TRY_CUDA(cudaEventCreate(&e0));
+    AGWN_TRY_CUDA(cudaEventCreate(&e1));
+    float best = 1e30f;
+    for (int rep = 0; rep < 4; ++rep)
+    {
+        AGWN_TRY_CUDA(cudaEventRecord(e0, ctx->stream));
+        k_ffma<<<grid, 256, 0, ctx->stream>>>(iters, 0.9999f, 1e-4f, sink);
+        AGWN_TRY_CUDA(cudaEventRecord(e1, ctx->stream));
+        AGWN_TRY_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        AGWN_TRY_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        if (rep > 0 && ms < best)
+            best = ms;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    double const flops = 2.0 * kChains * double(iters) * double(grid) * 256.0;
+    *tflops = flops / (double(best) * 1e-3) / 1e12;
+    return AGWN_OK;
+}

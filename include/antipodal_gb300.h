@@ -1,0 +1,162 @@
+/*
+ * antipodal_gb300.h -- C ABI of the GB300 batch generalized-winding-number (GWN) library.
+ *
+ * One shared library, libantipodal_gb300.so, built for sm_103a.  Every entry point takes plain pointers and
+ * sizes and returns an int status (AGWN_OK == 0).  A failing call leaves a human-readable reason in
+ * agwn_last_error_message() (per host thread).  The header-only C++20 front end
+ * (include/antipodal/cuda/gwn_cuda.hh) turns a non-zero status into std::runtime_error.
+ *
+ * Memory.  Every array argument may be host memory (pageable or pinned) or device memory; the library asks the
+ * CUDA runtime which one it is.  A call whose inputs and outputs are all device memory is asynchronous on the
+ * context's stream; a call that reads or writes any host array returns only after the host outputs are written.
+ * Device-side error flags (exhausted traversal stack, a bounded wait that ran out) are reported by the call
+ * that synchronises: the synchronous call itself, or agwn_context_synchronize().
+ *
+ * Layouts are the antipodal library's own value types, so spans of them can be passed straight through:
+ *   vec3<T>              3 x T                      (src/antipodal/math/common.hh:32-45)
+ *   weighted_segment3<T> pos0, pos1, weight = 7 x T (src/antipodal/math/common.hh:50-65)
+ *   triangle indices     3 x int32 per triangle     (NaiveIntersector::indices, intersector/intersector.hh:59)
+ * Paths cited in this header are relative to the antipodal project root.
+ *
+ * Threading: a context is used by one host thread at a time (the reference's PoolDispatcher likewise runs one
+ * job at a time, dispatcher/dispatcher_threadpool.hh:22-23).  Geometry handles (agwn_bvh, agwn_robust) are
+ * read-only after creation and may be shared by contexts on the same device.
+ */
+#ifndef ANTIPODAL_GB300_H
+#define ANTIPODAL_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define AGWN_ABI_VERSION 1
+
+/* ---- status ---------------------------------------------------------------------------------------------- */
+enum agwn_status
+{
+    AGWN_OK = 0,
+    AGWN_ERR_INVALID = 1,     /* bad argument: null pointer, negative size, unknown enum value            */
+    AGWN_ERR_CUDA = 2,        /* a CUDA runtime call failed                                               */
+    AGWN_ERR_NOMEM = 3,       /* a device allocation failed                                               */
+    AGWN_ERR_STACK = 4,       /* a BVH traversal stack was exhausted (degenerate hierarchy)               */
+    AGWN_ERR_TIMEOUT = 5,     /* a bounded device-side wait ran out; the result is not valid              */
+    AGWN_ERR_UNSUPPORTED = 6, /* combination not provided (e.g. the mixed fractional mode for float input) */
+    AGWN_ERR_NO_DEVICE = 7    /* no CUDA device, or the device ordinal does not exist                      */
+};
+
+const char* agwn_status_string(int status);
+/* Detail of the last failing call on this host thread ("" if none). */
+const char* agwn_last_error_message(void);
+int agwn_abi_version(void);
+
+/* ---- context: device, stream, scratch arena, options ----------------------------------------------------- */
+typedef struct agwn_context agwn_context;
+
+/* stream: a cudaStream_t to run on (cudaStreamLegacy, i.e. (void*)1, for the legacy default stream), or NULL to
+   let the context create its own non-blocking stream. */
+int agwn_context_create(int device, void* stream, agwn_context** out);
+int agwn_context_destroy(agwn_context* ctx);
+/* Waits for all work of the context and reports device-side error flags raised since the last check. */
+int agwn_context_synchronize(agwn_context* ctx);
+
+enum agwn_option
+{
+    /* Fractional-term precision for double inputs: AGWN_FRAC_EXACT (default) or AGWN_FRAC_MIXED. */
+    AGWN_OPT_FRAC_MODE = 0,
+    /* Mixed mode: a (query, segment) pair whose nearer endpoint is closer than tau * segment length is
+       evaluated in FP64 with the reference arithmetic.  Default 8. */
+    AGWN_OPT_MIXED_TAU = 1,
+    /* Queries owned by each thread in the fractional kernels (1, 2, 4 or 8).  Default 4. */
+    AGWN_OPT_QUERIES_PER_THREAD = 2,
+    /* Threads per block of the fractional kernels (64..256, a multiple of 32).  Default 256. */
+    AGWN_OPT_FRAC_BLOCK = 3,
+    /* Record CUDA events around the library's kernels and accumulate their device time (0/1).  Default 0. */
+    AGWN_OPT_TIMING = 4,
+    /* Segments per shared-memory tile of the fractional kernels (32..2048).  Default 512. */
+    AGWN_OPT_SEG_TILE = 5,
+    /* Mixed mode: a pair whose first-order FP32 error bound exceeds this many radians is evaluated in FP64.
+       Default 2e-8. */
+    AGWN_OPT_MIXED_TERM_ERR = 6
+};
+enum agwn_frac_mode
+{
+    AGWN_FRAC_EXACT = 0, /* the reference's arithmetic in the input precision, unfused (plain)             */
+    AGWN_FRAC_MIXED = 1  /* FP32 pairs with TwoSum accumulation; FP64 for near / branch-cut pairs          */
+};
+int agwn_context_set_option(agwn_context* ctx, int option, double value);
+int agwn_context_get_option(agwn_context* ctx, int option, double* value);
+
+enum agwn_kernel_class
+{
+    AGWN_K_FRACTIONAL = 0, /* fractional (boundary) kernels                        */
+    AGWN_K_INTEGER = 1,    /* integer-term traversal kernels                       */
+    AGWN_K_ROBUST = 2,     /* robust evaluator kernels                             */
+    AGWN_K_PARAMETRIC = 3, /* parametric GK15 kernels                              */
+    AGWN_K_OTHER = 4,      /* preparation, build and copy kernels                  */
+    AGWN_K_COUNT = 5
+};
+typedef struct agwn_stats
+{
+    double kernel_ms[AGWN_K_COUNT];   /* device time between the events around each launch (AGWN_OPT_TIMING) */
+    int64_t launches[AGWN_K_COUNT];   /* launches of the library's kernels, by class (always counted)        */
+    int64_t fp64_pairs;               /* mixed mode: (query, segment) pairs evaluated in FP64 (when timing)  */
+    int64_t pairs;                    /* mixed mode: all (query, segment) pairs evaluated (when timing)      */
+} agwn_stats;
+/* Reads (synchronising the stream first) and optionally resets the accumulated statistics. */
+int agwn_context_get_stats(agwn_context* ctx, agwn_stats* out, int reset);
+
+/* ---- mesh GWN: fractional term ----------------------------------------------------------------------------
+ * Replaces eval_gwnr_mesh_batch_fractional (src/antipodal/gwn_mesh.hh:67-83): for each query p,
+ * sum over boundary segments of weight * signed_spherical_tri_area_half_unorm(-x0, pos0 - p, pos1 - p),
+ * divided by 2 pi.  x0 is 3 values in host memory; it is not validated (the reference does not either). */
+int agwn_mesh_batch_fractional_f64(agwn_context* ctx, const double* positions, int64_t n, double* out,
+                                   const double* x0, const double* boundary, int64_t n_segments);
+int agwn_mesh_batch_fractional_f32(agwn_context* ctx, const float* positions, int64_t n, float* out,
+                                   const float* x0, const float* boundary, int64_t n_segments);
+
+/* ---- mesh GWN: integer term over a device LBVH -------------------------------------------------------------
+ * A CudaIntersector's device state: the triangles, copied, and a linear BVH built on the device (Morton codes,
+ * radix sort, Karras hierarchy, bottom-up boxes).  The counting rule is NaiveIntersector's Moller-Trumbore
+ * (src/antipodal/intersector/intersector.hh:61-100) in the input precision with unfused arithmetic, so counts
+ * match it bit for bit, including its double count of a ray through a shared edge. */
+typedef struct agwn_bvh agwn_bvh;
+int agwn_bvh_create_f64(agwn_context* ctx, const double* vertices, int64_t n_vertices, const int32_t* indices,
+                        int64_t n_indices, agwn_bvh** out);
+int agwn_bvh_create_f32(agwn_context* ctx, const float* vertices, int64_t n_vertices, const int32_t* indices,
+                        int64_t n_indices, agwn_bvh** out);
+int agwn_bvh_destroy(agwn_bvh* bvh);
+/* Hierarchy depth, nodes, triangles (for tests and roofline accounting). */
+int agwn_bvh_info(const agwn_bvh* bvh, int64_t* n_triangles, int32_t* depth);
+
+/* Replaces eval_gwnr_mesh_batch_integer (src/antipodal/gwn_mesh.hh:127-143) and
+ * NaiveIntersector::signed_intersection_count: out_counts[i] = signed crossings of the ray (p_i, dir). */
+int agwn_mesh_batch_integer_f64(agwn_context* ctx, const agwn_bvh* bvh, const double* positions, int64_t n,
+                                int32_t* out_counts, const double* dir);
+int agwn_mesh_batch_integer_f32(agwn_context* ctx, const agwn_bvh* bvh, const float* positions, int64_t n,
+                                int32_t* out_counts, const float* dir);
+
+/* Replaces eval_gwnr_mesh_batch (src/antipodal/gwn_mesh.hh:201-219): fractional + integer, fused per query.
+ * bvh may be NULL for a closed-free evaluation (integer term 0); boundary may be empty (n_segments 0). */
+int agwn_mesh_batch_f64(agwn_context* ctx, const agwn_bvh* bvh, const double* positions, int64_t n, double* out,
+                        const double* x0, const double* boundary, int64_t n_segments);
+int agwn_mesh_batch_f32(agwn_context* ctx, const agwn_bvh* bvh, const float* positions, int64_t n, float* out,
+                        const float* x0, const float* boundary, int64_t n_segments);
+
+/* Brute-force integer term (every query against every triangle; no hierarchy).  Same counting rule as above.
+ * For small meshes and as a cross-check of the traversal. */
+int agwn_mesh_batch_integer_bruteforce_f64(agwn_context* ctx, const double* vertices, int64_t n_vertices,
+                                           const int32_t* indices, int64_t n_indices, const double* positions,
+                                           int64_t n, int32_t* out_counts, const double* dir);
+
+/* ---- measurement ------------------------------------------------------------------------------------------
+ * FP32 fused-multiply-add throughput of the context's GPU at its current clocks, in TFLOP/s (best of three timed
+ * launches of independent FMA chains).  No reference counterpart: it is the denominator of the fractional
+ * kernel's compute roofline. */
+int agwn_probe_fp32_peak(agwn_context* ctx, double* tflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ANTIPODAL_GB300_H */

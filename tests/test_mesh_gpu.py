@@ -1,0 +1,179 @@
+"""Parity of the CUDA mesh path (fractional term, LBVH integer term, fused batch) with the CPU oracle.
+
+Mirrors the reference's tests (test/test_gwn_mesh.cc, test/test_intersector.cc, test/test_common.cc of the
+antipodal project) on the GPU, then extends them to the benchmark inputs and the edge cases of the kernels.
+Tolerances: exact form (double) 1e-12 absolute against the oracle -- the reference arithmetic up to atan2's last
+bit; float 2e-5; mixed form 1e-7 absolute (its accuracy target); integer counts bit-exact.
+"""
+
+import numpy as np
+import pytest
+
+from antipodal_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+TOL_EXACT64 = 1e-12
+TOL_EXACT32 = 2e-5
+TOL_MIXED = 1e-7
+
+
+def run_full(gwn, disp, verts, idx, q, x0, bnd, precision="exact"):
+    disp.set_precision(precision)
+    isect = gwn.CudaIntersector(disp, verts, idx)
+    out = np.empty(len(q), dtype=q.dtype)
+    gwn.eval_gwnr_mesh_batch(disp, isect, q, out, x0, bnd)
+    isect.close()
+    return out
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+@pytest.mark.parametrize("closed", [True, False])
+def test_cube_matches_baseline_and_oracle(gwn, disp, oracle, dtype, closed):
+    # test/test_gwn_mesh.cc:101-138: closed and +Y-open cube, eight probe points, x0 = normalize(.31,.57,.76)
+    verts = synth.CUBE_VERTS.astype(dtype)
+    idx = synth.CUBE_IDX_CLOSED if closed else synth.CUBE_IDX_OPEN_Y
+    bnd = np.zeros((0, 7), dtype) if closed else synth.cube_open_y_boundary(dtype)
+    x0 = synth.unit_x0(dtype)
+    q = synth.SAMPLE_POINTS.astype(dtype)
+    got = run_full(gwn, disp, verts, idx, q, x0, bnd)
+    base = oracle.gwn_baseline(q, verts, idx)
+    ref = oracle.full_naive(q, x0, verts, idx, bnd)
+    rel = 1e-4 if dtype == np.float32 else 1e-9
+    assert np.all(np.abs(got - base) <= rel * np.maximum(1.0, np.abs(base)))
+    tol = TOL_EXACT32 if dtype == np.float32 else TOL_EXACT64
+    np.testing.assert_allclose(got, ref, rtol=0, atol=tol)
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_intersector_cube_counts(gwn, disp, dtype):
+    # test/test_intersector.cc:78-106: inside 1, outside 0, three generic directions
+    verts = synth.CUBE_VERTS.astype(dtype)
+    isect = gwn.CudaIntersector(disp, verts, synth.CUBE_IDX_CLOSED)
+    q = np.array([[0, 0, 0], [0.1, -0.2, 0.3], [2, 0, 0], [-2, -2, -2]], dtype)
+    for d in ([0.31, 0.57, 0.76], [-0.6, 0.4, -0.69], [0.83, -0.21, 0.51]):
+        c = np.empty(4, np.int32)
+        gwn.eval_gwnr_mesh_batch_integer(disp, isect, q, c, np.array(d, dtype))
+        assert c.tolist() == [1, 1, 0, 0]
+
+
+def test_rotated_open_cube_full_size(gwn, disp, oracle):
+    verts, idx, bnd, q, x0 = synth.rotated_open_cube(seed=0, n_queries=100_000)
+    ref = oracle.full_naive(q, x0, verts, idx, bnd)
+    got = run_full(gwn, disp, verts, idx, q, x0, bnd, "exact")
+    assert np.max(np.abs(got - ref)) <= TOL_EXACT64
+    got = run_full(gwn, disp, verts, idx, q, x0, bnd, "mixed")
+    assert np.max(np.abs(got - ref)) <= TOL_MIXED
+    # integer term alone, bit exact
+    isect = gwn.CudaIntersector(disp, verts, idx)
+    c = np.empty(len(q), np.int32)
+    gwn.eval_gwnr_mesh_batch_integer(disp, isect, q, c, x0)
+    assert np.array_equal(c, oracle.int_naive(q, x0, verts, idx))
+
+
+def test_rotated_open_cube_float(gwn, disp, oracle):
+    verts, idx, bnd, q, x0 = synth.rotated_open_cube(seed=1, n_queries=20_000, dtype=np.float32)
+    isect = gwn.CudaIntersector(disp, verts, idx)
+    c = np.empty(len(q), np.int32)
+    gwn.eval_gwnr_mesh_batch_integer(disp, isect, q, c, x0)
+    assert np.array_equal(c, oracle.int_naive(q, x0, verts, idx))
+    out = np.empty(len(q), np.float32)
+    gwn.eval_gwnr_mesh_batch_fractional(disp, q, out, x0, bnd)
+    np.testing.assert_allclose(out, oracle.frac_batch(q, x0, bnd), rtol=0, atol=TOL_EXACT32)
+
+
+@pytest.mark.parametrize("n", [0, 1, 31, 33, 1000, 4097])
+@pytest.mark.parametrize("n_seg", [0, 1, 3])
+def test_ragged_sizes(gwn, disp, oracle, n, n_seg):
+    rng = np.random.default_rng(n * 7 + n_seg)
+    q = rng.uniform(-1.5, 1.5, size=(n, 3))
+    segs = np.concatenate([rng.uniform(-1, 1, size=(n_seg, 6)), rng.integers(1, 3, size=(n_seg, 1))], axis=1)
+    x0 = synth.unit_x0()
+    out = np.empty(n)
+    gwn.eval_gwnr_mesh_batch_fractional(disp, q, out, x0, segs)
+    np.testing.assert_allclose(out, oracle.frac_batch(q, x0, segs), rtol=0, atol=TOL_EXACT64)
+    disp.set_precision("mixed")
+    gwn.eval_gwnr_mesh_batch_fractional(disp, q, out, x0, segs)
+    np.testing.assert_allclose(out, oracle.frac_batch(q, x0, segs), rtol=0, atol=TOL_MIXED)
+
+
+@pytest.mark.parametrize("n_seg", [511, 512, 513, 1100])
+@pytest.mark.parametrize("qpt", [1, 2, 4, 8])
+def test_segment_tiles_and_queries_per_thread(gwn, oracle, n_seg, qpt):
+    # tile edges of the double-buffered shared-memory pipeline (tile 512) and every queries-per-thread variant
+    rng = np.random.default_rng(n_seg + qpt)
+    q = rng.uniform(-2, 2, size=(3001, 3))
+    a = rng.uniform(-1, 1, size=(n_seg, 3))
+    segs = np.concatenate([a, a + rng.normal(0, 0.05, size=(n_seg, 3)), np.ones((n_seg, 1))], axis=1)
+    x0 = synth.unit_x0()
+    ref = oracle.frac_batch(q, x0, segs)
+    with gwn.CudaDispatcher(queries_per_thread=qpt, seg_tile=512) as d:
+        out = np.empty(len(q))
+        gwn.eval_gwnr_mesh_batch_fractional(d, q, out, x0, segs)
+        np.testing.assert_allclose(out, ref, rtol=0, atol=TOL_EXACT64)
+        d.set_precision("mixed")
+        gwn.eval_gwnr_mesh_batch_fractional(d, q, out, x0, segs)
+        np.testing.assert_allclose(out, ref, rtol=0, atol=TOL_MIXED)
+
+
+def test_icosphere_subset_against_oracle(gwn, disp, oracle):
+    verts, idx, bnd, _, x0 = synth.open_icosphere(seed=0, grid=0)
+    q = synth.grid_queries(verts.min(0), verts.max(0), 14, 1.2)  # 2744 queries
+    ref_int = oracle.int_naive(q, x0, verts, idx)
+    isect = gwn.CudaIntersector(disp, verts, idx)
+    assert isect.info()["depth"] < 64
+    c = np.empty(len(q), np.int32)
+    gwn.eval_gwnr_mesh_batch_integer(disp, isect, q, c, x0)
+    assert np.array_equal(c, ref_int)
+    out = np.empty(len(q))
+    gwn.eval_gwnr_mesh_batch(disp, isect, q, out, x0, bnd)
+    ref = oracle.full_naive(q, x0, verts, idx, bnd)
+    assert np.max(np.abs(out - ref)) <= TOL_EXACT64
+    disp.set_precision("mixed")
+    gwn.eval_gwnr_mesh_batch(disp, isect, q, out, x0, bnd)
+    assert np.max(np.abs(out - ref)) <= TOL_MIXED
+
+
+def test_lbvh_counts_equal_bruteforce_on_grid(gwn, disp):
+    # the hierarchy only culls: on a 48^3 grid its counts equal the every-triangle scan's
+    verts, idx, bnd, _, x0 = synth.open_icosphere(seed=3, level=4, grid=0)
+    q = synth.grid_queries(verts.min(0), verts.max(0), 48, 1.3)
+    isect = gwn.CudaIntersector(disp, verts, idx)
+    a = np.empty(len(q), np.int32)
+    b = np.empty(len(q), np.int32)
+    gwn.eval_gwnr_mesh_batch_integer(disp, isect, q, a, x0)
+    gwn.eval_gwnr_mesh_batch_integer_bruteforce(disp, verts, idx, q, b, x0)
+    assert np.array_equal(a, b)
+
+
+def test_device_resident_tensors(gwn, oracle):
+    torch = pytest.importorskip("torch")
+    verts, idx, bnd, q, x0 = synth.rotated_open_cube(seed=2, n_queries=50_000)
+    ref = oracle.full_naive(q, x0, verts, idx, bnd)
+    dev = torch.device("cuda:0")
+    with gwn.CudaDispatcher(stream=torch.cuda.current_stream()) as d:
+        tq = torch.from_numpy(q).to(dev)
+        tb = torch.from_numpy(bnd).to(dev)
+        tv = torch.from_numpy(verts).to(dev)
+        ti = torch.from_numpy(idx).to(dev)
+        out = torch.empty(len(q), dtype=torch.float64, device=dev)
+        isect = gwn.CudaIntersector(d, tv, ti)
+        gwn.eval_gwnr_mesh_batch(d, isect, tq, out, x0, tb)
+        d.synchronize()
+        assert np.max(np.abs(out.cpu().numpy() - ref)) <= TOL_EXACT64
+
+
+def test_errors_are_reported(gwn, disp):
+    verts = synth.CUBE_VERTS
+    with pytest.raises(gwn.GwnError) as e:
+        gwn.CudaIntersector(disp, verts, np.array([0, 1, 99], np.int32))
+    assert e.value.status == 1
+    with pytest.raises(ValueError):
+        gwn.eval_gwnr_mesh_batch_fractional(disp, np.zeros((4, 3)), np.zeros(3), synth.unit_x0(), np.zeros((1, 7)))
+    with pytest.raises(gwn.GwnError):
+        disp.set_option(2, 3)  # queries per thread must be 1, 2, 4 or 8
+    isect32 = gwn.CudaIntersector(disp, verts.astype(np.float32), synth.CUBE_IDX_CLOSED)
+    with pytest.raises(gwn.GwnError):
+        gwn.eval_gwnr_mesh_batch_integer(disp, isect32, np.zeros((2, 3)), np.zeros(2, np.int32), synth.unit_x0())
+    with pytest.raises(TypeError):
+        disp.parallel_for(0, 4, lambda i: None)
