@@ -30,6 +30,7 @@
 //              The FP64 terms and the compensated FP32 sum are combined in FP64.
 
 #include "agwn_internal.cuh"
+#include "frac_kernels.cuh"
 #include "gwn_kernels.cuh"
 #include "tma.cuh"
 
@@ -39,512 +40,6 @@ namespace agwn
 {
 namespace
 {
-template <class T>
-struct alignas(16) SegX
-{
-    T p0x, p0y, p0z, p1x, p1y, p1z, w, pad;
-};
-// Mixed-mode segment: a = (P0_hi, w), b = (P1 - P0, |p1 - p0|), c = (P0_lo, index as bits).
-struct alignas(16) SegM
-{
-    float4 a, b, c;
-};
-struct Rot
-{
-    double m[9];
-};
-struct Frame
-{
-    double c[3];
-};
-
-template <class T>
-constexpr T kPi = T(3.141592653589793238462643383279502884L);
-
-// --------------------------------------------------------------------------------------------------------------
-// exact form (reference arithmetic)
-// --------------------------------------------------------------------------------------------------------------
-template <class S>
-__device__ __forceinline__ auto vos_exact(ev3<S> x1, ev3<S> v0, ev3<S> v1)
-{
-    S const l0 = ex_sqrt(edot(v0, v0));
-    S const l1 = ex_sqrt(edot(v1, v1));
-    S const num = edot(x1, ecross(v0, v1));
-    S const den = l0 * l1 + l1 * edot(x1, v0) + l0 * edot(x1, v1) + edot(v0, v1);
-    return ex_atan2(num, den);
-}
-
-template <class T>
-__global__ void k_prep_exact(const T* __restrict__ raw, int64_t n_seg, SegX<T>* __restrict__ out)
-{
-    for (int64_t s = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; s < n_seg; s += int64_t(gridDim.x) * blockDim.x)
-    {
-        const T* w = raw + 7 * s;
-        out[s] = SegX<T>{w[0], w[1], w[2], w[3], w[4], w[5], w[6], T(0)};
-    }
-}
-
-// Shared skeleton of both fractional kernels: persistent CTAs over query tiles, segment tiles in shared memory.
-// Policy provides: Seg type, per-thread state init (load), per-segment accumulate, and finish (store).
-template <class Seg>
-struct TilePipe
-{
-    Seg* buf[2];
-    uint64_t* bar;
-    const Seg* gseg;
-    int64_t n_seg;
-    int tile;
-    int n_tiles;
-    bool single;
-
-    __device__ __forceinline__ int tile_count(int st) const
-    {
-        int64_t const rem = n_seg - int64_t(st) * tile;
-        return int(rem < tile ? rem : tile);
-    }
-    // Issued by one thread: item `it` of the flattened (query tile, segment tile) sequence into buffer it & 1.
-    __device__ __forceinline__ void issue(int it) const
-    {
-        int const b = it & 1;
-        int const st = it % n_tiles;
-        unsigned const bytes = unsigned(tile_count(st)) * unsigned(sizeof(Seg));
-        mbar_arrive_expect_tx(&bar[b], bytes);
-        bulk_copy_g2s(buf[b], gseg + int64_t(st) * tile, bytes, &bar[b]);
-    }
-};
-
-template <class T, int K>
-__global__ void __launch_bounds__(256) k_frac_exact(const T* __restrict__ pos, int64_t n, T* __restrict__ out,
-                                                    const int32_t* __restrict__ counts, T x0x, T x0y, T x0z,
-                                                    const SegX<T>* __restrict__ seg, int64_t n_seg, int tile,
-                                                    int* flags)
-{
-    using S = typename exact_of<T>::type;
-    extern __shared__ __align__(128) unsigned char smem[];
-    __shared__ __align__(8) uint64_t bars[2];
-    __shared__ int abort_cta;
-
-    TilePipe<SegX<T>> pipe;
-    pipe.n_tiles = int((n_seg + tile - 1) / tile);
-    pipe.single = pipe.n_tiles == 1;
-    pipe.buf[0] = reinterpret_cast<SegX<T>*>(smem);
-    pipe.buf[1] = pipe.buf[0] + (pipe.single ? 0 : tile);
-    pipe.bar = bars;
-    pipe.gseg = seg;
-    pipe.n_seg = n_seg;
-    pipe.tile = tile;
-
-    int64_t const per_tile = int64_t(blockDim.x) * K;
-    int64_t const n_qtiles = (n + per_tile - 1) / per_tile;
-    int const my_qtiles = blockIdx.x < n_qtiles ? int((n_qtiles - 1 - blockIdx.x) / gridDim.x + 1) : 0;
-    int const n_items = pipe.single ? (my_qtiles > 0 ? 1 : 0) : my_qtiles * pipe.n_tiles;
-
-    if (threadIdx.x == 0)
-    {
-        mbar_init(&bars[0], 1);
-        mbar_init(&bars[1], 1);
-        fence_barrier_init();
-        abort_cta = 0;
-        if (n_items > 0)
-            pipe.issue(0);
-        if (n_items > 1)
-            pipe.issue(1);
-    }
-    __syncthreads();
-
-    S const x1x = S(-x0x), x1y = S(-x0y), x1z = S(-x0z);
-    ev3<S> const x1{x1x, x1y, x1z};
-    T const two_pi = T(2) * kPi<T>;
-
-    int it = 0;
-    for (int j = 0; j < my_qtiles; ++j)
-    {
-        int64_t const base = (blockIdx.x + int64_t(j) * gridDim.x) * per_tile + threadIdx.x;
-        ev3<S> p[K];
-        S area[K];
-#pragma unroll
-        for (int k = 0; k < K; ++k)
-        {
-            int64_t const i = base + int64_t(k) * blockDim.x;
-            int64_t const ii = i < n ? i : n - 1;
-            p[k] = {S(pos[3 * ii]), S(pos[3 * ii + 1]), S(pos[3 * ii + 2])};
-            area[k] = S(T(0));
-        }
-        for (int st = 0; st < pipe.n_tiles; ++st)
-        {
-            int const b = it & 1;
-            if (!pipe.single || j == 0)
-            {
-                bool ok = mbar_wait_bounded(&bars[b], unsigned((it >> 1) & 1), flags, 1);
-                if (!ok)
-                    abort_cta = 1;
-            }
-            __syncthreads();
-            if (abort_cta)
-                return;
-            SegX<T> const* sb = pipe.buf[b];
-            int const cnt = pipe.tile_count(st);
-            for (int s = 0; s < cnt; ++s)
-            {
-                SegX<T> const g = sb[s];
-                ev3<S> const a{S(g.p0x), S(g.p0y), S(g.p0z)};
-                ev3<S> const c{S(g.p1x), S(g.p1y), S(g.p1z)};
-                S const w = S(g.w);
-#pragma unroll
-                for (int k = 0; k < K; ++k)
-                {
-                    ev3<S> const v0 = a - p[k];
-                    ev3<S> const v1 = c - p[k];
-                    area[k] = area[k] + w * S(vos_exact(x1, v0, v1));
-                }
-            }
-            if (!pipe.single)
-            {
-                __syncthreads();
-                if (threadIdx.x == 0 && it + 2 < n_items)
-                    pipe.issue(it + 2);
-                ++it;
-            }
-        }
-#pragma unroll
-        for (int k = 0; k < K; ++k)
-        {
-            int64_t const i = base + int64_t(k) * blockDim.x;
-            if (i < n)
-            {
-                S v = area[k] / S(two_pi);
-                if (counts)
-                    v = v + S(T(counts[i]));
-                out[i] = v.v;
-            }
-        }
-    }
-}
-
-// --------------------------------------------------------------------------------------------------------------
-// mixed form
-// --------------------------------------------------------------------------------------------------------------
-
-// One block: bounding-box centre of all endpoints, then each segment moved into the x1 = +z frame around it.
-__global__ void __launch_bounds__(1024) k_prep_mixed(const double* __restrict__ raw, int64_t n_seg, Rot rot,
-                                                     Frame* __restrict__ frame, SegM* __restrict__ out,
-                                                     SegX<double>* __restrict__ out64)
-{
-    __shared__ double red[2][3][32];
-    double mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
-    for (int64_t s = threadIdx.x; s < n_seg; s += blockDim.x)
-    {
-        const double* w = raw + 7 * s;
-        for (int k = 0; k < 3; ++k)
-        {
-            mn[k] = fmin(mn[k], fmin(w[k], w[3 + k]));
-            mx[k] = fmax(mx[k], fmax(w[k], w[3 + k]));
-        }
-    }
-    int const lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int k = 0; k < 3; ++k)
-    {
-        for (int o = 16; o > 0; o >>= 1)
-        {
-            mn[k] = fmin(mn[k], __shfl_xor_sync(0xffffffffu, mn[k], o));
-            mx[k] = fmax(mx[k], __shfl_xor_sync(0xffffffffu, mx[k], o));
-        }
-        if (lane == 0)
-        {
-            red[0][k][warp] = mn[k];
-            red[1][k][warp] = mx[k];
-        }
-    }
-    __syncthreads();
-    __shared__ double centre[3];
-    if (threadIdx.x < 3)
-    {
-        int const k = threadIdx.x;
-        double a = INFINITY, b = -INFINITY;
-        for (int w = 0; w < int(blockDim.x + 31) / 32; ++w)
-        {
-            a = fmin(a, red[0][k][w]);
-            b = fmax(b, red[1][k][w]);
-        }
-        centre[k] = (n_seg > 0) ? 0.5 * (a + b) : 0.0;
-        frame->c[k] = centre[k];
-    }
-    __syncthreads();
-    double const cx = centre[0], cy = centre[1], cz = centre[2];
-    for (int64_t s = threadIdx.x; s < n_seg; s += blockDim.x)
-    {
-        const double* w = raw + 7 * s;
-        double P[2][3];
-        for (int e = 0; e < 2; ++e)
-        {
-            double const dx = w[3 * e] - cx, dy = w[3 * e + 1] - cy, dz = w[3 * e + 2] - cz;
-            for (int r = 0; r < 3; ++r)
-                P[e][r] = rot.m[3 * r] * dx + rot.m[3 * r + 1] * dy + rot.m[3 * r + 2] * dz;
-        }
-        float hi[3], lo[3], dv[3];
-        for (int r = 0; r < 3; ++r)
-        {
-            hi[r] = __double2float_rn(P[0][r]);
-            lo[r] = __double2float_rn(P[0][r] - double(hi[r]));
-            dv[r] = __double2float_rn(P[1][r] - P[0][r]);
-        }
-        double const ex = w[3] - w[0], ey = w[4] - w[1], ez = w[5] - w[2];
-        float const len = float(sqrt(ex * ex + ey * ey + ez * ez));
-        SegM m;
-        m.a = make_float4(hi[0], hi[1], hi[2], float(w[6]));
-        m.b = make_float4(dv[0], dv[1], dv[2], len);
-        m.c = make_float4(lo[0], lo[1], lo[2], __int_as_float(int(s)));
-        out[s] = m;
-        out64[s] = SegX<double>{w[0], w[1], w[2], w[3], w[4], w[5], w[6], 0.0};
-    }
-}
-
-__device__ __forceinline__ void two_sum_acc(float& acc, float& comp, float x)
-{
-    float const s = __fadd_rn(acc, x);
-    float const bp = __fsub_rn(s, acc);
-    float const ap = __fsub_rn(s, bp);
-    float const e = __fadd_rn(__fsub_rn(acc, ap), __fsub_rn(x, bp));
-    acc = s;
-    comp = __fadd_rn(comp, e);
-}
-
-template <int K>
-__global__ void __launch_bounds__(256) k_frac_mixed(const double* __restrict__ pos, int64_t n, double* __restrict__ out,
-                                                    const int32_t* __restrict__ counts, double x0x, double x0y,
-                                                    double x0z, Rot rot, const Frame* __restrict__ frame, float tau,
-                                                    float term_err,
-                                                    const SegM* __restrict__ seg,
-                                                    const SegX<double>* __restrict__ seg64, int64_t n_seg, int tile,
-                                                    int* flags, long long* counters, int count_pairs)
-{
-    extern __shared__ __align__(128) unsigned char smem[];
-    __shared__ __align__(8) uint64_t bars[2];
-    __shared__ int abort_cta;
-    __shared__ double centre[3];
-
-    TilePipe<SegM> pipe;
-    pipe.n_tiles = int((n_seg + tile - 1) / tile);
-    pipe.single = pipe.n_tiles == 1;
-    pipe.buf[0] = reinterpret_cast<SegM*>(smem);
-    pipe.buf[1] = pipe.buf[0] + (pipe.single ? 0 : tile);
-    pipe.bar = bars;
-    pipe.gseg = seg;
-    pipe.n_seg = n_seg;
-    pipe.tile = tile;
-
-    int64_t const per_tile = int64_t(blockDim.x) * K;
-    int64_t const n_qtiles = (n + per_tile - 1) / per_tile;
-    int const my_qtiles = blockIdx.x < n_qtiles ? int((n_qtiles - 1 - blockIdx.x) / gridDim.x + 1) : 0;
-    int const n_items = pipe.single ? (my_qtiles > 0 ? 1 : 0) : my_qtiles * pipe.n_tiles;
-
-    if (threadIdx.x == 0)
-    {
-        mbar_init(&bars[0], 1);
-        mbar_init(&bars[1], 1);
-        fence_barrier_init();
-        abort_cta = 0;
-        if (n_items > 0)
-            pipe.issue(0);
-        if (n_items > 1)
-            pipe.issue(1);
-    }
-    if (threadIdx.x < 3)
-        centre[threadIdx.x] = frame->c[threadIdx.x];
-    __syncthreads();
-
-    // Rounding bound per FP32 operation chain (4 eps32) and the largest accepted first-order error of one FP32 term.
-    constexpr float kEpsBound = 4.0f * 5.9604645e-8f;
-    double const two_pi = 2.0 * kPi<double>;
-    long long n64 = 0;
-
-    int it = 0;
-    for (int j = 0; j < my_qtiles; ++j)
-    {
-        int64_t const base = (blockIdx.x + int64_t(j) * gridDim.x) * per_tile + threadIdx.x;
-        float qhx[K], qhy[K], qhz[K], qlx[K], qly[K], qlz[K];
-        float acc[K], comp[K];
-        double acc64[K];
-        int64_t qi[K];
-#pragma unroll
-        for (int k = 0; k < K; ++k)
-        {
-            int64_t const i = base + int64_t(k) * blockDim.x;
-            int64_t const ii = i < n ? i : n - 1;
-            qi[k] = ii;
-            double const dx = pos[3 * ii] - centre[0], dy = pos[3 * ii + 1] - centre[1],
-                         dz = pos[3 * ii + 2] - centre[2];
-            double const Qx = rot.m[0] * dx + rot.m[1] * dy + rot.m[2] * dz;
-            double const Qy = rot.m[3] * dx + rot.m[4] * dy + rot.m[5] * dz;
-            double const Qz = rot.m[6] * dx + rot.m[7] * dy + rot.m[8] * dz;
-            qhx[k] = __double2float_rn(Qx);
-            qhy[k] = __double2float_rn(Qy);
-            qhz[k] = __double2float_rn(Qz);
-            qlx[k] = __double2float_rn(Qx - double(qhx[k]));
-            qly[k] = __double2float_rn(Qy - double(qhy[k]));
-            qlz[k] = __double2float_rn(Qz - double(qhz[k]));
-            acc[k] = 0.f;
-            comp[k] = 0.f;
-            acc64[k] = 0.0;
-        }
-        for (int st = 0; st < pipe.n_tiles; ++st)
-        {
-            int const b = it & 1;
-            if (!pipe.single || j == 0)
-            {
-                bool ok = mbar_wait_bounded(&bars[b], unsigned((it >> 1) & 1), flags, 2);
-                if (!ok)
-                    abort_cta = 1;
-            }
-            __syncthreads();
-            if (abort_cta)
-                return;
-            SegM const* sb = pipe.buf[b];
-            int const cnt = pipe.tile_count(st);
-            for (int s = 0; s < cnt; ++s)
-            {
-                float4 const A = sb[s].a, B = sb[s].b, C = sb[s].c;
-#pragma unroll
-                for (int k = 0; k < K; ++k)
-                {
-                    float const v0x = (A.x - qhx[k]) + (C.x - qlx[k]);
-                    float const v0y = (A.y - qhy[k]) + (C.y - qly[k]);
-                    float const v0z = (A.z - qhz[k]) + (C.z - qlz[k]);
-                    float const v1x = v0x + B.x, v1y = v0y + B.y, v1z = v0z + B.z;
-                    float const ta = v0x * B.y, tb = v0y * B.x;
-                    float const num = ta - tb;
-                    float const r0 = v0x * v0x + v0y * v0y;
-                    float const r1 = v1x * v1x + v1y * v1y;
-                    float const q0 = r0 + v0z * v0z;
-                    float const q1 = r1 + v1z * v1z;
-                    float const l0 = q0 * rsqrtf(q0);
-                    float const l1 = q1 * rsqrtf(q1);
-                    float const s0 = v0z >= 0.f ? l0 + v0z : __fdividef(r0, l0 - v0z);
-                    float const s1 = v1z >= 0.f ? l1 + v1z : __fdividef(r1, l1 - v1z);
-                    float const pxy = v0x * v1x, pyy = v0y * v1y;
-                    float const ss = s0 * s1;
-                    float const den = ss + (pxy + pyy);
-                    // first-order rounding bounds of num and den (a few eps of the magnitudes summed)
-                    float const dn = kEpsBound * (fabsf(ta) + fabsf(tb));
-                    float const dd = kEpsBound * (ss + fabsf(pxy) + fabsf(pyy));
-                    bool const ill = dn * fabsf(den) + dd * fabsf(num) > term_err * (num * num + den * den);
-                    bool const near = fminf(l0, l1) < tau * B.w || !(q0 > 0.f && q1 > 0.f) || ill;
-                    bool const branch = den < 0.f && fabsf(num) <= dn;
-                    if (near)
-                    {
-                        // exact form on the original doubles
-                        SegX<double> const g = seg64[__float_as_int(C.w)];
-                        int64_t const i = qi[k];
-                        ev3<rd> const p{rd(pos[3 * i]), rd(pos[3 * i + 1]), rd(pos[3 * i + 2])};
-                        ev3<rd> const x1{rd(-x0x), rd(-x0y), rd(-x0z)};
-                        ev3<rd> const v0 = ev3<rd>{rd(g.p0x), rd(g.p0y), rd(g.p0z)} - p;
-                        ev3<rd> const v1 = ev3<rd>{rd(g.p1x), rd(g.p1y), rd(g.p1z)} - p;
-                        acc64[k] = (rd(acc64[k]) + rd(g.w) * rd(vos_exact(x1, v0, v1))).v;
-                        n64 += 1;
-                    }
-                    else
-                    {
-                        float t = atan2f(num, den);
-                        if (branch)
-                        {
-                            // the reference's FP64 numerator decides the side of the branch cut
-                            SegX<double> const g = seg64[__float_as_int(C.w)];
-                            int64_t const i = qi[k];
-                            ev3<rd> const p{rd(pos[3 * i]), rd(pos[3 * i + 1]), rd(pos[3 * i + 2])};
-                            ev3<rd> const x1{rd(-x0x), rd(-x0y), rd(-x0z)};
-                            ev3<rd> const v0 = ev3<rd>{rd(g.p0x), rd(g.p0y), rd(g.p0z)} - p;
-                            ev3<rd> const v1 = ev3<rd>{rd(g.p1x), rd(g.p1y), rd(g.p1z)} - p;
-                            rd const num64 = edot(x1, ecross(v0, v1));
-                            // Keep the FP32 smooth part (it telescopes with the neighbouring segments) and move the
-                            // term to the reference's side of the cut: atan2 jumps by 2 pi there.
-                            bool const ref_pos = !signbit(num64.v);
-                            bool const f32_pos = !signbit(t);
-                            if (ref_pos != f32_pos)
-                                t += ref_pos ? 2.0f * kPi<float> : -2.0f * kPi<float>;
-                            n64 += 1;
-                        }
-                        two_sum_acc(acc[k], comp[k], A.w * t);
-                    }
-                }
-            }
-            if (!pipe.single)
-            {
-                __syncthreads();
-                if (threadIdx.x == 0 && it + 2 < n_items)
-                    pipe.issue(it + 2);
-                ++it;
-            }
-        }
-#pragma unroll
-        for (int k = 0; k < K; ++k)
-        {
-            int64_t const i = base + int64_t(k) * blockDim.x;
-            if (i < n)
-            {
-                double v = ((double(acc[k]) + double(comp[k])) + acc64[k]) / two_pi;
-                if (counts)
-                    v += double(counts[i]);
-                out[i] = v;
-            }
-        }
-    }
-    if (count_pairs)
-    {
-        // warp-aggregated statistics: pairs taken to FP64 and all pairs of valid queries
-        long long tot = 0;
-        for (int j = 0; j < my_qtiles; ++j)
-        {
-            int64_t const base = (blockIdx.x + int64_t(j) * gridDim.x) * per_tile + threadIdx.x;
-            for (int k = 0; k < K; ++k)
-                tot += (base + int64_t(k) * blockDim.x < n) ? n_seg : 0;
-        }
-        for (int o = 16; o > 0; o >>= 1)
-        {
-            n64 += __shfl_xor_sync(0xffffffffu, n64, o);
-            tot += __shfl_xor_sync(0xffffffffu, tot, o);
-        }
-        if ((threadIdx.x & 31) == 0)
-        {
-            atomicAdd(reinterpret_cast<unsigned long long*>(counters), static_cast<unsigned long long>(n64));
-            atomicAdd(reinterpret_cast<unsigned long long*>(counters + 1), static_cast<unsigned long long>(tot));
-        }
-    }
-}
-
-template <class T>
-__global__ void k_fill_counts(T* out, const int32_t* counts, int64_t n)
-{
-    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
-        out[i] = counts ? T(counts[i]) : T(0);
-}
-
-// Rotation whose third row is x1 = -x0 / |x0|: rows (e1, e2, x1_hat), right-handed.
-Rot make_rotation(const double* x0)
-{
-    double const n = std::sqrt(x0[0] * x0[0] + x0[1] * x0[1] + x0[2] * x0[2]);
-    double z[3] = {-x0[0] / n, -x0[1] / n, -x0[2] / n};
-    // helper axis least aligned with z
-    double a[3] = {0, 0, 0};
-    int m = 0;
-    for (int k = 1; k < 3; ++k)
-        if (std::fabs(z[k]) < std::fabs(z[m]))
-            m = k;
-    a[m] = 1.0;
-    double x[3] = {a[1] * z[2] - a[2] * z[1], a[2] * z[0] - a[0] * z[2], a[0] * z[1] - a[1] * z[0]};
-    double const xn = std::sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]);
-    for (double& v : x)
-        v /= xn;
-    double y[3] = {z[1] * x[2] - z[2] * x[1], z[2] * x[0] - z[0] * x[2], z[0] * x[1] - z[1] * x[0]};
-    Rot r;
-    for (int k = 0; k < 3; ++k)
-    {
-        r.m[k] = x[k];
-        r.m[3 + k] = y[k];
-        r.m[6 + k] = z[k];
-    }
-    return r;
-}
-
 template <class Kern>
 int launch_persistent(Context& ctx, Kern kernel, int block, size_t smem, int64_t n_qtiles, int* grid)
 {
