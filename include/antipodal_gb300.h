@@ -150,6 +150,20 @@ int agwn_mesh_batch_integer_bruteforce_f64(agwn_context* ctx, const double* vert
                                            const int32_t* indices, int64_t n_indices, const double* positions,
                                            int64_t n, int32_t* out_counts, const double* dir);
 
+/* ---- mixed-precision fractional term without allocation --------------------------------------------------
+ * No counterpart in the reference.  For callers that cannot allocate device memory -- a program whose own pool
+ * allocator owns the GPU's memory budget, or a plugin inside a framework whose allocator must not be bypassed --
+ * this runs the mixed form of agwn_mesh_batch_fractional_f64 (default tau and term-error bound, no integer term)
+ * with no context and no allocation.  Its scratch is one static device array sized for at most 8192 boundary
+ * segments (about 0.9 MB, held on every GPU that loads the library until the process exits); more segments are
+ * rejected with AGWN_ERR_INVALID.  positions, out and boundary must be device memory of the current device;
+ * x0 is 3 host doubles.  stream may be NULL (the default stream).  The first call on a device looks up the
+ * scratch array's device address, so make that call before any stream capture.  The call returns when the
+ * kernels have finished.  All calls share the one scratch array: calls that overlap on the GPU (from several
+ * host threads or streams) race and must be serialised by the caller. */
+int agwn_mesh_batch_fractional_mixed_noalloc_f64(void* stream, const double* positions, int64_t n, double* out,
+                                                 const double* x0, const double* boundary, int64_t n_segments);
+
 /* ---- measurement ------------------------------------------------------------------------------------------
  * FP32 fused-multiply-add throughput of the context's GPU at its current clocks, in TFLOP/s (best of three timed
  * launches of independent FMA chains).  No reference counterpart: it is the denominator of the fractional
