@@ -60,6 +60,17 @@ def dist_env():
     return ws, rank, local
 
 
+def reduce_max(x: float, device) -> float:
+    """The maximum of ``x`` over all ranks (the identity without a process group)."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(x)
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def workload(grid):
     from antipodal_gb300 import synth
     return synth.open_icosphere(seed=0, level=6, cap_deg=30.0, sigma=1e-3, grid=grid)
@@ -215,12 +226,7 @@ def run_ours(args):
             fn()
         e1.record(stream)
         barrier()
-        ms = e0.elapsed_time(e1)
-        if ws > 1:
-            t = torch.tensor([ms], device=dev)
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            ms = float(t.item())
-        return ms
+        return reduce_max(e0.elapsed_time(e1), dev)
 
     # plain FP64 form (reference arithmetic)
     disp.set_precision("exact")
@@ -265,11 +271,7 @@ def run_ours(args):
     for _ in range(args.steps):
         ag.eval_gwnr_mesh_batch(disp, isect, qn, on, x0, bnd)
     barrier()
-    e2e_s = time.perf_counter() - t0
-    if ws > 1:
-        t = torch.tensor([e2e_s], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = reduce_max(time.perf_counter() - t0, dev)
     e2e_value = ws * Q * args.steps / e2e_s
     e2e_match = bool(np.array_equal(on, out.cpu().numpy()))
 

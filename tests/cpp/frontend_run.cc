@@ -1,0 +1,50 @@
+// Runs the C++ front end (include/antipodal/cuda/gwn_cuda.hh) the way a reference user would: the +Y-open unit
+// cube of the reference tests, a 12^3 grid of queries, eval_gwnr_mesh_batch{,_fractional,_integer} through
+// CudaDispatcher / CudaIntersector in both precisions.  Prints one line per query:
+//   x y z full_exact full_mixed frac_exact count
+// or "error <status> <message>" when the library throws (e.g. no GPU).
+#include <antipodal/math/common.hh>
+#include <antipodal/cuda/gwn_cuda.hh>
+
+#include <cstdio>
+#include <vector>
+
+int main()
+{
+    using namespace antipodal;
+    std::vector<dvec3> const verts = {{-0.5, -0.5, -0.5}, {0.5, -0.5, -0.5}, {-0.5, 0.5, -0.5}, {0.5, 0.5, -0.5},
+                                      {-0.5, -0.5, 0.5},  {0.5, -0.5, 0.5},  {-0.5, 0.5, 0.5},  {0.5, 0.5, 0.5}};
+    std::vector<int> const idx = {0, 2, 1, 1, 2, 3, 4, 5, 6, 6, 5, 7, 0, 4, 2, 2, 4, 6, 1, 3, 5, 5, 3, 7, 0, 1, 4, 4, 1, 5};
+    std::vector<weighted_dsegment3> const bnd = {
+        {{verts[6], verts[2]}, 1.0}, {{verts[7], verts[6]}, 1.0}, {{verts[3], verts[7]}, 1.0}, {{verts[2], verts[3]}, 1.0}};
+    dvec3 const x0 = normalize(dvec3{0.31, 0.57, 0.76});
+    std::vector<dvec3> pts;
+    int const n = 12;
+    for (int k = 0; k < n; ++k)
+        for (int j = 0; j < n; ++j)
+            for (int i = 0; i < n; ++i)
+                pts.push_back({-1.5 + 3.0 * (i + 0.37) / n, -1.5 + 3.0 * (j + 0.61) / n, -1.5 + 3.0 * (k + 0.19) / n});
+    std::span<dvec3 const> const P{pts};
+    std::span<weighted_dsegment3 const> const B{bnd};
+    try
+    {
+        cuda::CudaDispatcher disp;
+        cuda::CudaIntersector<double> const isect{disp, verts, idx};
+        std::vector<double> exact(pts.size()), mixed(pts.size()), frac(pts.size());
+        std::vector<int> counts(pts.size());
+        eval_gwnr_mesh_batch(disp, isect, P, std::span<double>{exact}, x0, B);
+        eval_gwnr_mesh_batch_fractional(disp, P, std::span<double>{frac}, x0, B);
+        eval_gwnr_mesh_batch_integer(disp, isect, P, std::span<int>{counts}, x0);
+        disp.set_precision(cuda::precision::mixed);
+        eval_gwnr_mesh_batch(disp, isect, P, std::span<double>{mixed}, x0, B);
+        for (size_t q = 0; q < pts.size(); ++q)
+            std::printf("%.17g %.17g %.17g %.17g %.17g %.17g %d\n", pts[q].x, pts[q].y, pts[q].z, exact[q], mixed[q],
+                        frac[q], counts[q]);
+    }
+    catch (cuda::Error const& e)
+    {
+        std::printf("error %d %s\n", e.status(), e.what());
+        return 3;
+    }
+    return 0;
+}
