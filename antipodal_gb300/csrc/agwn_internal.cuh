@@ -75,6 +75,20 @@ enum scratch_slot
     S_COUNT = 10
 };
 
+// A hierarchy over one intersector's triangles in the frame of one ray direction, cached per context
+// (see lbvh.cu).  Keyed by the intersector's generation number and the direction's bits.
+struct RayCache
+{
+    unsigned long long generation = 0;
+    double dir[3] = {0, 0, 0};
+    int scalar_bytes = 0;
+    int32_t depth = 0;
+    int64_t n_tri = 0;
+    float frame[9] = {};
+    DevBuf nodes;
+    DevBuf tri;
+};
+
 struct Context
 {
     int device = 0;
@@ -85,6 +99,7 @@ struct Context
     long long* d_counters = nullptr; // [0] fp64 pairs, [1] pairs
     DevBuf scratch[S_COUNT];
     int sm_count = 0;
+    RayCache ray_cache;
 
     // options
     int frac_mode = AGWN_FRAC_EXACT;

@@ -271,6 +271,8 @@ int agwn_context_destroy(agwn_context* ctx)
         cudaStreamSynchronize(ctx->stream);
     for (auto& b : ctx->scratch)
         b.release();
+    ctx->ray_cache.nodes.release();
+    ctx->ray_cache.tri.release();
     for (int i = 0; i < Context::kMaxPending; ++i)
     {
         if (ctx->ev_begin[i])

@@ -5,17 +5,17 @@
 
 namespace agwn
 {
-// Device state of a CudaIntersector: triangles in hierarchy order and a linear BVH (see lbvh.cu).
+// Device state of a CudaIntersector: its triangles, copied.  The hierarchy that accelerates the integer term is
+// built per ray direction and cached in the context that queries it (see lbvh.cu).
 struct Bvh
 {
     int device = 0;
-    int scalar_bytes = 8;       // 8: double geometry, 4: float geometry
+    int scalar_bytes = 8;                // 8: double geometry, 4: float geometry
     int64_t n_tri = 0;
-    int32_t depth = 0;
-    void* tri = nullptr;        // n_tri x 9 scalars (a, b, c) in leaf order
-    void* nodes = nullptr;      // (n_tri - 1) x BvhNode
-    float* root_box = nullptr;  // 6 floats; used when n_tri == 1
-    double scene_scale = 1.0;   // max |coordinate| of the geometry, for the traversal tolerance
+    void* tri = nullptr;                 // n_tri x 9 scalars (a, b, c) in input order
+    double scene_scale = 1.0;            // max |coordinate| of the geometry, for the traversal tolerance
+    unsigned long long generation = 0;   // unique per intersector, keys the contexts' hierarchy caches
+    mutable int32_t depth = 0;           // depth of the most recently built hierarchy (0 before any query)
 };
 
 // Fractional term of the mesh GWN for `n` device-resident queries; adds `counts[i]` (if non-null).

@@ -1,24 +1,29 @@
-// Integer (ray-crossing) term of the mesh GWN over a linear BVH built on the device, and the CudaIntersector
-// C ABI.
+// Integer (ray-crossing) term of the mesh GWN, and the CudaIntersector C ABI.
 //
 // Counting rule: NaiveIntersector::signed_intersection_count (src/antipodal/intersector/intersector.hh:61-100):
 // Moller-Trumbore against (p, dir), t >= 0, sign of (e1 x e2) . dir, with its early rejections.  The test is
 // written with unfused, correctly rounded operations (rd/rf), so every candidate triangle gets exactly the CPU's
 // decision -- including the double count of a ray through an edge shared by two triangles.
 //
-// The hierarchy only culls.  Boxes are rounded outward to float and, at traversal time, grown by a tolerance
-// far above the float rounding of the ray origin and of the slab arithmetic, so a triangle that the exact test
-// would count is never culled: counts equal the linear scan's.
+// Acceleration.  All rays of one batch share the direction dir (the reference passes x0 to every query, and its
+// contract fixes x0 per mesh), so the hierarchy is built in the frame (u, v, w) with w along dir: a ray is the
+// point (u_q, v_q) plus the half-line w >= w_q.  A node is then hit iff its (u, v) box contains the query's point
+// and its largest w is not behind the query -- five float compares, no slab divisions, and boxes that are tight
+// around the projected triangles.  The hierarchy is built on the device when a context first queries an
+// intersector along a direction and cached in that context: (u, v) centroids -> 2 x 15-bit Morton codes ->
+// stable LSD radix sort in four 8-bit passes -> Karras (2012) hierarchy (ties broken by position) -> bottom-up
+// boxes with one atomic visit counter per node.  One triangle per leaf; the leaves' world-space vertices are
+// stored in leaf order as contiguous 9-scalar records for the exact test.
 //
-// Build (all on the device): triangle boxes and centroids -> 30-bit Morton codes -> stable LSD radix sort of
-// (code, triangle) in four 8-bit passes -> Karras (2012) hierarchy over the sorted codes (ties broken by
-// position) -> bottom-up boxes with one atomic visit counter per node.  Leaves hold one triangle each; the
-// triangles are copied into leaf order so a leaf's vertices are one contiguous 9-scalar record.
+// The hierarchy only culls.  Boxes are rounded outward to float and the comparisons are widened by a tolerance
+// far above the float rounding of the rotated query, so a triangle the exact test would count is never culled:
+// counts equal the linear scan's.
 
 #include "agwn_internal.cuh"
 #include "gwn_kernels.cuh"
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <vector>
 
@@ -26,21 +31,23 @@ namespace agwn
 {
 namespace
 {
-// Internal node: boxes of both children, so one 64-byte fetch decides both.  lo_l.w / lo_r.w hold the child
-// codes as int bits: >= 0 an internal node, < 0 the leaf ~code.
+// Internal node: boxes of both children in the ray frame, so one 64-byte fetch decides both.  lo_l.w / lo_r.w
+// hold the child codes as int bits: >= 0 an internal node, < 0 the leaf ~code.  Only the upper w bound is used.
 struct alignas(16) BvhNode
 {
     float4 lo_l, hi_l, lo_r, hi_r;
 };
 
 constexpr int kStackDepth = 64;
+std::atomic<unsigned long long> g_generation{1};
 
-__device__ __forceinline__ unsigned expand_bits(unsigned v)
+__device__ __forceinline__ unsigned expand_bits2(unsigned v)
 {
-    v = (v * 0x00010001u) & 0xFF0000FFu;
-    v = (v * 0x00000101u) & 0x0F00F00Fu;
-    v = (v * 0x00000011u) & 0xC30C30C3u;
-    v = (v * 0x00000005u) & 0x49249249u;
+    v &= 0x7fffu;
+    v = (v | (v << 8)) & 0x00FF00FFu;
+    v = (v | (v << 4)) & 0x0F0F0F0Fu;
+    v = (v | (v << 2)) & 0x33333333u;
+    v = (v | (v << 1)) & 0x55555555u;
     return v;
 }
 
@@ -54,97 +61,106 @@ __device__ __forceinline__ float float_unflip(unsigned u)
     return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
 }
 
+// Gathers the indexed triangles into 9-scalar records and finds the largest coordinate magnitude.  Raises
+// flags[FLAG_COUNT - 1] on an out-of-range index.
 template <class T>
-__device__ __forceinline__ float to_float_down(T v)
+__global__ void k_gather(const T* __restrict__ verts, int64_t nv, const int32_t* __restrict__ idx, int64_t n_tri,
+                         T* __restrict__ tri, unsigned* __restrict__ scale_bits, int* flags)
 {
-    if constexpr (sizeof(T) == 8)
-        return __double2float_rd(v);
-    else
-        return v;
-}
-template <class T>
-__device__ __forceinline__ float to_float_up(T v)
-{
-    if constexpr (sizeof(T) == 8)
-        return __double2float_ru(v);
-    else
-        return v;
-}
-
-// Per triangle: outward-rounded float box, centroid; scene centroid bounds (flipped-uint atomics) and the largest
-// coordinate magnitude.  Raises flags[FLAG_COUNT - 1] on an out-of-range index.
-template <class T>
-__global__ void k_tri_boxes(const T* __restrict__ verts, int64_t nv, const int32_t* __restrict__ idx, int64_t n_tri,
-                            float* __restrict__ box, float* __restrict__ cen, unsigned* __restrict__ cbounds,
-                            unsigned* __restrict__ scale_bits, int* flags)
-{
-    float cmn[3] = {INFINITY, INFINITY, INFINITY}, cmx[3] = {-INFINITY, -INFINITY, -INFINITY};
     float amax = 0.f;
     for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; t < n_tri; t += int64_t(gridDim.x) * blockDim.x)
     {
-        int32_t const i0 = idx[3 * t], i1 = idx[3 * t + 1], i2 = idx[3 * t + 2];
-        if (i0 < 0 || i1 < 0 || i2 < 0 || i0 >= nv || i1 >= nv || i2 >= nv)
+        for (int v = 0; v < 3; ++v)
         {
-            atomicOr(flags + FLAG_COUNT - 1, 1);
-            continue;
-        }
-        T const* a = verts + 3 * int64_t(i0);
-        T const* b = verts + 3 * int64_t(i1);
-        T const* c = verts + 3 * int64_t(i2);
-        for (int k = 0; k < 3; ++k)
-        {
-            T const mn = min(a[k], min(b[k], c[k]));
-            T const mx = max(a[k], max(b[k], c[k]));
-            float const lo = to_float_down(mn), hi = to_float_up(mx);
-            box[6 * t + k] = lo;
-            box[6 * t + 3 + k] = hi;
-            float const ce = 0.5f * (lo + hi);
-            cen[3 * t + k] = ce;
-            cmn[k] = fminf(cmn[k], ce);
-            cmx[k] = fmaxf(cmx[k], ce);
-            amax = fmaxf(amax, fmaxf(fabsf(lo), fabsf(hi)));
-        }
-    }
-    for (int k = 0; k < 3; ++k)
-    {
-        for (int o = 16; o > 0; o >>= 1)
-        {
-            cmn[k] = fminf(cmn[k], __shfl_xor_sync(0xffffffffu, cmn[k], o));
-            cmx[k] = fmaxf(cmx[k], __shfl_xor_sync(0xffffffffu, cmx[k], o));
+            int32_t const i = idx[3 * t + v];
+            bool const ok = i >= 0 && i < nv;
+            if (!ok)
+                atomicOr(flags + FLAG_COUNT - 1, 1);
+            for (int k = 0; k < 3; ++k)
+            {
+                T const c = ok ? verts[3 * int64_t(i) + k] : T(0);
+                tri[9 * t + 3 * v + k] = c;
+                amax = fmaxf(amax, fabsf(float(c)));
+            }
         }
     }
     for (int o = 16; o > 0; o >>= 1)
         amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, o));
     if ((threadIdx.x & 31) == 0)
-    {
-        for (int k = 0; k < 3; ++k)
-        {
-            atomicMin(cbounds + k, float_flip(cmn[k]));
-            atomicMax(cbounds + 3 + k, float_flip(cmx[k]));
-        }
         atomicMax(scale_bits, __float_as_uint(amax)); // non-negative floats order like their bits
-    }
 }
 
-__global__ void k_morton(const float* __restrict__ cen, int64_t n_tri, const unsigned* __restrict__ cbounds,
-                         unsigned* __restrict__ keys, unsigned* __restrict__ vals)
+struct Frame64
 {
-    float lo[3], ext[3];
-    for (int k = 0; k < 3; ++k)
+    double r[9]; // rows e1, e2, e3 (e3 = dir / |dir|)
+};
+
+// Per triangle: outward-rounded float box in the ray frame and its (u, v) centroid; (u, v) bounds of the
+// centroids as flipped-uint atomics.
+template <class T>
+__global__ void k_ray_boxes(const T* __restrict__ tri, int64_t n_tri, Frame64 f, float* __restrict__ box,
+                            float* __restrict__ cen, unsigned* __restrict__ cbounds)
+{
+    float cmn[2] = {INFINITY, INFINITY}, cmx[2] = {-INFINITY, -INFINITY};
+    for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; t < n_tri; t += int64_t(gridDim.x) * blockDim.x)
     {
-        lo[k] = float_unflip(cbounds[k]);
-        float const hi = float_unflip(cbounds[3 + k]);
-        ext[k] = hi - lo[k];
+        double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+        for (int v = 0; v < 3; ++v)
+        {
+            double const x = double(tri[9 * t + 3 * v]), y = double(tri[9 * t + 3 * v + 1]),
+                         z = double(tri[9 * t + 3 * v + 2]);
+            for (int r = 0; r < 3; ++r)
+            {
+                double const c = f.r[3 * r] * x + f.r[3 * r + 1] * y + f.r[3 * r + 2] * z;
+                lo[r] = fmin(lo[r], c);
+                hi[r] = fmax(hi[r], c);
+            }
+        }
+        for (int r = 0; r < 3; ++r)
+        {
+            box[6 * t + r] = __double2float_rd(lo[r]);
+            box[6 * t + 3 + r] = __double2float_ru(hi[r]);
+        }
+        for (int r = 0; r < 2; ++r)
+        {
+            float const c = float(0.5 * (lo[r] + hi[r]));
+            cen[2 * t + r] = c;
+            cmn[r] = fminf(cmn[r], c);
+            cmx[r] = fmaxf(cmx[r], c);
+        }
+    }
+    for (int r = 0; r < 2; ++r)
+        for (int o = 16; o > 0; o >>= 1)
+        {
+            cmn[r] = fminf(cmn[r], __shfl_xor_sync(0xffffffffu, cmn[r], o));
+            cmx[r] = fmaxf(cmx[r], __shfl_xor_sync(0xffffffffu, cmx[r], o));
+        }
+    if ((threadIdx.x & 31) == 0)
+        for (int r = 0; r < 2; ++r)
+        {
+            atomicMin(cbounds + r, float_flip(cmn[r]));
+            atomicMax(cbounds + 2 + r, float_flip(cmx[r]));
+        }
+}
+
+__global__ void k_morton2(const float* __restrict__ cen, int64_t n_tri, const unsigned* __restrict__ cbounds,
+                          unsigned* __restrict__ keys, unsigned* __restrict__ vals)
+{
+    float lo[2], ext[2];
+    for (int r = 0; r < 2; ++r)
+    {
+        lo[r] = float_unflip(cbounds[r]);
+        ext[r] = float_unflip(cbounds[2 + r]) - lo[r];
     }
     for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; t < n_tri; t += int64_t(gridDim.x) * blockDim.x)
     {
-        unsigned m[3];
-        for (int k = 0; k < 3; ++k)
+        unsigned m[2];
+        for (int r = 0; r < 2; ++r)
         {
-            float const u = ext[k] > 0.f ? (cen[3 * t + k] - lo[k]) / ext[k] : 0.5f;
-            m[k] = unsigned(fminf(fmaxf(u * 1024.f, 0.f), 1023.f));
+            float const u = ext[r] > 0.f ? (cen[2 * t + r] - lo[r]) / ext[r] : 0.5f;
+            m[r] = unsigned(fminf(fmaxf(u * 32768.f, 0.f), 32767.f));
         }
-        keys[t] = (expand_bits(m[0]) << 2) | (expand_bits(m[1]) << 1) | expand_bits(m[2]);
+        keys[t] = (expand_bits2(m[0]) << 1) | expand_bits2(m[1]);
         vals[t] = unsigned(t);
     }
 }
@@ -300,21 +316,16 @@ __global__ void k_karras(const unsigned* __restrict__ keys, int n, int* __restri
         parent_node[0] = -1;
 }
 
-// Leaf setup: copy each sorted triangle's vertices into leaf order and its box into leaf slots.
+// Leaf setup: each sorted triangle's world-space vertices and its ray-frame box into leaf order.
 template <class T>
-__global__ void k_leaves(const T* __restrict__ verts, const int32_t* __restrict__ idx,
-                         const unsigned* __restrict__ order, const float* __restrict__ box, int64_t n_tri,
-                         T* __restrict__ tri, float* __restrict__ leaf_box)
+__global__ void k_leaves(const T* __restrict__ tri_in, const unsigned* __restrict__ order,
+                         const float* __restrict__ box, int64_t n_tri, T* __restrict__ tri, float* __restrict__ leaf_box)
 {
     for (int64_t l = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; l < n_tri; l += int64_t(gridDim.x) * blockDim.x)
     {
         unsigned const t = order[l];
-        for (int v = 0; v < 3; ++v)
-        {
-            T const* p = verts + 3 * int64_t(idx[3 * int64_t(t) + v]);
-            for (int k = 0; k < 3; ++k)
-                tri[9 * l + 3 * v + k] = p[k];
-        }
+        for (int k = 0; k < 9; ++k)
+            tri[9 * l + k] = tri_in[9 * int64_t(t) + k];
         for (int k = 0; k < 6; ++k)
             leaf_box[6 * l + k] = box[6 * int64_t(t) + k];
     }
@@ -410,32 +421,21 @@ __device__ __forceinline__ int leaf_test(const T* __restrict__ tri, int leaf, ev
     return mt_sign(p, dir, a, b, c);
 }
 
-__device__ __forceinline__ bool slab(float4 lo, float4 hi, float ox, float oy, float oz, float ix, float iy, float iz,
-                                     float tol)
+struct Frame32
 {
-    float const tx0 = (lo.x - tol - ox) * ix, tx1 = (hi.x + tol - ox) * ix;
-    float const ty0 = (lo.y - tol - oy) * iy, ty1 = (hi.y + tol - oy) * iy;
-    float const tz0 = (lo.z - tol - oz) * iz, tz1 = (hi.z + tol - oz) * iz;
-    float const tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fminf(tz0, tz1));
-    float const tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fmaxf(tz0, tz1));
-    return tn <= tf && tf >= 0.f;
-}
+    float r[9];
+};
 
-__device__ __forceinline__ float safe_inv(float d)
-{
-    float const dd = fabsf(d) < 1e-30f ? copysignf(1e-30f, d) : d;
-    return 1.0f / dd;
-}
-
+// One query per thread: rotate it into the ray frame in float, walk the hierarchy with a per-thread stack, run
+// the exact test on every candidate leaf.
 template <class T>
 __global__ void __launch_bounds__(128) k_traverse(const BvhNode* __restrict__ nodes, const T* __restrict__ tri,
-                                                  int64_t n_tri, float scene_scale, const T* __restrict__ pos,
-                                                  int64_t n, int32_t* __restrict__ counts, T dx, T dy, T dz,
-                                                  int* flags)
+                                                  int64_t n_tri, float scene_scale, Frame32 f,
+                                                  const T* __restrict__ pos, int64_t n, int32_t* __restrict__ counts,
+                                                  T dx, T dy, T dz, int* flags)
 {
     using S = typename exact_of<T>::type;
     ev3<S> const dir{S(dx), S(dy), S(dz)};
-    float const ix = safe_inv(float(dx)), iy = safe_inv(float(dy)), iz = safe_inv(float(dz));
     for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
     {
         T const px = pos[3 * i], py = pos[3 * i + 1], pz = pos[3 * i + 2];
@@ -448,8 +448,12 @@ __global__ void __launch_bounds__(128) k_traverse(const BvhNode* __restrict__ no
         else if (n_tri > 1)
         {
             float const ox = float(px), oy = float(py), oz = float(pz);
+            float const u = f.r[0] * ox + f.r[1] * oy + f.r[2] * oz;
+            float const v = f.r[3] * ox + f.r[4] * oy + f.r[5] * oz;
+            float const w = f.r[6] * ox + f.r[7] * oy + f.r[8] * oz;
             float const qmax = fmaxf(fmaxf(fabsf(ox), fabsf(oy)), fabsf(oz));
-            float const tol = (qmax + scene_scale) * 3.0517578e-5f + 1e-30f; // 2^-15 of the coordinate scale
+            float const tol = (qmax + scene_scale) * 3.8146973e-6f + 1e-30f; // 2^-18 of the coordinate scale
+            float const ulo = u + tol, uhi = u - tol, vlo = v + tol, vhi = v - tol, wq = w - tol;
             int stack[kStackDepth];
             int sp = 0;
             int node = 0;
@@ -457,8 +461,10 @@ __global__ void __launch_bounds__(128) k_traverse(const BvhNode* __restrict__ no
             {
                 BvhNode const nd = nodes[node];
                 int const lc = __float_as_int(nd.lo_l.w), rc = __float_as_int(nd.lo_r.w);
-                bool const hl = slab(nd.lo_l, nd.hi_l, ox, oy, oz, ix, iy, iz, tol);
-                bool const hr = slab(nd.lo_r, nd.hi_r, ox, oy, oz, ix, iy, iz, tol);
+                bool const hl = nd.lo_l.x <= ulo && nd.hi_l.x >= uhi && nd.lo_l.y <= vlo && nd.hi_l.y >= vhi &&
+                                nd.hi_l.z >= wq;
+                bool const hr = nd.lo_r.x <= ulo && nd.hi_r.x >= uhi && nd.lo_r.y <= vlo && nd.hi_r.y >= vhi &&
+                                nd.hi_r.z >= wq;
                 int next = -1;
                 if (hl)
                 {
@@ -548,18 +554,15 @@ struct Tmp
 
 void bvh_free(Bvh* b)
 {
-    if (!b)
-        return;
-    if (b->tri)
+    if (b && b->tri)
         cudaFree(b->tri);
-    if (b->nodes)
-        cudaFree(b->nodes);
-    b->tri = nullptr;
-    b->nodes = nullptr;
+    if (b)
+        b->tri = nullptr;
 }
 
+// Copies the indexed triangles to the device.
 template <class T>
-int bvh_build(Context& ctx, const T* vertices, int64_t nv, const int32_t* indices, int64_t n_idx, Bvh* out)
+int bvh_make(Context& ctx, const T* vertices, int64_t nv, const int32_t* indices, int64_t n_idx, Bvh* out)
 {
     AGWN_CHECK_ARG(nv >= 0 && n_idx >= 0 && n_idx % 3 == 0, "index count must be a non-negative multiple of 3");
     AGWN_CHECK_ARG(n_idx / 3 < (int64_t(1) << 31) - 1, "too many triangles");
@@ -568,6 +571,7 @@ int bvh_build(Context& ctx, const T* vertices, int64_t nv, const int32_t* indice
     out->scalar_bytes = int(sizeof(T));
     out->n_tri = n_tri;
     out->device = ctx.device;
+    out->generation = g_generation.fetch_add(1);
     if (n_tri == 0)
         return AGWN_OK;
     cudaStream_t const st = ctx.stream;
@@ -575,43 +579,19 @@ int bvh_build(Context& ctx, const T* vertices, int64_t nv, const int32_t* indice
     const void* di = nullptr;
     AGWN_TRY(stage_in(ctx, vertices, sizeof(T) * 3 * nv, S_MISC0, &dv));
     AGWN_TRY(stage_in(ctx, indices, sizeof(int32_t) * n_idx, S_MISC1, &di));
-    const T* V = static_cast<const T*>(dv);
-    const int32_t* I = static_cast<const int32_t*>(di);
-
-    Tmp box, cen, misc, keys0, vals0, keys1, vals1, hist, left, right, pnode, pleaf, nbox, visit, leafbox;
-    AGWN_TRY(box.alloc(sizeof(float) * 6 * n_tri));
-    AGWN_TRY(cen.alloc(sizeof(float) * 3 * n_tri));
-    AGWN_TRY(misc.alloc(sizeof(unsigned) * 16));
-    AGWN_TRY(keys0.alloc(sizeof(unsigned) * n_tri));
-    AGWN_TRY(vals0.alloc(sizeof(unsigned) * n_tri));
-    AGWN_TRY(keys1.alloc(sizeof(unsigned) * n_tri));
-    AGWN_TRY(vals1.alloc(sizeof(unsigned) * n_tri));
-    int const n_rs_blocks = div_up(n_tri, kRsTile);
-    AGWN_TRY(hist.alloc(sizeof(unsigned) * 256 * n_rs_blocks));
-    AGWN_TRY(left.alloc(sizeof(int) * n_tri));
-    AGWN_TRY(right.alloc(sizeof(int) * n_tri));
-    AGWN_TRY(pnode.alloc(sizeof(int) * n_tri));
-    AGWN_TRY(pleaf.alloc(sizeof(int) * n_tri));
-    AGWN_TRY(nbox.alloc(sizeof(float) * 6 * n_tri));
-    AGWN_TRY(visit.alloc(sizeof(int) * n_tri));
-    AGWN_TRY(leafbox.alloc(sizeof(float) * 6 * n_tri));
-
-    unsigned init[8];
-    for (int k = 0; k < 3; ++k)
-    {
-        init[k] = 0xFFFFFFFFu; // min of flipped floats
-        init[3 + k] = 0u;      // max of flipped floats
-    }
-    init[6] = 0u; // scale bits
-    init[7] = 0u; // depth
-    AGWN_TRY_CUDA(cudaMemcpyAsync(misc.p, init, sizeof(init), cudaMemcpyHostToDevice, st));
+    AGWN_TRY_CUDA(cudaMalloc(&out->tri, sizeof(T) * 9 * n_tri));
+    Tmp misc;
+    AGWN_TRY(misc.alloc(sizeof(unsigned)));
+    AGWN_TRY_CUDA(cudaMemsetAsync(misc.p, 0, sizeof(unsigned), st));
     AGWN_TRY_CUDA(cudaMemsetAsync(ctx.d_flags + FLAG_COUNT - 1, 0, sizeof(int), st));
     int const g = std::min(div_up(n_tri, 256), 8 * ctx.sm_count);
     AGWN_TRY(ctx.launch_begin(AGWN_K_OTHER));
-    k_tri_boxes<T><<<g, 256, 0, st>>>(V, nv, I, n_tri, box.as<float>(), cen.as<float>(), misc.as<unsigned>(),
-                                      misc.as<unsigned>() + 6, ctx.d_flags);
+    k_gather<T><<<g, 256, 0, st>>>(static_cast<const T*>(dv), nv, static_cast<const int32_t*>(di), n_tri,
+                                   static_cast<T*>(out->tri), misc.as<unsigned>(), ctx.d_flags);
     AGWN_TRY(ctx.launch_end(AGWN_K_OTHER));
+    unsigned scale_bits = 0;
     int bad = 0;
+    AGWN_TRY_CUDA(cudaMemcpyAsync(&scale_bits, misc.p, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
     AGWN_TRY_CUDA(cudaMemcpyAsync(&bad, ctx.d_flags + FLAG_COUNT - 1, sizeof(int), cudaMemcpyDeviceToHost, st));
     AGWN_TRY_CUDA(cudaStreamSynchronize(st));
     if (bad)
@@ -619,58 +599,127 @@ int bvh_build(Context& ctx, const T* vertices, int64_t nv, const int32_t* indice
         AGWN_TRY_CUDA(cudaMemsetAsync(ctx.d_flags + FLAG_COUNT - 1, 0, sizeof(int), st));
         return fail(AGWN_ERR_INVALID, "triangle index out of range [0, %lld)", (long long)nv);
     }
-    AGWN_TRY(ctx.launch_begin(AGWN_K_OTHER));
-    k_morton<<<g, 256, 0, st>>>(cen.as<float>(), n_tri, misc.as<unsigned>(), keys0.as<unsigned>(),
-                                vals0.as<unsigned>());
-    AGWN_TRY(ctx.launch_end(AGWN_K_OTHER));
-    // four stable passes; the result lands back in keys0/vals0
-    unsigned *ka = keys0.as<unsigned>(), *va = vals0.as<unsigned>(), *kb = keys1.as<unsigned>(),
-             *vb = vals1.as<unsigned>();
-    for (int pass = 0; pass < 4; ++pass)
+    float scale;
+    std::memcpy(&scale, &scale_bits, sizeof(float));
+    out->scene_scale = scale;
+    return AGWN_OK;
+}
+
+// Orthonormal frame whose third row is dir / |dir|.
+Frame64 ray_frame(const double* dir)
+{
+    double const nn = std::sqrt(dir[0] * dir[0] + dir[1] * dir[1] + dir[2] * dir[2]);
+    double z[3] = {dir[0] / nn, dir[1] / nn, dir[2] / nn};
+    int m = 0;
+    for (int k = 1; k < 3; ++k)
+        if (std::fabs(z[k]) < std::fabs(z[m]))
+            m = k;
+    double a[3] = {0, 0, 0};
+    a[m] = 1.0;
+    double x[3] = {a[1] * z[2] - a[2] * z[1], a[2] * z[0] - a[0] * z[2], a[0] * z[1] - a[1] * z[0]};
+    double const xn = std::sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]);
+    for (double& c : x)
+        c /= xn;
+    double y[3] = {z[1] * x[2] - z[2] * x[1], z[2] * x[0] - z[0] * x[2], z[0] * x[1] - z[1] * x[0]};
+    Frame64 f;
+    for (int k = 0; k < 3; ++k)
     {
-        int const shift = 8 * pass;
-        AGWN_TRY(ctx.launch_begin(AGWN_K_OTHER));
-        k_rs_hist<<<n_rs_blocks, kRsBlock, 0, st>>>(ka, n_tri, shift, hist.as<unsigned>(), n_rs_blocks);
-        k_rs_scan<<<1, 1024, 0, st>>>(hist.as<unsigned>(), int64_t(256) * n_rs_blocks);
-        k_rs_scatter<<<n_rs_blocks, kRsBlock, 0, st>>>(ka, va, n_tri, shift, hist.as<unsigned>(), n_rs_blocks, kb, vb);
-        AGWN_TRY(ctx.launch_end(AGWN_K_OTHER));
-        std::swap(ka, kb);
-        std::swap(va, vb);
+        f.r[k] = x[k];
+        f.r[3 + k] = y[k];
+        f.r[6 + k] = z[k];
     }
-    T* tri = nullptr;
-    AGWN_TRY_CUDA(cudaMalloc(&tri, sizeof(T) * 9 * n_tri));
-    out->tri = tri;
-    AGWN_TRY(ctx.launch_begin(AGWN_K_OTHER));
-    k_leaves<T><<<g, 256, 0, st>>>(V, I, va, box.as<float>(), n_tri, tri, leafbox.as<float>());
-    AGWN_TRY(ctx.launch_end(AGWN_K_OTHER));
+    return f;
+}
+
+// The hierarchy of `bvh` in the frame of `dir`, built into ctx.ray_cache unless it is already there.
+template <class T>
+int ray_hierarchy(Context& ctx, const Bvh& bvh, const T* dir_host)
+{
+    RayCache& rc = ctx.ray_cache;
+    double const dir[3] = {double(dir_host[0]), double(dir_host[1]), double(dir_host[2])};
+    if (rc.generation == bvh.generation && rc.scalar_bytes == bvh.scalar_bytes &&
+        std::memcmp(rc.dir, dir, sizeof(dir)) == 0)
+        return AGWN_OK;
+    double const nn = dir[0] * dir[0] + dir[1] * dir[1] + dir[2] * dir[2];
+    AGWN_CHECK_ARG(nn > 0 && std::isfinite(nn), "ray direction must be finite and nonzero");
+    int64_t const n_tri = bvh.n_tri;
+    cudaStream_t const st = ctx.stream;
+    rc.generation = 0; // invalid until the build completes
+    Frame64 const f = ray_frame(dir);
+    AGWN_TRY_CUDA(cudaStreamSynchronize(st)); // the cache buffers may still be read by queued traversals
+    AGWN_TRY(rc.tri.reserve(sizeof(T) * 9 * n_tri));
+    AGWN_TRY(rc.nodes.reserve(sizeof(BvhNode) * std::max<int64_t>(1, n_tri - 1)));
+    T* tri = static_cast<T*>(rc.tri.ptr);
+    if (n_tri == 1)
+        AGWN_TRY_CUDA(cudaMemcpyAsync(tri, bvh.tri, sizeof(T) * 9, cudaMemcpyDeviceToDevice, st));
+    int32_t depth = 1;
     if (n_tri > 1)
     {
-        BvhNode* nodes = nullptr;
-        AGWN_TRY_CUDA(cudaMalloc(&nodes, sizeof(BvhNode) * (n_tri - 1)));
-        out->nodes = nodes;
+        Tmp box, cen, misc, keys0, vals0, keys1, vals1, hist, left, right, pnode, pleaf, nbox, visit, leafbox;
+        AGWN_TRY(box.alloc(sizeof(float) * 6 * n_tri));
+        AGWN_TRY(cen.alloc(sizeof(float) * 2 * n_tri));
+        AGWN_TRY(misc.alloc(sizeof(unsigned) * 8));
+        AGWN_TRY(keys0.alloc(sizeof(unsigned) * n_tri));
+        AGWN_TRY(vals0.alloc(sizeof(unsigned) * n_tri));
+        AGWN_TRY(keys1.alloc(sizeof(unsigned) * n_tri));
+        AGWN_TRY(vals1.alloc(sizeof(unsigned) * n_tri));
+        int const n_rs_blocks = div_up(n_tri, kRsTile);
+        AGWN_TRY(hist.alloc(sizeof(unsigned) * 256 * n_rs_blocks));
+        AGWN_TRY(left.alloc(sizeof(int) * n_tri));
+        AGWN_TRY(right.alloc(sizeof(int) * n_tri));
+        AGWN_TRY(pnode.alloc(sizeof(int) * n_tri));
+        AGWN_TRY(pleaf.alloc(sizeof(int) * n_tri));
+        AGWN_TRY(nbox.alloc(sizeof(float) * 6 * n_tri));
+        AGWN_TRY(visit.alloc(sizeof(int) * n_tri));
+        AGWN_TRY(leafbox.alloc(sizeof(float) * 6 * n_tri));
+        unsigned init[8] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0u, 0u, 0u, 0u, 0u, 0u}; // (u, v) min, (u, v) max, -, depth
+        AGWN_TRY_CUDA(cudaMemcpyAsync(misc.p, init, sizeof(init), cudaMemcpyHostToDevice, st));
         AGWN_TRY_CUDA(cudaMemsetAsync(visit.p, 0, sizeof(int) * n_tri, st));
+        int const g = std::min(div_up(n_tri, 256), 8 * ctx.sm_count);
         int const gb = div_up(n_tri, 256);
         AGWN_TRY(ctx.launch_begin(AGWN_K_OTHER));
+        k_ray_boxes<T><<<g, 256, 0, st>>>(static_cast<const T*>(bvh.tri), n_tri, f, box.as<float>(), cen.as<float>(),
+                                          misc.as<unsigned>());
+        k_morton2<<<g, 256, 0, st>>>(cen.as<float>(), n_tri, misc.as<unsigned>(), keys0.as<unsigned>(),
+                                     vals0.as<unsigned>());
+        unsigned *ka = keys0.as<unsigned>(), *va = vals0.as<unsigned>(), *kb = keys1.as<unsigned>(),
+                 *vb = vals1.as<unsigned>();
+        for (int pass = 0; pass < 4; ++pass)
+        {
+            int const shift = 8 * pass;
+            k_rs_hist<<<n_rs_blocks, kRsBlock, 0, st>>>(ka, n_tri, shift, hist.as<unsigned>(), n_rs_blocks);
+            k_rs_scan<<<1, 1024, 0, st>>>(hist.as<unsigned>(), int64_t(256) * n_rs_blocks);
+            k_rs_scatter<<<n_rs_blocks, kRsBlock, 0, st>>>(ka, va, n_tri, shift, hist.as<unsigned>(), n_rs_blocks, kb,
+                                                           vb);
+            std::swap(ka, kb);
+            std::swap(va, vb);
+        }
+        k_leaves<T><<<g, 256, 0, st>>>(static_cast<const T*>(bvh.tri), va, box.as<float>(), n_tri, tri,
+                                       leafbox.as<float>());
         k_karras<<<gb, 256, 0, st>>>(ka, int(n_tri), left.as<int>(), right.as<int>(), pnode.as<int>(),
                                      pleaf.as<int>());
         k_refit<<<gb, 256, 0, st>>>(int(n_tri), left.as<int>(), right.as<int>(), pnode.as<int>(), pleaf.as<int>(),
-                                    leafbox.as<float>(), nbox.as<float>(), visit.as<int>(), nodes);
+                                    leafbox.as<float>(), nbox.as<float>(), visit.as<int>(),
+                                    static_cast<BvhNode*>(rc.nodes.ptr));
         k_depth<<<gb, 256, 0, st>>>(int(n_tri), pnode.as<int>(), pleaf.as<int>(),
                                     reinterpret_cast<int*>(misc.as<unsigned>() + 7));
         AGWN_TRY(ctx.launch_end(AGWN_K_OTHER));
+        unsigned back[8];
+        AGWN_TRY_CUDA(cudaMemcpyAsync(back, misc.p, sizeof(back), cudaMemcpyDeviceToHost, st));
+        AGWN_TRY_CUDA(cudaStreamSynchronize(st));
+        depth = int32_t(back[7]);
+        if (depth > n_tri)
+            return fail(AGWN_ERR_CUDA, "hierarchy build produced a broken parent chain (depth %d for %lld triangles)",
+                        depth, (long long)n_tri);
     }
-    unsigned back[8];
-    AGWN_TRY_CUDA(cudaMemcpyAsync(back, misc.p, sizeof(back), cudaMemcpyDeviceToHost, st));
-    AGWN_TRY_CUDA(cudaStreamSynchronize(st));
-    float scale;
-    std::memcpy(&scale, &back[6], sizeof(float));
-    out->scene_scale = scale;
-    out->depth = n_tri > 1 ? int32_t(back[7]) : 1;
-    if (out->depth > n_tri)
-        return fail(AGWN_ERR_CUDA, "BVH build produced a broken hierarchy (depth %d for %lld triangles)", out->depth,
-                    (long long)n_tri);
-    if (out->depth >= kStackDepth)
-        set_message("BVH depth %d is at or above the traversal stack depth %d", out->depth, kStackDepth);
+    for (int k = 0; k < 9; ++k)
+        rc.frame[k] = float(f.r[k]);
+    std::memcpy(rc.dir, dir, sizeof(dir));
+    rc.scalar_bytes = bvh.scalar_bytes;
+    rc.n_tri = n_tri;
+    rc.depth = depth;
+    rc.generation = bvh.generation;
+    bvh.depth = depth;
     return AGWN_OK;
 }
 } // namespace
@@ -680,11 +729,21 @@ int integer_run(Context& ctx, const Bvh& bvh, const T* d_pos, int64_t n, int32_t
 {
     if (n == 0)
         return AGWN_OK;
+    if (bvh.n_tri == 0)
+    {
+        AGWN_TRY_CUDA(cudaMemsetAsync(d_counts, 0, sizeof(int32_t) * n, ctx.stream));
+        return AGWN_OK;
+    }
+    AGWN_TRY(ray_hierarchy<T>(ctx, bvh, dir_host));
+    Frame32 f;
+    for (int k = 0; k < 9; ++k)
+        f.r[k] = ctx.ray_cache.frame[k];
     int const block = 128;
     int const grid = int(std::min<int64_t>(div_up(n, block), int64_t(ctx.sm_count) * 16));
     AGWN_TRY(ctx.launch_begin(AGWN_K_INTEGER));
-    k_traverse<T><<<grid, block, 0, ctx.stream>>>(static_cast<const BvhNode*>(bvh.nodes), static_cast<const T*>(bvh.tri),
-                                                  bvh.n_tri, float(bvh.scene_scale), d_pos, n, d_counts, dir_host[0],
+    k_traverse<T><<<grid, block, 0, ctx.stream>>>(static_cast<const BvhNode*>(ctx.ray_cache.nodes.ptr),
+                                                  static_cast<const T*>(ctx.ray_cache.tri.ptr), bvh.n_tri,
+                                                  float(bvh.scene_scale), f, d_pos, n, d_counts, dir_host[0],
                                                   dir_host[1], dir_host[2], ctx.d_flags);
     return ctx.launch_end(AGWN_K_INTEGER);
 }
@@ -702,7 +761,7 @@ int bvh_create(agwn_context* ctx, const T* vertices, int64_t nv, const int32_t* 
     clear_message();
     AGWN_TRY_CUDA(cudaSetDevice(ctx->device));
     auto* b = new agwn_bvh{};
-    int const s = bvh_build<T>(*ctx, vertices, nv, indices, n_idx, b);
+    int const s = bvh_make<T>(*ctx, vertices, nv, indices, n_idx, b);
     if (s != AGWN_OK)
     {
         bvh_free(b);

@@ -121,9 +121,9 @@ def test_icosphere_subset_against_oracle(gwn, disp, oracle):
     q = synth.grid_queries(verts.min(0), verts.max(0), 14, 1.2)  # 2744 queries
     ref_int = oracle.int_naive(q, x0, verts, idx)
     isect = gwn.CudaIntersector(disp, verts, idx)
-    assert isect.info()["depth"] < 64
     c = np.empty(len(q), np.int32)
     gwn.eval_gwnr_mesh_batch_integer(disp, isect, q, c, x0)
+    assert 0 < isect.info()["depth"] < 64
     assert np.array_equal(c, ref_int)
     out = np.empty(len(q))
     gwn.eval_gwnr_mesh_batch(disp, isect, q, out, x0, bnd)
@@ -177,3 +177,20 @@ def test_errors_are_reported(gwn, disp):
         gwn.eval_gwnr_mesh_batch_integer(disp, isect32, np.zeros((2, 3)), np.zeros(2, np.int32), synth.unit_x0())
     with pytest.raises(TypeError):
         disp.parallel_for(0, 4, lambda i: None)
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_integer_term_along_many_directions(gwn, disp, oracle, dtype):
+    # the hierarchy is built per ray direction and cached per context: switch directions back and forth,
+    # including axis-aligned and unnormalised ones, and compare with the scan of every triangle
+    verts, idx, _, _, _ = synth.open_icosphere(seed=6, level=4, grid=0)
+    verts = verts.astype(dtype)
+    rng = np.random.default_rng(6)
+    q = rng.uniform(-1.4, 1.4, size=(4000, 3)).astype(dtype)
+    isect = gwn.CudaIntersector(disp, verts, idx)
+    dirs = [synth.unit_x0(), [1, 0, 0], [0, -1, 0], [0, 0, 5.0], [-3e-3, 2e-3, 1e-3], synth.unit_x0(), [1, 0, 0]]
+    for d in dirs:
+        d = np.asarray(d, dtype)
+        c = np.empty(len(q), np.int32)
+        gwn.eval_gwnr_mesh_batch_integer(disp, isect, q, c, d)
+        assert np.array_equal(c, oracle.int_naive(q, d, verts, idx)), d
