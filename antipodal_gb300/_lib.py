@@ -53,6 +53,7 @@ SIGNATURES = {
     "agwn_mesh_batch_f32": (_I, [_P, _P, _P, _I64, _P, _P, _P, _I64]),
     "agwn_mesh_batch_integer_bruteforce_f64": (_I, [_P, _P, _I64, _P, _I64, _P, _I64, _P, _P]),
     "agwn_probe_fp32_peak": (_I, [_P, C.POINTER(_D)]),
+    "agwn_probe_atan2": (_I, [_P, _P, _P, _I64, _P, _P]),
 }
 
 _lock = threading.Lock()

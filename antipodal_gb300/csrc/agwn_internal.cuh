@@ -87,6 +87,7 @@ struct RayCache
     float frame[9] = {};
     DevBuf nodes;
     DevBuf tri;
+    DevBuf leaf_uv;
 };
 
 struct Context

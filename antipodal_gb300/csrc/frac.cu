@@ -110,6 +110,7 @@ int fractional_run(Context& ctx, const T* d_pos, int64_t n, T* d_out, const int3
     }
     else
     {
+        AGWN_CHECK_ARG(n_seg < (int64_t(1) << 24), "the mixed form takes at most 2^24 - 1 boundary segments");
         const double* raw = reinterpret_cast<const double*>(d_seg_raw);
         double x0d[3] = {double(x0_host[0]), double(x0_host[1]), double(x0_host[2])};
         double const x0n = x0d[0] * x0d[0] + x0d[1] * x0d[1] + x0d[2] * x0d[2];
@@ -122,7 +123,7 @@ int fractional_run(Context& ctx, const T* d_pos, int64_t n, T* d_out, const int3
         AGWN_TRY(ctx.scratch_reserve(S_SEGS_RAW, sizeof(SegX<double>) * n_seg, reinterpret_cast<void**>(&seg64)));
         AGWN_TRY(ctx.scratch_reserve(S_FRAME, sizeof(Frame), reinterpret_cast<void**>(&frame)));
         AGWN_TRY(ctx.launch_begin(AGWN_K_OTHER));
-        k_prep_mixed<<<1, 1024, 0, ctx.stream>>>(raw, n_seg, rot, frame, seg, seg64);
+        k_prep_mixed<<<1, 1024, 0, ctx.stream>>>(raw, n_seg, rot, float(ctx.mixed_tau), frame, seg, seg64);
         AGWN_TRY(ctx.launch_end(AGWN_K_OTHER));
         size_t const smem = size_t(nbuf) * tile * sizeof(SegM);
         float const tau = float(ctx.mixed_tau);

@@ -17,7 +17,7 @@ struct alignas(16) SegX
 {
     T p0x, p0y, p0z, p1x, p1y, p1z, w, pad;
 };
-// Mixed-mode segment: a = (P0_hi, w), b = (P1 - P0, |p1 - p0|), c = (P0_lo, index as bits).
+// Mixed-mode segment: a = (P0_hi, w), b = (P1 - P0, tau * |p1 - p0|), c = (P0_lo, index as bits).
 struct alignas(16) SegM
 {
     float4 a, b, c;
@@ -200,7 +200,7 @@ __global__ void __launch_bounds__(256) k_frac_exact(const T* __restrict__ pos, i
 
 // One block: bounding-box centre of all endpoints, then each segment moved into the x1 = +z frame around it.
 __global__ void __launch_bounds__(1024) k_prep_mixed(const double* __restrict__ raw, int64_t n_seg, Rot rot,
-                                                     Frame* __restrict__ frame, SegM* __restrict__ out,
+                                                     float tau, Frame* __restrict__ frame, SegM* __restrict__ out,
                                                      SegX<double>* __restrict__ out64)
 {
     __shared__ double red[2][3][32];
@@ -265,7 +265,7 @@ __global__ void __launch_bounds__(1024) k_prep_mixed(const double* __restrict__ 
         float const len = float(sqrt(ex * ex + ey * ey + ez * ez));
         SegM m;
         m.a = make_float4(hi[0], hi[1], hi[2], float(w[6]));
-        m.b = make_float4(dv[0], dv[1], dv[2], len);
+        m.b = make_float4(dv[0], dv[1], dv[2], tau * len);
         m.c = make_float4(lo[0], lo[1], lo[2], __int_as_float(int(s)));
         out[s] = m;
         out64[s] = SegX<double>{w[0], w[1], w[2], w[3], w[4], w[5], w[6], 0.0};
@@ -282,19 +282,93 @@ __device__ __forceinline__ void two_sum_acc(float& acc, float& comp, float x)
     comp = __fadd_rn(comp, e);
 }
 
+// atan2 for the FP32 terms, our own: reduce to t = min(|y|, |x|) / max(|y|, |x|) in [0, 1], evaluate
+// atan(t) = t * P(t^2) with a degree-8 polynomial P, then unfold the octant.  P's coefficients come from a
+// minimax fit of atan(t) / t on [0, 1] by the Remez exchange algorithm (relative error 1.5e-8 in exact arithmetic,
+// below float's 6e-8; about 3 ulp overall in float with the approximate division).
+__device__ __forceinline__ float atan2_fast(float y, float x)
+{
+    float const ax = fabsf(x), ay = fabsf(y);
+    float const mx = fmaxf(ax, ay), mn = fminf(ax, ay);
+    float const t = __fdividef(mn, fmaxf(mx, 1e-37f));
+    float const s = t * t;
+    float p = 0.0028498897585520423f;
+    p = fmaf(p, s, -0.01606862951374933f);
+    p = fmaf(p, s, 0.04269152017510156f);
+    p = fmaf(p, s, -0.07504294615760822f);
+    p = fmaf(p, s, 0.10640934061441572f);
+    p = fmaf(p, s, -0.1420364447570674f);
+    p = fmaf(p, s, 0.1999261939280182f);
+    p = fmaf(p, s, -0.3333307334510578f);
+    p = fmaf(p, s, 0.9999999847657755f);
+    float a = t * p;
+    a = ay > ax ? 1.5707963267948966f - a : a;
+    a = x < 0.f ? 3.141592653589793f - a : a;
+    return copysignf(a, y);
+}
+
+// Per-warp queue of (query, segment) pairs that go to FP64: packed (segment << 8) | (lane << 3) | k.
+// Pairs are appended as the warp meets them and evaluated 32 at a time, one per lane, so the FP64 pipe works
+// with full warps instead of one divergent lane per warp step.
+template <int K>
+struct Fp64Queue
+{
+    static constexpr unsigned kCap = 64u * K; // > 31 left over + 32 * K added per segment
+    uint32_t* e;                              // kCap entries of this warp
+    double* res;                              // 32 results of this warp
+    unsigned head = 0, tail = 0;              // warp-uniform counters
+};
+
+template <int K>
+__device__ __forceinline__ void fp64_flush(Fp64Queue<K>& q, unsigned c, int lane, int warp, int64_t tile_base,
+                                           const double* __restrict__ pos, int64_t n,
+                                           const SegX<double>* __restrict__ seg64, ev3<rd> x1, double (&acc64)[K])
+{
+    __syncwarp();
+    if (unsigned(lane) < c)
+    {
+        uint32_t const e = q.e[(q.head + lane) & (Fp64Queue<K>::kCap - 1)];
+        int const owner = (e >> 3) & 31, kk = e & 7;
+        int64_t i = tile_base + int64_t(kk) * blockDim.x + warp * 32 + owner;
+        i = i < n ? i : n - 1;
+        SegX<double> const g = seg64[e >> 8];
+        ev3<rd> const p{rd(pos[3 * i]), rd(pos[3 * i + 1]), rd(pos[3 * i + 2])};
+        ev3<rd> const v0 = ev3<rd>{rd(g.p0x), rd(g.p0y), rd(g.p0z)} - p;
+        ev3<rd> const v1 = ev3<rd>{rd(g.p1x), rd(g.p1y), rd(g.p1z)} - p;
+        q.res[lane] = (rd(g.w) * rd(vos_exact(x1, v0, v1))).v;
+    }
+    __syncwarp();
+    for (unsigned j = 0; j < c; ++j)
+    {
+        uint32_t const e = q.e[(q.head + j) & (Fp64Queue<K>::kCap - 1)];
+        if (int((e >> 3) & 31) == lane)
+        {
+            double const r = q.res[j];
+#pragma unroll
+            for (int k = 0; k < K; ++k)
+                if (int(e & 7) == k)
+                    acc64[k] += r;
+        }
+    }
+    __syncwarp();
+    q.head += c;
+}
+
 template <int K>
 __global__ void __launch_bounds__(256) k_frac_mixed(const double* __restrict__ pos, int64_t n, double* __restrict__ out,
                                                     const int32_t* __restrict__ counts, double x0x, double x0y,
                                                     double x0z, Rot rot, const Frame* __restrict__ frame, float tau,
-                                                    float term_err,
-                                                    const SegM* __restrict__ seg,
+                                                    float term_err, const SegM* __restrict__ seg,
                                                     const SegX<double>* __restrict__ seg64, int64_t n_seg, int tile,
                                                     int* flags, long long* counters, int count_pairs)
 {
+    (void)tau;
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ __align__(8) uint64_t bars[2];
     __shared__ int abort_cta;
     __shared__ double centre[3];
+    __shared__ uint32_t q_entries[8][Fp64Queue<K>::kCap];
+    __shared__ double q_results[8][32];
 
     TilePipe<SegM> pipe;
     pipe.n_tiles = int((n_seg + tile - 1) / tile);
@@ -310,6 +384,8 @@ __global__ void __launch_bounds__(256) k_frac_mixed(const double* __restrict__ p
     int64_t const n_qtiles = (n + per_tile - 1) / per_tile;
     int const my_qtiles = blockIdx.x < n_qtiles ? int((n_qtiles - 1 - blockIdx.x) / gridDim.x + 1) : 0;
     int const n_items = pipe.single ? (my_qtiles > 0 ? 1 : 0) : my_qtiles * pipe.n_tiles;
+    int const lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned const lt = (1u << lane) - 1u;
 
     if (threadIdx.x == 0)
     {
@@ -326,25 +402,27 @@ __global__ void __launch_bounds__(256) k_frac_mixed(const double* __restrict__ p
         centre[threadIdx.x] = frame->c[threadIdx.x];
     __syncthreads();
 
-    // Rounding bound per FP32 operation chain (4 eps32) and the largest accepted first-order error of one FP32 term.
+    // Rounding bound per FP32 operation chain (4 eps32).
     constexpr float kEpsBound = 4.0f * 5.9604645e-8f;
     double const two_pi = 2.0 * kPi<double>;
-    long long n64 = 0;
+    ev3<rd> const x1{rd(-x0x), rd(-x0y), rd(-x0z)};
+    Fp64Queue<K> fq;
+    fq.e = q_entries[warp];
+    fq.res = q_results[warp];
 
     int it = 0;
     for (int j = 0; j < my_qtiles; ++j)
     {
-        int64_t const base = (blockIdx.x + int64_t(j) * gridDim.x) * per_tile + threadIdx.x;
+        int64_t const tile_base = (blockIdx.x + int64_t(j) * gridDim.x) * per_tile;
+        int64_t const base = tile_base + threadIdx.x;
         float qhx[K], qhy[K], qhz[K], qlx[K], qly[K], qlz[K];
         float acc[K], comp[K];
         double acc64[K];
-        int64_t qi[K];
 #pragma unroll
         for (int k = 0; k < K; ++k)
         {
             int64_t const i = base + int64_t(k) * blockDim.x;
             int64_t const ii = i < n ? i : n - 1;
-            qi[k] = ii;
             double const dx = pos[3 * ii] - centre[0], dy = pos[3 * ii + 1] - centre[1],
                          dz = pos[3 * ii + 2] - centre[2];
             double const Qx = rot.m[0] * dx + rot.m[1] * dy + rot.m[2] * dz;
@@ -374,6 +452,7 @@ __global__ void __launch_bounds__(256) k_frac_mixed(const double* __restrict__ p
                 return;
             SegM const* sb = pipe.buf[b];
             int const cnt = pipe.tile_count(st);
+            uint32_t const sg0 = uint32_t(st) * uint32_t(tile);
             for (int s = 0; s < cnt; ++s)
             {
                 float4 const A = sb[s].a, B = sb[s].b, C = sb[s].c;
@@ -400,45 +479,23 @@ __global__ void __launch_bounds__(256) k_frac_mixed(const double* __restrict__ p
                     // first-order rounding bounds of num and den (a few eps of the magnitudes summed)
                     float const dn = kEpsBound * (fabsf(ta) + fabsf(tb));
                     float const dd = kEpsBound * (ss + fabsf(pxy) + fabsf(pyy));
-                    bool const ill = dn * fabsf(den) + dd * fabsf(num) > term_err * (num * num + den * den);
-                    bool const near = fminf(l0, l1) < tau * B.w || !(q0 > 0.f && q1 > 0.f) || ill;
-                    bool const branch = den < 0.f && fabsf(num) <= dn;
-                    if (near)
+                    bool const need = fminf(l0, l1) < B.w || !(q0 > 0.f && q1 > 0.f) ||
+                                      dn * fabsf(den) + dd * fabsf(num) > term_err * (num * num + den * den) ||
+                                      (den < 0.f && fabsf(num) <= dn);
+                    unsigned const m = __ballot_sync(0xffffffffu, need);
+                    if (m)
                     {
-                        // exact form on the original doubles
-                        SegX<double> const g = seg64[__float_as_int(C.w)];
-                        int64_t const i = qi[k];
-                        ev3<rd> const p{rd(pos[3 * i]), rd(pos[3 * i + 1]), rd(pos[3 * i + 2])};
-                        ev3<rd> const x1{rd(-x0x), rd(-x0y), rd(-x0z)};
-                        ev3<rd> const v0 = ev3<rd>{rd(g.p0x), rd(g.p0y), rd(g.p0z)} - p;
-                        ev3<rd> const v1 = ev3<rd>{rd(g.p1x), rd(g.p1y), rd(g.p1z)} - p;
-                        acc64[k] = (rd(acc64[k]) + rd(g.w) * rd(vos_exact(x1, v0, v1))).v;
-                        n64 += 1;
+                        if (need)
+                            fq.e[(fq.tail + __popc(m & lt)) & (Fp64Queue<K>::kCap - 1)] =
+                                ((sg0 + uint32_t(s)) << 8) | (uint32_t(lane) << 3) | uint32_t(k);
+                        fq.tail += __popc(m);
                     }
-                    else
-                    {
-                        float t = atan2f(num, den);
-                        if (branch)
-                        {
-                            // the reference's FP64 numerator decides the side of the branch cut
-                            SegX<double> const g = seg64[__float_as_int(C.w)];
-                            int64_t const i = qi[k];
-                            ev3<rd> const p{rd(pos[3 * i]), rd(pos[3 * i + 1]), rd(pos[3 * i + 2])};
-                            ev3<rd> const x1{rd(-x0x), rd(-x0y), rd(-x0z)};
-                            ev3<rd> const v0 = ev3<rd>{rd(g.p0x), rd(g.p0y), rd(g.p0z)} - p;
-                            ev3<rd> const v1 = ev3<rd>{rd(g.p1x), rd(g.p1y), rd(g.p1z)} - p;
-                            rd const num64 = edot(x1, ecross(v0, v1));
-                            // Keep the FP32 smooth part (it telescopes with the neighbouring segments) and move the
-                            // term to the reference's side of the cut: atan2 jumps by 2 pi there.
-                            bool const ref_pos = !signbit(num64.v);
-                            bool const f32_pos = !signbit(t);
-                            if (ref_pos != f32_pos)
-                                t += ref_pos ? 2.0f * kPi<float> : -2.0f * kPi<float>;
-                            n64 += 1;
-                        }
-                        two_sum_acc(acc[k], comp[k], A.w * t);
-                    }
+                    if (!need)
+                        two_sum_acc(acc[k], comp[k], A.w * atan2_fast(num, den));
                 }
+                // drain full batches: at most 31 + 32 * K entries stay queued, below the ring's capacity
+                while (fq.tail - fq.head >= 32)
+                    fp64_flush<K>(fq, 32, lane, warp, tile_base, pos, n, seg64, x1, acc64);
             }
             if (!pipe.single)
             {
@@ -447,6 +504,11 @@ __global__ void __launch_bounds__(256) k_frac_mixed(const double* __restrict__ p
                     pipe.issue(it + 2);
                 ++it;
             }
+        }
+        while (fq.tail != fq.head)
+        {
+            unsigned const c = min(32u, fq.tail - fq.head);
+            fp64_flush<K>(fq, c, lane, warp, tile_base, pos, n, seg64, x1, acc64);
         }
 #pragma unroll
         for (int k = 0; k < K; ++k)
@@ -461,26 +523,22 @@ __global__ void __launch_bounds__(256) k_frac_mixed(const double* __restrict__ p
             }
         }
     }
-    if (count_pairs)
+    if (count_pairs && lane == 0)
     {
-        // warp-aggregated statistics: pairs taken to FP64 and all pairs of valid queries
+        // statistics: pairs taken to FP64 (queue entries, valid queries or not) and all pairs of valid queries
         long long tot = 0;
         for (int j = 0; j < my_qtiles; ++j)
         {
-            int64_t const base = (blockIdx.x + int64_t(j) * gridDim.x) * per_tile + threadIdx.x;
+            int64_t const b0 = (blockIdx.x + int64_t(j) * gridDim.x) * per_tile + warp * 32;
             for (int k = 0; k < K; ++k)
-                tot += (base + int64_t(k) * blockDim.x < n) ? n_seg : 0;
+            {
+                int64_t const first = b0 + int64_t(k) * blockDim.x;
+                int64_t const valid = first >= n ? 0 : (n - first < 32 ? n - first : 32);
+                tot += valid * n_seg;
+            }
         }
-        for (int o = 16; o > 0; o >>= 1)
-        {
-            n64 += __shfl_xor_sync(0xffffffffu, n64, o);
-            tot += __shfl_xor_sync(0xffffffffu, tot, o);
-        }
-        if ((threadIdx.x & 31) == 0)
-        {
-            atomicAdd(reinterpret_cast<unsigned long long*>(counters), static_cast<unsigned long long>(n64));
-            atomicAdd(reinterpret_cast<unsigned long long*>(counters + 1), static_cast<unsigned long long>(tot));
-        }
+        atomicAdd(reinterpret_cast<unsigned long long*>(counters), static_cast<unsigned long long>(fq.tail));
+        atomicAdd(reinterpret_cast<unsigned long long*>(counters + 1), static_cast<unsigned long long>(tot));
     }
 }
 

@@ -316,10 +316,12 @@ __global__ void k_karras(const unsigned* __restrict__ keys, int n, int* __restri
         parent_node[0] = -1;
 }
 
-// Leaf setup: each sorted triangle's world-space vertices and its ray-frame box into leaf order.
+// Leaf setup: each sorted triangle's world-space vertices, its ray-frame box and its vertices projected on the
+// (u, v) plane (rounded to float; 8 floats per leaf: u0 v0 u1 v1 u2 v2 0 0) into leaf order.
 template <class T>
 __global__ void k_leaves(const T* __restrict__ tri_in, const unsigned* __restrict__ order,
-                         const float* __restrict__ box, int64_t n_tri, T* __restrict__ tri, float* __restrict__ leaf_box)
+                         const float* __restrict__ box, int64_t n_tri, Frame64 f, T* __restrict__ tri,
+                         float* __restrict__ leaf_box, float* __restrict__ leaf_uv)
 {
     for (int64_t l = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; l < n_tri; l += int64_t(gridDim.x) * blockDim.x)
     {
@@ -328,6 +330,15 @@ __global__ void k_leaves(const T* __restrict__ tri_in, const unsigned* __restric
             tri[9 * l + k] = tri_in[9 * int64_t(t) + k];
         for (int k = 0; k < 6; ++k)
             leaf_box[6 * l + k] = box[6 * int64_t(t) + k];
+        for (int v = 0; v < 3; ++v)
+        {
+            double const x = double(tri_in[9 * int64_t(t) + 3 * v]), y = double(tri_in[9 * int64_t(t) + 3 * v + 1]),
+                         z = double(tri_in[9 * int64_t(t) + 3 * v + 2]);
+            leaf_uv[8 * l + 2 * v] = float(f.r[0] * x + f.r[1] * y + f.r[2] * z);
+            leaf_uv[8 * l + 2 * v + 1] = float(f.r[3] * x + f.r[4] * y + f.r[5] * z);
+        }
+        leaf_uv[8 * l + 6] = 0.f;
+        leaf_uv[8 * l + 7] = 0.f;
     }
 }
 
@@ -426,13 +437,43 @@ struct Frame32
     float r[9];
 };
 
-// One query per thread: rotate it into the ray frame in float, walk the hierarchy with a per-thread stack, run
-// the exact test on every candidate leaf.
+// Conservative float pre-test of a leaf: false only if the query's (u, v) point lies outside the projected
+// triangle by more than the rounding of every coordinate involved can explain, i.e. on the positive side of one
+// edge and the negative side of another, each by more than its margin.  `delta` bounds the absolute error of any
+// float (u, v) coordinate (the query's, rotated in float, and the vertices', rounded from FP64).  An edge function
+// e = du*rv - dv*ru then errs by at most 3*delta*(|du| + |dv| + |ru| + |rv|); the margin takes 8*delta.  The exact
+// Moller-Trumbore test decides every leaf that passes.
+__device__ __forceinline__ bool may_hit(const float4* __restrict__ leaf_uv, int leaf, float u, float v, float m8)
+{
+    float4 const a = leaf_uv[2 * leaf], b = leaf_uv[2 * leaf + 1];
+    float const pu[3] = {a.x, a.z, b.x}, pv[3] = {a.y, a.w, b.y};
+    bool pos = false, neg = false;
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+    {
+        int const k1 = (k + 1) % 3;
+        float const du = pu[k1] - pu[k], dv = pv[k1] - pv[k], ru = u - pu[k], rv = v - pv[k];
+        float const e = du * rv - dv * ru;
+        float const m = m8 * (fabsf(du) + fabsf(dv) + fabsf(ru) + fabsf(rv));
+        pos |= e > m;
+        neg |= e < -m;
+    }
+    return !(pos && neg);
+}
+
+// One query per thread.  The walk itself is float work only; the exact (FP64 for double input) leaf tests are
+// the expensive part, so candidate leaves that pass the float pre-test are collected during the walk and tested
+// after it: the lanes of a warp then run their j-th exact test together instead of one divergent lane at a time
+// in the middle of the walk.  A full candidate list is tested early, so any number of candidates is handled.
+constexpr int kTravBlock = 128;
+constexpr int kCand = 8;
+
 template <class T>
-__global__ void __launch_bounds__(128) k_traverse(const BvhNode* __restrict__ nodes, const T* __restrict__ tri,
-                                                  int64_t n_tri, float scene_scale, Frame32 f,
-                                                  const T* __restrict__ pos, int64_t n, int32_t* __restrict__ counts,
-                                                  T dx, T dy, T dz, int* flags)
+__global__ void __launch_bounds__(kTravBlock) k_traverse(const BvhNode* __restrict__ nodes, const T* __restrict__ tri,
+                                                         const float4* __restrict__ leaf_uv, int64_t n_tri,
+                                                         float scene_scale, Frame32 f, const T* __restrict__ pos,
+                                                         int64_t n, int32_t* __restrict__ counts, T dx, T dy, T dz,
+                                                         int* flags)
 {
     using S = typename exact_of<T>::type;
     ev3<S> const dir{S(dx), S(dy), S(dz)};
@@ -454,6 +495,9 @@ __global__ void __launch_bounds__(128) k_traverse(const BvhNode* __restrict__ no
             float const qmax = fmaxf(fmaxf(fabsf(ox), fabsf(oy)), fabsf(oz));
             float const tol = (qmax + scene_scale) * 3.8146973e-6f + 1e-30f; // 2^-18 of the coordinate scale
             float const ulo = u + tol, uhi = u - tol, vlo = v + tol, vhi = v - tol, wq = w - tol;
+            float const m8 = 8.0f * 1e-6f * (qmax + scene_scale);            // 8 * delta of may_hit
+            int cand[kCand];
+            int nc = 0;
             int stack[kStackDepth];
             int sp = 0;
             int node = 0;
@@ -468,15 +512,34 @@ __global__ void __launch_bounds__(128) k_traverse(const BvhNode* __restrict__ no
                 int next = -1;
                 if (hl)
                 {
-                    if (lc < 0)
-                        sum += leaf_test<T>(tri, ~lc, p, dir);
-                    else
+                    if (lc >= 0)
                         next = lc;
+                    else if (may_hit(leaf_uv, ~lc, u, v, m8))
+                    {
+                        if (nc == kCand)
+                        {
+                            for (int j = 0; j < kCand; ++j)
+                                sum += leaf_test<T>(tri, cand[j], p, dir);
+                            nc = 0;
+                        }
+                        cand[nc++] = ~lc;
+                    }
                 }
                 if (hr)
                 {
                     if (rc < 0)
-                        sum += leaf_test<T>(tri, ~rc, p, dir);
+                    {
+                        if (may_hit(leaf_uv, ~rc, u, v, m8))
+                        {
+                            if (nc == kCand)
+                            {
+                                for (int j = 0; j < kCand; ++j)
+                                    sum += leaf_test<T>(tri, cand[j], p, dir);
+                                nc = 0;
+                            }
+                            cand[nc++] = ~rc;
+                        }
+                    }
                     else if (next < 0)
                         next = rc;
                     else
@@ -496,6 +559,8 @@ __global__ void __launch_bounds__(128) k_traverse(const BvhNode* __restrict__ no
                 else
                     break;
             }
+            for (int j = 0; j < nc; ++j)
+                sum += leaf_test<T>(tri, cand[j], p, dir);
         }
         counts[i] = sum;
     }
@@ -649,6 +714,7 @@ int ray_hierarchy(Context& ctx, const Bvh& bvh, const T* dir_host)
     AGWN_TRY_CUDA(cudaStreamSynchronize(st)); // the cache buffers may still be read by queued traversals
     AGWN_TRY(rc.tri.reserve(sizeof(T) * 9 * n_tri));
     AGWN_TRY(rc.nodes.reserve(sizeof(BvhNode) * std::max<int64_t>(1, n_tri - 1)));
+    AGWN_TRY(rc.leaf_uv.reserve(sizeof(float) * 8 * n_tri));
     T* tri = static_cast<T*>(rc.tri.ptr);
     if (n_tri == 1)
         AGWN_TRY_CUDA(cudaMemcpyAsync(tri, bvh.tri, sizeof(T) * 9, cudaMemcpyDeviceToDevice, st));
@@ -694,8 +760,8 @@ int ray_hierarchy(Context& ctx, const Bvh& bvh, const T* dir_host)
             std::swap(ka, kb);
             std::swap(va, vb);
         }
-        k_leaves<T><<<g, 256, 0, st>>>(static_cast<const T*>(bvh.tri), va, box.as<float>(), n_tri, tri,
-                                       leafbox.as<float>());
+        k_leaves<T><<<g, 256, 0, st>>>(static_cast<const T*>(bvh.tri), va, box.as<float>(), n_tri, f, tri,
+                                       leafbox.as<float>(), static_cast<float*>(rc.leaf_uv.ptr));
         k_karras<<<gb, 256, 0, st>>>(ka, int(n_tri), left.as<int>(), right.as<int>(), pnode.as<int>(),
                                      pleaf.as<int>());
         k_refit<<<gb, 256, 0, st>>>(int(n_tri), left.as<int>(), right.as<int>(), pnode.as<int>(), pleaf.as<int>(),
@@ -738,11 +804,12 @@ int integer_run(Context& ctx, const Bvh& bvh, const T* d_pos, int64_t n, int32_t
     Frame32 f;
     for (int k = 0; k < 9; ++k)
         f.r[k] = ctx.ray_cache.frame[k];
-    int const block = 128;
+    int const block = kTravBlock;
     int const grid = int(std::min<int64_t>(div_up(n, block), int64_t(ctx.sm_count) * 16));
     AGWN_TRY(ctx.launch_begin(AGWN_K_INTEGER));
     k_traverse<T><<<grid, block, 0, ctx.stream>>>(static_cast<const BvhNode*>(ctx.ray_cache.nodes.ptr),
-                                                  static_cast<const T*>(ctx.ray_cache.tri.ptr), bvh.n_tri,
+                                                  static_cast<const T*>(ctx.ray_cache.tri.ptr),
+                                                  static_cast<const float4*>(ctx.ray_cache.leaf_uv.ptr), bvh.n_tri,
                                                   float(bvh.scene_scale), f, d_pos, n, d_counts, dir_host[0],
                                                   dir_host[1], dir_host[2], ctx.d_flags);
     return ctx.launch_end(AGWN_K_INTEGER);

@@ -118,8 +118,10 @@ extern "C" int agwn_mesh_batch_fractional_mixed_noalloc_f64(void* stream, const 
         AGWN_TRY_CUDA(cudaStreamSynchronize(st));
         return AGWN_OK;
     }
+    Context defaults; // option defaults only (no resources)
     Rot const rot = make_rotation(x0);
-    k_prep_mixed<<<1, 1024, 0, st>>>(boundary, n_segments, rot, &scr->frame, scr->seg, scr->seg64);
+    k_prep_mixed<<<1, 1024, 0, st>>>(boundary, n_segments, rot, float(defaults.mixed_tau), &scr->frame, scr->seg,
+                                     scr->seg64);
     AGWN_TRY_CUDA(cudaGetLastError());
 
     int const tile = int(std::min<int64_t>(kNoAllocTile, n_segments));
@@ -133,7 +135,6 @@ extern "C" int agwn_mesh_batch_fractional_mixed_noalloc_f64(void* stream, const 
     int64_t const per_tile = int64_t(kNoAllocBlock) * kNoAllocK;
     int64_t const n_qtiles = (n + per_tile - 1) / per_tile;
     int const grid = int(std::max<int64_t>(1, std::min<int64_t>(n_qtiles, int64_t(per_sm) * sm_count)));
-    Context defaults; // option defaults only (no resources)
     kern<<<grid, kNoAllocBlock, smem, st>>>(positions, n, out, nullptr, x0[0], x0[1], x0[2], rot, &scr->frame,
                                             float(defaults.mixed_tau), float(defaults.mixed_term_err), scr->seg,
                                             scr->seg64, n_segments, tile, scr->flags, scr->counters, 0);

@@ -2,6 +2,7 @@
 // fractional kernel's compute roofline (the kernel is bound by the FP32 pipe, not by HBM or tensor cores).
 
 #include "agwn_internal.cuh"
+#include "frac_kernels.cuh"
 
 namespace agwn
 {
@@ -64,5 +65,46 @@ extern "C" int agwn_probe_fp32_peak(agwn_context* ctx, double* tflops)
     cudaEventDestroy(e1);
     double const flops = 2.0 * kChains * double(iters) * double(grid) * 256.0;
     *tflops = flops / (double(best) * 1e-3) / 1e12;
+    return AGWN_OK;
+}
+
+namespace agwn
+{
+namespace
+{
+__global__ void k_atan2_pair(const float* __restrict__ y, const float* __restrict__ x, int64_t n,
+                             float* __restrict__ ours, float* __restrict__ ref)
+{
+    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+    {
+        ours[i] = atan2_fast(y[i], x[i]);
+        ref[i] = atan2f(y[i], x[i]);
+    }
+}
+} // namespace
+} // namespace agwn
+
+extern "C" int agwn_probe_atan2(agwn_context* ctx, const float* y, const float* x, int64_t n, float* ours, float* ref)
+{
+    AGWN_CHECK_ARG(ctx && n >= 0 && (n == 0 || (y && x && ours && ref)), "bad arguments");
+    AGWN_TRY_CUDA(cudaSetDevice(ctx->device));
+    if (n == 0)
+        return AGWN_OK;
+    const void *dy = nullptr, *dx = nullptr;
+    void *d_ours = nullptr, *d_ref = nullptr;
+    bool h1 = false, h2 = false;
+    AGWN_TRY(stage_in(*ctx, y, sizeof(float) * n, S_MISC0, &dy));
+    AGWN_TRY(stage_in(*ctx, x, sizeof(float) * n, S_MISC1, &dx));
+    AGWN_TRY(stage_out(*ctx, ours, sizeof(float) * n, S_MISC2, &d_ours, &h1));
+    AGWN_TRY(stage_out(*ctx, ref, sizeof(float) * n, S_MISC3, &d_ref, &h2));
+    k_atan2_pair<<<std::min<int64_t>(div_up(n, 256), 4 * ctx->sm_count), 256, 0, ctx->stream>>>(
+        static_cast<const float*>(dy), static_cast<const float*>(dx), n, static_cast<float*>(d_ours),
+        static_cast<float*>(d_ref));
+    AGWN_TRY_CUDA(cudaGetLastError());
+    if (h1)
+        AGWN_TRY_CUDA(cudaMemcpyAsync(ours, d_ours, sizeof(float) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    if (h2)
+        AGWN_TRY_CUDA(cudaMemcpyAsync(ref, d_ref, sizeof(float) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    AGWN_TRY_CUDA(cudaStreamSynchronize(ctx->stream));
     return AGWN_OK;
 }

@@ -194,3 +194,23 @@ def test_integer_term_along_many_directions(gwn, disp, oracle, dtype):
         c = np.empty(len(q), np.int32)
         gwn.eval_gwnr_mesh_batch_integer(disp, isect, q, c, d)
         assert np.array_equal(c, oracle.int_naive(q, d, verts, idx)), d
+
+
+def test_own_atan2_against_cuda_and_fp64(gwn, disp):
+    # the mixed kernel's float atan2 (octant reduction + minimax polynomial): max error within 6 ulp of the
+    # result, measured against FP64 atan2; CUDA's atan2f is shown alongside
+    rng = np.random.default_rng(17)
+    y = np.concatenate([rng.standard_normal(200_000), rng.uniform(-1, 1, 50_000) * 1e-6,
+                        [0.0, -0.0, 1.0, -1.0, 1e-30, 3.0]]).astype(np.float32)
+    x = np.concatenate([rng.standard_normal(200_000), rng.uniform(-1, 1, 50_000),
+                        [1.0, -1.0, 0.0, 0.0, -1.0, -1e-30]]).astype(np.float32)
+    ours = np.empty_like(y)
+    ref = np.empty_like(y)
+    assert gwn.library().agwn_probe_atan2(disp.handle, y.ctypes.data, x.ctypes.data, len(y), ours.ctypes.data,
+                                          ref.ctypes.data) == 0
+    exact = np.arctan2(y.astype(np.float64), x.astype(np.float64))
+    ulp = np.spacing(np.abs(exact).astype(np.float32)).astype(np.float64)
+    err_ours = np.abs(ours - exact) / ulp
+    err_cuda = np.abs(ref - exact) / ulp
+    assert np.max(err_ours) <= 6.0, np.max(err_ours)
+    assert np.max(err_cuda) <= 6.0
