@@ -114,8 +114,8 @@ class CudaDispatcher:
     have no device form here, and the library has no CPU fallback.
     """
 
-    def __init__(self, device: int = 0, stream=None, precision: str = "exact", tau: float = 8.0,
-                 term_err: float = 2e-8, queries_per_thread: int = 4, block: int = 256, seg_tile: int = 512,
+    def __init__(self, device: int = 0, stream=None, precision: str = "exact", tau: float = 4.0,
+                 term_err: float = 3e-8, queries_per_thread: int = 2, block: int = 128, seg_tile: int = 512,
                  timing: bool = False):
         lib = library()
         handle = None

@@ -104,10 +104,10 @@ struct Context
 
     // options
     int frac_mode = AGWN_FRAC_EXACT;
-    double mixed_tau = 8.0;
-    double mixed_term_err = 2e-8;
-    int queries_per_thread = 4;
-    int frac_block = 256;
+    double mixed_tau = 4.0;
+    double mixed_term_err = 3e-8;
+    int queries_per_thread = 2;
+    int frac_block = 128;
     int seg_tile = 512;
     int timing = 0;
 

@@ -285,12 +285,9 @@ __device__ __forceinline__ void two_sum_acc(float& acc, float& comp, float x)
 // atan2 for the FP32 terms, our own: reduce to t = min(|y|, |x|) / max(|y|, |x|) in [0, 1], evaluate
 // atan(t) = t * P(t^2) with a degree-8 polynomial P, then unfold the octant.  P's coefficients come from a
 // minimax fit of atan(t) / t on [0, 1] by the Remez exchange algorithm (relative error 1.5e-8 in exact arithmetic,
-// below float's 6e-8; about 3 ulp overall in float with the approximate division).
-__device__ __forceinline__ float atan2_fast(float y, float x)
+// below float's 6e-8; about 3 ulp overall in float with the approximate reciprocal).
+__device__ __forceinline__ float atan_unit(float t)
 {
-    float const ax = fabsf(x), ay = fabsf(y);
-    float const mx = fmaxf(ax, ay), mn = fminf(ax, ay);
-    float const t = __fdividef(mn, fmaxf(mx, 1e-37f));
     float const s = t * t;
     float p = 0.0028498897585520423f;
     p = fmaf(p, s, -0.01606862951374933f);
@@ -301,10 +298,21 @@ __device__ __forceinline__ float atan2_fast(float y, float x)
     p = fmaf(p, s, 0.1999261939280182f);
     p = fmaf(p, s, -0.3333307334510578f);
     p = fmaf(p, s, 0.9999999847657755f);
-    float a = t * p;
-    a = ay > ax ? 1.5707963267948966f - a : a;
+    return t * p;
+}
+// atan2(y, x) given |x| and |y| already divided by max(|x|, |y|) (so the larger is 1).
+__device__ __forceinline__ float atan2_scaled(float y, float x, float ax1, float ay1)
+{
+    float a = atan_unit(fminf(ax1, ay1));
+    a = ay1 > ax1 ? 1.5707963267948966f - a : a;
     a = x < 0.f ? 3.141592653589793f - a : a;
     return copysignf(a, y);
+}
+__device__ __forceinline__ float atan2_fast(float y, float x)
+{
+    float const ax = fabsf(x), ay = fabsf(y);
+    float const inv = __fdividef(1.f, fmaxf(fmaxf(ax, ay), 1e-37f));
+    return atan2_scaled(y, x, ax * inv, ay * inv);
 }
 
 // Per-warp queue of (query, segment) pairs that go to FP64: packed (segment << 8) | (lane << 3) | k.
@@ -354,8 +362,15 @@ __device__ __forceinline__ void fp64_flush(Fp64Queue<K>& q, unsigned c, int lane
     q.head += c;
 }
 
+// Blocks per SM the mixed kernel is compiled for: registers per thread scale with the queries per thread.
 template <int K>
-__global__ void __launch_bounds__(256) k_frac_mixed(const double* __restrict__ pos, int64_t n, double* __restrict__ out,
+constexpr int mixed_min_blocks()
+{
+    return K >= 8 ? 1 : (K >= 4 ? 2 : (K >= 2 ? 3 : 4));
+}
+
+template <int K>
+__global__ void __launch_bounds__(256, mixed_min_blocks<K>()) k_frac_mixed(const double* __restrict__ pos, int64_t n, double* __restrict__ out,
                                                     const int32_t* __restrict__ counts, double x0x, double x0y,
                                                     double x0z, Rot rot, const Frame* __restrict__ frame, float tau,
                                                     float term_err, const SegM* __restrict__ seg,
@@ -471,17 +486,26 @@ __global__ void __launch_bounds__(256) k_frac_mixed(const double* __restrict__ p
                     float const q1 = r1 + v1z * v1z;
                     float const l0 = q0 * rsqrtf(q0);
                     float const l1 = q1 * rsqrtf(q1);
-                    float const s0 = v0z >= 0.f ? l0 + v0z : __fdividef(r0, l0 - v0z);
-                    float const s1 = v1z >= 0.f ? l1 + v1z : __fdividef(r1, l1 - v1z);
+                    // l + z = n / d with (n, d) = (l + z, 1) for z >= 0 and (x^2 + y^2, l - z) for z < 0, free of
+                    // cancellation.  Scaling num and den by the positive D = d0 * d1 leaves the angle unchanged and
+                    // removes both divisions: den * D = n0 * n1 + (v0.x*v1.x + v0.y*v1.y) * D.
+                    float const n0 = v0z >= 0.f ? l0 + v0z : r0, d0 = v0z >= 0.f ? 1.f : l0 - v0z;
+                    float const n1 = v1z >= 0.f ? l1 + v1z : r1, d1 = v1z >= 0.f ? 1.f : l1 - v1z;
+                    float const D = d0 * d1, nn = n0 * n1;
                     float const pxy = v0x * v1x, pyy = v0y * v1y;
-                    float const ss = s0 * s1;
-                    float const den = ss + (pxy + pyy);
-                    // first-order rounding bounds of num and den (a few eps of the magnitudes summed)
-                    float const dn = kEpsBound * (fabsf(ta) + fabsf(tb));
-                    float const dd = kEpsBound * (ss + fabsf(pxy) + fabsf(pyy));
-                    bool const need = fminf(l0, l1) < B.w || !(q0 > 0.f && q1 > 0.f) ||
-                                      dn * fabsf(den) + dd * fabsf(num) > term_err * (num * num + den * den) ||
-                                      (den < 0.f && fabsf(num) <= dn);
+                    float const num_s = num * D;
+                    float const den_s = fmaf(pxy + pyy, D, nn);
+                    // first-order rounding bounds: num errs by about eps * sn and den by about eps * sd, so the angle
+                    // errs by at most eps * (sn * |den| + sd * |num|) / (num^2 + den^2).  With both divided by
+                    // M = max(|num|, |den|) (one reciprocal, reused by atan2) that is <= eps * (sn * ad1 + sd * an1) / M.
+                    float const sn = (fabsf(ta) + fabsf(tb)) * D;
+                    float const sd = fmaf(fabsf(pxy) + fabsf(pyy), D, nn);
+                    float const an = fabsf(num_s), ad = fabsf(den_s);
+                    float const inv = __fdividef(1.f, fmaxf(fmaxf(an, ad), 1e-37f));
+                    float const an1 = an * inv, ad1 = ad * inv;
+                    bool const need = fminf(l0, l1) < B.w || !(q0 > 0.f && q1 > 0.f) || !(nn + ad < INFINITY) ||
+                                      kEpsBound * fmaf(sn, ad1, sd * an1) * inv > term_err ||
+                                      (den_s < 0.f && an <= kEpsBound * sn);
                     unsigned const m = __ballot_sync(0xffffffffu, need);
                     if (m)
                     {
@@ -491,7 +515,7 @@ __global__ void __launch_bounds__(256) k_frac_mixed(const double* __restrict__ p
                         fq.tail += __popc(m);
                     }
                     if (!need)
-                        two_sum_acc(acc[k], comp[k], A.w * atan2_fast(num, den));
+                        two_sum_acc(acc[k], comp[k], A.w * atan2_scaled(num_s, den_s, ad1, an1));
                 }
                 // drain full batches: at most 31 + 32 * K entries stay queued, below the ring's capacity
                 while (fq.tail - fq.head >= 32)

@@ -66,18 +66,18 @@ enum agwn_option
     /* Fractional-term precision for double inputs: AGWN_FRAC_EXACT (default) or AGWN_FRAC_MIXED. */
     AGWN_OPT_FRAC_MODE = 0,
     /* Mixed mode: a (query, segment) pair whose nearer endpoint is closer than tau * segment length is
-       evaluated in FP64 with the reference arithmetic.  Default 8. */
+       evaluated in FP64 with the reference arithmetic.  Default 4. */
     AGWN_OPT_MIXED_TAU = 1,
-    /* Queries owned by each thread in the fractional kernels (1, 2, 4 or 8).  Default 4. */
+    /* Queries owned by each thread in the fractional kernels (1, 2, 4 or 8).  Default 2. */
     AGWN_OPT_QUERIES_PER_THREAD = 2,
-    /* Threads per block of the fractional kernels (64..256, a multiple of 32).  Default 256. */
+    /* Threads per block of the fractional kernels (64..256, a multiple of 32).  Default 128. */
     AGWN_OPT_FRAC_BLOCK = 3,
     /* Record CUDA events around the library's kernels and accumulate their device time (0/1).  Default 0. */
     AGWN_OPT_TIMING = 4,
     /* Segments per shared-memory tile of the fractional kernels (32..2048).  Default 512. */
     AGWN_OPT_SEG_TILE = 5,
     /* Mixed mode: a pair whose first-order FP32 error bound exceeds this many radians is evaluated in FP64.
-       Default 2e-8. */
+       Default 3e-8. */
     AGWN_OPT_MIXED_TERM_ERR = 6
 };
 enum agwn_frac_mode
