@@ -23,8 +23,9 @@ from . import _lib
 from ._lib import FRAC_EXACT, FRAC_MIXED, Stats
 
 __all__ = [
-    "GwnError", "CudaDispatcher", "CudaIntersector", "eval_gwnr_mesh_batch_fractional",
-    "eval_gwnr_mesh_batch_integer", "eval_gwnr_mesh_batch", "build_boundary_segments", "library",
+    "GwnError", "CudaDispatcher", "CudaIntersector", "CudaRobustMeshGwn", "eval_gwnr_mesh_batch_fractional",
+    "eval_gwnr_mesh_batch_integer", "eval_gwnr_mesh_batch", "eval_gwnr_mesh_batch_robust", "build_boundary_segments",
+    "library",
 ]
 
 
@@ -239,6 +240,79 @@ class CudaIntersector:
             pass
 
 
+class CudaRobustMeshGwn:
+    """RobustMeshGwn<T, Precision> (src/antipodal/gwn_mesh_robust.hh:170-424) on the device.
+
+    ``precision`` is "int64_grid", "int128_grid" or "exact_float"; None picks the reference's default
+    (int64_grid for float32 geometry, exact_float for float64).  Counts equal the reference's bit for bit.
+    """
+
+    POLICIES = {"int64_grid": 0, "int128_grid": 1, "exact_float": 2}
+
+    def __init__(self, dispatcher: CudaDispatcher, vertices, indices, boundary, precision: str | None = None):
+        dt = _dtype_of(vertices)
+        if dt not in (np.float64, np.float32):
+            raise TypeError("vertices must be float64 or float32")
+        self.dtype = dt
+        self.kind = "f64" if dt is np.float64 else "f32"
+        self.precision = precision or ("exact_float" if dt is np.float64 else "int64_grid")
+        v = _View(vertices, dt, 3, "vertices")
+        i = _View(indices, np.int32, None, "indices")
+        b = _View(boundary, dt, 7, "boundary")
+        h = C.c_void_p()
+        fn = getattr(library(), f"agwn_robust_create_{self.kind}")
+        _check(fn(dispatcher.handle, self.POLICIES[self.precision], v.ptr, v.n, i.ptr, i.n, b.ptr, b.n, C.byref(h)),
+               "agwn_robust_create")
+        self._h = h
+        self.dispatcher = dispatcher
+
+    @property
+    def handle(self):
+        if self._h is None:
+            raise RuntimeError("evaluator is closed")
+        return self._h
+
+    @staticmethod
+    def axis():
+        """The fixed ray direction of the integer term (gwn_mesh_robust.hh:226)."""
+        return np.array([-1.0, 0.0, 0.0])
+
+    def info(self) -> dict:
+        c = (C.c_double * 3)()
+        sc = C.c_double()
+        d = C.c_int32()
+        _check(library().agwn_robust_info(self.handle, C.cast(c, C.c_void_p), C.byref(sc), C.byref(d)),
+               "agwn_robust_info")
+        return {"center": list(c), "scale": sc.value, "depth": d.value}
+
+    def evaluate(self, positions, out=None, counts=None, fractional=None, dispatcher: CudaDispatcher | None = None):
+        """Full GWN per query (and optionally the integer count and the fractional term)."""
+        p = _View(positions, self.dtype, 3, "positions")
+        if out is None:
+            out = np.empty(p.n, self.dtype)
+        o = _View(out, self.dtype, None, "out", writable=True)
+        c = _View(counts, np.int32, None, "counts", writable=True) if counts is not None else None
+        f = _View(fractional, self.dtype, None, "fractional", writable=True) if fractional is not None else None
+        if o.n != p.n or (c and c.n != p.n) or (f and f.n != p.n):
+            raise ValueError("positions and outputs must have the same size")
+        fn = getattr(library(), f"agwn_robust_eval_{self.kind}")
+        d = dispatcher or self.dispatcher
+        _check(fn(d.handle, self.handle, p.ptr, p.n, o.ptr, c.ptr if c else None, f.ptr if f else None),
+               "agwn_robust_eval")
+        return out
+
+    def close(self):
+        if getattr(self, "_h", None) is not None:
+            library().agwn_robust_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 # --------------------------------------------------------------------------------------------------------------
 # batch functions (src/antipodal/gwn_mesh.hh)
 # --------------------------------------------------------------------------------------------------------------
@@ -306,3 +380,8 @@ def build_boundary_segments(vertices, indices) -> np.ndarray:
     from .synth import boundary_segments
     v = np.asarray(vertices)
     return boundary_segments(v, np.asarray(indices, np.int32)).astype(v.dtype)
+
+
+def eval_gwnr_mesh_batch_robust(dispatcher: CudaDispatcher, robust: CudaRobustMeshGwn, positions, out_wnrs):
+    """gwn_mesh_robust.hh:441-456: out_wnrs[i] = robust.eval(positions[i])."""
+    robust.evaluate(positions, out_wnrs, dispatcher=dispatcher)

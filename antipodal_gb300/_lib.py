@@ -52,6 +52,12 @@ SIGNATURES = {
     "agwn_mesh_batch_f64": (_I, [_P, _P, _P, _I64, _P, _P, _P, _I64]),
     "agwn_mesh_batch_f32": (_I, [_P, _P, _P, _I64, _P, _P, _P, _I64]),
     "agwn_mesh_batch_integer_bruteforce_f64": (_I, [_P, _P, _I64, _P, _I64, _P, _I64, _P, _P]),
+    "agwn_robust_create_f64": (_I, [_P, _I, _P, _I64, _P, _I64, _P, _I64, _PP]),
+    "agwn_robust_create_f32": (_I, [_P, _I, _P, _I64, _P, _I64, _P, _I64, _PP]),
+    "agwn_robust_destroy": (_I, [_P]),
+    "agwn_robust_info": (_I, [_P, _P, C.POINTER(_D), C.POINTER(C.c_int32)]),
+    "agwn_robust_eval_f64": (_I, [_P, _P, _P, _I64, _P, _P, _P]),
+    "agwn_robust_eval_f32": (_I, [_P, _P, _P, _I64, _P, _P, _P]),
     "agwn_probe_fp32_peak": (_I, [_P, C.POINTER(_D)]),
     "agwn_probe_atan2": (_I, [_P, _P, _P, _I64, _P, _P]),
 }

@@ -75,19 +75,33 @@ enum scratch_slot
     S_COUNT = 10
 };
 
-// A hierarchy over one intersector's triangles in the frame of one ray direction, cached per context
-// (see lbvh.cu).  Keyed by the intersector's generation number and the direction's bits.
+// A hierarchy over triangles in the frame of one ray direction (built by build_hier, lbvh.cu): internal nodes,
+// the triangles in leaf order, their projected (u, v) corners, the frame and the depth.
+struct Hier
+{
+    DevBuf nodes;
+    DevBuf tri;
+    DevBuf leaf_uv;
+    int32_t depth = 0;
+    int64_t n_tri = 0;
+    float frame[9] = {};
+    double scale = 1.0; // largest |coordinate| of the triangles
+    void release()
+    {
+        nodes.release();
+        tri.release();
+        leaf_uv.release();
+    }
+};
+
+// The hierarchy of one intersector along one direction, cached per context.  Keyed by the intersector's
+// generation number and the direction's bits.
 struct RayCache
 {
     unsigned long long generation = 0;
     double dir[3] = {0, 0, 0};
     int scalar_bytes = 0;
-    int32_t depth = 0;
-    int64_t n_tri = 0;
-    float frame[9] = {};
-    DevBuf nodes;
-    DevBuf tri;
-    DevBuf leaf_uv;
+    Hier h;
 };
 
 struct Context

@@ -271,9 +271,7 @@ int agwn_context_destroy(agwn_context* ctx)
         cudaStreamSynchronize(ctx->stream);
     for (auto& b : ctx->scratch)
         b.release();
-    ctx->ray_cache.nodes.release();
-    ctx->ray_cache.tri.release();
-    ctx->ray_cache.leaf_uv.release();
+    ctx->ray_cache.h.release();
     for (int i = 0; i < Context::kMaxPending; ++i)
     {
         if (ctx->ev_begin[i])

@@ -21,6 +21,7 @@
 
 #include "agwn_internal.cuh"
 #include "gwn_kernels.cuh"
+#include "hier.cuh"
 
 #include <algorithm>
 #include <atomic>
@@ -31,14 +32,7 @@ namespace agwn
 {
 namespace
 {
-// Internal node: boxes of both children in the ray frame, so one 64-byte fetch decides both.  lo_l.w / lo_r.w
-// hold the child codes as int bits: >= 0 an internal node, < 0 the leaf ~code.  Only the upper w bound is used.
-struct alignas(16) BvhNode
-{
-    float4 lo_l, hi_l, lo_r, hi_r;
-};
 
-constexpr int kStackDepth = 64;
 std::atomic<unsigned long long> g_generation{1};
 
 __device__ __forceinline__ unsigned expand_bits2(unsigned v)
@@ -90,18 +84,14 @@ __global__ void k_gather(const T* __restrict__ verts, int64_t nv, const int32_t*
         atomicMax(scale_bits, __float_as_uint(amax)); // non-negative floats order like their bits
 }
 
-struct Frame64
-{
-    double r[9]; // rows e1, e2, e3 (e3 = dir / |dir|)
-};
-
 // Per triangle: outward-rounded float box in the ray frame and its (u, v) centroid; (u, v) bounds of the
 // centroids as flipped-uint atomics.
 template <class T>
 __global__ void k_ray_boxes(const T* __restrict__ tri, int64_t n_tri, Frame64 f, float* __restrict__ box,
-                            float* __restrict__ cen, unsigned* __restrict__ cbounds)
+                            float* __restrict__ cen, unsigned* __restrict__ cbounds, unsigned* __restrict__ scale_bits)
 {
     float cmn[2] = {INFINITY, INFINITY}, cmx[2] = {-INFINITY, -INFINITY};
+    float amax = 0.f;
     for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; t < n_tri; t += int64_t(gridDim.x) * blockDim.x)
     {
         double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
@@ -120,6 +110,7 @@ __global__ void k_ray_boxes(const T* __restrict__ tri, int64_t n_tri, Frame64 f,
         {
             box[6 * t + r] = __double2float_rd(lo[r]);
             box[6 * t + 3 + r] = __double2float_ru(hi[r]);
+            amax = fmaxf(amax, fmaxf(fabsf(box[6 * t + r]), fabsf(box[6 * t + 3 + r])));
         }
         for (int r = 0; r < 2; ++r)
         {
@@ -135,12 +126,17 @@ __global__ void k_ray_boxes(const T* __restrict__ tri, int64_t n_tri, Frame64 f,
             cmn[r] = fminf(cmn[r], __shfl_xor_sync(0xffffffffu, cmn[r], o));
             cmx[r] = fmaxf(cmx[r], __shfl_xor_sync(0xffffffffu, cmx[r], o));
         }
+    for (int o = 16; o > 0; o >>= 1)
+        amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, o));
     if ((threadIdx.x & 31) == 0)
+    {
         for (int r = 0; r < 2; ++r)
         {
             atomicMin(cbounds + r, float_flip(cmn[r]));
             atomicMax(cbounds + 2 + r, float_flip(cmx[r]));
         }
+        atomicMax(scale_bits, __float_as_uint(amax)); // non-negative floats order like their bits
+    }
 }
 
 __global__ void k_morton2(const float* __restrict__ cen, int64_t n_tri, const unsigned* __restrict__ cbounds,
@@ -432,35 +428,6 @@ __device__ __forceinline__ int leaf_test(const T* __restrict__ tri, int leaf, ev
     return mt_sign(p, dir, a, b, c);
 }
 
-struct Frame32
-{
-    float r[9];
-};
-
-// Conservative float pre-test of a leaf: false only if the query's (u, v) point lies outside the projected
-// triangle by more than the rounding of every coordinate involved can explain, i.e. on the positive side of one
-// edge and the negative side of another, each by more than its margin.  `delta` bounds the absolute error of any
-// float (u, v) coordinate (the query's, rotated in float, and the vertices', rounded from FP64).  An edge function
-// e = du*rv - dv*ru then errs by at most 3*delta*(|du| + |dv| + |ru| + |rv|); the margin takes 8*delta.  The exact
-// Moller-Trumbore test decides every leaf that passes.
-__device__ __forceinline__ bool may_hit(const float4* __restrict__ leaf_uv, int leaf, float u, float v, float m8)
-{
-    float4 const a = leaf_uv[2 * leaf], b = leaf_uv[2 * leaf + 1];
-    float const pu[3] = {a.x, a.z, b.x}, pv[3] = {a.y, a.w, b.y};
-    bool pos = false, neg = false;
-#pragma unroll
-    for (int k = 0; k < 3; ++k)
-    {
-        int const k1 = (k + 1) % 3;
-        float const du = pu[k1] - pu[k], dv = pv[k1] - pv[k], ru = u - pu[k], rv = v - pv[k];
-        float const e = du * rv - dv * ru;
-        float const m = m8 * (fabsf(du) + fabsf(dv) + fabsf(ru) + fabsf(rv));
-        pos |= e > m;
-        neg |= e < -m;
-    }
-    return !(pos && neg);
-}
-
 // One query per thread.  The walk itself is float work only; the exact (FP64 for double input) leaf tests are
 // the expensive part, so candidate leaves that pass the float pre-test are collected during the walk and tested
 // after it: the lanes of a warp then run their j-th exact test together instead of one divergent lane at a time
@@ -494,71 +461,22 @@ __global__ void __launch_bounds__(kTravBlock) k_traverse(const BvhNode* __restri
             float const w = f.r[6] * ox + f.r[7] * oy + f.r[8] * oz;
             float const qmax = fmaxf(fmaxf(fabsf(ox), fabsf(oy)), fabsf(oz));
             float const tol = (qmax + scene_scale) * 3.8146973e-6f + 1e-30f; // 2^-18 of the coordinate scale
-            float const ulo = u + tol, uhi = u - tol, vlo = v + tol, vhi = v - tol, wq = w - tol;
             float const m8 = 8.0f * 1e-6f * (qmax + scene_scale);            // 8 * delta of may_hit
             int cand[kCand];
             int nc = 0;
-            int stack[kStackDepth];
-            int sp = 0;
-            int node = 0;
-            while (true)
-            {
-                BvhNode const nd = nodes[node];
-                int const lc = __float_as_int(nd.lo_l.w), rc = __float_as_int(nd.lo_r.w);
-                bool const hl = nd.lo_l.x <= ulo && nd.hi_l.x >= uhi && nd.lo_l.y <= vlo && nd.hi_l.y >= vhi &&
-                                nd.hi_l.z >= wq;
-                bool const hr = nd.lo_r.x <= ulo && nd.hi_r.x >= uhi && nd.lo_r.y <= vlo && nd.hi_r.y >= vhi &&
-                                nd.hi_r.z >= wq;
-                int next = -1;
-                if (hl)
-                {
-                    if (lc >= 0)
-                        next = lc;
-                    else if (may_hit(leaf_uv, ~lc, u, v, m8))
-                    {
-                        if (nc == kCand)
-                        {
-                            for (int j = 0; j < kCand; ++j)
-                                sum += leaf_test<T>(tri, cand[j], p, dir);
-                            nc = 0;
-                        }
-                        cand[nc++] = ~lc;
-                    }
-                }
-                if (hr)
-                {
-                    if (rc < 0)
-                    {
-                        if (may_hit(leaf_uv, ~rc, u, v, m8))
-                        {
-                            if (nc == kCand)
-                            {
-                                for (int j = 0; j < kCand; ++j)
-                                    sum += leaf_test<T>(tri, cand[j], p, dir);
-                                nc = 0;
-                            }
-                            cand[nc++] = ~rc;
-                        }
-                    }
-                    else if (next < 0)
-                        next = rc;
-                    else
-                    {
-                        if (sp == kStackDepth)
-                        {
-                            atomicOr(flags + FLAG_STACK, 1);
-                            break;
-                        }
-                        stack[sp++] = rc;
-                    }
-                }
-                if (next >= 0)
-                    node = next;
-                else if (sp > 0)
-                    node = stack[--sp];
-                else
-                    break;
-            }
+            bool const ok = hier_walk(nodes, leaf_uv, u, v, w, tol, m8,
+                                      [&](int leaf)
+                                      {
+                                          if (nc == kCand)
+                                          {
+                                              for (int j = 0; j < kCand; ++j)
+                                                  sum += leaf_test<T>(tri, cand[j], p, dir);
+                                              nc = 0;
+                                          }
+                                          cand[nc++] = leaf;
+                                      });
+            if (!ok)
+                atomicOr(flags + FLAG_STACK, 1);
             for (int j = 0; j < nc; ++j)
                 sum += leaf_test<T>(tri, cand[j], p, dir);
         }
@@ -670,7 +588,8 @@ int bvh_make(Context& ctx, const T* vertices, int64_t nv, const int32_t* indices
     return AGWN_OK;
 }
 
-// Orthonormal frame whose third row is dir / |dir|.
+} // namespace
+
 Frame64 ray_frame(const double* dir)
 {
     double const nn = std::sqrt(dir[0] * dir[0] + dir[1] * dir[1] + dir[2] * dir[2]);
@@ -696,29 +615,26 @@ Frame64 ray_frame(const double* dir)
     return f;
 }
 
-// The hierarchy of `bvh` in the frame of `dir`, built into ctx.ray_cache unless it is already there.
 template <class T>
-int ray_hierarchy(Context& ctx, const Bvh& bvh, const T* dir_host)
+int build_hier(Context& ctx, const T* tri_in, int64_t n_tri, const double* dir, Hier& out, unsigned* order_out)
 {
-    RayCache& rc = ctx.ray_cache;
-    double const dir[3] = {double(dir_host[0]), double(dir_host[1]), double(dir_host[2])};
-    if (rc.generation == bvh.generation && rc.scalar_bytes == bvh.scalar_bytes &&
-        std::memcmp(rc.dir, dir, sizeof(dir)) == 0)
-        return AGWN_OK;
     double const nn = dir[0] * dir[0] + dir[1] * dir[1] + dir[2] * dir[2];
     AGWN_CHECK_ARG(nn > 0 && std::isfinite(nn), "ray direction must be finite and nonzero");
-    int64_t const n_tri = bvh.n_tri;
     cudaStream_t const st = ctx.stream;
-    rc.generation = 0; // invalid until the build completes
     Frame64 const f = ray_frame(dir);
-    AGWN_TRY_CUDA(cudaStreamSynchronize(st)); // the cache buffers may still be read by queued traversals
-    AGWN_TRY(rc.tri.reserve(sizeof(T) * 9 * n_tri));
-    AGWN_TRY(rc.nodes.reserve(sizeof(BvhNode) * std::max<int64_t>(1, n_tri - 1)));
-    AGWN_TRY(rc.leaf_uv.reserve(sizeof(float) * 8 * n_tri));
-    T* tri = static_cast<T*>(rc.tri.ptr);
+    AGWN_TRY_CUDA(cudaStreamSynchronize(st)); // the buffers may still be read by queued traversals
+    AGWN_TRY(out.tri.reserve(sizeof(T) * 9 * std::max<int64_t>(1, n_tri)));
+    AGWN_TRY(out.nodes.reserve(sizeof(BvhNode) * std::max<int64_t>(1, n_tri - 1)));
+    AGWN_TRY(out.leaf_uv.reserve(sizeof(float) * 8 * std::max<int64_t>(1, n_tri)));
+    T* tri = static_cast<T*>(out.tri.ptr);
+    int32_t depth = n_tri > 0 ? 1 : 0;
+    unsigned scale_bits = 0;
     if (n_tri == 1)
-        AGWN_TRY_CUDA(cudaMemcpyAsync(tri, bvh.tri, sizeof(T) * 9, cudaMemcpyDeviceToDevice, st));
-    int32_t depth = 1;
+    {
+        AGWN_TRY_CUDA(cudaMemcpyAsync(tri, tri_in, sizeof(T) * 9, cudaMemcpyDeviceToDevice, st));
+        if (order_out)
+            AGWN_TRY_CUDA(cudaMemsetAsync(order_out, 0, sizeof(unsigned), st));
+    }
     if (n_tri > 1)
     {
         Tmp box, cen, misc, keys0, vals0, keys1, vals1, hist, left, right, pnode, pleaf, nbox, visit, leafbox;
@@ -738,14 +654,15 @@ int ray_hierarchy(Context& ctx, const Bvh& bvh, const T* dir_host)
         AGWN_TRY(nbox.alloc(sizeof(float) * 6 * n_tri));
         AGWN_TRY(visit.alloc(sizeof(int) * n_tri));
         AGWN_TRY(leafbox.alloc(sizeof(float) * 6 * n_tri));
-        unsigned init[8] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0u, 0u, 0u, 0u, 0u, 0u}; // (u, v) min, (u, v) max, -, depth
+        // (u, v) min, (u, v) max, largest |coordinate| bits, -, -, depth
+        unsigned init[8] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0u, 0u, 0u, 0u, 0u, 0u};
         AGWN_TRY_CUDA(cudaMemcpyAsync(misc.p, init, sizeof(init), cudaMemcpyHostToDevice, st));
         AGWN_TRY_CUDA(cudaMemsetAsync(visit.p, 0, sizeof(int) * n_tri, st));
         int const g = std::min(div_up(n_tri, 256), 8 * ctx.sm_count);
         int const gb = div_up(n_tri, 256);
         AGWN_TRY(ctx.launch_begin(AGWN_K_OTHER));
-        k_ray_boxes<T><<<g, 256, 0, st>>>(static_cast<const T*>(bvh.tri), n_tri, f, box.as<float>(), cen.as<float>(),
-                                          misc.as<unsigned>());
+        k_ray_boxes<T><<<g, 256, 0, st>>>(tri_in, n_tri, f, box.as<float>(), cen.as<float>(), misc.as<unsigned>(),
+                                          misc.as<unsigned>() + 4);
         k_morton2<<<g, 256, 0, st>>>(cen.as<float>(), n_tri, misc.as<unsigned>(), keys0.as<unsigned>(),
                                      vals0.as<unsigned>());
         unsigned *ka = keys0.as<unsigned>(), *va = vals0.as<unsigned>(), *kb = keys1.as<unsigned>(),
@@ -760,32 +677,57 @@ int ray_hierarchy(Context& ctx, const Bvh& bvh, const T* dir_host)
             std::swap(ka, kb);
             std::swap(va, vb);
         }
-        k_leaves<T><<<g, 256, 0, st>>>(static_cast<const T*>(bvh.tri), va, box.as<float>(), n_tri, f, tri,
-                                       leafbox.as<float>(), static_cast<float*>(rc.leaf_uv.ptr));
+        k_leaves<T><<<g, 256, 0, st>>>(tri_in, va, box.as<float>(), n_tri, f, tri, leafbox.as<float>(),
+                                       static_cast<float*>(out.leaf_uv.ptr));
         k_karras<<<gb, 256, 0, st>>>(ka, int(n_tri), left.as<int>(), right.as<int>(), pnode.as<int>(),
                                      pleaf.as<int>());
         k_refit<<<gb, 256, 0, st>>>(int(n_tri), left.as<int>(), right.as<int>(), pnode.as<int>(), pleaf.as<int>(),
                                     leafbox.as<float>(), nbox.as<float>(), visit.as<int>(),
-                                    static_cast<BvhNode*>(rc.nodes.ptr));
+                                    static_cast<BvhNode*>(out.nodes.ptr));
         k_depth<<<gb, 256, 0, st>>>(int(n_tri), pnode.as<int>(), pleaf.as<int>(),
                                     reinterpret_cast<int*>(misc.as<unsigned>() + 7));
         AGWN_TRY(ctx.launch_end(AGWN_K_OTHER));
+        if (order_out)
+            AGWN_TRY_CUDA(cudaMemcpyAsync(order_out, va, sizeof(unsigned) * n_tri, cudaMemcpyDeviceToDevice, st));
         unsigned back[8];
         AGWN_TRY_CUDA(cudaMemcpyAsync(back, misc.p, sizeof(back), cudaMemcpyDeviceToHost, st));
         AGWN_TRY_CUDA(cudaStreamSynchronize(st));
         depth = int32_t(back[7]);
+        scale_bits = back[4];
         if (depth > n_tri)
             return fail(AGWN_ERR_CUDA, "hierarchy build produced a broken parent chain (depth %d for %lld triangles)",
                         depth, (long long)n_tri);
     }
+    float scale = 0.f;
+    std::memcpy(&scale, &scale_bits, sizeof(float));
     for (int k = 0; k < 9; ++k)
-        rc.frame[k] = float(f.r[k]);
+        out.frame[k] = float(f.r[k]);
+    out.depth = depth;
+    out.n_tri = n_tri;
+    out.scale = scale;
+    return AGWN_OK;
+}
+
+template int build_hier<double>(Context&, const double*, int64_t, const double*, Hier&, unsigned*);
+template int build_hier<float>(Context&, const float*, int64_t, const double*, Hier&, unsigned*);
+
+namespace
+{
+// The hierarchy of `bvh` in the frame of `dir`, built into ctx.ray_cache unless it is already there.
+template <class T>
+int ray_hierarchy(Context& ctx, const Bvh& bvh, const T* dir_host)
+{
+    RayCache& rc = ctx.ray_cache;
+    double const dir[3] = {double(dir_host[0]), double(dir_host[1]), double(dir_host[2])};
+    if (rc.generation == bvh.generation && rc.scalar_bytes == bvh.scalar_bytes &&
+        std::memcmp(rc.dir, dir, sizeof(dir)) == 0)
+        return AGWN_OK;
+    rc.generation = 0; // invalid until the build completes
+    AGWN_TRY(build_hier<T>(ctx, static_cast<const T*>(bvh.tri), bvh.n_tri, dir, rc.h, nullptr));
     std::memcpy(rc.dir, dir, sizeof(dir));
     rc.scalar_bytes = bvh.scalar_bytes;
-    rc.n_tri = n_tri;
-    rc.depth = depth;
     rc.generation = bvh.generation;
-    bvh.depth = depth;
+    bvh.depth = rc.h.depth;
     return AGWN_OK;
 }
 } // namespace
@@ -803,13 +745,13 @@ int integer_run(Context& ctx, const Bvh& bvh, const T* d_pos, int64_t n, int32_t
     AGWN_TRY(ray_hierarchy<T>(ctx, bvh, dir_host));
     Frame32 f;
     for (int k = 0; k < 9; ++k)
-        f.r[k] = ctx.ray_cache.frame[k];
+        f.r[k] = ctx.ray_cache.h.frame[k];
     int const block = kTravBlock;
     int const grid = int(std::min<int64_t>(div_up(n, block), int64_t(ctx.sm_count) * 16));
     AGWN_TRY(ctx.launch_begin(AGWN_K_INTEGER));
-    k_traverse<T><<<grid, block, 0, ctx.stream>>>(static_cast<const BvhNode*>(ctx.ray_cache.nodes.ptr),
-                                                  static_cast<const T*>(ctx.ray_cache.tri.ptr),
-                                                  static_cast<const float4*>(ctx.ray_cache.leaf_uv.ptr), bvh.n_tri,
+    k_traverse<T><<<grid, block, 0, ctx.stream>>>(static_cast<const BvhNode*>(ctx.ray_cache.h.nodes.ptr),
+                                                  static_cast<const T*>(ctx.ray_cache.h.tri.ptr),
+                                                  static_cast<const float4*>(ctx.ray_cache.h.leaf_uv.ptr), bvh.n_tri,
                                                   float(bvh.scene_scale), f, d_pos, n, d_counts, dir_host[0],
                                                   dir_host[1], dir_host[2], ctx.d_flags);
     return ctx.launch_end(AGWN_K_INTEGER);

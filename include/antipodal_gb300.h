@@ -150,6 +150,36 @@ int agwn_mesh_batch_integer_bruteforce_f64(agwn_context* ctx, const double* vert
                                            const int32_t* indices, int64_t n_indices, const double* positions,
                                            int64_t n, int32_t* out_counts, const double* dir);
 
+/* ---- robust mesh GWN ---------------------------------------------------------------------------------------
+ * Replaces RobustMeshGwn<T, Precision> (src/antipodal/gwn_mesh_robust.hh:170-424) and eval_gwnr_mesh_batch_robust
+ * (:441-456): fractional and integer terms along the fixed -x ray, both decided by one exact predicate
+ * (src/antipodal/math/robust_predicates.hh).  The evaluator owns device copies of the quantised (or, for
+ * exact_float, double) triangles and swapped boundary, and a hierarchy that replaces Embree's traversal; the
+ * caller's arrays need not outlive it.  Counts equal the reference's bit for bit; the fractional term matches it
+ * up to the last bits of atan2.  Precision policy: */
+enum agwn_robust_policy
+{
+    AGWN_ROBUST_INT64_GRID = 0,  /* 20-bit grid, 64-bit determinants (the reference's default for float)     */
+    AGWN_ROBUST_INT128_GRID = 1, /* 50-bit grid, 128-bit determinants                                        */
+    AGWN_ROBUST_EXACT_FLOAT = 2  /* double coordinates, exact determinant signs (the default for double)     */
+};
+typedef struct agwn_robust agwn_robust;
+int agwn_robust_create_f64(agwn_context* ctx, int policy, const double* vertices, int64_t n_vertices,
+                           const int32_t* indices, int64_t n_indices, const double* boundary, int64_t n_segments,
+                           agwn_robust** out);
+int agwn_robust_create_f32(agwn_context* ctx, int policy, const float* vertices, int64_t n_vertices,
+                           const int32_t* indices, int64_t n_indices, const float* boundary, int64_t n_segments,
+                           agwn_robust** out);
+int agwn_robust_destroy(agwn_robust* robust);
+/* Quantisation centre (3 doubles) and scale, and the hierarchy depth. */
+int agwn_robust_info(const agwn_robust* robust, double* center, double* scale, int32_t* depth);
+/* out_gwn[i] = RobustMeshGwn::eval(p_i); optional out_counts[i] = signed_intersection_count(p_i) and
+ * out_frac[i] = fractional(p_i) (either may be NULL). */
+int agwn_robust_eval_f64(agwn_context* ctx, const agwn_robust* robust, const double* positions, int64_t n,
+                         double* out_gwn, int32_t* out_counts, double* out_frac);
+int agwn_robust_eval_f32(agwn_context* ctx, const agwn_robust* robust, const float* positions, int64_t n,
+                         float* out_gwn, int32_t* out_counts, float* out_frac);
+
 /* ---- mixed-precision fractional term without allocation --------------------------------------------------
  * No counterpart in the reference.  For callers that cannot allocate device memory -- a program whose own pool
  * allocator owns the GPU's memory budget, or a plugin inside a framework whose allocator must not be bypassed --

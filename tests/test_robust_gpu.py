@@ -1,0 +1,102 @@
+"""Parity of the device robust evaluator (RobustMeshGwn) with the reference and the oracle.
+
+Golden fixtures are outputs of the reference's own RobustMeshGwn (compiled here with the project's fake Embree
+backend) on the meshes and queries of test/test_gwn_mesh_robust.cc; counts must match bit for bit under every
+(scalar, policy), the fractional term and the full GWN up to atan2's last bits (1e-12 double, 1e-6 float).
+"""
+
+import os
+
+import numpy as np
+import pytest
+
+from antipodal_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "reference_golden.npz")
+POLICIES = ["int64_grid", "int128_grid", "exact_float"]
+
+
+@pytest.fixture(scope="module")
+def golden():
+    return np.load(GOLDEN)
+
+
+def run(gwn, disp, pol, v, i, b, q):
+    r = gwn.CudaRobustMeshGwn(disp, v, i, b, precision=pol)
+    out = np.empty(len(q), q.dtype)
+    cnt = np.empty(len(q), np.int32)
+    fr = np.empty(len(q), q.dtype)
+    r.evaluate(q, out, cnt, fr)
+    r.close()
+    return out, cnt, fr
+
+
+@pytest.mark.parametrize("pol", POLICIES)
+@pytest.mark.parametrize("dt,tag,tol", [(np.float64, "f64", 1e-12), (np.float32, "f32", 1e-6)])
+def test_robust_matches_reference_golden(gwn, disp, golden, pol, dt, tag, tol):
+    names = sorted({k.split("_f64_")[0][len("robust_"):] for k in golden.files if k.startswith("robust_") and "_f64_" in k})
+    for name in names:
+        v, i, q = golden[f"robust_{name}_verts"], golden[f"robust_{name}_idx"], golden[f"robust_{name}_queries"]
+        b = synth.boundary_segments(v, i)
+        g, c, f = run(gwn, disp, pol, v.astype(dt), i, b.astype(dt), q.astype(dt))
+        assert np.array_equal(c, golden[f"robust_{name}_{tag}_{pol}_count"]), name
+        np.testing.assert_allclose(f, golden[f"robust_{name}_{tag}_{pol}_frac"], rtol=0, atol=tol, err_msg=name)
+        np.testing.assert_allclose(g, golden[f"robust_{name}_{tag}_{pol}_gwn"], rtol=0, atol=tol, err_msg=name)
+
+
+@pytest.mark.parametrize("pol", POLICIES)
+def test_robust_matches_oracle_on_noisy_open_mesh(gwn, disp, oracle, pol):
+    # an open icosphere (level 4) with queries everywhere, including 1e-9 .. 1e-3 from the surface
+    v, idx, b, _, _ = synth.open_icosphere(seed=11, level=4, grid=0)
+    rng = np.random.default_rng(11)
+    q_far = rng.uniform(-1.4, 1.4, size=(3000, 3))
+    t = rng.integers(len(idx) // 3, size=2000)
+    tri = v[idx.reshape(-1, 3)[t]]
+    bary = rng.dirichlet([1, 1, 1], size=len(t))
+    p = np.einsum("ij,ijk->ik", bary, tri)
+    n = np.cross(tri[:, 1] - tri[:, 0], tri[:, 2] - tri[:, 0])
+    n /= np.linalg.norm(n, axis=1, keepdims=True)
+    d = 10 ** rng.uniform(-9, -3, size=len(t)) * rng.choice([-1.0, 1.0], size=len(t))
+    q = np.concatenate([q_far, p + d[:, None] * n])
+    g, c, f = run(gwn, disp, pol, v, idx, b, q)
+    rg, rc, rf = oracle.robust_eval(pol, v, idx, b, q)
+    assert np.array_equal(c, rc)
+    assert np.max(np.abs(f - rf)) <= 1e-12
+    assert np.max(np.abs(g - rg)) <= 1e-12
+
+
+def test_robust_grazing_sweep_is_smooth(gwn, disp):
+    # test/test_gwn_mesh_robust.cc:224-287: across a grazed edge the robust GWN does not jump
+    v = np.array([[0, 0, 0], [0, 1, 0], [0, 0, 1]], np.float64)
+    i = np.array([0, 1, 2], np.int32)
+    q = np.array([[100.0, 0.7 - 5e-7 + 1e-6 * k / 1000.0, 0.3] for k in range(1001)])
+    for pol in POLICIES:
+        g, _, _ = run(gwn, disp, pol, v, i, synth.boundary_segments(v, i), q)
+        assert np.max(np.abs(np.diff(g))) < 0.1
+
+
+def test_robust_two_tori_small(gwn, disp, oracle):
+    # a small version of the robust stress input: two interpenetrating perturbed tori with holes
+    v, idx, b, q = synth.two_tori(seed=4, n_tris=20_000, n_holes=6, n_queries=6000)
+    for pol in ("int128_grid", "exact_float"):
+        g, c, f = run(gwn, disp, pol, v, idx, b, q)
+        rg, rc, rf = oracle.robust_eval(pol, v, idx, b, q)
+        assert np.array_equal(c, rc), pol
+        assert np.max(np.abs(g - rg)) <= 1e-11, pol
+
+
+def test_robust_empty_and_device_inputs(gwn, disp):
+    torch = pytest.importorskip("torch")
+    v, i = synth.CUBE_VERTS, synth.CUBE_IDX_CLOSED
+    q = synth.SAMPLE_POINTS
+    g, c, _ = run(gwn, disp, "exact_float", v, i, np.zeros((0, 7)), q)
+    assert np.array_equal(c, np.rint(g).astype(np.int32))
+    dev = torch.device("cuda:0")
+    with gwn.CudaDispatcher(stream=torch.cuda.current_stream(dev)) as d:
+        r = gwn.CudaRobustMeshGwn(d, torch.from_numpy(v).to(dev), torch.from_numpy(i).to(dev),
+                                  torch.zeros((0, 7), dtype=torch.float64, device=dev))
+        out = torch.empty(len(q), dtype=torch.float64, device=dev)
+        gwn.eval_gwnr_mesh_batch_robust(d, r, torch.from_numpy(q).to(dev), out)
+        d.synchronize()
+        assert np.array_equal(out.cpu().numpy(), g)
