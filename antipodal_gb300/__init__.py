@@ -25,7 +25,7 @@ from ._lib import FRAC_EXACT, FRAC_MIXED, Stats
 __all__ = [
     "GwnError", "CudaDispatcher", "CudaIntersector", "CudaRobustMeshGwn", "eval_gwnr_mesh_batch_fractional",
     "eval_gwnr_mesh_batch_integer", "eval_gwnr_mesh_batch", "eval_gwnr_mesh_batch_robust", "build_boundary_segments",
-    "library",
+    "IntegrateConfig", "IntegratorGK15", "eval_gwnr_parametric_batch_fractional", "unpack_pair_stats", "library",
 ]
 
 
@@ -57,7 +57,10 @@ def _is_torch(a) -> bool:
 def _dtype_of(a):
     if _is_torch(a):
         import torch
-        return {torch.float64: np.float64, torch.float32: np.float32, torch.int32: np.int32}.get(a.dtype)
+        table = {torch.float64: np.float64, torch.float32: np.float32, torch.int32: np.int32, torch.uint8: np.uint8}
+        if hasattr(torch, "uint32"):
+            table[torch.uint32] = np.uint32
+        return table.get(a.dtype)
     return np.asarray(a).dtype.type
 
 
@@ -385,3 +388,66 @@ def build_boundary_segments(vertices, indices) -> np.ndarray:
 def eval_gwnr_mesh_batch_robust(dispatcher: CudaDispatcher, robust: CudaRobustMeshGwn, positions, out_wnrs):
     """gwn_mesh_robust.hh:441-456: out_wnrs[i] = robust.eval(positions[i])."""
     robust.evaluate(positions, out_wnrs, dispatcher=dispatcher)
+
+
+# --------------------------------------------------------------------------------------------------------------
+# parametric surfaces (src/antipodal/gwn_parametric.hh)
+# --------------------------------------------------------------------------------------------------------------
+class IntegrateConfig:
+    """integrate_config (src/antipodal/math/integrate.hh:11-22): min_depth, max_depth, tol (halved per level)."""
+
+    def __init__(self, min_depth: int = 0, max_depth: int = 10, tol: float = 1e-6):
+        self.min_depth, self.max_depth, self.tol = int(min_depth), int(max_depth), float(tol)
+
+    def __repr__(self):
+        return f"IntegrateConfig(min_depth={self.min_depth}, max_depth={self.max_depth}, tol={self.tol:g})"
+
+
+class IntegratorGK15:
+    """The plain adaptive G7-K15 integrator (src/antipodal/math/integrate_gk15.hh:63-290), run on the device."""
+
+    def start_depths(self, dispatcher, positions, x0, curves, cfg):
+        return None
+
+
+def unpack_pair_stats(stats):
+    """Split agwn_param_batch_fractional_bezier3_f64's packed per-pair stats into (leaves, shallowest leaf depth,
+    deepest leaf depth)."""
+    s = np.asarray(stats.cpu() if _is_torch(stats) else stats).astype(np.uint32)
+    return (s & 0xFFFF).astype(np.int32), ((s >> 16) & 0xFF).astype(np.int32), (s >> 24).astype(np.int32)
+
+
+def eval_gwnr_parametric_batch_fractional(dispatcher: CudaDispatcher, positions, out_wnrs, x0, curves,
+                                          cfg: IntegrateConfig | None = None, integrator=None, *, start_depth=None,
+                                          pair_stats=None, nodes_per_query=None):
+    """gwn_parametric.hh:168-186 for boundaries of cubic Bezier curves: out_wnrs[i] = (sum over curves of the
+    adaptive GK15 integral of w - d_eta over [0, 1]) / (4 pi).
+
+    curves: (c, 12) or (c, 4, 3) float64 control points, in the order for_each_boundary visits them.
+    integrator: IntegratorGK15 (default, the plain method) or an object with a start_depths(...) method returning
+    per-(query, curve) start depths (the learned proposal); start_depth may also be given directly as an
+    (n, c) uint8 array.  pair_stats (n, c) uint32 and nodes_per_query (n,) int32 are optional outputs."""
+    cfg = cfg or IntegrateConfig()
+    p = _View(positions, np.float64, 3, "positions")
+    o = _View(out_wnrs, np.float64, None, "out_wnrs", writable=True)
+    if p.n != o.n:
+        raise ValueError("positions and out_wnrs must have the same size")
+    c = _View(curves, np.float64, 12, "curves")
+    if start_depth is None and integrator is not None:
+        start_depth = integrator.start_depths(dispatcher, positions, x0, curves, cfg)
+    sd = _View(start_depth, np.uint8, None, "start_depth") if start_depth is not None else None
+    if sd is not None and sd.n != p.n * c.n:
+        raise ValueError("start_depth must hold one byte per (query, curve) pair")
+    st = _View(pair_stats, np.uint32, None, "pair_stats", writable=True) if pair_stats is not None else None
+    if st is not None and st.n != p.n * c.n:
+        raise ValueError("pair_stats must hold one entry per (query, curve) pair")
+    nd = _View(nodes_per_query, np.int32, None, "nodes_per_query", writable=True) \
+        if nodes_per_query is not None else None
+    if nd is not None and nd.n != p.n:
+        raise ValueError("nodes_per_query must hold one entry per query")
+    _, xp = x = _vec3(x0, np.float64)
+    fn = library().agwn_param_batch_fractional_bezier3_f64
+    _check(fn(dispatcher.handle, p.ptr, p.n, o.ptr, xp, c.ptr, c.n, cfg.min_depth, cfg.max_depth, cfg.tol,
+              sd.ptr if sd else None, st.ptr if st else None, nd.ptr if nd else None),
+           "eval_gwnr_parametric_batch_fractional")
+    del x

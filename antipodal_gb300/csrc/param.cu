@@ -1,0 +1,365 @@
+// Parametric fractional GWN over cubic Bezier boundary curves with adaptive G7-K15 quadrature:
+// eval_gwnr_parametric_batch_fractional (src/antipodal/gwn_parametric.hh:168-186) with IntegratorGK15
+// (src/antipodal/math/integrate_gk15.hh:63-290) and the integrand of gwn_parametric.hh:73-103.
+//
+// One thread per query walks the curves in order (curves staged in shared memory by cp.async.bulk) and
+// integrates each with an explicit stack instead of recursion.  A panel is (depth, index): its end points are the
+// dyadic numbers index * 2^-depth and its local tolerance tol * 2^-depth, exactly what the reference's halving
+// computes, so a panel fits in 32 bits.  A second stack of values replays the reference's `left + right`
+// summation order (post-order), and the integrand and the G7/K15 sums are written unfused, so the result equals
+// the CPU reference bit for bit.
+//
+// Proposal hook: a per-(query, curve) start depth s (from the learned proposal; 0 for the plain method).  Panels
+// above depth s are split without being evaluated; every panel at depth >= s is evaluated and accepted or split by
+// the reference's own rule.  When s does not exceed the shallowest leaf the plain method would accept, the two
+// produce the same leaves and the same value; a larger s only refines further.
+
+#include "agwn_internal.cuh"
+#include "tma.cuh"
+
+#include <cmath>
+
+namespace agwn
+{
+namespace
+{
+constexpr int kParamMaxDepth = 24; // deepest panel the integrator can reach (2^24 panels per curve)
+constexpr int kParamBlock = 128;
+constexpr int kParamTileMax = 1024; // curves staged per tile (96 KB of shared memory)
+
+struct alignas(16) Bez
+{
+    double c[12];
+};
+
+// G7-K15 abscissae and weights: the published Gauss-Kronrod constants at the precision the reference carries
+// (integrate_gk15.hh:13-36); identical doubles make the sums identical.
+__constant__ double kGkX[8] = {0.0,
+                               0.9914553711208126,
+                               0.9491079123427585,
+                               0.8648644233597691,
+                               0.7415311855993945,
+                               0.5860872354676911,
+                               0.4058451513773972,
+                               0.2077849550078985};
+__constant__ double kGkWk[8] = {0.2094821410847278, 0.0229353220105292, 0.0630920926299786, 0.1047900103222502,
+                                0.1406532597155259, 0.1690047266392679, 0.1903505780647854, 0.2044329400752989};
+constexpr double kGkWgCenter = 0.4179591836734694;
+constexpr double kGkWg2 = 0.1294849661688697;
+constexpr double kGkWg4 = 0.2797053914892767;
+constexpr double kGkWg6 = 0.3818300505051189;
+
+struct dual
+{
+    rd v, d;
+};
+__device__ __forceinline__ dual dmul(dual a, dual b)
+{
+    return {a.v * b.v, a.d * b.v + a.v * b.d};
+}
+__device__ __forceinline__ dual smul(rd s, dual b)
+{
+    return {s * b.v, s * b.d};
+}
+
+// w(t) - d_eta(t) for the cubic Bezier curve c at parameter t, with the dual-number evaluation of the curve
+// (Bernstein basis, summed c0*b0 + c1*b1 + c2*b2 + c3*b3) and normalize_fd (src/antipodal/math/fwd_diff.hh:497-532).
+__device__ __forceinline__ double integrand(const double* c, ev3<rd> p, ev3<rd> x0, double tt)
+{
+    dual const t{rd(tt), rd(1.0)};
+    dual const u{rd(1.0) - rd(tt), rd(-1.0)};
+    dual const b0 = dmul(dmul(u, u), u);
+    dual const b1 = dmul(dmul(smul(rd(3.0), u), u), t);
+    dual const b2 = dmul(dmul(smul(rd(3.0), u), t), t);
+    dual const b3 = dmul(dmul(t, t), t);
+    rd phi[3], dphi[3];
+    for (int k = 0; k < 3; ++k)
+    {
+        phi[k] = rd(c[k]) * b0.v + rd(c[3 + k]) * b1.v + rd(c[6 + k]) * b2.v + rd(c[9 + k]) * b3.v;
+        dphi[k] = rd(c[k]) * b0.d + rd(c[3 + k]) * b1.d + rd(c[6 + k]) * b2.d + rd(c[9 + k]) * b3.d;
+    }
+    ev3<rd> const r{phi[0] - p.x, phi[1] - p.y, phi[2] - p.z};
+    ev3<rd> const dr{dphi[0], dphi[1], dphi[2]};
+    rd const q = r.x * r.x + r.y * r.y + r.z * r.z;
+    rd const q1 = rd(2.0) * (r.x * dr.x + r.y * dr.y + r.z * dr.z);
+    rd const s = ex_sqrt(q);
+    rd const inv_s = rd(1.0) / s;
+    rd const s1 = q1 * (rd(0.5) * inv_s);
+    ev3<rd> G, Gp;
+    G.x = r.x * inv_s;
+    G.y = r.y * inv_s;
+    G.z = r.z * inv_s;
+    Gp.x = (dr.x - G.x * s1) * inv_s;
+    Gp.y = (dr.y - G.y * s1) * inv_s;
+    Gp.z = (dr.z - G.z * s1) * inv_s;
+    ev3<rd> const x1{-x0.x, -x0.y, -x0.z};
+    rd const a = edot(x0, G);
+    rd const ap = edot(x0, Gp);
+    ev3<rd> const X = x0 - ev3<rd>{G.x * a, G.y * a, G.z * a};
+    ev3<rd> const Xp = ev3<rd>{G.x * -ap, G.y * -ap, G.z * -ap} - ev3<rd>{Gp.x * a, Gp.y * a, Gp.z * a};
+    rd const d_eta = edot(G, ecross(X, Xp)) / edot(X, X);
+    rd const b = edot(x1, G);
+    rd const bp = edot(x1, Gp);
+    ev3<rd> const v = G - ev3<rd>{x1.x * b, x1.y * b, x1.z * b};
+    ev3<rd> const vp = Gp - ev3<rd>{x1.x * bp, x1.y * bp, x1.z * bp};
+    rd const w = edot(x1, ecross(v, vp)) / edot(v, v);
+    return (w - d_eta).v;
+}
+
+// One GK15 panel (depth, j) = [j 2^-depth, (j+1) 2^-depth] of curve c: the Kronrod and Gauss estimates in the
+// reference's node and summation order (integrate_gk15.hh:155-217).  Returns Ik; *err = |Ik - Ig|.
+__device__ __forceinline__ double gk15_panel(const double* c, ev3<rd> p, ev3<rd> x0, int depth, uint32_t j,
+                                             double* err)
+{
+    double const scale = ldexp(1.0, -depth);
+    double const aa = double(j) * scale, bb = double(j + 1) * scale; // exact: j < 2^24
+    rd const cc = (rd(aa) + rd(bb)) * rd(0.5);
+    rd const h = (rd(bb) - rd(aa)) * rd(0.5);
+    double const f0 = integrand(c, p, x0, cc.v);
+    double fm[8], fp[8];
+#pragma unroll 1
+    for (int k = 1; k <= 7; ++k)
+    {
+        rd const dx = h * rd(kGkX[k]);
+        fm[k] = integrand(c, p, x0, (cc - dx).v);
+        fp[k] = integrand(c, p, x0, (cc + dx).v);
+    }
+    rd ig = rd(kGkWgCenter) * rd(f0);
+    rd ik = rd(kGkWk[0]) * rd(f0);
+    ik = ik + rd(kGkWk[1]) * (rd(fm[1]) + rd(fp[1]));
+    {
+        rd const s2 = rd(fm[2]) + rd(fp[2]);
+        ik = ik + rd(kGkWk[2]) * s2;
+        ig = ig + rd(kGkWg2) * s2;
+    }
+    ik = ik + rd(kGkWk[3]) * (rd(fm[3]) + rd(fp[3]));
+    {
+        rd const s4 = rd(fm[4]) + rd(fp[4]);
+        ik = ik + rd(kGkWk[4]) * s4;
+        ig = ig + rd(kGkWg4) * s4;
+    }
+    ik = ik + rd(kGkWk[5]) * (rd(fm[5]) + rd(fp[5]));
+    {
+        rd const s6 = rd(fm[6]) + rd(fp[6]);
+        ik = ik + rd(kGkWk[6]) * s6;
+        ig = ig + rd(kGkWg6) * s6;
+    }
+    ik = ik + rd(kGkWk[7]) * (rd(fm[7]) + rd(fp[7]));
+    ig = ig * h;
+    ik = ik * h;
+    *err = fabs((ik - ig).v);
+    return ik.v;
+}
+
+// out[q] = (sum over curves of the curve integral) / (4 pi).
+//
+// Each thread owns one query and walks the panel tree of one curve after another in a single flat loop, so that
+// a lane whose curve needs few panels moves on to its next curve instead of idling until the warp's deepest
+// tree is done.  The walk needs no stack: after a split the next panel is the left child (depth + 1, 2j); after
+// an accepted leaf the walk climbs while the finished node is a right child (j odd), combining left + right from
+// `pending` (the finished left sibling's value per level), then moves to the right sibling (depth, j + 1).
+// Panels above the pair's start depth are never evaluated: a walk entering such a panel descends to its
+// leftmost descendant at the start depth.  The summation order is the reference's post-order left + right.
+//
+// start_depth: per (query, curve), row-major [n][n_curves], nullable = all 0.  stats (nullable): per (query,
+// curve) packed as leaves | shallowest leaf depth << 16 | deepest leaf depth << 24.  nodes_total (nullable):
+// panels evaluated per query.
+__global__ void __launch_bounds__(kParamBlock) k_param_gk15(const double* __restrict__ pos, int64_t n,
+                                                            double* __restrict__ out, double x0x, double x0y,
+                                                            double x0z, const Bez* __restrict__ curves,
+                                                            int64_t n_curves, int tile, int min_depth, int max_depth,
+                                                            double tol, const uint8_t* __restrict__ start_depth,
+                                                            uint32_t* __restrict__ stats,
+                                                            int32_t* __restrict__ nodes_total, int* flags)
+{
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ __align__(8) uint64_t bar;
+    Bez* const buf = reinterpret_cast<Bez*>(smem);
+    ev3<rd> const x0{rd(x0x), rd(x0y), rd(x0z)};
+    int64_t const n_blocks_q = (n + blockDim.x - 1) / blockDim.x;
+    int const n_tiles = int((n_curves + tile - 1) / tile);
+    // tol * 2^-depth by repeated halving, as the recursion computes it (exact unless it reaches subnormals)
+    double tol_at[kParamMaxDepth + 1];
+    tol_at[0] = tol;
+    for (int l = 1; l <= kParamMaxDepth; ++l)
+        tol_at[l] = __dmul_rn(tol_at[l - 1], 0.5);
+    if (threadIdx.x == 0)
+    {
+        mbar_init(&bar, 1);
+        fence_barrier_init();
+    }
+    __syncthreads();
+    unsigned phase = 0;
+    for (int64_t qb = blockIdx.x; qb < n_blocks_q; qb += gridDim.x)
+    {
+        int64_t const i = qb * blockDim.x + threadIdx.x;
+        int64_t const ii = i < n ? i : n - 1;
+        ev3<rd> const p{rd(pos[3 * ii]), rd(pos[3 * ii + 1]), rd(pos[3 * ii + 2])};
+        rd sum = rd(0.0);
+        int nodes = 0;
+        for (int t = 0; t < n_tiles; ++t)
+        {
+            int64_t const c0 = int64_t(t) * tile;
+            int const cnt = int(n_curves - c0 < tile ? n_curves - c0 : int64_t(tile));
+            __syncthreads(); // the buffer is free
+            if (threadIdx.x == 0)
+            {
+                unsigned const bytes = unsigned(cnt) * unsigned(sizeof(Bez));
+                mbar_arrive_expect_tx(&bar, bytes);
+                bulk_copy_g2s(buf, curves + c0, bytes, &bar);
+            }
+            if (!mbar_wait_bounded(&bar, phase, flags, 4))
+                return; // every thread of the block times out on the same barrier
+            phase ^= 1u;
+
+            double pending[kParamMaxDepth + 1];
+            int k = 0;
+            int64_t pair = ii * n_curves + c0;
+            int s = start_depth ? min(int(start_depth[pair]), max_depth) : 0;
+            int d = s;
+            uint32_t j = 0;
+            int leaves = 0, dmin = 255, dmax = 0;
+            while (k < cnt)
+            {
+                double err;
+                double v = gk15_panel(buf[k].c, p, x0, d, j, &err);
+                ++nodes;
+                if (!(d >= max_depth || (d >= min_depth && err <= tol_at[d])))
+                {
+                    ++d; // split: left child next
+                    j <<= 1;
+                    continue;
+                }
+                ++leaves;
+                dmin = min(dmin, d);
+                dmax = max(dmax, d);
+                while (d > 0 && (j & 1u))
+                {
+                    v = __dadd_rn(pending[d], v); // left + right
+                    --d;
+                    j >>= 1;
+                }
+                if (d > 0)
+                {
+                    pending[d] = v; // a finished left child: its right sibling is next
+                    ++j;
+                    while (d < s)
+                    {
+                        ++d;
+                        j <<= 1;
+                    }
+                    continue;
+                }
+                // the root is done: v is this curve's integral
+                sum = sum + rd(v);
+                if (stats && i < n)
+                    stats[pair] = uint32_t(min(leaves, 0xffff)) | (uint32_t(dmin) << 16) | (uint32_t(dmax) << 24);
+                ++k;
+                ++pair;
+                if (k < cnt)
+                {
+                    s = start_depth ? min(int(start_depth[pair]), max_depth) : 0;
+                    d = s;
+                    j = 0;
+                    leaves = 0;
+                    dmin = 255;
+                    dmax = 0;
+                }
+            }
+        }
+        if (i < n)
+        {
+            out[i] = (sum / (rd(4.0) * rd(3.141592653589793238462643383279502884))).v;
+            if (nodes_total)
+                nodes_total[i] = nodes;
+        }
+    }
+}
+} // namespace
+
+int param_run(Context& ctx, const double* d_pos, int64_t n, double* d_out, const double* x0, const double* d_curves,
+              int64_t n_curves, int min_depth, int max_depth, double tol, const uint8_t* d_start, uint32_t* d_stats,
+              int32_t* d_nodes)
+{
+    if (n == 0)
+        return AGWN_OK;
+    if (n_curves == 0)
+    {
+        AGWN_TRY_CUDA(cudaMemsetAsync(d_out, 0, sizeof(double) * n, ctx.stream));
+        if (d_nodes)
+            AGWN_TRY_CUDA(cudaMemsetAsync(d_nodes, 0, sizeof(int32_t) * n, ctx.stream));
+        return AGWN_OK;
+    }
+    int const tile = int(std::min<int64_t>(kParamTileMax, n_curves));
+    size_t const smem = size_t(tile) * sizeof(Bez);
+    AGWN_TRY_CUDA(cudaFuncSetAttribute(k_param_gk15, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+    int per_sm = 0;
+    AGWN_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_param_gk15, kParamBlock, smem));
+    if (per_sm < 1)
+        return fail(AGWN_ERR_UNSUPPORTED, "parametric kernel does not fit on an SM");
+    int64_t const n_blocks_q = (n + kParamBlock - 1) / kParamBlock;
+    int const grid = int(std::max<int64_t>(1, std::min<int64_t>(n_blocks_q, int64_t(per_sm) * ctx.sm_count)));
+    AGWN_TRY(ctx.launch_begin(AGWN_K_PARAMETRIC));
+    k_param_gk15<<<grid, kParamBlock, smem, ctx.stream>>>(d_pos, n, d_out, x0[0], x0[1], x0[2],
+                                                         reinterpret_cast<const Bez*>(d_curves), n_curves, tile,
+                                                         min_depth, max_depth, tol, d_start, d_stats, d_nodes,
+                                                         ctx.d_flags);
+    return ctx.launch_end(AGWN_K_PARAMETRIC);
+}
+} // namespace agwn
+
+using namespace agwn;
+
+extern "C" int agwn_param_batch_fractional_bezier3_f64(agwn_context* ctx, const double* positions, int64_t n,
+                                                       double* out, const double* x0, const double* curves,
+                                                       int64_t n_curves, int min_depth, int max_depth, double tol,
+                                                       const uint8_t* start_depth, uint32_t* pair_stats,
+                                                       int32_t* nodes_per_query)
+{
+    AGWN_CHECK_ARG(ctx && x0, "null context/x0");
+    AGWN_CHECK_ARG(n >= 0 && n_curves >= 0 && (n == 0 || (positions && out)) && (n_curves == 0 || curves),
+                   "bad arguments");
+    AGWN_CHECK_ARG(min_depth >= 0 && max_depth >= 0 && max_depth <= kParamMaxDepth,
+                   "depths must be in [0, %d] (max_depth bounds the explicit stack)", kParamMaxDepth);
+    AGWN_CHECK_ARG(std::isfinite(tol) && tol >= 0, "tol must be finite and >= 0");
+    AGWN_CHECK_ARG(n_curves < (int64_t(1) << 31), "too many curves");
+    clear_message();
+    AGWN_TRY_CUDA(cudaSetDevice(ctx->device));
+    if (n == 0)
+        return AGWN_OK;
+    const void *dpos = nullptr, *dcur = nullptr, *dstart = nullptr;
+    void *dout = nullptr, *dstats = nullptr, *dnodes = nullptr;
+    bool h_out = false, h_stats = false, h_nodes = false;
+    AGWN_TRY(stage_in(*ctx, positions, sizeof(double) * 3 * n, S_QUERIES, &dpos));
+    AGWN_TRY(stage_in(*ctx, curves, sizeof(double) * 12 * n_curves, S_MISC0, &dcur));
+    if (start_depth)
+        AGWN_TRY(stage_in(*ctx, start_depth, size_t(n) * n_curves, S_MISC1, &dstart));
+    AGWN_TRY(stage_out(*ctx, out, sizeof(double) * n, S_OUT, &dout, &h_out));
+    if (pair_stats)
+        AGWN_TRY(stage_out(*ctx, pair_stats, sizeof(uint32_t) * size_t(n) * n_curves, S_MISC2, &dstats, &h_stats));
+    if (nodes_per_query)
+        AGWN_TRY(stage_out(*ctx, nodes_per_query, sizeof(int32_t) * n, S_COUNTS, &dnodes, &h_nodes));
+    // curves must be 16-byte aligned for the bulk copy; a host array was staged into aligned scratch
+    if (reinterpret_cast<uintptr_t>(dcur) % 16 != 0)
+    {
+        void* aligned = nullptr;
+        AGWN_TRY(ctx->scratch_reserve(S_SEGS, sizeof(double) * 12 * n_curves, &aligned));
+        AGWN_TRY_CUDA(cudaMemcpyAsync(aligned, dcur, sizeof(double) * 12 * n_curves, cudaMemcpyDeviceToDevice,
+                                      ctx->stream));
+        dcur = aligned;
+    }
+    AGWN_TRY(param_run(*ctx, static_cast<const double*>(dpos), n, static_cast<double*>(dout), x0,
+                       static_cast<const double*>(dcur), n_curves, min_depth, max_depth, tol,
+                       static_cast<const uint8_t*>(dstart), static_cast<uint32_t*>(dstats),
+                       static_cast<int32_t*>(dnodes)));
+    if (h_out)
+        AGWN_TRY_CUDA(cudaMemcpyAsync(out, dout, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    if (h_stats)
+        AGWN_TRY_CUDA(cudaMemcpyAsync(pair_stats, dstats, sizeof(uint32_t) * size_t(n) * n_curves,
+                                      cudaMemcpyDeviceToHost, ctx->stream));
+    if (h_nodes)
+        AGWN_TRY_CUDA(cudaMemcpyAsync(nodes_per_query, dnodes, sizeof(int32_t) * n, cudaMemcpyDeviceToHost,
+                                      ctx->stream));
+    bool const sync = h_out || h_stats || h_nodes || dpos != positions || dcur != curves;
+    return sync ? ctx->check_flags() : AGWN_OK;
+}

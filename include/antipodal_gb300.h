@@ -180,6 +180,24 @@ int agwn_robust_eval_f64(agwn_context* ctx, const agwn_robust* robust, const dou
 int agwn_robust_eval_f32(agwn_context* ctx, const agwn_robust* robust, const float* positions, int64_t n,
                          float* out_gwn, int32_t* out_counts, float* out_frac);
 
+/* ---- parametric surfaces ----------------------------------------------------------------------------------
+ * Replaces eval_gwnr_parametric_batch_fractional (src/antipodal/gwn_parametric.hh:168-186) with the default
+ * IntegratorGK15 (src/antipodal/math/integrate_gk15.hh:63-290) and integrate_config {min_depth, max_depth, tol}
+ * (src/antipodal/math/integrate.hh:11-22), for boundaries made of cubic Bezier curves: `curves` holds 12 doubles
+ * per curve (control points c0..c3, xyz each), in the order for_each_boundary would visit them.  The reference
+ * takes the curve as a functor; the C ABI fixes it to this one curve type (the only one the reference's tests
+ * integrate besides straight lines, which are cubics with collinear control points).
+ * out[i] = (sum over curves of the adaptive GK15 integral of w - d_eta on [0, 1]) / (4 pi), bit-identical to the
+ * reference's double evaluation.  max_depth <= 24.
+ * start_depth (nullable, n * n_curves bytes, row-major [query][curve]): panels shallower than start_depth are split
+ * without being evaluated -- the hook for a proposed refinement depth (agwn_param_propose_depth); NULL = the plain
+ * integrator.  pair_stats (nullable, n * n_curves uint32): accepted leaves | shallowest leaf depth << 16 | deepest
+ * leaf depth << 24.  nodes_per_query (nullable, n int32): panels evaluated for each query. */
+int agwn_param_batch_fractional_bezier3_f64(agwn_context* ctx, const double* positions, int64_t n, double* out,
+                                            const double* x0, const double* curves, int64_t n_curves, int min_depth,
+                                            int max_depth, double tol, const uint8_t* start_depth,
+                                            uint32_t* pair_stats, int32_t* nodes_per_query);
+
 /* ---- mixed-precision fractional term without allocation --------------------------------------------------
  * No counterpart in the reference.  For callers that cannot allocate device memory -- a program whose own pool
  * allocator owns the GPU's memory budget, or a plugin inside a framework whose allocator must not be bypassed --
