@@ -25,7 +25,8 @@ from ._lib import FRAC_EXACT, FRAC_MIXED, Stats
 __all__ = [
     "GwnError", "CudaDispatcher", "CudaIntersector", "CudaRobustMeshGwn", "eval_gwnr_mesh_batch_fractional",
     "eval_gwnr_mesh_batch_integer", "eval_gwnr_mesh_batch", "eval_gwnr_mesh_batch_robust", "build_boundary_segments",
-    "IntegrateConfig", "IntegratorGK15", "eval_gwnr_parametric_batch_fractional", "unpack_pair_stats", "library",
+    "IntegrateConfig", "IntegratorGK15", "eval_gwnr_parametric_batch_fractional", "unpack_pair_stats",
+    "LearnedGK15Proposal", "library",
 ]
 
 
@@ -438,7 +439,8 @@ def eval_gwnr_parametric_batch_fractional(dispatcher: CudaDispatcher, positions,
     sd = _View(start_depth, np.uint8, None, "start_depth") if start_depth is not None else None
     if sd is not None and sd.n != p.n * c.n:
         raise ValueError("start_depth must hold one byte per (query, curve) pair")
-    st = _View(pair_stats, np.uint32, None, "pair_stats", writable=True) if pair_stats is not None else None
+    st_dt = np.int32 if pair_stats is not None and _dtype_of(pair_stats) is np.int32 else np.uint32  # same bits
+    st = _View(pair_stats, st_dt, None, "pair_stats", writable=True) if pair_stats is not None else None
     if st is not None and st.n != p.n * c.n:
         raise ValueError("pair_stats must hold one entry per (query, curve) pair")
     nd = _View(nodes_per_query, np.int32, None, "nodes_per_query", writable=True) \
@@ -451,3 +453,154 @@ def eval_gwnr_parametric_batch_fractional(dispatcher: CudaDispatcher, positions,
               sd.ptr if sd else None, st.ptr if st else None, nd.ptr if nd else None),
            "eval_gwnr_parametric_batch_fractional")
     del x
+
+
+class LearnedGK15Proposal:
+    """Learned start depths for IntegratorGK15 on the parametric path (no counterpart in the reference).
+
+    A 12 -> 64 -> 64 -> 16 MLP, run and trained on the GPU's tensor cores (BF16 weights and activations, FP32
+    accumulation), predicts for each (query, curve) pair the shallowest depth at which the plain integrator
+    accepts a panel.  Used as ``integrator=`` of eval_gwnr_parametric_batch_fractional, it only chooses where the
+    plain integrator starts evaluating; every evaluated panel is still accepted or refined by the plain error
+    test, so the plain method is both the fallback and the judge.  ``alpha`` bounds the predicted probability
+    that a proposed depth overshoots the true one (an overshoot costs extra panels and refines beyond the plain
+    tree; it never skips the error test).
+    """
+
+    FORMAT = 1
+
+    def __init__(self, dispatcher: CudaDispatcher, seed: int = 0, n_classes: int = 11, alpha: float = 0.02,
+                 params=None):
+        self.dispatcher = dispatcher
+        self.n_classes = int(n_classes)
+        self.alpha = float(alpha)
+        h = C.c_void_p()
+        _check(library().agwn_mlp_create(dispatcher.handle, int(seed) & 0xFFFFFFFFFFFFFFFF, C.byref(h)),
+               "agwn_mlp_create")
+        self._h = h
+        if params is not None:
+            self.params = params
+
+    @property
+    def handle(self):
+        if self._h is None:
+            raise RuntimeError("network is closed")
+        return self._h
+
+    @property
+    def params(self) -> np.ndarray:
+        out = np.empty(library().agwn_mlp_param_count(), np.float32)
+        _check(library().agwn_mlp_get_params(self.dispatcher.handle, self.handle, out.ctypes.data),
+               "agwn_mlp_get_params")
+        return out
+
+    @params.setter
+    def params(self, value):
+        v = np.ascontiguousarray(value, np.float32).ravel()
+        if v.size != library().agwn_mlp_param_count():
+            raise ValueError(f"expected {library().agwn_mlp_param_count()} parameters, got {v.size}")
+        _check(library().agwn_mlp_set_params(self.dispatcher.handle, self.handle, v.ctypes.data),
+               "agwn_mlp_set_params")
+
+    def save(self, path):
+        """Write the FP32 weights and the decision settings (the only state the proposal has) to an .npz file."""
+        np.savez(path, params=self.params, n_classes=self.n_classes, alpha=self.alpha, format=self.FORMAT)
+
+    @classmethod
+    def load(cls, dispatcher: CudaDispatcher, path):
+        z = np.load(path)
+        if int(z["format"]) != cls.FORMAT:
+            raise ValueError(f"{path}: unsupported format {int(z['format'])}")
+        return cls(dispatcher, n_classes=int(z["n_classes"]), alpha=float(z["alpha"]), params=z["params"])
+
+    # -- data ---------------------------------------------------------------------------------------------------
+    def features(self, positions, x0, curves, tol: float):
+        """The 12 features of every (query, curve) pair, (n * c, 12) float32 (a device tensor for device input)."""
+        p = _View(positions, np.float64, 3, "positions")
+        c = _View(curves, np.float64, 12, "curves")
+        out = _empty_like_input(positions, (p.n * c.n, 12), np.float32)
+        o = _View(out, np.float32, None, "features", writable=True)
+        _, xp = x = _vec3(x0, np.float64)
+        _check(library().agwn_param_features_bezier3_f64(self.dispatcher.handle, p.ptr, p.n, xp, c.ptr, c.n,
+                                                         float(tol), o.ptr), "agwn_param_features_bezier3_f64")
+        del x
+        return out
+
+    def labels(self, positions, x0, curves, cfg: IntegrateConfig):
+        """Training labels: the plain integrator's shallowest accepted depth for every pair, (n * c,) uint8."""
+        p = _View(positions, np.float64, 3, "positions")
+        c = _View(curves, np.float64, 12, "curves")
+        stats = _empty_like_input(positions, (p.n, c.n), np.uint32)
+        out = _empty_like_input(positions, (p.n,), np.float64)
+        eval_gwnr_parametric_batch_fractional(self.dispatcher, positions, out, x0, curves, cfg, pair_stats=stats)
+        if _is_torch(stats):
+            return ((stats.view(-1).to(__import__("torch").int64) >> 16) & 0xFF).to(__import__("torch").uint8)
+        return ((stats.ravel() >> 16) & 0xFF).astype(np.uint8)
+
+    # -- training -----------------------------------------------------------------------------------------------
+    def loss_grad(self, features, labels):
+        """Mean cross-entropy and its gradient on the given rows, from the device training kernels."""
+        f = _View(features, np.float32, 12, "features")
+        lb = _View(labels, np.uint8, None, "labels")
+        if lb.n != f.n:
+            raise ValueError("one label per feature row")
+        g = np.empty(library().agwn_mlp_param_count(), np.float32)
+        loss = C.c_double()
+        _check(library().agwn_mlp_loss_grad(self.dispatcher.handle, self.handle, f.ptr, lb.ptr, f.n, self.n_classes,
+                                            g.ctypes.data, C.byref(loss)), "agwn_mlp_loss_grad")
+        return loss.value, g
+
+    def train(self, features, labels, steps: int = 3000, batch: int = 8192, lr: float = 2e-3, seed: int = 1):
+        """Adam on mini-batches drawn from (features, labels); returns each step's mean loss."""
+        f = _View(features, np.float32, 12, "features")
+        lb = _View(labels, np.uint8, None, "labels")
+        if lb.n != f.n:
+            raise ValueError("one label per feature row")
+        hist = np.empty(max(int(steps), 0), np.float32)
+        _check(library().agwn_mlp_train(self.dispatcher.handle, self.handle, f.ptr, lb.ptr, f.n, self.n_classes,
+                                        int(steps), int(batch), float(lr), int(seed) & 0xFFFFFFFFFFFFFFFF,
+                                        hist.ctypes.data if hist.size else None), "agwn_mlp_train")
+        return hist
+
+    def fit(self, positions, x0, curves, cfg: IntegrateConfig, **train_kw):
+        """Label (query, curve) pairs with the plain integrator, compute their features and train on them."""
+        lab = self.labels(positions, x0, curves, cfg)
+        feat = self.features(positions, x0, curves, cfg.tol)
+        return self.train(feat, lab, **train_kw)
+
+    # -- inference ----------------------------------------------------------------------------------------------
+    def start_depths(self, dispatcher, positions, x0, curves, cfg: IntegrateConfig, logits=None):
+        """Proposed start depth of every pair, (n, c) uint8 (a device tensor for device input)."""
+        p = _View(positions, np.float64, 3, "positions")
+        c = _View(curves, np.float64, 12, "curves")
+        out = _empty_like_input(positions, (p.n, c.n), np.uint8)
+        o = _View(out, np.uint8, None, "start_depth", writable=True)
+        lg = _View(logits, np.float32, 16, "logits", writable=True) if logits is not None else None
+        _, xp = x = _vec3(x0, np.float64)
+        _check(library().agwn_param_propose_depth_bezier3_f64(
+            dispatcher.handle, self.handle, p.ptr, p.n, xp, c.ptr, c.n, self.n_classes, cfg.min_depth, cfg.max_depth,
+            cfg.tol, self.alpha, o.ptr, lg.ptr if lg else None), "agwn_param_propose_depth_bezier3_f64")
+        del x
+        return out
+
+    def close(self):
+        if getattr(self, "_h", None) is not None:
+            library().agwn_mlp_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _empty_like_input(like, shape, dtype):
+    """An output array on the same side (host numpy / device torch) as the input ``like``."""
+    if _is_torch(like) and like.is_cuda:
+        import torch
+        tdt = {np.float32: torch.float32, np.float64: torch.float64, np.uint8: torch.uint8, np.int32: torch.int32}
+        if dtype is np.uint32:
+            return torch.empty(shape, dtype=torch.int32, device=like.device)  # same bits, viewed as uint32
+        return torch.empty(shape, dtype=tdt[dtype], device=like.device)
+    return np.empty(shape, dtype)

@@ -61,6 +61,16 @@ SIGNATURES = {
     "agwn_probe_fp32_peak": (_I, [_P, C.POINTER(_D)]),
     "agwn_probe_atan2": (_I, [_P, _P, _P, _I64, _P, _P]),
     "agwn_param_batch_fractional_bezier3_f64": (_I, [_P, _P, _I64, _P, _P, _P, _I64, _I, _I, _D, _P, _P, _P]),
+    "agwn_mlp_param_count": (_I, []),
+    "agwn_mlp_create": (_I, [_P, C.c_uint64, _PP]),
+    "agwn_mlp_destroy": (_I, [_P]),
+    "agwn_mlp_set_params": (_I, [_P, _P, _P]),
+    "agwn_mlp_get_params": (_I, [_P, _P, _P]),
+    "agwn_param_features_bezier3_f64": (_I, [_P, _P, _I64, _P, _P, _I64, _D, _P]),
+    "agwn_mlp_loss_grad": (_I, [_P, _P, _P, _P, _I64, _I, _P, _P]),
+    "agwn_mlp_train": (_I, [_P, _P, _P, _P, _I64, _I, _I, _I, C.c_float, C.c_uint64, _P]),
+    "agwn_param_propose_depth_bezier3_f64": (_I, [_P, _P, _P, _I64, _P, _P, _I64, _I, _I, _I, _D, C.c_float, _P,
+                                                  _P]),
 }
 
 _lock = threading.Lock()

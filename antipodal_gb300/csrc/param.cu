@@ -153,31 +153,40 @@ __device__ __forceinline__ double gk15_panel(const double* c, ev3<rd> p, ev3<rd>
 
 // out[q] = (sum over curves of the curve integral) / (4 pi).
 //
-// Each thread owns one query and walks the panel tree of one curve after another in a single flat loop, so that
-// a lane whose curve needs few panels moves on to its next curve instead of idling until the warp's deepest
-// tree is done.  The walk needs no stack: after a split the next panel is the left child (depth + 1, 2j); after
-// an accepted leaf the walk climbs while the finished node is a right child (j odd), combining left + right from
+// The cost of one (query, curve) integral is heavy-tailed: a query whose line along x0 passes close to a curve
+// needs a deep tree there.  So the work is shared out by pair, not by query.  A block owns up to kParamBlock
+// queries and, for each shared-memory tile of curves, the pool of (query, curve) pairs of that tile; a lane that
+// finishes its pair takes the next one from the pool (one shared-memory atomic per warp).  Each lane walks its
+// pair's panel tree without a stack: after a split the next panel is the left child (depth + 1, 2j); after an
+// accepted leaf the walk climbs while the finished node is a right child (j odd), combining left + right from
 // `pending` (the finished left sibling's value per level), then moves to the right sibling (depth, j + 1).
-// Panels above the pair's start depth are never evaluated: a walk entering such a panel descends to its
-// leftmost descendant at the start depth.  The summation order is the reference's post-order left + right.
+// Panels above the pair's start depth are not evaluated: the walk descends to the leftmost descendant at the
+// start depth.  A finished pair's integral goes to the block's slab of `pair_vals`; after the tile each thread
+// adds its query's row in curve order.  Every sum is the reference's (post-order left + right within a curve,
+// curves in order), so the result does not depend on how the pairs were shared out.
 //
 // start_depth: per (query, curve), row-major [n][n_curves], nullable = all 0.  stats (nullable): per (query,
 // curve) packed as leaves | shallowest leaf depth << 16 | deepest leaf depth << 24.  nodes_total (nullable):
-// panels evaluated per query.
+// panels evaluated per query.  pair_vals: gridDim.x * kParamBlock * tile doubles.
 __global__ void __launch_bounds__(kParamBlock) k_param_gk15(const double* __restrict__ pos, int64_t n,
                                                             double* __restrict__ out, double x0x, double x0y,
                                                             double x0z, const Bez* __restrict__ curves,
                                                             int64_t n_curves, int tile, int min_depth, int max_depth,
                                                             double tol, const uint8_t* __restrict__ start_depth,
                                                             uint32_t* __restrict__ stats,
-                                                            int32_t* __restrict__ nodes_total, int* flags)
+                                                            int32_t* __restrict__ nodes_total,
+                                                            double* __restrict__ pair_vals, int* flags)
 {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ __align__(8) uint64_t bar;
+    __shared__ int s_next;
+    __shared__ int s_nodes[kParamBlock];
     Bez* const buf = reinterpret_cast<Bez*>(smem);
+    double* const slab = pair_vals + size_t(blockIdx.x) * kParamBlock * tile;
     ev3<rd> const x0{rd(x0x), rd(x0y), rd(x0z)};
-    int64_t const n_blocks_q = (n + blockDim.x - 1) / blockDim.x;
+    int64_t const n_blocks_q = (n + kParamBlock - 1) / kParamBlock;
     int const n_tiles = int((n_curves + tile - 1) / tile);
+    unsigned const lane = threadIdx.x & 31u;
     // tol * 2^-depth by repeated halving, as the recursion computes it (exact unless it reaches subnormals)
     double tol_at[kParamMaxDepth + 1];
     tol_at[0] = tol;
@@ -192,18 +201,18 @@ __global__ void __launch_bounds__(kParamBlock) k_param_gk15(const double* __rest
     unsigned phase = 0;
     for (int64_t qb = blockIdx.x; qb < n_blocks_q; qb += gridDim.x)
     {
-        int64_t const i = qb * blockDim.x + threadIdx.x;
-        int64_t const ii = i < n ? i : n - 1;
-        ev3<rd> const p{rd(pos[3 * ii]), rd(pos[3 * ii + 1]), rd(pos[3 * ii + 2])};
+        int64_t const q0 = qb * kParamBlock;
+        int const nq = int(n - q0 < kParamBlock ? n - q0 : int64_t(kParamBlock));
         rd sum = rd(0.0);
-        int nodes = 0;
+        s_nodes[threadIdx.x] = 0;
         for (int t = 0; t < n_tiles; ++t)
         {
             int64_t const c0 = int64_t(t) * tile;
             int const cnt = int(n_curves - c0 < tile ? n_curves - c0 : int64_t(tile));
-            __syncthreads(); // the buffer is free
+            __syncthreads(); // the tile buffer and the slab are free
             if (threadIdx.x == 0)
             {
+                s_next = 0;
                 unsigned const bytes = unsigned(cnt) * unsigned(sizeof(Bez));
                 mbar_arrive_expect_tx(&bar, bytes);
                 bulk_copy_g2s(buf, curves + c0, bytes, &bar);
@@ -212,18 +221,52 @@ __global__ void __launch_bounds__(kParamBlock) k_param_gk15(const double* __rest
                 return; // every thread of the block times out on the same barrier
             phase ^= 1u;
 
-            double pending[kParamMaxDepth + 1];
-            int k = 0;
-            int64_t pair = ii * n_curves + c0;
-            int s = start_depth ? min(int(start_depth[pair]), max_depth) : 0;
-            int d = s;
+            int const total = cnt * nq; // pairs in this tile's pool, curve-major
+            int pi = -1;                // this lane's pair, -1 = needs one
+            bool drained = false;
+            int k = 0, ql = 0, s = 0, d = 0, leaves = 0, dmin = 0, dmax = 0, pnodes = 0;
             uint32_t j = 0;
-            int leaves = 0, dmin = 255, dmax = 0;
-            while (k < cnt)
+            ev3<rd> p{};
+            double pending[kParamMaxDepth + 1];
+            for (;;)
             {
+                unsigned const want = __ballot_sync(0xffffffffu, pi < 0 && !drained);
+                if (want)
+                {
+                    int base = 0;
+                    unsigned const leader = __ffs(want) - 1;
+                    if (lane == leader)
+                        base = atomicAdd(&s_next, __popc(want));
+                    base = __shfl_sync(0xffffffffu, base, leader);
+                    if (want & (1u << lane))
+                    {
+                        int const mine = base + __popc(want & ((1u << lane) - 1u));
+                        if (mine < total)
+                        {
+                            pi = mine;
+                            k = mine / nq;
+                            ql = mine - k * nq;
+                            int64_t const q = q0 + ql;
+                            p = ev3<rd>{rd(pos[3 * q]), rd(pos[3 * q + 1]), rd(pos[3 * q + 2])};
+                            s = start_depth ? min(int(start_depth[q * n_curves + c0 + k]), max_depth) : 0;
+                            d = s;
+                            j = 0;
+                            leaves = 0;
+                            dmin = 255;
+                            dmax = 0;
+                            pnodes = 0;
+                        }
+                        else
+                            drained = true;
+                    }
+                }
+                if (!__any_sync(0xffffffffu, pi >= 0))
+                    break;
+                if (pi < 0)
+                    continue;
                 double err;
                 double v = gk15_panel(buf[k].c, p, x0, d, j, &err);
-                ++nodes;
+                ++pnodes;
                 if (!(d >= max_depth || (d >= min_depth && err <= tol_at[d])))
                 {
                     ++d; // split: left child next
@@ -250,28 +293,26 @@ __global__ void __launch_bounds__(kParamBlock) k_param_gk15(const double* __rest
                     }
                     continue;
                 }
-                // the root is done: v is this curve's integral
-                sum = sum + rd(v);
-                if (stats && i < n)
-                    stats[pair] = uint32_t(min(leaves, 0xffff)) | (uint32_t(dmin) << 16) | (uint32_t(dmax) << 24);
-                ++k;
-                ++pair;
-                if (k < cnt)
-                {
-                    s = start_depth ? min(int(start_depth[pair]), max_depth) : 0;
-                    d = s;
-                    j = 0;
-                    leaves = 0;
-                    dmin = 255;
-                    dmax = 0;
-                }
+                // the root is done: v is this pair's integral
+                slab[size_t(k) * kParamBlock + ql] = v;
+                if (stats)
+                    stats[(q0 + ql) * n_curves + c0 + k] = uint32_t(min(leaves, 0xffff)) | (uint32_t(dmin) << 16) |
+                                                           (uint32_t(dmax) << 24);
+                atomicAdd(&s_nodes[ql], pnodes);
+                pi = -1;
             }
+            __syncthreads(); // the slab is complete
+            if (int(threadIdx.x) < nq)
+                for (int kk = 0; kk < cnt; ++kk)
+                    sum = sum + rd(slab[size_t(kk) * kParamBlock + threadIdx.x]);
         }
-        if (i < n)
+        __syncthreads(); // s_nodes is complete
+        if (int(threadIdx.x) < nq)
         {
+            int64_t const i = q0 + threadIdx.x;
             out[i] = (sum / (rd(4.0) * rd(3.141592653589793238462643383279502884))).v;
             if (nodes_total)
-                nodes_total[i] = nodes;
+                nodes_total[i] = s_nodes[threadIdx.x];
         }
     }
 }
@@ -299,11 +340,14 @@ int param_run(Context& ctx, const double* d_pos, int64_t n, double* d_out, const
         return fail(AGWN_ERR_UNSUPPORTED, "parametric kernel does not fit on an SM");
     int64_t const n_blocks_q = (n + kParamBlock - 1) / kParamBlock;
     int const grid = int(std::max<int64_t>(1, std::min<int64_t>(n_blocks_q, int64_t(per_sm) * ctx.sm_count)));
+    double* pair_vals = nullptr;
+    AGWN_TRY(ctx.scratch_reserve(S_SEGS_RAW, sizeof(double) * size_t(grid) * kParamBlock * tile,
+                                 reinterpret_cast<void**>(&pair_vals)));
     AGWN_TRY(ctx.launch_begin(AGWN_K_PARAMETRIC));
     k_param_gk15<<<grid, kParamBlock, smem, ctx.stream>>>(d_pos, n, d_out, x0[0], x0[1], x0[2],
                                                          reinterpret_cast<const Bez*>(d_curves), n_curves, tile,
                                                          min_depth, max_depth, tol, d_start, d_stats, d_nodes,
-                                                         ctx.d_flags);
+                                                         pair_vals, ctx.d_flags);
     return ctx.launch_end(AGWN_K_PARAMETRIC);
 }
 } // namespace agwn

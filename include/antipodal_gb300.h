@@ -198,6 +198,40 @@ int agwn_param_batch_fractional_bezier3_f64(agwn_context* ctx, const double* pos
                                             int max_depth, double tol, const uint8_t* start_depth,
                                             uint32_t* pair_stats, int32_t* nodes_per_query);
 
+/* ---- learned GK15 depth proposal ----------------------------------------------------------------------------
+ * No counterpart in the reference.  A 12 -> 64 -> 64 -> 16 MLP (ReLU; BF16 weights and activations on the
+ * tensor cores, FP32 accumulation, FP32 master weights) predicts, for each (query, curve) pair, the shallowest
+ * depth at which the plain integrator accepts a panel (the "label": bits 16..23 of pair_stats).  Its proposal is
+ * passed to agwn_param_batch_fractional_bezier3_f64 as start_depth; every evaluated panel is still accepted or
+ * split by the plain error test, and wherever the proposal does not exceed the label the result is bit-identical
+ * to the plain integrator's.
+ * Parameter blob (agwn_mlp_param_count() floats): W1[64][16] (input columns 12..15 unused, kept 0), b1[64],
+ * W2[64][64], b2[64], W3[16][64], b3[16]; each W is [out][in]. */
+typedef struct agwn_mlp agwn_mlp;
+int agwn_mlp_param_count(void);
+int agwn_mlp_create(agwn_context* ctx, uint64_t seed, agwn_mlp** out); /* He-uniform weights, zero biases */
+int agwn_mlp_destroy(agwn_mlp* mlp);
+int agwn_mlp_set_params(agwn_context* ctx, agwn_mlp* mlp, const float* params); /* host blob; resets Adam */
+int agwn_mlp_get_params(agwn_context* ctx, const agwn_mlp* mlp, float* params);  /* host blob */
+/* The 12 features of every (query, curve) pair, row-major [n * n_curves][12] floats (host or device). */
+int agwn_param_features_bezier3_f64(agwn_context* ctx, const double* positions, int64_t n, const double* x0,
+                                    const double* curves, int64_t n_curves, double tol, float* features);
+/* Mean softmax cross-entropy over the first n_classes logits and its gradient (agwn_mlp_param_count() floats,
+ * host) on n labelled feature rows, computed by the training kernels. */
+int agwn_mlp_loss_grad(agwn_context* ctx, const agwn_mlp* mlp, const float* features, const uint8_t* labels,
+                       int64_t n, int n_classes, float* grads, double* loss);
+/* `steps` Adam steps (lr, beta1 0.9, beta2 0.999) on mini-batches of `batch` rows (a multiple of 128) drawn from
+ * the n rows by a hash of (seed, step, row).  loss_per_step (nullable, host): each step's mean loss. */
+int agwn_mlp_train(agwn_context* ctx, agwn_mlp* mlp, const float* features, const uint8_t* labels, int64_t n,
+                   int n_classes, int steps, int batch, float lr, uint64_t seed, float* loss_per_step);
+/* Proposed start depth of every (query, curve) pair ([n][n_curves] bytes): the largest s whose predicted
+ * probability of a shallower label, P(label < s), is at most alpha, raised to min_depth and capped at max_depth.
+ * logits (nullable): [n * n_curves][16] floats. */
+int agwn_param_propose_depth_bezier3_f64(agwn_context* ctx, const agwn_mlp* mlp, const double* positions, int64_t n,
+                                         const double* x0, const double* curves, int64_t n_curves, int n_classes,
+                                         int min_depth, int max_depth, double tol, float alpha,
+                                         uint8_t* start_depth, float* logits);
+
 /* ---- mixed-precision fractional term without allocation --------------------------------------------------
  * No counterpart in the reference.  For callers that cannot allocate device memory -- a program whose own pool
  * allocator owns the GPU's memory budget, or a plugin inside a framework whose allocator must not be bypassed --

@@ -914,3 +914,249 @@ double orc_gk15_known(int fn, double a, double b, int min_depth, int max_depth, 
     return r;
 }
 } // extern "C"
+
+// ---------------------------------------------------------------------------------------------------------------
+// Learned GK15 depth proposal: features and the MLP's loss and gradient (no reference counterpart).  The checker
+// for the device training kernels: the same network in double precision, rounding to BF16 exactly where the
+// device feeds a tensor-core product (inputs, weights, hidden activations, output gradients) and nowhere else.
+// ---------------------------------------------------------------------------------------------------------------
+namespace orc
+{
+namespace mlp
+{
+constexpr int F = 12, FP = 16, H = 64, C = 16;
+constexpr int oW1 = 0, oB1 = oW1 + H * FP, oW2 = oB1 + H, oB2 = oW2 + H * H, oW3 = oB2 + H, oB3 = oW3 + C * H,
+              n_params = oB3 + C;
+
+// float -> bfloat16 -> float, round to nearest even
+inline double bf16(double v)
+{
+    float f = float(v);
+    uint32_t u;
+    std::memcpy(&u, &f, 4);
+    if ((u & 0x7fffffffu) > 0x7f800000u)
+        return f;
+    u += 0x7fffu + ((u >> 16) & 1u);
+    u &= 0xffff0000u;
+    std::memcpy(&f, &u, 4);
+    return f;
+}
+
+struct d3
+{
+    double x, y, z;
+};
+inline d3 sub3(d3 a, d3 b)
+{
+    return {a.x - b.x, a.y - b.y, a.z - b.z};
+}
+inline double dot3(d3 a, d3 b)
+{
+    return a.x * b.x + a.y * b.y + a.z * b.z;
+}
+inline double len3(d3 a)
+{
+    return std::sqrt(dot3(a, a));
+}
+inline double angle3(d3 a, d3 b)
+{
+    d3 const c{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+    return std::atan2(len3(c), dot3(a, b));
+}
+inline double seg_dist0(d3 a, d3 b, double* tpar)
+{
+    d3 const e = sub3(b, a);
+    double const ee = dot3(e, e);
+    double t = ee > 0 ? -dot3(a, e) / ee : 0.0;
+    t = std::min(std::max(t, 0.0), 1.0);
+    *tpar = t;
+    return len3({a.x + t * e.x, a.y + t * e.y, a.z + t * e.z});
+}
+inline double lg(double v)
+{
+    return std::log2(std::max(v, 1e-30)) * 0.125;
+}
+
+// The 12 pair features (the device computes the same formulas in float).
+void features(double const* c, double const* p, double const* x0in, double tol_feat, float* f)
+{
+    d3 r[4];
+    for (int i = 0; i < 4; ++i)
+        r[i] = {double(float(c[3 * i] - p[0])), double(float(c[3 * i + 1] - p[1])), double(float(c[3 * i + 2] - p[2]))};
+    d3 const x0{double(float(x0in[0])), double(float(x0in[1])), double(float(x0in[2]))};
+    double L = 0;
+    d3 e[3];
+    for (int i = 0; i < 3; ++i)
+    {
+        e[i] = sub3(r[i + 1], r[i]);
+        L += len3(e[i]);
+    }
+    L = std::max(L, 1e-30);
+    double dpoly = 3e38, t;
+    for (int i = 0; i < 3; ++i)
+        dpoly = std::min(dpoly, seg_dist0(r[i], r[i + 1], &t));
+    double nmin = 3e38, nmax = 0;
+    for (int i = 0; i < 4; ++i)
+    {
+        nmin = std::min(nmin, len3(r[i]));
+        nmax = std::max(nmax, len3(r[i]));
+    }
+    double const chord = len3(sub3(r[3], r[0]));
+    double flat = 0;
+    for (int i = 1; i <= 2; ++i)
+        flat = std::max(flat, seg_dist0(sub3(r[0], r[i]), sub3(r[3], r[i]), &t));
+    double const turning = angle3(e[0], e[1]) + angle3(e[1], e[2]);
+    double const subt = angle3(r[0], r[1]) + angle3(r[1], r[2]) + angle3(r[2], r[3]);
+    d3 u[4];
+    for (int i = 0; i < 4; ++i)
+    {
+        double const a = dot3(r[i], x0);
+        u[i] = {r[i].x - a * x0.x, r[i].y - a * x0.y, r[i].z - a * x0.z};
+    }
+    double dline = 3e38, axial = 0;
+    for (int i = 0; i < 3; ++i)
+    {
+        double const d = seg_dist0(u[i], u[i + 1], &t);
+        if (d < dline)
+        {
+            dline = d;
+            d3 const q{r[i].x + t * e[i].x, r[i].y + t * e[i].y, r[i].z + t * e[i].z};
+            axial = dot3(q, x0) / std::max(len3(q), 1e-30);
+        }
+    }
+    double v[F] = {lg(dpoly / L),
+                   lg(nmin / L),
+                   lg(nmax / L),
+                   lg(L),
+                   chord / L,
+                   flat / L,
+                   turning / kPi<double>,
+                   subt / kPi<double>,
+                   lg(dline / L),
+                   lg(std::max(dline, 1e-30) / std::max(dpoly, 1e-30)),
+                   axial,
+                   tol_feat};
+    for (int i = 0; i < F; ++i)
+        f[i] = float(std::min(std::max(v[i], -8.0), 8.0));
+}
+
+// Forward pass of one sample; returns the logits and keeps the pre-activations and BF16 activations.
+struct Acts
+{
+    double x[FP], z1[H], h1[H], z2[H], h2[H], z3[C];
+};
+void forward(float const* prm, float const* feat, Acts& a)
+{
+    for (int k = 0; k < FP; ++k)
+        a.x[k] = k < F ? bf16(feat[k]) : 0.0;
+    for (int o = 0; o < H; ++o)
+    {
+        double s = 0;
+        for (int k = 0; k < FP; ++k)
+            s += bf16(prm[oW1 + o * FP + k]) * a.x[k];
+        a.z1[o] = double(float(s + prm[oB1 + o]));
+        a.h1[o] = bf16(std::max(a.z1[o], 0.0));
+    }
+    for (int o = 0; o < H; ++o)
+    {
+        double s = 0;
+        for (int k = 0; k < H; ++k)
+            s += bf16(prm[oW2 + o * H + k]) * a.h1[k];
+        a.z2[o] = double(float(s + prm[oB2 + o]));
+        a.h2[o] = bf16(std::max(a.z2[o], 0.0));
+    }
+    for (int c = 0; c < C; ++c)
+    {
+        double s = 0;
+        for (int k = 0; k < H; ++k)
+            s += bf16(prm[oW3 + c * H + k]) * a.h2[k];
+        a.z3[c] = s + prm[oB3 + c];
+    }
+}
+} // namespace mlp
+} // namespace orc
+
+extern "C"
+{
+int orc_mlp_param_count()
+{
+    return orc::mlp::n_params;
+}
+
+void orc_param_features_bezier3(double const* pos, int64_t n, double const* x0, double const* curves, int64_t n_curves,
+                                double tol, float* out)
+{
+    double const tf = std::log10(tol) / 10.0;
+    for (int64_t q = 0; q < n; ++q)
+        for (int64_t c = 0; c < n_curves; ++c)
+            orc::mlp::features(curves + 12 * c, pos + 3 * q, x0, double(float(tf)), out + (q * n_curves + c) * 12);
+}
+
+void orc_mlp_logits(float const* params, float const* feats, int64_t n, double* logits)
+{
+    using namespace orc::mlp;
+    for (int64_t i = 0; i < n; ++i)
+    {
+        Acts a;
+        forward(params, feats + F * i, a);
+        for (int c = 0; c < C; ++c)
+            logits[i * C + c] = a.z3[c];
+    }
+}
+
+// Mean softmax cross-entropy over the first n_classes logits and its gradient, laid out like the parameters.
+void orc_mlp_loss_grad(float const* params, float const* feats, uint8_t const* labels, int64_t n, int n_classes,
+                       double* grads, double* loss)
+{
+    using namespace orc::mlp;
+    std::fill(grads, grads + n_params, 0.0);
+    double total = 0;
+    double const inv_n = 1.0 / double(n);
+    for (int64_t i = 0; i < n; ++i)
+    {
+        Acts a;
+        forward(params, feats + F * i, a);
+        int const lab = std::min(int(labels[i]), n_classes - 1);
+        double m = -1e300;
+        for (int c = 0; c < n_classes; ++c)
+            m = std::max(m, a.z3[c]);
+        double sum = 0, ex[C] = {};
+        for (int c = 0; c < n_classes; ++c)
+            sum += (ex[c] = std::exp(a.z3[c] - m));
+        total += std::log(sum) + m - a.z3[lab];
+        double dz3[C] = {}, dz3b[C] = {};
+        for (int c = 0; c < n_classes; ++c)
+        {
+            dz3[c] = (ex[c] / sum - (c == lab ? 1.0 : 0.0)) * inv_n;
+            dz3b[c] = bf16(dz3[c]);
+            grads[oB3 + c] += dz3[c];
+            for (int k = 0; k < H; ++k)
+                grads[oW3 + c * H + k] += dz3b[c] * a.h2[k];
+        }
+        double dz2[H], dz2b[H];
+        for (int k = 0; k < H; ++k)
+        {
+            double s = 0;
+            for (int c = 0; c < C; ++c)
+                s += dz3b[c] * bf16(params[oW3 + c * H + k]);
+            dz2[k] = a.z2[k] > 0 ? s : 0.0;
+            dz2b[k] = bf16(dz2[k]);
+            grads[oB2 + k] += dz2[k];
+            for (int j = 0; j < H; ++j)
+                grads[oW2 + k * H + j] += dz2b[k] * a.h1[j];
+        }
+        for (int j = 0; j < H; ++j)
+        {
+            double s = 0;
+            for (int k = 0; k < H; ++k)
+                s += dz2b[k] * bf16(params[oW2 + k * H + j]);
+            double const dz1 = a.z1[j] > 0 ? s : 0.0;
+            double const dz1b = bf16(dz1);
+            grads[oB1 + j] += dz1;
+            for (int f = 0; f < FP; ++f)
+                grads[oW1 + j * FP + f] += dz1b * a.x[f];
+        }
+    }
+    *loss = total * inv_n;
+}
+} // extern "C"

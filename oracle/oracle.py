@@ -75,6 +75,11 @@ class Oracle:
         self._pred = self._fn("predicates", _I, _I, _P, _P, _P, _P, _I64, _P, _P, _P)
         self._param = self._fn("param_frac_bezier3_f64", None, _P, _I64, _P, _P, _P, _I64, _I, _I, _D, _P, _P, _I)
         self._gk15 = self._fn("gk15_known", _D, _I, _D, _D, _I, _I, _D, C.POINTER(_D), C.POINTER(_I))
+        if not self.reference:
+            self._feat = self._fn("param_features_bezier3", None, _P, _I64, _P, _P, _I64, _D, _P)
+            self._mlp_logits = self._fn("mlp_logits", None, _P, _P, _I64, _P)
+            self._mlp_grad = self._fn("mlp_loss_grad", None, _P, _P, _P, _I64, _I, _P, _P)
+            self.mlp_param_count = self._fn("mlp_param_count", _I)()
 
     @staticmethod
     def _dt(a):
@@ -169,3 +174,24 @@ class Oracle:
         err, leaves = _D(0.0), _I(0)
         r = self._gk15(fn, a, b, min_depth, max_depth, tol, C.byref(err), C.byref(leaves))
         return r, err.value, leaves.value
+
+    # -- learned proposal (the network's checker; no reference counterpart) -------------------------------------
+    def param_features(self, pos, x0, ctrl, tol):
+        pos, x0, ctrl = _c(pos, np.float64), _c(x0, np.float64), _c(ctrl, np.float64).reshape(-1, 12)
+        out = np.empty((len(pos) * len(ctrl), 12), np.float32)
+        self._feat(_ptr(pos), len(pos), _ptr(x0), _ptr(ctrl), len(ctrl), tol, _ptr(out))
+        return out
+
+    def mlp_logits(self, params, feats):
+        params, feats = _c(params, np.float32), _c(feats, np.float32).reshape(-1, 12)
+        out = np.empty((len(feats), 16), np.float64)
+        self._mlp_logits(_ptr(params), _ptr(feats), len(feats), _ptr(out))
+        return out
+
+    def mlp_loss_grad(self, params, feats, labels, n_classes):
+        params, feats = _c(params, np.float32), _c(feats, np.float32).reshape(-1, 12)
+        labels = _c(labels, np.uint8)
+        grads = np.empty(self.mlp_param_count, np.float64)
+        loss = _D(0.0)
+        self._mlp_grad(_ptr(params), _ptr(feats), _ptr(labels), len(feats), n_classes, _ptr(grads), C.byref(loss))
+        return loss.value, grads
