@@ -26,7 +26,7 @@ __all__ = [
     "GwnError", "CudaDispatcher", "CudaIntersector", "CudaRobustMeshGwn", "eval_gwnr_mesh_batch_fractional",
     "eval_gwnr_mesh_batch_integer", "eval_gwnr_mesh_batch", "eval_gwnr_mesh_batch_robust", "build_boundary_segments",
     "IntegrateConfig", "IntegratorGK15", "eval_gwnr_parametric_batch_fractional", "unpack_pair_stats",
-    "LearnedGK15Proposal", "library",
+    "LearnedGK15Proposal", "CudaRobustBatch", "library",
 ]
 
 
@@ -384,6 +384,94 @@ def build_boundary_segments(vertices, indices) -> np.ndarray:
     from .synth import boundary_segments
     v = np.asarray(vertices)
     return boundary_segments(v, np.asarray(indices, np.int32)).astype(v.dtype)
+
+
+class CudaRobustBatch:
+    """Many CudaRobustMeshGwn meshes with their own query arrays, evaluated in one persistent launch.
+
+    Equivalent to ``eval_gwnr_mesh_batch_robust(disp, meshes[i], positions[i], outs[i])`` for every i, bit for
+    bit (no reference counterpart for the batching itself).  positions / outs / counts are CUDA tensors, kept
+    alive by this object; the meshes must stay open while it is used.  ``tune()`` picks the launch configuration
+    by timing every candidate; ``run(graph=True)`` replays a captured CUDA graph after the first call.
+    """
+
+    def __init__(self, dispatcher: CudaDispatcher, meshes, positions, outs, counts=None):
+        if not (len(meshes) == len(positions) == len(outs)) or not meshes:
+            raise ValueError("one positions and one out array per mesh")
+        if counts is not None and len(counts) != len(meshes):
+            raise ValueError("one counts array per mesh")
+        self.dispatcher = dispatcher
+        self._keep = []
+        pp, nq, oo, cc = [], [], [], []
+        for i, (m, p, o) in enumerate(zip(meshes, positions, outs)):
+            if not (_is_torch(p) and p.is_cuda and _is_torch(o) and o.is_cuda):
+                raise TypeError(f"mesh {i}: positions and out must be CUDA tensors")
+            pv = _View(p, m.dtype, 3, f"positions[{i}]")
+            ov = _View(o, m.dtype, None, f"out[{i}]", writable=True)
+            if pv.n != ov.n:
+                raise ValueError(f"mesh {i}: positions and out sizes differ")
+            cv = None
+            if counts is not None and counts[i] is not None:
+                cv = _View(counts[i], np.int32, None, f"counts[{i}]", writable=True)
+                if cv.n != pv.n:
+                    raise ValueError(f"mesh {i}: counts size differs")
+            self._keep += [pv, ov, cv]
+            pp.append(pv.ptr or 0)
+            nq.append(pv.n)
+            oo.append(ov.ptr or 0)
+            cc.append(cv.ptr if cv else 0)
+        n = len(meshes)
+        self._meshes = list(meshes)
+        arr_m = (C.c_void_p * n)(*[m.handle.value for m in meshes])
+        arr_p = (C.c_void_p * n)(*pp)
+        arr_n = (C.c_int64 * n)(*nq)
+        arr_o = (C.c_void_p * n)(*oo)
+        arr_c = (C.c_void_p * n)(*cc) if counts is not None else None
+        h = C.c_void_p()
+        _check(library().agwn_batch_create(dispatcher.handle, C.cast(arr_m, C.c_void_p), n, C.cast(arr_p, C.c_void_p),
+                                           C.cast(arr_n, C.c_void_p), C.cast(arr_o, C.c_void_p),
+                                           C.cast(arr_c, C.c_void_p) if arr_c is not None else None, C.byref(h)),
+               "agwn_batch_create")
+        self._h = h
+
+    @property
+    def handle(self):
+        if self._h is None:
+            raise RuntimeError("batch is closed")
+        return self._h
+
+    def tune(self, repeats: int = 2) -> dict:
+        _check(library().agwn_batch_tune(self.dispatcher.handle, self.handle, int(repeats)), "agwn_batch_tune")
+        return self.info()
+
+    def set_config(self, block: int, k: int, seg_tile: int, stack: int):
+        cfg = (C.c_int32 * 4)(block, k, seg_tile, stack)
+        _check(library().agwn_batch_set_config(self.handle, C.cast(cfg, C.c_void_p)), "agwn_batch_set_config")
+
+    def info(self) -> dict:
+        cfg = (C.c_int32 * 4)()
+        ncap = C.c_int32(64)
+        ms = (C.c_double * 64)()
+        items, tq, tp = C.c_int64(), C.c_int64(), C.c_double()
+        _check(library().agwn_batch_info(self.handle, C.cast(cfg, C.c_void_p), C.byref(ncap), C.cast(ms, C.c_void_p),
+                                         C.byref(items), C.byref(tq), C.byref(tp)), "agwn_batch_info")
+        return {"config": {"block": cfg[0], "k": cfg[1], "seg_tile": cfg[2], "stack": cfg[3]},
+                "candidates": ncap.value, "tune_ms": list(ms[:min(ncap.value, 64)]), "items": items.value,
+                "queries": tq.value, "pairs": tp.value}
+
+    def run(self, graph: bool = True):
+        _check(library().agwn_batch_run(self.dispatcher.handle, self.handle, 1 if graph else 0), "agwn_batch_run")
+
+    def close(self):
+        if getattr(self, "_h", None) is not None:
+            library().agwn_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def eval_gwnr_mesh_batch_robust(dispatcher: CudaDispatcher, robust: CudaRobustMeshGwn, positions, out_wnrs):

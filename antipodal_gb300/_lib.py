@@ -61,6 +61,12 @@ SIGNATURES = {
     "agwn_probe_fp32_peak": (_I, [_P, C.POINTER(_D)]),
     "agwn_probe_atan2": (_I, [_P, _P, _P, _I64, _P, _P]),
     "agwn_param_batch_fractional_bezier3_f64": (_I, [_P, _P, _I64, _P, _P, _P, _I64, _I, _I, _D, _P, _P, _P]),
+    "agwn_batch_create": (_I, [_P, _P, C.c_int32, _P, _P, _P, _P, _PP]),
+    "agwn_batch_destroy": (_I, [_P]),
+    "agwn_batch_tune": (_I, [_P, _P, C.c_int32]),
+    "agwn_batch_set_config": (_I, [_P, _P]),
+    "agwn_batch_info": (_I, [_P, _P, _P, _P, _P, _P, _P]),
+    "agwn_batch_run": (_I, [_P, _P, C.c_int32]),
     "agwn_mlp_param_count": (_I, []),
     "agwn_mlp_create": (_I, [_P, C.c_uint64, _PP]),
     "agwn_mlp_destroy": (_I, [_P]),

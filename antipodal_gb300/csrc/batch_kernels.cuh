@@ -1,0 +1,221 @@
+// The persistent batch kernel: CTAs take work items (one mesh, a range of its queries) from a device queue
+// (one atomicAdd per item) until it is empty, and evaluate RobustMeshGwn::eval for every query of the item:
+// the integer count by the mesh's ray-frame hierarchy with the exact leaf test, the fractional term over the
+// mesh's boundary staged through shared memory.  Per query the arithmetic and its order are those of the
+// one-mesh kernels (robust.cuh), so the results equal agwn_robust_eval's bit for bit whatever the schedule.
+// Included by batch_p64.cu / batch_p128.cu / batch_pf.cu, one policy each, to compile in parallel.
+#pragma once
+
+#include "batch.cuh"
+#include "robust.cuh"
+#include "tma.cuh"
+
+namespace agwn
+{
+namespace
+{
+template <class P, int kStack>
+__device__ __forceinline__ int batch_count(const BMesh& m, const Frame32& f, qv3<typename P::C> q, int* flags)
+{
+    using C = typename P::C;
+    const C* const tri = static_cast<const C*>(m.tri);
+    if (m.n_tri == 0)
+        return 0;
+    if (m.n_tri == 1)
+        return robust_crossing<P>(q, tri);
+    float const ox = float(P::cdbl(q.x)), oy = float(P::cdbl(q.y)), oz = float(P::cdbl(q.z));
+    float const u = f.r[0] * ox + f.r[1] * oy + f.r[2] * oz;
+    float const v = f.r[3] * ox + f.r[4] * oy + f.r[5] * oz;
+    float const w = f.r[6] * ox + f.r[7] * oy + f.r[8] * oz;
+    float const qmax = fmaxf(fmaxf(fabsf(ox), fabsf(oy)), fabsf(oz));
+    float const tol = (qmax + m.scene_scale) * 3.8146973e-6f + 1e-30f;
+    float const m8 = 8.0f * 1e-6f * (qmax + m.scene_scale);
+    int sum = 0;
+    int cand[kRobCand];
+    int nc = 0;
+    bool const ok = hier_walk<kStack>(m.nodes, m.leaf_uv, u, v, w, tol, m8,
+                                      [&](int leaf)
+                                      {
+                                          if (nc == kRobCand)
+                                          {
+                                              for (int j = 0; j < kRobCand; ++j)
+                                                  sum += robust_crossing<P>(q, tri + 9 * int64_t(cand[j]));
+                                              nc = 0;
+                                          }
+                                          cand[nc++] = leaf;
+                                      });
+    if (!ok)
+        atomicOr(flags + FLAG_STACK, 1);
+    for (int j = 0; j < nc; ++j)
+        sum += robust_crossing<P>(q, tri + 9 * int64_t(cand[j]));
+    return sum;
+}
+
+template <class T, class P, int K, int kStack>
+__global__ void __launch_bounds__(256) k_batch(const BMesh* __restrict__ meshes, const BItem* __restrict__ items,
+                                               int n_items, int* __restrict__ head, int tile, int* flags)
+{
+    using C = typename P::C;
+    using Seg = RSeg<C>;
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ __align__(8) uint64_t bars[2];
+    __shared__ int s_item;
+    __shared__ int abort_cta;
+    Seg* const buf[2] = {reinterpret_cast<Seg*>(smem), reinterpret_cast<Seg*>(smem) + tile};
+    if (threadIdx.x == 0)
+    {
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
+        fence_barrier_init();
+        abort_cta = 0;
+    }
+    __syncthreads();
+    constexpr double f_norm = 2.0 / (4.0 * 3.141592653589793238462643383279502884);
+    unsigned seq = 0; // tile loads this CTA issued before the current item: load g uses buffer g & 1, parity g >> 1
+    for (;;)
+    {
+        if (threadIdx.x == 0)
+            s_item = atomicAdd(head, 1);
+        __syncthreads();
+        int const item_idx = s_item;
+        if (item_idx >= n_items)
+            return;
+        BItem const item = items[item_idx];
+        BMesh const& m = meshes[item.mesh];
+        const Seg* const gseg = static_cast<const Seg*>(m.seg);
+        int64_t const n_seg = m.n_seg;
+        const T* const pos = static_cast<const T*>(m.pos);
+        T* const out = static_cast<T*>(m.out);
+        Quant const qz{{m.qc[0], m.qc[1], m.qc[2]}, m.qs};
+        Frame32 f;
+#pragma unroll
+        for (int k = 0; k < 9; ++k)
+            f.r[k] = m.frame[k];
+        int const n_tiles = n_seg > 0 ? int((n_seg + tile - 1) / tile) : 0;
+        bool const single = n_tiles == 1;
+        int64_t const per_sub = int64_t(blockDim.x) * K;
+        int const n_sub = int((item.q1 - item.q0 + per_sub - 1) / per_sub);
+        int const total = n_tiles == 0 ? 0 : (single ? 1 : n_sub * n_tiles);
+        auto issue = [&](int it)
+        {
+            unsigned const g = seq + unsigned(it);
+            int const b = int(g & 1u);
+            int const st = it % n_tiles;
+            int64_t const rem = n_seg - int64_t(st) * tile;
+            unsigned const bytes = unsigned(rem < tile ? rem : tile) * unsigned(sizeof(Seg));
+            mbar_arrive_expect_tx(&bars[b], bytes);
+            bulk_copy_g2s(buf[b], gseg + int64_t(st) * tile, bytes, &bars[b]);
+        };
+        if (threadIdx.x == 0)
+        {
+            if (total > 0)
+                issue(0);
+            if (total > 1)
+                issue(1);
+        }
+        int it = 0;
+        for (int sub = 0; sub < n_sub; ++sub)
+        {
+            qv3<C> q[K];
+            int cnt[K];
+            double half[K];
+            int64_t idx[K];
+#pragma unroll
+            for (int k = 0; k < K; ++k)
+            {
+                idx[k] = item.q0 + sub * per_sub + int64_t(k) * blockDim.x + threadIdx.x;
+                int64_t const ii = idx[k] < item.q1 ? idx[k] : item.q1 - 1;
+                q[k] = quantize<P>(double(pos[3 * ii]), double(pos[3 * ii + 1]), double(pos[3 * ii + 2]), qz);
+                cnt[k] = batch_count<P, kStack>(m, f, q[k], flags);
+                half[k] = 0.0;
+            }
+            for (int st = 0; st < n_tiles; ++st)
+            {
+                unsigned const g = seq + unsigned(it);
+                int const b = int(g & 1u);
+                if (!single || sub == 0)
+                    if (!mbar_wait_bounded(&bars[b], (g >> 1) & 1u, flags, 5))
+                        abort_cta = 1;
+                __syncthreads();
+                if (abort_cta)
+                    return;
+                Seg const* const sb = buf[b];
+                int64_t const rem = n_seg - int64_t(st) * tile;
+                int const cnt_s = int(rem < tile ? rem : tile);
+                for (int s = 0; s < cnt_s; ++s)
+                {
+                    Seg const sgm = sb[s];
+#pragma unroll
+                    for (int k = 0; k < K; ++k)
+                        half[k] = __dadd_rn(half[k], __dmul_rn(sgm.w, robust_contrib<P>(q[k], sgm)));
+                }
+                if (!single)
+                {
+                    __syncthreads(); // buffer b is free again
+                    if (threadIdx.x == 0 && it + 2 < total)
+                        issue(it + 2);
+                    ++it;
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < K; ++k)
+                if (idx[k] < item.q1)
+                {
+                    T const fr = T(__dmul_rn(half[k], f_norm));
+                    out[idx[k]] = fr + T(cnt[k]);
+                    if (m.counts)
+                        m.counts[idx[k]] = cnt[k];
+                }
+        }
+        seq += unsigned(total);
+        __syncthreads(); // s_item and the buffers are free for the next item
+    }
+}
+
+template <class T, class P>
+using BatchKernel = void (*)(const BMesh*, const BItem*, int, int*, int, int*);
+
+template <class T, class P>
+BatchKernel<T, P> pick_batch_kernel(const BConf& c)
+{
+    if (c.k == 1)
+        return c.stack <= 32 ? k_batch<T, P, 1, 32> : k_batch<T, P, 1, 64>;
+    return c.stack <= 32 ? k_batch<T, P, 2, 32> : k_batch<T, P, 2, 64>;
+}
+
+template <class T, class P>
+int batch_occupancy_t(const BConf& c, size_t smem, int* per_sm)
+{
+    auto const kern = pick_batch_kernel<T, P>(c);
+    AGWN_TRY_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+    AGWN_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, kern, c.block, smem));
+    return AGWN_OK;
+}
+
+template <class T, class P>
+int batch_launch_t(cudaStream_t st, const BConf& c, int grid, size_t smem, const BMesh* meshes, const BItem* items,
+                   int n_items, int* head, int* flags)
+{
+    auto const kern = pick_batch_kernel<T, P>(c);
+    kern<<<grid, c.block, smem, st>>>(meshes, items, n_items, head, c.seg_tile, flags);
+    AGWN_TRY_CUDA(cudaGetLastError());
+    return AGWN_OK;
+}
+
+template <class P>
+struct BatchOpsFor
+{
+    static int occupancy(int scalar_bytes, const BConf& c, size_t smem, int* per_sm)
+    {
+        return scalar_bytes == 4 ? batch_occupancy_t<float, P>(c, smem, per_sm)
+                                 : batch_occupancy_t<double, P>(c, smem, per_sm);
+    }
+    static int launch(int scalar_bytes, cudaStream_t st, const BConf& c, int grid, size_t smem, const BMesh* meshes,
+                      const BItem* items, int n_items, int* head, int* flags)
+    {
+        return scalar_bytes == 4 ? batch_launch_t<float, P>(st, c, grid, smem, meshes, items, n_items, head, flags)
+                                 : batch_launch_t<double, P>(st, c, grid, smem, meshes, items, n_items, head, flags);
+    }
+};
+} // namespace
+} // namespace agwn

@@ -50,13 +50,14 @@ __device__ __forceinline__ bool may_hit(const float4* __restrict__ leaf_uv, int 
 }
 
 // Walks the hierarchy for the query point (u, v) and depth w, calling emit(leaf) for every leaf whose box the ray
-// {(u, v, w') : w' >= w} meets (widened by tol) and that passes may_hit.  Returns false if the stack overflowed.
-template <class Emit>
+// {(u, v, w') : w' >= w} meets (widened by tol) and that passes may_hit.  Returns false if the stack of kStack
+// pending subtrees overflowed (a hierarchy of depth d needs at most d - 1).
+template <int kStack = kStackDepth, class Emit>
 __device__ __forceinline__ bool hier_walk(const BvhNode* __restrict__ nodes, const float4* __restrict__ leaf_uv,
                                           float u, float v, float w, float tol, float m8, Emit&& emit)
 {
     float const ulo = u + tol, uhi = u - tol, vlo = v + tol, vhi = v - tol, wq = w - tol;
-    int stack[kStackDepth];
+    int stack[kStack];
     int sp = 0;
     int node = 0;
     while (true)
@@ -86,7 +87,7 @@ __device__ __forceinline__ bool hier_walk(const BvhNode* __restrict__ nodes, con
                 next = rc;
             else
             {
-                if (sp == kStackDepth)
+                if (sp == kStack)
                     return false;
                 stack[sp++] = rc;
             }

@@ -180,6 +180,32 @@ int agwn_robust_eval_f64(agwn_context* ctx, const agwn_robust* robust, const dou
 int agwn_robust_eval_f32(agwn_context* ctx, const agwn_robust* robust, const float* positions, int64_t n,
                          float* out_gwn, int32_t* out_counts, float* out_frac);
 
+/* ---- many robust meshes in one persistent launch ----------------------------------------------------------
+ * No single reference counterpart: the result equals calling eval_gwnr_mesh_batch_robust
+ * (src/antipodal/gwn_mesh_robust.hh:441-456) once per mesh -- out_i[j] = meshes[i].eval(positions_i[j]) --
+ * bit for bit, for meshes and query arrays of any (uneven) sizes.  All meshes share the scalar type and the
+ * precision policy; positions[i] (n_queries[i] * 3 scalars), out[i] and the optional counts[i] (integer term)
+ * are device memory and, like the meshes, must outlive the plan.  The plan holds the device work list (ranges of
+ * one mesh's queries, longest first) and the launch configuration.
+ *   agwn_batch_tune: times every configuration {block 128/256, queries per thread 1/2, segment tile 256/512/1024,
+ *     traversal stack 32/64 (32 only where every hierarchy is shallower)} on a sample of every mesh's queries,
+ *     `repeats` times each, and keeps the fastest.
+ *   agwn_batch_run: one persistent launch over the whole work list on the context's stream; with use_graph the
+ *     queue reset and the launch are captured into a CUDA graph on the first run (and again after the
+ *     configuration changes) and replayed afterwards.
+ *   agwn_batch_info: config = {block, queries per thread, segment tile, stack}; *n_candidates in: capacity of
+ *     tune_ms, out: number of candidates; tune_ms: each candidate's sample time (-1 = did not fit / not run). */
+typedef struct agwn_batch agwn_batch;
+int agwn_batch_create(agwn_context* ctx, const agwn_robust* const* meshes, int32_t n_meshes,
+                      const void* const* positions, const int64_t* n_queries, void* const* out,
+                      int32_t* const* counts, agwn_batch** plan);
+int agwn_batch_destroy(agwn_batch* plan);
+int agwn_batch_tune(agwn_context* ctx, agwn_batch* plan, int32_t repeats);
+int agwn_batch_set_config(agwn_batch* plan, const int32_t* config);
+int agwn_batch_info(const agwn_batch* plan, int32_t* config, int32_t* n_candidates, double* tune_ms,
+                    int64_t* n_items, int64_t* total_queries, double* total_pairs);
+int agwn_batch_run(agwn_context* ctx, agwn_batch* plan, int32_t use_graph);
+
 /* ---- parametric surfaces ----------------------------------------------------------------------------------
  * Replaces eval_gwnr_parametric_batch_fractional (src/antipodal/gwn_parametric.hh:168-186) with the default
  * IntegratorGK15 (src/antipodal/math/integrate_gk15.hh:63-290) and integrate_config {min_depth, max_depth, tol}
