@@ -175,6 +175,12 @@ class CudaDispatcher:
         _check(library().agwn_probe_fp32_peak(self.handle, C.byref(v)), "agwn_probe_fp32_peak")
         return v.value
 
+    def probe_fp64_peak(self) -> float:
+        """Measured FP64 FMA throughput of this GPU, TFLOP/s."""
+        v = C.c_double()
+        _check(library().agwn_probe_fp64_peak(self.handle, C.byref(v)), "agwn_probe_fp64_peak")
+        return v.value
+
     def parallel_for(self, begin, end, f):  # noqa: D401 - concept member, deliberately unavailable
         raise TypeError("CudaDispatcher runs the library's GWN kernels only; generic host callables are not "
                         "executed (no CPU fallback)")

@@ -60,6 +60,7 @@ SIGNATURES = {
     "agwn_robust_eval_f32": (_I, [_P, _P, _P, _I64, _P, _P, _P]),
     "agwn_probe_fp32_peak": (_I, [_P, C.POINTER(_D)]),
     "agwn_probe_atan2": (_I, [_P, _P, _P, _I64, _P, _P]),
+    "agwn_probe_fp64_peak": (_I, [_P, _P]),
     "agwn_param_batch_fractional_bezier3_f64": (_I, [_P, _P, _I64, _P, _P, _P, _I64, _I, _I, _D, _P, _P, _P]),
     "agwn_batch_create": (_I, [_P, _P, C.c_int32, _P, _P, _P, _P, _PP]),
     "agwn_batch_destroy": (_I, [_P]),

@@ -31,10 +31,62 @@ __global__ void __launch_bounds__(256) k_ffma(int iters, float a, float b, float
     if (s == -1.2345e-30f)
         sink[0] = s;
 }
+// The same for FP64 fused multiply-add (the parametric integrator's pipe).
+__global__ void __launch_bounds__(256) k_dfma(int iters, double a, double b, double* sink)
+{
+    double v[kChains];
+#pragma unroll
+    for (int c = 0; c < kChains; ++c)
+        v[c] = a + double(threadIdx.x + c);
+    for (int i = 0; i < iters; ++i)
+    {
+#pragma unroll
+        for (int c = 0; c < kChains; ++c)
+            v[c] = fma(v[c], a, b);
+    }
+    double s = 0.0;
+#pragma unroll
+    for (int c = 0; c < kChains; ++c)
+        s += v[c];
+    if (s == -1.2345e-300)
+        sink[0] = s;
+}
 } // namespace
 } // namespace agwn
 
 using namespace agwn;
+
+extern "C" int agwn_probe_fp64_peak(agwn_context* ctx, double* tflops)
+{
+    AGWN_CHECK_ARG(ctx && tflops, "null argument");
+    AGWN_TRY_CUDA(cudaSetDevice(ctx->device));
+    double* sink = nullptr;
+    AGWN_TRY(ctx->scratch_reserve(S_MISC3, sizeof(double), reinterpret_cast<void**>(&sink)));
+    int per_sm = 0;
+    AGWN_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_dfma, 256, 0));
+    int const grid = ctx->sm_count * per_sm;
+    int const iters = 1 << 10;
+    cudaEvent_t e0, e1;
+    AGWN_TRY_CUDA(cudaEventCreate(&e0));
+    AGWN_TRY_CUDA(cudaEventCreate(&e1));
+    float best = 1e30f;
+    for (int rep = 0; rep < 4; ++rep)
+    {
+        AGWN_TRY_CUDA(cudaEventRecord(e0, ctx->stream));
+        k_dfma<<<grid, 256, 0, ctx->stream>>>(iters, 0.9999, 1e-4, sink);
+        AGWN_TRY_CUDA(cudaEventRecord(e1, ctx->stream));
+        AGWN_TRY_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        AGWN_TRY_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        if (rep > 0 && ms < best)
+            best = ms;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    double const flops = 2.0 * kChains * double(iters) * double(grid) * 256.0;
+    *tflops = flops / (double(best) * 1e-3) / 1e12;
+    return AGWN_OK;
+}
 
 extern "C" int agwn_probe_fp32_peak(agwn_context* ctx, double* tflops)
 {

@@ -50,6 +50,11 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample budget")
     ap.add_argument("--plain-steps", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--config", choices=["mesh", "cube", "batch", "robust", "param"], default="mesh",
+                    help="mesh: the headline single-mesh workload (default); the others are the secondary "
+                         "workloads, each printing its own JSON line (see run_secondary)")
+    ap.add_argument("--scale", type=float, default=1.0,
+                    help="secondary workloads: fraction of the full query count (batch: of the grid side)")
     return ap.parse_args()
 
 
@@ -340,10 +345,263 @@ def run_ours(args):
     return 0
 
 
+# ---- secondary workloads ----------------------------------------------------------------------------------------
+# Each prints one JSON line: the same metric (queries/s) on another configuration, the chosen form against the
+# plain one where the configuration has both, accuracy against the CPU oracle on a seeded sample, and the CPU
+# oracle's rate on a bounded sample.  Run with --config {cube, batch, robust, param}; single GPU only.
+
+def _timer(stream):
+    import torch
+
+    def timed(n, fn):
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(n):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / n
+    return timed
+
+
+def _oracle():
+    from oracle.oracle import Oracle, LIB, build
+    if not os.path.exists(LIB):
+        build()
+    return Oracle()
+
+
+def _cpu_sample_rate(fn, n_total, seconds, unit_per_item=1.0):
+    """Times fn(m) (m items, all host threads inside fn) on a sample sized to about ``seconds``."""
+    m = 16
+    t0 = time.perf_counter()
+    fn(m)
+    dt = max(time.perf_counter() - t0, 1e-6)
+    m = int(min(n_total, max(m, m * seconds / dt)))
+    t0 = time.perf_counter()
+    fn(m)
+    dt = time.perf_counter() - t0
+    return m * unit_per_item / dt, m
+
+
+def run_cube(args, ag, torch, stream, disp, timed):
+    """Rotated open unit cube (10 triangles, 4 boundary segments), 1e5 float64 queries; full GWN."""
+    from antipodal_gb300 import synth
+    verts, idx, bnd, q, x0 = synth.rotated_open_cube(seed=0, n_queries=int(100_000 * args.scale))
+    Q = len(q)
+    isect = ag.CudaIntersector(disp, verts, idx)
+    qd, bd = torch.from_numpy(q).cuda(), torch.from_numpy(bnd).cuda()
+    plain, out = torch.empty(Q, dtype=torch.float64, device="cuda"), torch.empty(Q, dtype=torch.float64, device="cuda")
+    disp.set_precision("exact")
+    for _ in range(args.warmup):
+        ag.eval_gwnr_mesh_batch(disp, isect, qd, plain, x0, bd)
+    ms_plain = timed(args.steps, lambda: ag.eval_gwnr_mesh_batch(disp, isect, qd, plain, x0, bd))
+    disp.set_precision("mixed")
+    for _ in range(args.warmup):
+        ag.eval_gwnr_mesh_batch(disp, isect, qd, out, x0, bd)
+    ms = timed(args.steps, lambda: ag.eval_gwnr_mesh_batch(disp, isect, qd, out, x0, bd))
+    o = _oracle()
+    ref = o.full_naive(q, x0, verts, idx, bnd)
+    rate, m = _cpu_sample_rate(lambda m: o.full_naive(q[:m], x0, verts, idx, bnd), Q, args.cpu_seconds)
+    isect.close()
+    return {"metric": METRIC, "value": Q / (ms * 1e-3), "unit": "queries/s", "ms_per_step": ms,
+            "config": {"workload": "rotated open unit cube, 10 triangles, 4 boundary segments, "
+                                   f"{Q} uniform float64 queries in [-1.5,1.5]^3, full GWN", "queries": Q},
+            "plain": {"value": Q / (ms_plain * 1e-3), "ms_per_step": ms_plain},
+            "chosen_over_plain": ms_plain / ms,
+            "accuracy": {"max_abs_err_plain_vs_cpu_oracle": float(np.abs(plain.cpu().numpy() - ref).max()),
+                         "max_abs_err_chosen_vs_cpu_oracle": float(np.abs(out.cpu().numpy() - ref).max())},
+            "cpu_baseline": {"value": rate, "unit": "queries/s", "cores": os.cpu_count(), "kind": "port",
+                             "sample": f"first {m} queries, full GWN"}}
+
+
+def batch_workload(scale, seed=2024, n_meshes=64):
+    """64 noisy icospheres / tori (1e3..2e5 triangles, log-uniform; 1..20 holes), one float32 grid each with side
+    log-uniform in [64, 192] (times ``scale``)."""
+    import math
+    from antipodal_gb300 import synth
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n_meshes):
+        ntri = int(math.exp(rng.uniform(math.log(1e3), math.log(2e5))))
+        kind = "icosphere" if rng.random() < 0.5 else "torus"
+        v, i = synth.noisy_mesh(kind, ntri, int(rng.integers(1, 21)), rng)
+        b = synth.boundary_segments(v, i)
+        side = max(4, int(round(math.exp(rng.uniform(math.log(64), math.log(192))) * scale)))
+        q = synth.grid_queries(v.min(0), v.max(0), side).astype(np.float32)
+        out.append((v.astype(np.float32), i, b.astype(np.float32), q))
+    return out
+
+
+def run_batch(args, ag, torch, stream, disp, timed):
+    """64 uneven robust meshes (int64_grid, float32), one persistent launch replayed from a CUDA graph."""
+    wl = batch_workload(args.scale)
+    meshes = [ag.CudaRobustMeshGwn(disp, v, i, b, precision="int64_grid") for v, i, b, _ in wl]
+    pos = [torch.from_numpy(q).cuda() for *_, q in wl]
+    outs = [torch.empty(len(q), dtype=torch.float32, device="cuda") for *_, q in wl]
+    ref_outs = [torch.empty_like(o) for o in outs]
+    batch = ag.CudaRobustBatch(disp, meshes, pos, outs)
+    t0 = time.perf_counter()
+    tuned = batch.tune(repeats=2)
+    tune_s = time.perf_counter() - t0
+    Q = tuned["queries"]
+    for _ in range(args.warmup):
+        batch.run(graph=True)
+    ms = timed(args.steps, lambda: batch.run(graph=True))
+
+    def per_mesh():
+        for r, p, o in zip(meshes, pos, ref_outs):
+            r.evaluate(p, o)
+    per_mesh()
+    ms_loop = timed(max(1, args.plain_steps), per_mesh)
+    same = all(torch.equal(a, b) for a, b in zip(outs, ref_outs))
+    # the CPU oracle (the reference's RobustMeshGwn rule) on a few queries of every mesh
+    o = _oracle()
+    worst, n_diff = 0.0, 0
+    for (v, i, b, q), out in zip(wl[:8], outs[:8]):
+        pick = np.random.default_rng(5).choice(len(q), size=min(len(q), 200), replace=False)
+        gw, _, _ = o.robust_eval("int64_grid", v, i, b, q[pick])
+        got = out.cpu().numpy()[pick]
+        worst = max(worst, float(np.abs(got.astype(np.float64) - gw.astype(np.float64)).max()))
+        n_diff += int(np.sum(got != gw))
+
+    v0, i0, b0, q0 = wl[0]
+    rate, m = _cpu_sample_rate(lambda m: o.robust_eval("int64_grid", v0, i0, b0, q0[:m]), len(q0), args.cpu_seconds)
+    for x in meshes:
+        x.close()
+    batch.close()
+    return {"metric": METRIC, "value": Q / (ms * 1e-3), "unit": "queries/s", "ms_per_step": ms,
+            "config": {"workload": "64 noisy icospheres/tori (1e3..2e5 triangles, 1..20 holes), one float32 grid "
+                                   f"each (side log-uniform 64..192 x {args.scale}), RobustMeshGwn<float, "
+                                   "int64_grid>, one persistent launch, CUDA graph", "queries": Q,
+                       "pair_units": tuned["pairs"], "items": tuned["items"], "tuned": tuned["config"],
+                       "tune_seconds": tune_s},
+            "plain": {"value": Q / (ms_loop * 1e-3), "ms_per_step": ms_loop,
+                      "form": "one agwn_robust_eval call per mesh (two launches each)"},
+            "chosen_over_plain": ms_loop / ms,
+            "accuracy": {"bit_identical_to_per_mesh": bool(same),
+                         "sample_max_abs_err_vs_cpu_oracle": worst, "sample_values_not_identical": n_diff,
+                         "sample_size": 8 * 200},
+            "cpu_baseline": {"value": rate, "unit": "queries/s", "cores": os.cpu_count(), "kind": "port",
+                             "sample": f"first {m} queries of mesh 0 ({len(b0)} segments), RobustMeshGwn rule"}}
+
+
+def run_robust(args, ag, torch, stream, disp, timed):
+    """Two interpenetrating perturbed tori (1M triangles, 20 holes), 1e7 float64 queries, half within
+    1e-9..1e-3 of the surface; RobustMeshGwn<double, int128_grid> and <double, exact_float>."""
+    from antipodal_gb300 import synth
+    v, i, b, q = synth.two_tori(seed=0, n_queries=int(10_000_000 * args.scale))
+    Q = len(q)
+    qd = torch.from_numpy(q).cuda()
+    res = {}
+    o = _oracle()
+    pick = np.random.default_rng(9).choice(Q, size=400, replace=False)
+    for pol in ("int128_grid", "exact_float"):
+        t0 = time.perf_counter()
+        r = ag.CudaRobustMeshGwn(disp, v, i, b, precision=pol)
+        disp.synchronize()
+        build_ms = 1e3 * (time.perf_counter() - t0)
+        out = torch.empty(Q, dtype=torch.float64, device="cuda")
+        cnt = torch.empty(Q, dtype=torch.int32, device="cuda")
+        r.evaluate(qd, out, cnt)
+        ms = timed(args.steps, lambda: r.evaluate(qd, out, cnt))
+        gw, rc, _ = o.robust_eval(pol, v, i, b, q[pick])
+        res[pol] = {"value": Q / (ms * 1e-3), "ms_per_step": ms, "build_ms": build_ms,
+                    "sample_count_mismatches_vs_cpu_oracle": int(np.sum(cnt.cpu().numpy()[pick] != rc)),
+                    "sample_max_abs_err_vs_cpu_oracle": float(np.abs(out.cpu().numpy()[pick] - gw).max())}
+        r.close()
+    rate, m = _cpu_sample_rate(lambda m: o.robust_eval("exact_float", v, i, b, q[:m]), Q, args.cpu_seconds)
+    return {"metric": METRIC, "value": res["exact_float"]["value"], "unit": "queries/s",
+            "ms_per_step": res["exact_float"]["ms_per_step"],
+            "config": {"workload": f"two perturbed tori, {len(i) // 3} triangles, {len(b)} boundary segments, "
+                                   f"{Q} float64 queries (half uniform, half 1e-9..1e-3 off the surface)",
+                       "queries": Q},
+            "policies": res,
+            "cpu_baseline": {"value": rate, "unit": "queries/s", "cores": os.cpu_count(), "kind": "port",
+                             "sample": f"first {m} queries, exact_float"}}
+
+
+def run_param(args, ag, torch, stream, disp, timed):
+    """256 bicubic patches (1,024 boundary cubics), float64 queries (30% within 1e-3 of a curve), GK15 at
+    tol 1e-10: the plain adaptive integrator against the learned start-depth proposal (trained here)."""
+    from antipodal_gb300 import synth
+    n_q = max(64, int(1_000_000 * args.scale))
+    curves, q, x0 = synth.bezier_patches(seed=0, n_patches=256, n_queries=n_q)
+    cfg = ag.IntegrateConfig(0, 10, 1e-10)
+    net = ag.LearnedGK15Proposal(disp, seed=3, n_classes=11, alpha=0.02)
+    tc, tq, tx = synth.bezier_patches(seed=101, n_patches=256, n_queries=2000)
+    t0 = time.perf_counter()
+    tqd, tcd = torch.from_numpy(tq).cuda(), torch.from_numpy(tc).cuda()
+    lab = net.labels(tqd, tx, tcd, cfg)
+    feat = net.features(tqd, tx, tcd, cfg.tol)
+    hist = net.train(feat, lab, steps=4000, batch=8192, lr=2e-3, seed=1)
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t0
+    Q, Cn = len(q), len(curves)
+    qd, cd = torch.from_numpy(q).cuda(), torch.from_numpy(curves).cuda()
+    plain = torch.empty(Q, dtype=torch.float64, device="cuda")
+    out = torch.empty_like(plain)
+    nodes_p = torch.empty(Q, dtype=torch.int32, device="cuda")
+    nodes_l = torch.empty_like(nodes_p)
+    ag.eval_gwnr_parametric_batch_fractional(disp, qd, plain, x0, cd, cfg, nodes_per_query=nodes_p)
+    ms_plain = timed(args.steps, lambda: ag.eval_gwnr_parametric_batch_fractional(disp, qd, plain, x0, cd, cfg))
+    ag.eval_gwnr_parametric_batch_fractional(disp, qd, out, x0, cd, cfg, integrator=net, nodes_per_query=nodes_l)
+    ms = timed(args.steps, lambda: ag.eval_gwnr_parametric_batch_fractional(disp, qd, out, x0, cd, cfg,
+                                                                            integrator=net))
+    err = float((out - plain).abs().max().item())
+    panels_p, panels_l = int(nodes_p.sum().item()), int(nodes_l.sum().item())
+    fp64 = disp.probe_fp64_peak()
+    achieved = panels_p * 15 * 150 / (ms_plain * 1e-3) / 1e12
+    o = _oracle()
+    pick = np.random.default_rng(4).choice(Q, size=32, replace=False)
+    ref = o.param_frac_bezier3(q[pick], x0, curves, 0, 10, 1e-10)
+    rate, m = _cpu_sample_rate(lambda m: o.param_frac_bezier3(q[:m], x0, curves, 0, 10, 1e-10), Q, args.cpu_seconds)
+    net.close()
+    return {"metric": METRIC, "value": Q / (ms * 1e-3), "unit": "queries/s", "ms_per_step": ms,
+            "config": {"workload": f"256 bicubic Bezier patches ({Cn} boundary cubics), {Q} float64 queries "
+                                   "(30% within 1e-3 of a curve), adaptive GK15 tol 1e-10, max depth 10",
+                       "queries": Q, "pairs": Q * Cn},
+            "plain": {"value": Q / (ms_plain * 1e-3), "ms_per_step": ms_plain, "panels_per_pair": panels_p / (Q * Cn)},
+            "learned": {"panels_per_pair": panels_l / (Q * Cn), "train_seconds": train_s,
+                        "train_loss_first_last": [float(hist[:20].mean()), float(hist[-100:].mean())],
+                        "labels": int(lab.numel())},
+            "chosen_over_plain": ms_plain / ms,
+            "accuracy": {"max_abs_err_learned_vs_plain": err,
+                         "sample_plain_bit_identical_to_cpu_oracle": bool(np.array_equal(plain.cpu().numpy()[pick], ref))},
+            "roofline": {"bound": "fp64", "achieved": achieved, "peak": fp64, "unit": "TFLOP/s",
+                         "frac": achieved / fp64,
+                         "note": "plain integrator, 15 integrand evaluations x 150 algorithmic FP64 flop per panel; "
+                                 "peak = FP64 FMA rate measured on this GPU in this run"},
+            "cpu_baseline": {"value": rate, "unit": "queries/s", "cores": os.cpu_count(), "kind": "port",
+                             "sample": f"first {m} queries x {Cn} curves"}}
+
+
+def run_secondary(args):
+    import torch
+    import antipodal_gb300 as ag
+    torch.cuda.set_device(0)
+    stream = torch.cuda.current_stream()
+    disp = ag.CudaDispatcher(device=0, stream=stream)
+    timed = _timer(stream)
+    fn = {"cube": run_cube, "batch": run_batch, "robust": run_robust, "param": run_param}[args.config]
+    clocks = Clocks(0)
+    clocks.start()
+    line = fn(args, ag, torch, stream, disp, timed)
+    line["clocks"] = clocks.stop()
+    line.update({"n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+                 "scaling": "weak", "vs_baseline": None, "data": "synthetic", "config_name": args.config})
+    print(json.dumps(line), flush=True)
+    disp.close()
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.config != "mesh":
+        return run_secondary(args)
     return run_ours(args)
 
 

@@ -277,6 +277,8 @@ int agwn_mesh_batch_fractional_mixed_noalloc_f64(void* stream, const double* pos
  * launches of independent FMA chains).  No reference counterpart: it is the denominator of the fractional
  * kernel's compute roofline. */
 int agwn_probe_fp32_peak(agwn_context* ctx, double* tflops);
+/* The same for FP64 fused multiply-add: the denominator of the parametric integrator's roofline. */
+int agwn_probe_fp64_peak(agwn_context* ctx, double* tflops);
 /* The mixed kernel's own float atan2 and CUDA's atan2f on the same n inputs (host or device arrays), for testing
  * the former's error.  No reference counterpart. */
 int agwn_probe_atan2(agwn_context* ctx, const float* y, const float* x, int64_t n, float* ours, float* cuda_ref);
