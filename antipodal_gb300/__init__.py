@@ -528,7 +528,8 @@ def eval_gwnr_parametric_batch_fractional(dispatcher: CudaDispatcher, positions,
     if p.n != o.n:
         raise ValueError("positions and out_wnrs must have the same size")
     c = _View(curves, np.float64, 12, "curves")
-    if start_depth is None and integrator is not None:
+    learned = start_depth is None and isinstance(integrator, LearnedGK15Proposal)
+    if start_depth is None and integrator is not None and not learned:
         start_depth = integrator.start_depths(dispatcher, positions, x0, curves, cfg)
     sd = _View(start_depth, np.uint8, None, "start_depth") if start_depth is not None else None
     if sd is not None and sd.n != p.n * c.n:
@@ -542,10 +543,16 @@ def eval_gwnr_parametric_batch_fractional(dispatcher: CudaDispatcher, positions,
     if nd is not None and nd.n != p.n:
         raise ValueError("nodes_per_query must hold one entry per query")
     _, xp = x = _vec3(x0, np.float64)
-    fn = library().agwn_param_batch_fractional_bezier3_f64
-    _check(fn(dispatcher.handle, p.ptr, p.n, o.ptr, xp, c.ptr, c.n, cfg.min_depth, cfg.max_depth, cfg.tol,
-              sd.ptr if sd else None, st.ptr if st else None, nd.ptr if nd else None),
-           "eval_gwnr_parametric_batch_fractional")
+    if learned:  # propose and integrate in one call; the start depths stay in device scratch
+        fn = library().agwn_param_batch_fractional_learned_bezier3_f64
+        _check(fn(dispatcher.handle, integrator.handle, p.ptr, p.n, o.ptr, xp, c.ptr, c.n, integrator.n_classes,
+                  cfg.min_depth, cfg.max_depth, cfg.tol, integrator.alpha, st.ptr if st else None,
+                  nd.ptr if nd else None), "eval_gwnr_parametric_batch_fractional")
+    else:
+        fn = library().agwn_param_batch_fractional_bezier3_f64
+        _check(fn(dispatcher.handle, p.ptr, p.n, o.ptr, xp, c.ptr, c.n, cfg.min_depth, cfg.max_depth, cfg.tol,
+                  sd.ptr if sd else None, st.ptr if st else None, nd.ptr if nd else None),
+               "eval_gwnr_parametric_batch_fractional")
     del x
 
 

@@ -151,6 +151,15 @@ int stage_in(Context& ctx, const void* src, size_t bytes, int slot, const void**
 // Output staging: returns `dst` for device memory, else scratch `slot`; `*host` tells whether a copy back is due.
 int stage_out(Context& ctx, void* dst, size_t bytes, int slot, void** dev, bool* host);
 
+// ---- parametric path (param.cu, mlp.cu) ----------------------------------------------------------------------
+// Device-side runners behind the parametric entry points; all pointers are device memory of the context's GPU.
+int param_run(Context& ctx, const double* d_pos, int64_t n, double* d_out, const double* x0, const double* d_curves,
+              int64_t n_curves, int min_depth, int max_depth, double tol, const uint8_t* d_start, uint32_t* d_stats,
+              int32_t* d_nodes);
+int mlp_propose_run(Context& ctx, const agwn_mlp* mlp, const double* d_pos, int64_t n, const double* x0,
+                    const double* d_curves, int64_t n_curves, int n_classes, int min_depth, int max_depth, double tol,
+                    float alpha, uint8_t* d_start, float* d_logits);
+
 // ---- launch geometry ---------------------------------------------------------------------------------------
 inline int div_up(int64_t a, int64_t b)
 {

@@ -1029,6 +1029,35 @@ extern "C" int agwn_mlp_train(agwn_context* ctx, agwn_mlp* mlp, const float* fea
     return st != AGWN_OK ? st : ctx->check_flags();
 }
 
+namespace agwn
+{
+int mlp_propose_run(Context& ctx, const agwn_mlp* mlp, const double* d_pos, int64_t n, const double* x0,
+                    const double* d_curves, int64_t n_curves, int n_classes, int min_depth, int max_depth, double tol,
+                    float alpha, uint8_t* d_start, float* d_logits)
+{
+    AGWN_CHECK_ARG(ctx.device == mlp->device, "the network lives on device %d, the context on %d", mlp->device,
+                   ctx.device);
+    AGWN_CHECK_ARG(n_classes >= 2 && n_classes <= kC, "n_classes must be in [2, %d]", kC);
+    AGWN_CHECK_ARG(alpha >= 0.f && alpha < 1.f, "alpha must be in [0, 1)");
+    AGWN_TRY(mlp_smem_setup());
+    int64_t const total = n * n_curves;
+    if (total == 0)
+        return AGWN_OK;
+    int per_sm = 0;
+    AGWN_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_propose, kInferWarps * 32,
+                                                               sizeof(InferSmem)));
+    int64_t const n_groups = div_up(total, 32);
+    int const grid = int(std::max<int64_t>(1, std::min<int64_t>(div_up(n_groups, kInferWarps),
+                                                                int64_t(std::max(per_sm, 1)) * ctx.sm_count)));
+    AGWN_TRY(ctx.launch_begin(AGWN_K_PARAMETRIC));
+    k_propose<<<grid, kInferWarps * 32, sizeof(InferSmem), ctx.stream>>>(
+        static_cast<const __nv_bfloat16*>(mlp->wb.ptr), static_cast<const float*>(mlp->params.ptr), d_pos, n,
+        float(x0[0]), float(x0[1]), float(x0[2]), d_curves, n_curves, float(std::log10(tol) / 10.0), n_classes, alpha,
+        min_depth, max_depth, d_start, d_logits);
+    return ctx.launch_end(AGWN_K_PARAMETRIC);
+}
+} // namespace agwn
+
 extern "C" int agwn_param_propose_depth_bezier3_f64(agwn_context* ctx, const agwn_mlp* mlp, const double* positions,
                                                     int64_t n, const double* x0, const double* curves,
                                                     int64_t n_curves, int n_classes, int min_depth, int max_depth,
@@ -1037,9 +1066,8 @@ extern "C" int agwn_param_propose_depth_bezier3_f64(agwn_context* ctx, const agw
     AGWN_TRY(check_mlp(ctx, mlp));
     AGWN_CHECK_ARG(x0 && n >= 0 && n_curves >= 0, "bad arguments");
     AGWN_CHECK_ARG((n == 0 || n_curves == 0) || (positions && curves && (start_depth || logits)), "null array");
-    AGWN_CHECK_ARG(n_classes >= 2 && n_classes <= kC, "n_classes must be in [2, %d]", kC);
     AGWN_CHECK_ARG(min_depth >= 0 && max_depth >= 0 && max_depth <= 255, "bad depths");
-    AGWN_CHECK_ARG(std::isfinite(tol) && tol > 0 && alpha >= 0.f && alpha < 1.f, "bad tol/alpha");
+    AGWN_CHECK_ARG(std::isfinite(tol) && tol > 0, "bad tol");
     clear_message();
     int64_t const total = n * n_curves;
     if (total == 0)
@@ -1053,19 +1081,9 @@ extern "C" int agwn_param_propose_depth_bezier3_f64(agwn_context* ctx, const agw
         AGWN_TRY(stage_out(*ctx, start_depth, size_t(total), S_MISC1, &dsd, &h_sd));
     if (logits)
         AGWN_TRY(stage_out(*ctx, logits, sizeof(float) * kC * total, S_MISC2, &dlog, &h_log));
-    int per_sm = 0;
-    AGWN_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_propose, kInferWarps * 32,
-                                                               sizeof(InferSmem)));
-    int64_t const n_groups = div_up(total, 32);
-    int const grid = int(std::max<int64_t>(1, std::min<int64_t>(div_up(n_groups, kInferWarps),
-                                                                int64_t(std::max(per_sm, 1)) * ctx->sm_count)));
-    AGWN_TRY(ctx->launch_begin(AGWN_K_PARAMETRIC));
-    k_propose<<<grid, kInferWarps * 32, sizeof(InferSmem), ctx->stream>>>(
-        static_cast<const __nv_bfloat16*>(mlp->wb.ptr), static_cast<const float*>(mlp->params.ptr),
-        static_cast<const double*>(dpos), n, float(x0[0]), float(x0[1]), float(x0[2]),
-        static_cast<const double*>(dcur), n_curves, float(std::log10(tol) / 10.0), n_classes, alpha, min_depth,
-        max_depth, static_cast<uint8_t*>(dsd), static_cast<float*>(dlog));
-    AGWN_TRY(ctx->launch_end(AGWN_K_PARAMETRIC));
+    AGWN_TRY(mlp_propose_run(*ctx, mlp, static_cast<const double*>(dpos), n, x0, static_cast<const double*>(dcur),
+                             n_curves, n_classes, min_depth, max_depth, tol, alpha, static_cast<uint8_t*>(dsd),
+                             static_cast<float*>(dlog)));
     if (h_sd)
         AGWN_TRY_CUDA(cudaMemcpyAsync(start_depth, dsd, size_t(total), cudaMemcpyDeviceToHost, ctx->stream));
     if (h_log)

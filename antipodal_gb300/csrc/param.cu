@@ -354,11 +354,13 @@ int param_run(Context& ctx, const double* d_pos, int64_t n, double* d_out, const
 
 using namespace agwn;
 
-extern "C" int agwn_param_batch_fractional_bezier3_f64(agwn_context* ctx, const double* positions, int64_t n,
-                                                       double* out, const double* x0, const double* curves,
-                                                       int64_t n_curves, int min_depth, int max_depth, double tol,
-                                                       const uint8_t* start_depth, uint32_t* pair_stats,
-                                                       int32_t* nodes_per_query)
+namespace
+{
+// The parametric entry points: stage, optionally propose start depths with the learned network (mlp != NULL), run
+// the integrator, copy host outputs back.
+int param_entry(agwn_context* ctx, const agwn_mlp* mlp, int n_classes, float alpha, const double* positions, int64_t n,
+                double* out, const double* x0, const double* curves, int64_t n_curves, int min_depth, int max_depth,
+                double tol, const uint8_t* start_depth, uint32_t* pair_stats, int32_t* nodes_per_query)
 {
     AGWN_CHECK_ARG(ctx && x0, "null context/x0");
     AGWN_CHECK_ARG(n >= 0 && n_curves >= 0 && (n == 0 || (positions && out)) && (n_curves == 0 || curves),
@@ -367,6 +369,7 @@ extern "C" int agwn_param_batch_fractional_bezier3_f64(agwn_context* ctx, const 
                    "depths must be in [0, %d] (max_depth bounds the explicit stack)", kParamMaxDepth);
     AGWN_CHECK_ARG(std::isfinite(tol) && tol >= 0, "tol must be finite and >= 0");
     AGWN_CHECK_ARG(n_curves < (int64_t(1) << 31), "too many curves");
+    AGWN_CHECK_ARG(!mlp || tol > 0, "the learned proposal needs tol > 0");
     clear_message();
     AGWN_TRY_CUDA(cudaSetDevice(ctx->device));
     if (n == 0)
@@ -392,6 +395,15 @@ extern "C" int agwn_param_batch_fractional_bezier3_f64(agwn_context* ctx, const 
                                       ctx->stream));
         dcur = aligned;
     }
+    if (mlp && n_curves > 0)
+    {
+        void* proposed = nullptr;
+        AGWN_TRY(ctx->scratch_reserve(S_MISC1, size_t(n) * n_curves, &proposed));
+        AGWN_TRY(mlp_propose_run(*ctx, mlp, static_cast<const double*>(dpos), n, x0, static_cast<const double*>(dcur),
+                                 n_curves, n_classes, min_depth, max_depth, tol, alpha,
+                                 static_cast<uint8_t*>(proposed), nullptr));
+        dstart = proposed;
+    }
     AGWN_TRY(param_run(*ctx, static_cast<const double*>(dpos), n, static_cast<double*>(dout), x0,
                        static_cast<const double*>(dcur), n_curves, min_depth, max_depth, tol,
                        static_cast<const uint8_t*>(dstart), static_cast<uint32_t*>(dstats),
@@ -406,4 +418,27 @@ extern "C" int agwn_param_batch_fractional_bezier3_f64(agwn_context* ctx, const 
                                       ctx->stream));
     bool const sync = h_out || h_stats || h_nodes || dpos != positions || dcur != curves;
     return sync ? ctx->check_flags() : AGWN_OK;
+}
+} // namespace
+
+extern "C" int agwn_param_batch_fractional_bezier3_f64(agwn_context* ctx, const double* positions, int64_t n,
+                                                       double* out, const double* x0, const double* curves,
+                                                       int64_t n_curves, int min_depth, int max_depth, double tol,
+                                                       const uint8_t* start_depth, uint32_t* pair_stats,
+                                                       int32_t* nodes_per_query)
+{
+    return param_entry(ctx, nullptr, 0, 0.f, positions, n, out, x0, curves, n_curves, min_depth, max_depth, tol,
+                       start_depth, pair_stats, nodes_per_query);
+}
+
+extern "C" int agwn_param_batch_fractional_learned_bezier3_f64(agwn_context* ctx, const agwn_mlp* mlp,
+                                                               const double* positions, int64_t n, double* out,
+                                                               const double* x0, const double* curves,
+                                                               int64_t n_curves, int n_classes, int min_depth,
+                                                               int max_depth, double tol, float alpha,
+                                                               uint32_t* pair_stats, int32_t* nodes_per_query)
+{
+    AGWN_CHECK_ARG(mlp, "null network");
+    return param_entry(ctx, mlp, n_classes, alpha, positions, n, out, x0, curves, n_curves, min_depth, max_depth, tol,
+                       nullptr, pair_stats, nodes_per_query);
 }

@@ -55,6 +55,9 @@ def parse():
                          "workloads, each printing its own JSON line (see run_secondary)")
     ap.add_argument("--scale", type=float, default=1.0,
                     help="secondary workloads: fraction of the full query count (batch: of the grid side)")
+    ap.add_argument("--patches", type=int, default=256, help="param workload: bicubic patches (4 curves each)")
+    ap.add_argument("--batch-config", default=None,
+                    help="batch workload: fixed launch configuration 'block,k,seg_tile,stack' instead of tuning")
     return ap.parse_args()
 
 
@@ -443,7 +446,11 @@ def run_batch(args, ag, torch, stream, disp, timed):
     ref_outs = [torch.empty_like(o) for o in outs]
     batch = ag.CudaRobustBatch(disp, meshes, pos, outs)
     t0 = time.perf_counter()
-    tuned = batch.tune(repeats=2)
+    if args.batch_config:
+        batch.set_config(*[int(x) for x in args.batch_config.split(",")])
+        tuned = batch.info()
+    else:
+        tuned = batch.tune(repeats=2)
     tune_s = time.perf_counter() - t0
     Q = tuned["queries"]
     for _ in range(args.warmup):
@@ -527,7 +534,7 @@ def run_param(args, ag, torch, stream, disp, timed):
     tol 1e-10: the plain adaptive integrator against the learned start-depth proposal (trained here)."""
     from antipodal_gb300 import synth
     n_q = max(64, int(1_000_000 * args.scale))
-    curves, q, x0 = synth.bezier_patches(seed=0, n_patches=256, n_queries=n_q)
+    curves, q, x0 = synth.bezier_patches(seed=0, n_patches=args.patches, n_queries=n_q)
     cfg = ag.IntegrateConfig(0, 10, 1e-10)
     net = ag.LearnedGK15Proposal(disp, seed=3, n_classes=11, alpha=0.02)
     tc, tq, tx = synth.bezier_patches(seed=101, n_patches=256, n_queries=2000)
@@ -559,7 +566,7 @@ def run_param(args, ag, torch, stream, disp, timed):
     rate, m = _cpu_sample_rate(lambda m: o.param_frac_bezier3(q[:m], x0, curves, 0, 10, 1e-10), Q, args.cpu_seconds)
     net.close()
     return {"metric": METRIC, "value": Q / (ms * 1e-3), "unit": "queries/s", "ms_per_step": ms,
-            "config": {"workload": f"256 bicubic Bezier patches ({Cn} boundary cubics), {Q} float64 queries "
+            "config": {"workload": f"{args.patches} bicubic Bezier patches ({Cn} boundary cubics), {Q} float64 queries "
                                    "(30% within 1e-3 of a curve), adaptive GK15 tol 1e-10, max depth 10",
                        "queries": Q, "pairs": Q * Cn},
             "plain": {"value": Q / (ms_plain * 1e-3), "ms_per_step": ms_plain, "panels_per_pair": panels_p / (Q * Cn)},

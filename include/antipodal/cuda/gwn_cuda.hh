@@ -17,9 +17,11 @@
 // status and the library's message.  Size mismatches, which the reference asserts, throw std::invalid_argument.
 
 #include <antipodal/math/common.hh>
+#include <antipodal/math/integrate.hh>
 
 #include <antipodal_gb300.h>
 
+#include <array>
 #include <cstdint>
 #include <mutex>
 #include <span>
@@ -27,6 +29,7 @@
 #include <string>
 #include <type_traits>
 #include <utility>
+#include <vector>
 
 namespace antipodal::cuda
 {
@@ -159,6 +162,245 @@ private:
     mutable std::mutex m_mutex;
 };
 
+// Precision policies of the robust evaluator.  The reference's tags (src/antipodal/math/robust_predicates.hh:
+// robust::int64_grid, int128_grid, exact_float) work as well: a policy is recognised by its coord type.
+struct int64_grid
+{
+    using coord = std::int32_t;
+};
+struct int128_grid
+{
+    using coord = std::int64_t;
+};
+struct exact_float
+{
+    using coord = double;
+};
+template <class T>
+using default_precision = std::conditional_t<std::is_same_v<T, float>, int64_grid, exact_float>;
+
+namespace detail
+{
+template <class P>
+constexpr int policy_of()
+{
+    using C = typename P::coord;
+    static_assert(std::is_same_v<C, std::int32_t> || std::is_same_v<C, std::int64_t> || std::is_same_v<C, double>,
+                  "precision policy: coord must be int32_t (int64_grid), int64_t (int128_grid) or double (exact_float)");
+    return std::is_same_v<C, std::int32_t> ? AGWN_ROBUST_INT64_GRID
+                                           : (std::is_same_v<C, std::int64_t> ? AGWN_ROBUST_INT128_GRID
+                                                                              : AGWN_ROBUST_EXACT_FLOAT);
+}
+} // namespace detail
+
+// RobustMeshGwn<T, Precision> (src/antipodal/gwn_mesh_robust.hh:170-424) on the device: the mesh is quantised and
+// its ray-frame hierarchy built on the GPU.  Counts equal the reference's bit for bit under every policy.
+// eval / fractional / signed_intersection_count are the concept members (one GPU round trip per point); use
+// eval_gwnr_mesh_batch_robust or evaluate() for throughput.
+template <class T, class Precision = default_precision<T>>
+class CudaRobustMeshGwn
+{
+    static_assert(std::is_same_v<T, float> || std::is_same_v<T, double>, "float or double geometry");
+
+public:
+    using precision = Precision;
+
+    CudaRobustMeshGwn(CudaDispatcher& disp, std::span<vec3<T> const> vertices, std::span<int const> indices,
+                      std::span<weighted_segment3<T> const> boundary)
+      : m_disp(&disp)
+    {
+        static_assert(sizeof(vec3<T>) == 3 * sizeof(T) && sizeof(weighted_segment3<T>) == 7 * sizeof(T));
+        auto const* v = reinterpret_cast<T const*>(vertices.data());
+        auto const* i = reinterpret_cast<std::int32_t const*>(indices.data());
+        auto const* b = reinterpret_cast<T const*>(boundary.data());
+        constexpr int pol = detail::policy_of<Precision>();
+        if constexpr (std::is_same_v<T, double>)
+            check(agwn_robust_create_f64(disp.handle(), pol, v, std::int64_t(vertices.size()), i,
+                                         std::int64_t(indices.size()), b, std::int64_t(boundary.size()), &m_r),
+                  "agwn_robust_create_f64");
+        else
+            check(agwn_robust_create_f32(disp.handle(), pol, v, std::int64_t(vertices.size()), i,
+                                         std::int64_t(indices.size()), b, std::int64_t(boundary.size()), &m_r),
+                  "agwn_robust_create_f32");
+    }
+    ~CudaRobustMeshGwn()
+    {
+        if (m_r)
+            agwn_robust_destroy(m_r);
+    }
+    CudaRobustMeshGwn(CudaRobustMeshGwn const&) = delete;
+    CudaRobustMeshGwn& operator=(CudaRobustMeshGwn const&) = delete;
+
+    // Full GWN (and optionally the integer and fractional terms) of a batch; spans may be host or device memory.
+    void evaluate(std::span<vec3<T> const> positions, std::span<T> out, std::span<int> counts = {},
+                  std::span<T> fractional = {}) const
+    {
+        if (out.size() != positions.size() || (!counts.empty() && counts.size() != positions.size()) ||
+            (!fractional.empty() && fractional.size() != positions.size()))
+            throw std::invalid_argument("CudaRobustMeshGwn::evaluate: positions and outputs differ in size");
+        auto const* p = reinterpret_cast<T const*>(positions.data());
+        auto* c = counts.empty() ? nullptr : reinterpret_cast<std::int32_t*>(counts.data());
+        T* f = fractional.empty() ? nullptr : fractional.data();
+        if constexpr (std::is_same_v<T, double>)
+            check(agwn_robust_eval_f64(m_disp->handle(), m_r, p, std::int64_t(positions.size()), out.data(), c, f),
+                  "agwn_robust_eval_f64");
+        else
+            check(agwn_robust_eval_f32(m_disp->handle(), m_r, p, std::int64_t(positions.size()), out.data(), c, f),
+                  "agwn_robust_eval_f32");
+    }
+
+    [[nodiscard]] T eval(vec3<T> p) const
+    {
+        T out{};
+        evaluate(std::span<vec3<T> const>{&p, 1}, std::span<T>{&out, 1});
+        return out;
+    }
+    [[nodiscard]] T fractional(vec3<T> p) const
+    {
+        T out{}, fr{};
+        int c = 0;
+        evaluate(std::span<vec3<T> const>{&p, 1}, std::span<T>{&out, 1}, std::span<int>{&c, 1}, std::span<T>{&fr, 1});
+        return fr;
+    }
+    [[nodiscard]] int signed_intersection_count(vec3<T> p) const
+    {
+        T out{};
+        int c = 0;
+        evaluate(std::span<vec3<T> const>{&p, 1}, std::span<T>{&out, 1}, std::span<int>{&c, 1});
+        return c;
+    }
+
+    [[nodiscard]] agwn_robust const* handle() const noexcept { return m_r; }
+
+private:
+    CudaDispatcher* m_disp;
+    agwn_robust* m_r = nullptr;
+};
+
+// Many CudaRobustMeshGwn meshes, each with its own device arrays of queries and results, evaluated in one
+// persistent launch over a device work queue (no reference counterpart; the values equal
+// eval_gwnr_mesh_batch_robust per mesh bit for bit).  tune() times the launch configurations on a sample and
+// keeps the fastest; run() replays a CUDA graph after the first call.  Meshes and arrays must outlive the batch.
+template <class T, class Precision = default_precision<T>>
+class CudaRobustBatch
+{
+public:
+    struct Job
+    {
+        CudaRobustMeshGwn<T, Precision> const* mesh;
+        vec3<T> const* positions; // device
+        std::int64_t n;
+        T* out;                   // device
+        int* counts = nullptr;    // device, optional
+    };
+
+    CudaRobustBatch(CudaDispatcher& disp, std::span<Job const> jobs) : m_disp(&disp)
+    {
+        std::vector<agwn_robust const*> m;
+        std::vector<void const*> p;
+        std::vector<std::int64_t> n;
+        std::vector<void*> o;
+        std::vector<std::int32_t*> c;
+        for (auto const& j : jobs)
+        {
+            m.push_back(j.mesh->handle());
+            p.push_back(j.positions);
+            n.push_back(j.n);
+            o.push_back(j.out);
+            c.push_back(reinterpret_cast<std::int32_t*>(j.counts));
+        }
+        check(agwn_batch_create(disp.handle(), m.data(), std::int32_t(m.size()), p.data(), n.data(), o.data(),
+                                c.data(), &m_b),
+              "agwn_batch_create");
+    }
+    ~CudaRobustBatch()
+    {
+        if (m_b)
+            agwn_batch_destroy(m_b);
+    }
+    CudaRobustBatch(CudaRobustBatch const&) = delete;
+    CudaRobustBatch& operator=(CudaRobustBatch const&) = delete;
+
+    void tune(int repeats = 2) { check(agwn_batch_tune(m_disp->handle(), m_b, repeats), "agwn_batch_tune"); }
+    void run(bool graph = true) { check(agwn_batch_run(m_disp->handle(), m_b, graph ? 1 : 0), "agwn_batch_run"); }
+    // {threads per CTA, queries per thread, segment tile, traversal stack}
+    [[nodiscard]] std::array<std::int32_t, 4> config() const
+    {
+        std::array<std::int32_t, 4> c{};
+        check(agwn_batch_info(m_b, c.data(), nullptr, nullptr, nullptr, nullptr, nullptr), "agwn_batch_info");
+        return c;
+    }
+
+private:
+    CudaDispatcher* m_disp;
+    agwn_batch* m_b = nullptr;
+};
+
+// Boundary of a parametric surface made of cubic Bezier curves (control points c0..c3 per curve), in the order the
+// reference's for_each_boundary would visit them: the device-representable form of ForEachBoundary
+// (src/antipodal/gwn_parametric.hh:34-41).
+struct CubicBezierBoundary
+{
+    std::span<std::array<vec3<double>, 4> const> curves;
+};
+
+// Learned start depths for the plain GK15 integrator (no reference counterpart): a 12 -> 64 -> 64 -> 16 MLP on
+// the tensor cores, trained on the plain integrator's depths.  Passed as the integrator of the parametric batch
+// function; every evaluated panel is still accepted or refined by the plain error test.
+class LearnedGK15Proposal
+{
+public:
+    explicit LearnedGK15Proposal(CudaDispatcher& disp, std::uint64_t seed = 0, int n_classes = 11,
+                                 float alpha = 0.02f)
+      : m_disp(&disp), m_classes(n_classes), m_alpha(alpha)
+    {
+        check(agwn_mlp_create(disp.handle(), seed, &m_mlp), "agwn_mlp_create");
+    }
+    ~LearnedGK15Proposal()
+    {
+        if (m_mlp)
+            agwn_mlp_destroy(m_mlp);
+    }
+    LearnedGK15Proposal(LearnedGK15Proposal const&) = delete;
+    LearnedGK15Proposal& operator=(LearnedGK15Proposal const&) = delete;
+
+    [[nodiscard]] std::vector<float> params() const
+    {
+        std::vector<float> p(static_cast<std::size_t>(agwn_mlp_param_count()));
+        check(agwn_mlp_get_params(m_disp->handle(), m_mlp, p.data()), "agwn_mlp_get_params");
+        return p;
+    }
+    void set_params(std::span<float const> p)
+    {
+        if (p.size() != std::size_t(agwn_mlp_param_count()))
+            throw std::invalid_argument("LearnedGK15Proposal::set_params: wrong parameter count");
+        check(agwn_mlp_set_params(m_disp->handle(), m_mlp, p.data()), "agwn_mlp_set_params");
+    }
+    // features: rows of 12 floats from agwn_param_features_bezier3_f64; labels: the plain integrator's shallowest
+    // accepted depth per row.  Returns each step's mean loss.
+    std::vector<float> train(std::span<float const> features, std::span<std::uint8_t const> labels, int steps,
+                             int batch = 8192, float lr = 2e-3f, std::uint64_t seed = 1)
+    {
+        if (features.size() != 12 * labels.size())
+            throw std::invalid_argument("LearnedGK15Proposal::train: 12 features per label");
+        std::vector<float> loss(std::size_t(steps > 0 ? steps : 0));
+        check(agwn_mlp_train(m_disp->handle(), m_mlp, features.data(), labels.data(), std::int64_t(labels.size()),
+                             m_classes, steps, batch, lr, seed, loss.empty() ? nullptr : loss.data()),
+              "agwn_mlp_train");
+        return loss;
+    }
+
+    [[nodiscard]] agwn_mlp const* handle() const noexcept { return m_mlp; }
+    [[nodiscard]] int n_classes() const noexcept { return m_classes; }
+    [[nodiscard]] float alpha() const noexcept { return m_alpha; }
+
+private:
+    CudaDispatcher* m_disp;
+    agwn_mlp* m_mlp = nullptr;
+    int m_classes;
+    float m_alpha;
+};
+
 namespace detail
 {
 template <class T>
@@ -238,5 +480,50 @@ void eval_gwnr_mesh_batch(cuda::CudaDispatcher& dispatcher, cuda::CudaIntersecto
                                         std::int64_t(positions.size()), out_wnrs.data(), x,
                                         cuda::detail::raw(boundary), std::int64_t(boundary.size())),
                     "eval_gwnr_mesh_batch");
+}
+
+// gwn_mesh_robust.hh:441-456 on the GPU: out_wnrs[i] = robust.eval(positions[i]).
+template <class T, class Precision>
+void eval_gwnr_mesh_batch_robust(cuda::CudaDispatcher&, cuda::CudaRobustMeshGwn<T, Precision> const& robust,
+                                 std::span<vec3<T> const> positions, std::span<T> out_wnrs)
+{
+    cuda::detail::same_size(positions.size(), out_wnrs.size(), "eval_gwnr_mesh_batch_robust");
+    robust.evaluate(positions, out_wnrs);
+}
+
+// gwn_parametric.hh:168-186 on the GPU, for cubic Bezier boundaries and the default IntegratorGK15: the same
+// value bit for bit.  A non-template function, so it is preferred over the reference's template.
+inline void eval_gwnr_parametric_batch_fractional(cuda::CudaDispatcher& dispatcher,
+                                                  std::span<vec3<double> const> positions, std::span<double> out_wnrs,
+                                                  vec3<double> x0, cuda::CubicBezierBoundary const& boundary,
+                                                  integrate_config const& cfg = {})
+{
+    cuda::detail::same_size(positions.size(), out_wnrs.size(), "eval_gwnr_parametric_batch_fractional");
+    static_assert(sizeof(std::array<vec3<double>, 4>) == 12 * sizeof(double));
+    double const x[3] = {x0.x, x0.y, x0.z};
+    cuda::check(agwn_param_batch_fractional_bezier3_f64(
+                    dispatcher.handle(), cuda::detail::raw(positions), std::int64_t(positions.size()),
+                    out_wnrs.data(), x, reinterpret_cast<double const*>(boundary.curves.data()),
+                    std::int64_t(boundary.curves.size()), cfg.min_depth, cfg.max_depth, cfg.tol, nullptr, nullptr,
+                    nullptr),
+                "eval_gwnr_parametric_batch_fractional");
+}
+
+// The same with the learned start-depth proposal as the integrator.
+inline void eval_gwnr_parametric_batch_fractional(cuda::CudaDispatcher& dispatcher,
+                                                  std::span<vec3<double> const> positions, std::span<double> out_wnrs,
+                                                  vec3<double> x0, cuda::CubicBezierBoundary const& boundary,
+                                                  integrate_config const& cfg,
+                                                  cuda::LearnedGK15Proposal const& integrator)
+{
+    cuda::detail::same_size(positions.size(), out_wnrs.size(), "eval_gwnr_parametric_batch_fractional");
+    double const x[3] = {x0.x, x0.y, x0.z};
+    cuda::check(agwn_param_batch_fractional_learned_bezier3_f64(
+                    dispatcher.handle(), integrator.handle(), cuda::detail::raw(positions),
+                    std::int64_t(positions.size()), out_wnrs.data(), x,
+                    reinterpret_cast<double const*>(boundary.curves.data()), std::int64_t(boundary.curves.size()),
+                    integrator.n_classes(), cfg.min_depth, cfg.max_depth, cfg.tol, integrator.alpha(), nullptr,
+                    nullptr),
+                "eval_gwnr_parametric_batch_fractional");
 }
 } // namespace antipodal

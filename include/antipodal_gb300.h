@@ -258,6 +258,14 @@ int agwn_param_propose_depth_bezier3_f64(agwn_context* ctx, const agwn_mlp* mlp,
                                          int min_depth, int max_depth, double tol, float alpha,
                                          uint8_t* start_depth, float* logits);
 
+/* agwn_param_batch_fractional_bezier3_f64 with start depths proposed by `mlp` in the same call (kept in device
+ * scratch): the learned form of eval_gwnr_parametric_batch_fractional. */
+int agwn_param_batch_fractional_learned_bezier3_f64(agwn_context* ctx, const agwn_mlp* mlp, const double* positions,
+                                                    int64_t n, double* out, const double* x0, const double* curves,
+                                                    int64_t n_curves, int n_classes, int min_depth, int max_depth,
+                                                    double tol, float alpha, uint32_t* pair_stats,
+                                                    int32_t* nodes_per_query);
+
 /* ---- mixed-precision fractional term without allocation --------------------------------------------------
  * No counterpart in the reference.  For callers that cannot allocate device memory -- a program whose own pool
  * allocator owns the GPU's memory budget, or a plugin inside a framework whose allocator must not be bypassed --

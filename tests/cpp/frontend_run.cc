@@ -1,11 +1,14 @@
 // Runs the C++ front end (include/antipodal/cuda/gwn_cuda.hh) the way a reference user would: the +Y-open unit
 // cube of the reference tests, a 12^3 grid of queries, eval_gwnr_mesh_batch{,_fractional,_integer} through
-// CudaDispatcher / CudaIntersector in both precisions.  Prints one line per query:
-//   x y z full_exact full_mixed frac_exact count
+// CudaDispatcher / CudaIntersector in both precisions, eval_gwnr_mesh_batch_robust through CudaRobustMeshGwn
+// (exact_float), and eval_gwnr_parametric_batch_fractional over the open cube's boundary as straight cubic Bezier
+// curves (tol 1e-6).  Prints one line per query:
+//   x y z full_exact full_mixed frac_exact count robust param_frac
 // or "error <status> <message>" when the library throws (e.g. no GPU).
 #include <antipodal/math/common.hh>
 #include <antipodal/cuda/gwn_cuda.hh>
 
+#include <array>
 #include <cstdio>
 #include <vector>
 
@@ -37,9 +40,27 @@ int main()
         eval_gwnr_mesh_batch_integer(disp, isect, P, std::span<int>{counts}, x0);
         disp.set_precision(cuda::precision::mixed);
         eval_gwnr_mesh_batch(disp, isect, P, std::span<double>{mixed}, x0, B);
+        disp.set_precision(cuda::precision::exact);
+
+        std::vector<double> robust(pts.size()), param(pts.size());
+        cuda::CudaRobustMeshGwn<double> const rob{disp, verts, idx, B};
+        eval_gwnr_mesh_batch_robust(disp, rob, P, std::span<double>{robust});
+
+        std::vector<std::array<dvec3, 4>> curves;
+        for (auto const& ws : bnd)
+        {
+            dvec3 const a = ws.segment.pos0, b = ws.segment.pos1;
+            curves.push_back({a, dvec3{(2 * a.x + b.x) / 3, (2 * a.y + b.y) / 3, (2 * a.z + b.z) / 3},
+                              dvec3{(a.x + 2 * b.x) / 3, (a.y + 2 * b.y) / 3, (a.z + 2 * b.z) / 3}, b});
+        }
+        integrate_config cfg;
+        cfg.tol = 1e-6;
+        eval_gwnr_parametric_batch_fractional(disp, P, std::span<double>{param}, x0,
+                                              cuda::CubicBezierBoundary{std::span<std::array<dvec3, 4> const>{curves}},
+                                              cfg);
         for (size_t q = 0; q < pts.size(); ++q)
-            std::printf("%.17g %.17g %.17g %.17g %.17g %.17g %d\n", pts[q].x, pts[q].y, pts[q].z, exact[q], mixed[q],
-                        frac[q], counts[q]);
+            std::printf("%.17g %.17g %.17g %.17g %.17g %.17g %d %.17g %.17g\n", pts[q].x, pts[q].y, pts[q].z, exact[q],
+                        mixed[q], frac[q], counts[q], robust[q], param[q]);
     }
     catch (cuda::Error const& e)
     {

@@ -90,8 +90,11 @@ def test_frontend_compiles_against_reference_headers(tmp_path):
     src = tmp_path / "use.cc"
     src.write_text("""
 #include <antipodal/gwn_mesh.hh>
+#include <antipodal/gwn_parametric.hh>
+#include <antipodal/math/robust_predicates.hh>
 #include <antipodal/dispatcher/dispatcher_threadpool.hh>
 #include <antipodal/cuda/gwn_cuda.hh>
+#include <array>
 #include <vector>
 using namespace antipodal;
 void run(cuda::CudaDispatcher& d, cuda::CudaIntersector<double> const& i, std::vector<dvec3> const& p,
@@ -99,6 +102,22 @@ void run(cuda::CudaDispatcher& d, cuda::CudaIntersector<double> const& i, std::v
     eval_gwnr_mesh_batch(d, i, std::span<dvec3 const>{p}, std::span<double>{o}, x0, std::span<weighted_dsegment3 const>{b});
     eval_gwnr_mesh_batch_fractional(d, std::span<dvec3 const>{p}, std::span<double>{o}, x0, std::span<weighted_dsegment3 const>{b});
     eval_gwnr_mesh_batch_integer(d, i, std::span<dvec3 const>{p}, std::span<int>{c}, x0);
+    // robust (the reference's precision tags are accepted) and parametric overloads
+    cuda::CudaRobustMeshGwn<double, robust::int128_grid> rob{d, std::span<dvec3 const>{p}, std::span<int const>{},
+                                                             std::span<weighted_dsegment3 const>{b}};
+    eval_gwnr_mesh_batch_robust(d, rob, std::span<dvec3 const>{p}, std::span<double>{o});
+    std::vector<std::array<dvec3, 4>> curves;
+    cuda::CubicBezierBoundary const cb{std::span<std::array<dvec3, 4> const>{curves}};
+    eval_gwnr_parametric_batch_fractional(d, std::span<dvec3 const>{p}, std::span<double>{o}, x0, cb);
+    eval_gwnr_parametric_batch_fractional(d, std::span<dvec3 const>{p}, std::span<double>{o}, x0, cb,
+                                          integrate_config{0, 10, 1e-10});
+    cuda::LearnedGK15Proposal net{d};
+    eval_gwnr_parametric_batch_fractional(d, std::span<dvec3 const>{p}, std::span<double>{o}, x0, cb,
+                                          integrate_config{}, net);
+    std::vector<cuda::CudaRobustBatch<double, robust::int128_grid>::Job> jobs{{&rob, p.data(), 0, o.data()}};
+    cuda::CudaRobustBatch<double, robust::int128_grid> batch{d, jobs};
+    batch.tune();
+    batch.run();
     // the reference's CPU path still works alongside
     PoolDispatcher pool{2};
     NaiveIntersector<double> naive{std::span<dvec3 const>{p}, std::span<int const>{}};

@@ -35,3 +35,10 @@ def test_frontend_program_matches_oracle(gwn, oracle, tmp_path):
     assert np.max(np.abs(rows[:, 4] - full)) <= 1e-7
     assert np.max(np.abs(rows[:, 5] - oracle.frac_batch(q, x0, bnd))) <= 1e-12
     assert np.array_equal(rows[:, 6].astype(np.int32), oracle.int_naive(q, x0, verts, idx))
+    # robust (exact_float) and parametric overloads
+    rob, _, _ = oracle.robust_eval("exact_float", verts, idx, bnd, q)
+    assert np.max(np.abs(rows[:, 7] - rob)) <= 1e-12
+    lines = np.stack([np.concatenate([s[0:3], (2 * s[0:3] + s[3:6]) / 3, (s[0:3] + 2 * s[3:6]) / 3, s[3:6]])
+                      for s in bnd])
+    par = oracle.param_frac_bezier3(q, x0, lines, 0, 10, 1e-6)
+    assert np.max(np.abs(rows[:, 8] - par)) <= 1e-15
