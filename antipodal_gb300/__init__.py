@@ -175,6 +175,19 @@ class CudaDispatcher:
         _check(library().agwn_probe_fp32_peak(self.handle, C.byref(v)), "agwn_probe_fp32_peak")
         return v.value
 
+    def set_robust_precision(self, precision: str):
+        """Robust evaluator under int64_grid: "exact" (default; the reference's FP64 fractional term) or "mixed"
+        (FP32 pairs on the exact integer differences under a first-order error estimate, the others in FP64).
+        Counts are unchanged."""
+        modes = {"exact": _lib.ROBUST_EXACT, "mixed": _lib.ROBUST_MIXED}
+        if precision not in modes:
+            raise ValueError("robust precision must be 'exact' or 'mixed'")
+        self.set_option(_lib.OPT_ROBUST_MODE, modes[precision])
+
+    def set_robust_term_err(self, radians: float):
+        """Robust mixed mode: per-pair error estimate above which a pair is evaluated in FP64 (default 1e-7)."""
+        self.set_option(_lib.OPT_ROBUST_TERM_ERR, float(radians))
+
     def probe_fp64_peak(self) -> float:
         """Measured FP64 FMA throughput of this GPU, TFLOP/s."""
         v = C.c_double()

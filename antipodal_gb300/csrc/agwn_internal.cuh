@@ -120,6 +120,8 @@ struct Context
     int frac_mode = AGWN_FRAC_EXACT;
     double mixed_tau = 4.0;
     double mixed_term_err = 3e-8;
+    int robust_mode = AGWN_ROBUST_EXACT;
+    double robust_term_err = 1e-7;
     int queries_per_thread = 2;
     int frac_block = 128;
     int seg_tile = 512;

@@ -23,6 +23,7 @@ struct agwn_batch
     int scalar_bytes = 8;
     int n_meshes = 0;
     int max_depth = 0;
+    int64_t max_segments = 0;
     int64_t total_queries = 0;
     double total_pairs = 0;
     agwn::DevBuf meshes, items, sample, head;
@@ -34,6 +35,9 @@ struct agwn_batch
     cudaGraphExec_t exec = nullptr;
     agwn::BConf graph_conf{0, 0, 0, 0};
     int graph_grid = 0;
+    bool graph_mixed = false;
+    double graph_term_err = 0;
+    bool graph_counting = false;
     std::vector<double> tune_ms; // per candidate, in candidate order
     std::vector<agwn::BConf> candidates;
 };
@@ -58,15 +62,21 @@ bool is_device_ptr(const void* p, int device)
     return (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) && a.device == device;
 }
 
-size_t smem_of(const agwn_batch& b, const BConf& c)
+bool mixed_of(const agwn_batch& b, const Context& ctx)
 {
-    return 2 * size_t(c.seg_tile) * ops_of(b.policy).seg_bytes;
+    return ops_of(b.policy).has_mixed && ctx.robust_mode == AGWN_ROBUST_MIXED && b.max_segments < (int64_t(1) << 24);
+}
+
+size_t smem_of(const agwn_batch& b, const BConf& c, bool mixed)
+{
+    return 2 * size_t(c.seg_tile) * (ops_of(b.policy).seg_bytes + (mixed ? sizeof(float) : 0));
 }
 
 int grid_of(const agwn_batch& b, const Context& ctx, const BConf& c, int* grid)
 {
     int per_sm = 0;
-    AGWN_TRY(ops_of(b.policy).occupancy(b.scalar_bytes, c, smem_of(b, c), &per_sm));
+    bool const mixed = mixed_of(b, ctx);
+    AGWN_TRY(ops_of(b.policy).occupancy(b.scalar_bytes, c, mixed, smem_of(b, c, mixed), &per_sm));
     if (per_sm < 1)
         return fail(AGWN_ERR_UNSUPPORTED, "batch kernel configuration {%d, %d, %d, %d} does not fit on an SM", c.block,
                     c.k, c.seg_tile, c.stack);
@@ -76,9 +86,11 @@ int grid_of(const agwn_batch& b, const Context& ctx, const BConf& c, int* grid)
 
 int launch(agwn_batch& b, Context& ctx, cudaStream_t st, const BConf& c, int grid, const BItem* items, int n_items)
 {
+    bool const mixed = mixed_of(b, ctx);
     AGWN_TRY_CUDA(cudaMemsetAsync(b.head.ptr, 0, sizeof(int), st));
-    return ops_of(b.policy).launch(b.scalar_bytes, st, c, grid, smem_of(b, c), static_cast<const BMesh*>(b.meshes.ptr),
-                                   items, n_items, static_cast<int*>(b.head.ptr), ctx.d_flags);
+    return ops_of(b.policy).launch(b.scalar_bytes, st, c, mixed, float(ctx.robust_term_err), grid,
+                                   smem_of(b, c, mixed), static_cast<const BMesh*>(b.meshes.ptr), items, n_items,
+                                   static_cast<int*>(b.head.ptr), ctx.d_flags, ctx.timing ? ctx.d_counters : nullptr);
 }
 
 void drop_graph(agwn_batch& b)
@@ -121,6 +133,7 @@ extern "C" int agwn_batch_create(agwn_context* ctx, const agwn_robust* const* me
     int const sb = meshes[0] ? meshes[0]->scalar_bytes : 0;
     std::vector<BMesh> hm(n_meshes);
     int max_depth = 0;
+    int64_t max_segments = 0;
     int64_t total_q = 0;
     for (int i = 0; i < n_meshes; ++i)
     {
@@ -158,6 +171,7 @@ extern "C" int agwn_batch_create(agwn_context* ctx, const agwn_robust* const* me
         m.scene_scale = float(r->hier.scale);
         if (r->n_tri > 1)
             max_depth = std::max(max_depth, int(r->hier.depth));
+        max_segments = std::max(max_segments, r->n_seg);
         total_q += n_queries[i];
     }
     AGWN_CHECK_ARG(max_depth < 64, "hierarchy depth %d exceeds the traversal stack", max_depth);
@@ -201,6 +215,7 @@ extern "C" int agwn_batch_create(agwn_context* ctx, const agwn_robust* const* me
     b->scalar_bytes = sb;
     b->n_meshes = n_meshes;
     b->max_depth = max_depth;
+    b->max_segments = max_segments;
     b->total_queries = total_q;
     b->total_pairs = total_cost;
     b->n_items = int(sorted.size());
@@ -369,9 +384,11 @@ extern "C" int agwn_batch_run(agwn_context* ctx, agwn_batch* plan, int32_t use_g
         AGWN_TRY(launch(*plan, *ctx, ctx->stream, c, grid, items, plan->n_items));
         return ctx->launch_end(AGWN_K_ROBUST);
     }
+    bool const mixed = mixed_of(*plan, *ctx);
     bool const same = plan->exec && plan->graph_conf.block == c.block && plan->graph_conf.k == c.k &&
                       plan->graph_conf.seg_tile == c.seg_tile && plan->graph_conf.stack == c.stack &&
-                      plan->graph_grid == grid;
+                      plan->graph_grid == grid && plan->graph_mixed == mixed &&
+                      plan->graph_term_err == ctx->robust_term_err && plan->graph_counting == ctx->timing;
     if (!same)
     {
         drop_graph(*plan);
@@ -385,6 +402,9 @@ extern "C" int agwn_batch_run(agwn_context* ctx, agwn_batch* plan, int32_t use_g
         AGWN_TRY_CUDA(cudaGraphInstantiate(&plan->exec, plan->graph, 0));
         plan->graph_conf = c;
         plan->graph_grid = grid;
+        plan->graph_mixed = mixed;
+        plan->graph_term_err = ctx->robust_term_err;
+        plan->graph_counting = ctx->timing;
     }
     AGWN_TRY(ctx->launch_begin(AGWN_K_ROBUST));
     AGWN_TRY_CUDA(cudaGraphLaunch(plan->exec, ctx->stream));

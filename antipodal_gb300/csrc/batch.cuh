@@ -44,12 +44,14 @@ struct BConf
 
 // Per-policy operations, defined in batch_p64.cu (int64_grid), batch_p128.cu (int128_grid) and batch_pf.cu
 // (exact_float).  scalar_bytes: 4 or 8.  The queue head must be zero when the kernel starts.
+// mixed selects the FP32-pair form (int64_grid only; ignored by the other policies).
 struct BatchPolicyOps
 {
     size_t seg_bytes; // one boundary segment in shared memory
-    int (*occupancy)(int scalar_bytes, const BConf& c, size_t smem, int* per_sm);
-    int (*launch)(int scalar_bytes, cudaStream_t st, const BConf& c, int grid, size_t smem, const BMesh* meshes,
-                  const BItem* items, int n_items, int* head, int* flags);
+    bool has_mixed;   // the policy has an FP32-pair form
+    int (*occupancy)(int scalar_bytes, const BConf& c, bool mixed, size_t smem, int* per_sm);
+    int (*launch)(int scalar_bytes, cudaStream_t st, const BConf& c, bool mixed, float term_err, int grid, size_t smem,
+                  const BMesh* meshes, const BItem* items, int n_items, int* head, int* flags, long long* counters);
 };
 extern const BatchPolicyOps kBatchP64, kBatchP128, kBatchPF;
 } // namespace agwn

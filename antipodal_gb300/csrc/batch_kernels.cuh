@@ -51,9 +51,11 @@ __device__ __forceinline__ int batch_count(const BMesh& m, const Frame32& f, qv3
     return sum;
 }
 
-template <class T, class P, int K, int kStack>
+// Mixed (int64_grid only): FP32 pairs under robust_pair_f32's error bound, TwoSum-accumulated; the rest in FP64.
+template <class T, class P, int K, int kStack, bool Mixed>
 __global__ void __launch_bounds__(256) k_batch(const BMesh* __restrict__ meshes, const BItem* __restrict__ items,
-                                               int n_items, int* __restrict__ head, int tile, int* flags)
+                                               int n_items, int* __restrict__ head, int tile, int* flags,
+                                               float term_err, long long* counters)
 {
     using C = typename P::C;
     using Seg = RSeg<C>;
@@ -62,6 +64,14 @@ __global__ void __launch_bounds__(256) k_batch(const BMesh* __restrict__ meshes,
     __shared__ int s_item;
     __shared__ int abort_cta;
     Seg* const buf[2] = {reinterpret_cast<Seg*>(smem), reinterpret_cast<Seg*>(smem) + tile};
+    float* const wts = reinterpret_cast<float*>(reinterpret_cast<Seg*>(smem) + 2 * tile); // Mixed: 2 * tile
+    __shared__ uint32_t q_entries[Mixed ? 8 : 1][RQueue<K>::kCap];
+    __shared__ double q_results[Mixed ? 8 : 1][32];
+    int const lane = threadIdx.x & 31;
+    RQueue<K> fq;
+    fq.e = q_entries[Mixed ? threadIdx.x / 32 : 0];
+    fq.res = q_results[Mixed ? threadIdx.x / 32 : 0];
+    unsigned long long pairs = 0;
     if (threadIdx.x == 0)
     {
         mbar_init(&bars[0], 1);
@@ -79,7 +89,14 @@ __global__ void __launch_bounds__(256) k_batch(const BMesh* __restrict__ meshes,
         __syncthreads();
         int const item_idx = s_item;
         if (item_idx >= n_items)
+        {
+            if (Mixed && counters && lane == 0)
+            {
+                atomicAdd(reinterpret_cast<unsigned long long*>(counters), (unsigned long long)fq.tail);
+                atomicAdd(reinterpret_cast<unsigned long long*>(counters + 1), pairs);
+            }
             return;
+        }
         BItem const item = items[item_idx];
         BMesh const& m = meshes[item.mesh];
         const Seg* const gseg = static_cast<const Seg*>(m.seg);
@@ -119,6 +136,7 @@ __global__ void __launch_bounds__(256) k_batch(const BMesh* __restrict__ meshes,
             qv3<C> q[K];
             int cnt[K];
             double half[K];
+            float acc[K], comp[K];
             int64_t idx[K];
 #pragma unroll
             for (int k = 0; k < K; ++k)
@@ -128,12 +146,14 @@ __global__ void __launch_bounds__(256) k_batch(const BMesh* __restrict__ meshes,
                 q[k] = quantize<P>(double(pos[3 * ii]), double(pos[3 * ii + 1]), double(pos[3 * ii + 2]), qz);
                 cnt[k] = batch_count<P, kStack>(m, f, q[k], flags);
                 half[k] = 0.0;
+                acc[k] = comp[k] = 0.f;
             }
             for (int st = 0; st < n_tiles; ++st)
             {
                 unsigned const g = seq + unsigned(it);
                 int const b = int(g & 1u);
-                if (!single || sub == 0)
+                bool const landed = !single || sub == 0;
+                if (landed)
                     if (!mbar_wait_bounded(&bars[b], (g >> 1) & 1u, flags, 5))
                         abort_cta = 1;
                 __syncthreads();
@@ -142,12 +162,41 @@ __global__ void __launch_bounds__(256) k_batch(const BMesh* __restrict__ meshes,
                 Seg const* const sb = buf[b];
                 int64_t const rem = n_seg - int64_t(st) * tile;
                 int const cnt_s = int(rem < tile ? rem : tile);
-                for (int s = 0; s < cnt_s; ++s)
+                if constexpr (Mixed)
                 {
-                    Seg const sgm = sb[s];
+                    if (landed)
+                    {
+                        tile_weights(sb, cnt_s, wts + b * tile);
+                        __syncthreads();
+                    }
+                    float const* const wb = wts + b * tile;
+                    uint32_t const seg0 = uint32_t(int64_t(st) * tile);
+                    for (int s = 0; s < cnt_s; ++s)
+                    {
+                        Seg const sgm = sb[s];
 #pragma unroll
-                    for (int k = 0; k < K; ++k)
-                        half[k] = __dadd_rn(half[k], __dmul_rn(sgm.w, robust_contrib<P>(q[k], sgm)));
+                        for (int k = 0; k < K; ++k)
+                        {
+                            float th;
+                            bool const ok = robust_pair_f32<P>(q[k], sgm, term_err, &th);
+                            rq_push(fq, !ok, seg0 + uint32_t(s), lane, k);
+                            if (ok)
+                                two_sum_acc(acc[k], comp[k], wb[s] * th);
+                        }
+                        while (fq.tail - fq.head >= 32)
+                            rq_flush<P, K>(fq, 32, lane, gseg, q, half);
+                    }
+                    pairs += 32ull * K * unsigned(cnt_s);
+                }
+                else
+                {
+                    for (int s = 0; s < cnt_s; ++s)
+                    {
+                        Seg const sgm = sb[s];
+#pragma unroll
+                        for (int k = 0; k < K; ++k)
+                            half[k] = __dadd_rn(half[k], __dmul_rn(sgm.w, robust_contrib<P>(q[k], sgm)));
+                    }
                 }
                 if (!single)
                 {
@@ -157,10 +206,15 @@ __global__ void __launch_bounds__(256) k_batch(const BMesh* __restrict__ meshes,
                     ++it;
                 }
             }
+            if constexpr (Mixed)
+                while (fq.tail != fq.head)
+                    rq_flush<P, K>(fq, min(32u, fq.tail - fq.head), lane, gseg, q, half);
 #pragma unroll
             for (int k = 0; k < K; ++k)
                 if (idx[k] < item.q1)
                 {
+                    if constexpr (Mixed)
+                        half[k] = __dadd_rn(half[k], __dadd_rn(double(acc[k]), double(comp[k])));
                     T const fr = T(__dmul_rn(half[k], f_norm));
                     out[idx[k]] = fr + T(cnt[k]);
                     if (m.counts)
@@ -173,31 +227,38 @@ __global__ void __launch_bounds__(256) k_batch(const BMesh* __restrict__ meshes,
 }
 
 template <class T, class P>
-using BatchKernel = void (*)(const BMesh*, const BItem*, int, int*, int, int*);
+using BatchKernel = void (*)(const BMesh*, const BItem*, int, int*, int, int*, float, long long*);
 
 template <class T, class P>
-BatchKernel<T, P> pick_batch_kernel(const BConf& c)
+BatchKernel<T, P> pick_batch_kernel(const BConf& c, bool mixed)
 {
+    if constexpr (std::is_same_v<P, P64>)
+        if (mixed)
+        {
+            if (c.k == 1)
+                return c.stack <= 32 ? k_batch<T, P, 1, 32, true> : k_batch<T, P, 1, 64, true>;
+            return c.stack <= 32 ? k_batch<T, P, 2, 32, true> : k_batch<T, P, 2, 64, true>;
+        }
     if (c.k == 1)
-        return c.stack <= 32 ? k_batch<T, P, 1, 32> : k_batch<T, P, 1, 64>;
-    return c.stack <= 32 ? k_batch<T, P, 2, 32> : k_batch<T, P, 2, 64>;
+        return c.stack <= 32 ? k_batch<T, P, 1, 32, false> : k_batch<T, P, 1, 64, false>;
+    return c.stack <= 32 ? k_batch<T, P, 2, 32, false> : k_batch<T, P, 2, 64, false>;
 }
 
 template <class T, class P>
-int batch_occupancy_t(const BConf& c, size_t smem, int* per_sm)
+int batch_occupancy_t(const BConf& c, bool mixed, size_t smem, int* per_sm)
 {
-    auto const kern = pick_batch_kernel<T, P>(c);
+    auto const kern = pick_batch_kernel<T, P>(c, mixed);
     AGWN_TRY_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
     AGWN_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, kern, c.block, smem));
     return AGWN_OK;
 }
 
 template <class T, class P>
-int batch_launch_t(cudaStream_t st, const BConf& c, int grid, size_t smem, const BMesh* meshes, const BItem* items,
-                   int n_items, int* head, int* flags)
+int batch_launch_t(cudaStream_t st, const BConf& c, bool mixed, float term_err, int grid, size_t smem,
+                   const BMesh* meshes, const BItem* items, int n_items, int* head, int* flags, long long* counters)
 {
-    auto const kern = pick_batch_kernel<T, P>(c);
-    kern<<<grid, c.block, smem, st>>>(meshes, items, n_items, head, c.seg_tile, flags);
+    auto const kern = pick_batch_kernel<T, P>(c, mixed);
+    kern<<<grid, c.block, smem, st>>>(meshes, items, n_items, head, c.seg_tile, flags, term_err, counters);
     AGWN_TRY_CUDA(cudaGetLastError());
     return AGWN_OK;
 }
@@ -205,16 +266,19 @@ int batch_launch_t(cudaStream_t st, const BConf& c, int grid, size_t smem, const
 template <class P>
 struct BatchOpsFor
 {
-    static int occupancy(int scalar_bytes, const BConf& c, size_t smem, int* per_sm)
+    static int occupancy(int scalar_bytes, const BConf& c, bool mixed, size_t smem, int* per_sm)
     {
-        return scalar_bytes == 4 ? batch_occupancy_t<float, P>(c, smem, per_sm)
-                                 : batch_occupancy_t<double, P>(c, smem, per_sm);
+        return scalar_bytes == 4 ? batch_occupancy_t<float, P>(c, mixed, smem, per_sm)
+                                 : batch_occupancy_t<double, P>(c, mixed, smem, per_sm);
     }
-    static int launch(int scalar_bytes, cudaStream_t st, const BConf& c, int grid, size_t smem, const BMesh* meshes,
-                      const BItem* items, int n_items, int* head, int* flags)
+    static int launch(int scalar_bytes, cudaStream_t st, const BConf& c, bool mixed, float term_err, int grid,
+                      size_t smem, const BMesh* meshes, const BItem* items, int n_items, int* head, int* flags,
+                      long long* counters)
     {
-        return scalar_bytes == 4 ? batch_launch_t<float, P>(st, c, grid, smem, meshes, items, n_items, head, flags)
-                                 : batch_launch_t<double, P>(st, c, grid, smem, meshes, items, n_items, head, flags);
+        return scalar_bytes == 4 ? batch_launch_t<float, P>(st, c, mixed, term_err, grid, smem, meshes, items,
+                                                            n_items, head, flags, counters)
+                                 : batch_launch_t<double, P>(st, c, mixed, term_err, grid, smem, meshes, items,
+                                                             n_items, head, flags, counters);
     }
 };
 } // namespace

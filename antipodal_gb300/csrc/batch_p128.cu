@@ -3,5 +3,6 @@
 
 namespace agwn
 {
-const BatchPolicyOps kBatchP128 = {sizeof(RSeg<P128::C>), &BatchOpsFor<P128>::occupancy, &BatchOpsFor<P128>::launch};
+const BatchPolicyOps kBatchP128 = {sizeof(RSeg<P128::C>), false, &BatchOpsFor<P128>::occupancy,
+                                &BatchOpsFor<P128>::launch};
 } // namespace agwn

@@ -3,5 +3,6 @@
 
 namespace agwn
 {
-const BatchPolicyOps kBatchP64 = {sizeof(RSeg<P64::C>), &BatchOpsFor<P64>::occupancy, &BatchOpsFor<P64>::launch};
+const BatchPolicyOps kBatchP64 = {sizeof(RSeg<P64::C>), true, &BatchOpsFor<P64>::occupancy,
+                                &BatchOpsFor<P64>::launch};
 } // namespace agwn

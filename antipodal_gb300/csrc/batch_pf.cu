@@ -3,5 +3,6 @@
 
 namespace agwn
 {
-const BatchPolicyOps kBatchPF = {sizeof(RSeg<PF::C>), &BatchOpsFor<PF>::occupancy, &BatchOpsFor<PF>::launch};
+const BatchPolicyOps kBatchPF = {sizeof(RSeg<PF::C>), false, &BatchOpsFor<PF>::occupancy,
+                                &BatchOpsFor<PF>::launch};
 } // namespace agwn

@@ -332,6 +332,14 @@ int agwn_context_set_option(agwn_context* ctx, int option, double value)
         AGWN_CHECK_ARG(std::isfinite(value) && value > 0.0 && value <= 1.0, "term error bound must be in (0, 1]");
         ctx->mixed_term_err = value;
         return AGWN_OK;
+    case AGWN_OPT_ROBUST_MODE:
+        AGWN_CHECK_ARG(value == AGWN_ROBUST_EXACT || value == AGWN_ROBUST_MIXED, "robust mode must be 0 or 1");
+        ctx->robust_mode = int(value);
+        return AGWN_OK;
+    case AGWN_OPT_ROBUST_TERM_ERR:
+        AGWN_CHECK_ARG(std::isfinite(value) && value > 0.0 && value <= 1.0, "term error bound must be in (0, 1]");
+        ctx->robust_term_err = value;
+        return AGWN_OK;
     default:
         return fail(AGWN_ERR_INVALID, "unknown option %d", option);
     }
@@ -359,6 +367,12 @@ int agwn_context_get_option(agwn_context* ctx, int option, double* value)
         return AGWN_OK;
     case AGWN_OPT_SEG_TILE:
         *value = ctx->seg_tile;
+        return AGWN_OK;
+    case AGWN_OPT_ROBUST_MODE:
+        *value = ctx->robust_mode;
+        return AGWN_OK;
+    case AGWN_OPT_ROBUST_TERM_ERR:
+        *value = ctx->robust_term_err;
         return AGWN_OK;
     case AGWN_OPT_MIXED_TERM_ERR:
         *value = ctx->mixed_term_err;

@@ -175,8 +175,15 @@ int robust_run(Context& ctx, const Robust& r, const T* d_pos, int64_t n, T* d_ou
     using Seg = RSeg<C>;
     int const tile = int(std::max<int64_t>(1, std::min<int64_t>(ctx.seg_tile, r.n_seg)));
     int const n_tiles = int((r.n_seg + tile - 1) / tile);
-    size_t const smem = size_t(n_tiles <= 1 ? 1 : 2) * tile * sizeof(Seg);
-    auto kern = k_robust_frac<T, P>;
+    // the mixed form (int64_grid only) adds the tiles' FP32 weights after two segment buffers
+    bool const mixed =
+        std::is_same_v<P, P64> && ctx.robust_mode == AGWN_ROBUST_MIXED && r.n_seg < (int64_t(1) << 24);
+    size_t const smem = mixed ? 2 * size_t(tile) * (sizeof(Seg) + sizeof(float))
+                              : size_t(n_tiles <= 1 ? 1 : 2) * tile * sizeof(Seg);
+    auto kern = k_robust_frac<T, P, false>;
+    if constexpr (std::is_same_v<P, P64>)
+        if (mixed)
+            kern = k_robust_frac<T, P, true>;
     AGWN_TRY_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
     int per_sm = 0;
     AGWN_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kRobBlock, smem));
@@ -186,7 +193,8 @@ int robust_run(Context& ctx, const Robust& r, const T* d_pos, int64_t n, T* d_ou
     int const grid = int(std::max<int64_t>(1, std::min<int64_t>(n_qtiles, int64_t(per_sm) * ctx.sm_count)));
     AGWN_TRY(ctx.launch_begin(AGWN_K_ROBUST));
     kern<<<grid, kRobBlock, smem, st>>>(d_pos, n, qz, static_cast<const Seg*>(r.seg), r.n_seg, tile, d_counts, d_out,
-                                        d_frac, ctx.d_flags);
+                                        d_frac, ctx.d_flags, float(ctx.robust_term_err),
+                                        ctx.timing ? ctx.d_counters : nullptr);
     return ctx.launch_end(AGWN_K_ROBUST);
 }
 

@@ -11,6 +11,7 @@
 
 #include <cfloat>
 #include <cmath>
+#include <type_traits>
 
 #include "robust_handle.cuh"
 
@@ -471,11 +472,135 @@ __device__ __forceinline__ double robust_contrib(qv3<typename P::C> q, RSeg<type
     return den < 0.0 ? double(sg) * pi : 0.0;
 }
 
-template <class T, class P>
+// ---- mixed precision (int64_grid) -------------------------------------------------------------------------------
+// The fractional term of one (query, segment) pair on the FP32 pipe, when a first-order error estimate says it is
+// close to the FP64 value.  Under int64_grid the differences v = p - q are exact integers; below 2^24 they are
+// exact floats.  The atan2 numerator num = v0.z v1.y - v0.y v1.z and y0 y1 + z0 z1 come from TwoProduct FMAs
+// (error ~2 ulp of the result), |v|, l + x (or (y^2 + z^2) / (l - x) when x < 0, the reference's cancellation-free
+// form) from an approximate rsqrt and reciprocal.  With 4 eps32 per operand chain -- the estimate of the mesh
+// kernel's mixed form -- num errs by E_n = 4u |num| and den = A B + yz by E_d = 4u (|A B| + |yz|), so the angle errs
+// by about (|num| E_d + |den| E_n) / (num^2 + den^2).  The pair stays in FP32 when that is at most term_err;
+// otherwise, when num == 0 (where the reference takes its exact branches), or when a difference is too large to
+// be exact in float, this returns false and the caller evaluates the pair in FP64 with the reference's formula.
+template <class P>
+__device__ __forceinline__ bool robust_pair_f32(qv3<typename P::C> q, RSeg<typename P::C> const& s, float term_err,
+                                                float* theta)
+{
+    static_assert(std::is_same_v<typename P::C, int32_t>, "FP32 pairs are for the int64_grid policy");
+    int32_t const v0x = s.p0[0] - q.x, v0y = s.p0[1] - q.y, v0z = s.p0[2] - q.z;
+    int32_t const v1x = s.p1[0] - q.x, v1y = s.p1[1] - q.y, v1z = s.p1[2] - q.z;
+    // all six below 2^24 in magnitude: (v + 2^24) as unsigned below 2^25
+    unsigned const lim = 1u << 25, off = 1u << 24;
+    bool const small = unsigned(v0x) + off < lim && unsigned(v0y) + off < lim && unsigned(v0z) + off < lim &&
+                       unsigned(v1x) + off < lim && unsigned(v1y) + off < lim && unsigned(v1z) + off < lim;
+    if (!small || (long long)v0z * v1y == (long long)v0y * v1z)
+        return false;
+    float const x0 = float(v0x), y0 = float(v0y), z0 = float(v0z);
+    float const x1 = float(v1x), y1 = float(v1y), z1 = float(v1z);
+    float const pn = y0 * z1, en = fmaf(y0, z1, -pn);
+    float const numf = fmaf(z0, y1, -pn) - en;
+    float const pz = z0 * z1, ez = fmaf(z0, z1, -pz);
+    float const yzf = fmaf(y0, y1, pz) + ez;
+    float const yz0 = fmaf(y0, y0, z0 * z0), yz1 = fmaf(y1, y1, z1 * z1);
+    float const s0 = fmaf(x0, x0, yz0), s1 = fmaf(x1, x1, yz1);
+    float const l0 = s0 * rsqrtf(s0), l1 = s1 * rsqrtf(s1);
+    float const a = x0 >= 0.f ? l0 + x0 : __fdividef(yz0, l0 - x0);
+    float const b = x1 >= 0.f ? l1 + x1 : __fdividef(yz1, l1 - x1);
+    float const ab = a * b;
+    float const den = ab + yzf;
+    float const an = fabsf(numf), ad = fabsf(den);
+    float const inv = __fdividef(1.f, fmaxf(an, ad));
+    float const an1 = an * inv, ad1 = ad * inv;
+    constexpr float k4u = 4.f * 5.9604645e-8f;
+    float const bound = k4u * fmaf(an1, (fabsf(ab) + fabsf(yzf)) * inv, ad1 * an1) / fmaf(an1, an1, ad1 * ad1);
+    if (!(bound <= term_err))
+        return false;
+    *theta = atan2_scaled(numf, den, ad1, an1);
+    return true;
+}
+
+// The FP32 weights of one shared-memory tile of segments, written by the block after the tile has landed.
+template <class Seg>
+__device__ __forceinline__ void tile_weights(Seg const* sb, int cnt, float* w)
+{
+    for (int s = threadIdx.x; s < cnt; s += blockDim.x)
+        w[s] = __double2float_rn(sb[s].w);
+}
+
+// Per-warp queue of the pairs robust_pair_f32 turned down, evaluated in FP64 32 at a time (one per lane), so
+// that the narrow FP64 pipe runs full warps instead of one diverged lane.  Entry: (segment << 8) | (lane << 3) | k,
+// with the segment's index in the mesh's boundary array (below 2^24).
+template <int K>
+struct RQueue
+{
+    static constexpr unsigned kCap = 64u * K; // > 31 left over + 32 * K appended per segment
+    uint32_t* e;
+    double* res;
+    unsigned head = 0, tail = 0; // warp-uniform
+};
+
+// Appends this lane's pair if it was turned down (every lane of the warp calls it).
+template <int K>
+__device__ __forceinline__ void rq_push(RQueue<K>& fq, bool down, uint32_t seg, int lane, int k)
+{
+    unsigned const m = __ballot_sync(0xffffffffu, down);
+    if (m)
+    {
+        if (down)
+            fq.e[(fq.tail + __popc(m & ((1u << lane) - 1u))) & (RQueue<K>::kCap - 1)] =
+                (seg << 8) | (uint32_t(lane) << 3) | uint32_t(k);
+        fq.tail += __popc(m);
+    }
+}
+
+// Evaluates the next c (<= 32) queued pairs, one per lane, and adds each result to its owner's half[k] in queue
+// order (so each query's FP64 terms keep segment order).  Every lane of the warp calls it.
+template <class P, int K>
+__device__ __forceinline__ void rq_flush(RQueue<K>& fq, unsigned c, int lane, const RSeg<typename P::C>* gseg,
+                                         const qv3<typename P::C> (&q)[K], double (&half)[K])
+{
+    using C = typename P::C;
+    __syncwarp();
+    uint32_t const e = fq.e[(fq.head + min(unsigned(lane), c - 1)) & (RQueue<K>::kCap - 1)];
+    int const owner = int((e >> 3) & 31u), kk = int(e & 7u);
+    qv3<C> qq = q[0];
+#pragma unroll
+    for (int k = 0; k < K; ++k)
+    {
+        C const x = __shfl_sync(0xffffffffu, q[k].x, owner), y = __shfl_sync(0xffffffffu, q[k].y, owner),
+                z = __shfl_sync(0xffffffffu, q[k].z, owner);
+        if (kk == k)
+            qq = {x, y, z};
+    }
+    if (unsigned(lane) < c)
+    {
+        RSeg<C> const sg = gseg[e >> 8];
+        fq.res[lane] = __dmul_rn(sg.w, robust_contrib<P>(qq, sg));
+    }
+    __syncwarp();
+    for (unsigned j = 0; j < c; ++j)
+    {
+        uint32_t const ej = fq.e[(fq.head + j) & (RQueue<K>::kCap - 1)];
+        if (int((ej >> 3) & 31u) == lane)
+        {
+            double const r = fq.res[j];
+#pragma unroll
+            for (int k = 0; k < K; ++k)
+                if (int(ej & 7u) == k)
+                    half[k] = __dadd_rn(half[k], r);
+        }
+    }
+    __syncwarp();
+    fq.head += c;
+}
+
+// Mixed = true (int64_grid only): FP32 pairs through robust_pair_f32 with TwoSum accumulation, the others in FP64.
+template <class T, class P, bool Mixed = false>
 __global__ void __launch_bounds__(kRobBlock) k_robust_frac(const T* __restrict__ pos, int64_t n, Quant qz,
                                                            const RSeg<typename P::C>* __restrict__ seg, int64_t n_seg,
                                                            int tile, const int32_t* __restrict__ counts,
-                                                           T* __restrict__ out, T* __restrict__ out_frac, int* flags)
+                                                           T* __restrict__ out, T* __restrict__ out_frac, int* flags,
+                                                           float term_err, long long* counters)
 {
     using Seg = RSeg<typename P::C>;
     extern __shared__ __align__(128) unsigned char smem[];
@@ -490,6 +615,14 @@ __global__ void __launch_bounds__(kRobBlock) k_robust_frac(const T* __restrict__
     pipe.gseg = seg;
     pipe.n_seg = n_seg;
     pipe.tile = tile;
+    float* const wts = reinterpret_cast<float*>(reinterpret_cast<Seg*>(smem) + 2 * tile); // Mixed: 2 * tile floats
+    constexpr int kWarps = kRobBlock / 32;
+    __shared__ uint32_t q_entries[Mixed ? kWarps : 1][RQueue<1>::kCap];
+    __shared__ double q_results[Mixed ? kWarps : 1][32];
+    int const lane = threadIdx.x & 31;
+    RQueue<1> fq;
+    fq.e = q_entries[Mixed ? threadIdx.x / 32 : 0];
+    fq.res = q_results[Mixed ? threadIdx.x / 32 : 0];
     int64_t const per_tile = blockDim.x;
     int64_t const n_qtiles = (n + per_tile - 1) / per_tile;
     int const my_qtiles = blockIdx.x < n_qtiles ? int((n_qtiles - 1 - blockIdx.x) / gridDim.x + 1) : 0;
@@ -514,10 +647,14 @@ __global__ void __launch_bounds__(kRobBlock) k_robust_frac(const T* __restrict__
         int64_t const ii = i < n ? i : n - 1;
         auto const q = quantize<P>(double(pos[3 * ii]), double(pos[3 * ii + 1]), double(pos[3 * ii + 2]), qz);
         double half = 0.0;
+        float acc = 0.f, comp = 0.f;
+        decltype(q) qarr[1] = {q};
+        double harr[1] = {0.0};
         for (int st = 0; st < pipe.n_tiles && n_seg > 0; ++st)
         {
             int const b = it & 1;
-            if (!pipe.single || j == 0)
+            bool const landed = !pipe.single || j == 0;
+            if (landed)
                 if (!mbar_wait_bounded(&bars[b], unsigned((it >> 1) & 1), flags, 3))
                     abort_cta = 1;
             __syncthreads();
@@ -525,10 +662,34 @@ __global__ void __launch_bounds__(kRobBlock) k_robust_frac(const T* __restrict__
                 return;
             Seg const* sb = pipe.buf[b];
             int const cnt = pipe.tile_count(st);
-            for (int s = 0; s < cnt; ++s)
+            if constexpr (Mixed)
             {
-                Seg const sgm = sb[s];
-                half = __dadd_rn(half, __dmul_rn(sgm.w, robust_contrib<P>(q, sgm)));
+                if (landed)
+                {
+                    tile_weights(sb, cnt, wts + b * tile);
+                    __syncthreads();
+                }
+                float const* wb = wts + b * tile;
+                uint32_t const seg0 = uint32_t(int64_t(st) * tile);
+                for (int s = 0; s < cnt; ++s)
+                {
+                    Seg const sgm = sb[s];
+                    float th;
+                    bool const ok = robust_pair_f32<P>(q, sgm, term_err, &th);
+                    rq_push(fq, !ok, seg0 + uint32_t(s), lane, 0);
+                    if (ok)
+                        two_sum_acc(acc, comp, wb[s] * th);
+                    while (fq.tail - fq.head >= 32)
+                        rq_flush<P, 1>(fq, 32, lane, seg, qarr, harr);
+                }
+            }
+            else
+            {
+                for (int s = 0; s < cnt; ++s)
+                {
+                    Seg const sgm = sb[s];
+                    half = __dadd_rn(half, __dmul_rn(sgm.w, robust_contrib<P>(q, sgm)));
+                }
             }
             if (!pipe.single)
             {
@@ -537,6 +698,19 @@ __global__ void __launch_bounds__(kRobBlock) k_robust_frac(const T* __restrict__
                     pipe.issue(it + 2);
                 ++it;
             }
+        }
+        if constexpr (Mixed)
+        {
+            while (fq.tail != fq.head)
+                rq_flush<P, 1>(fq, min(32u, fq.tail - fq.head), lane, seg, qarr, harr);
+            half = __dadd_rn(harr[0], __dadd_rn(double(acc), double(comp)));
+            if (counters && lane == 0)
+            {
+                atomicAdd(reinterpret_cast<unsigned long long*>(counters), (unsigned long long)fq.tail);
+                atomicAdd(reinterpret_cast<unsigned long long*>(counters + 1), 32ull * (unsigned long long)n_seg);
+            }
+            fq.tail = fq.head = 0; // the queue is empty; every lane restarts its copy of the counters
+
         }
         if (i < n)
         {

@@ -438,13 +438,15 @@ def batch_workload(scale, seed=2024, n_meshes=64):
 
 
 def run_batch(args, ag, torch, stream, disp, timed):
-    """64 uneven robust meshes (int64_grid, float32), one persistent launch replayed from a CUDA graph."""
+    """64 uneven robust meshes (int64_grid, float32), one persistent launch replayed from a CUDA graph.
+    Chosen: the batch with FP32 pairs under the error bound; plain: one exact (FP64) evaluation call per mesh."""
     wl = batch_workload(args.scale)
     meshes = [ag.CudaRobustMeshGwn(disp, v, i, b, precision="int64_grid") for v, i, b, _ in wl]
     pos = [torch.from_numpy(q).cuda() for *_, q in wl]
     outs = [torch.empty(len(q), dtype=torch.float32, device="cuda") for *_, q in wl]
     ref_outs = [torch.empty_like(o) for o in outs]
     batch = ag.CudaRobustBatch(disp, meshes, pos, outs)
+    disp.set_robust_precision("mixed")
     t0 = time.perf_counter()
     if args.batch_config:
         batch.set_config(*[int(x) for x in args.batch_config.split(",")])
@@ -457,22 +459,51 @@ def run_batch(args, ag, torch, stream, disp, timed):
         batch.run(graph=True)
     ms = timed(args.steps, lambda: batch.run(graph=True))
 
+    # plain: the reference's FP64 fractional term, one call per mesh; and the same FP64 form batched
+    disp.set_robust_precision("exact")
+
     def per_mesh():
         for r, p, o in zip(meshes, pos, ref_outs):
             r.evaluate(p, o)
     per_mesh()
     ms_loop = timed(max(1, args.plain_steps), per_mesh)
-    same = all(torch.equal(a, b) for a, b in zip(outs, ref_outs))
-    # the CPU oracle (the reference's RobustMeshGwn rule) on a few queries of every mesh
+    batch.run(graph=True)
+    ms_exact_batch = timed(max(1, args.plain_steps), lambda: batch.run(graph=True))
+    exact_batch_same = all(torch.equal(a, b) for a, b in zip(outs, ref_outs))
+    disp.set_robust_precision("mixed")
+    disp.set_option(ag._lib.OPT_TIMING, 1)
+    disp.stats(reset=True)
+    batch.run(graph=True)
+    st = disp.stats(reset=True)
+    disp.set_option(ag._lib.OPT_TIMING, 0)
+    torch.cuda.synchronize()
+    fp64_frac = st["fp64_pairs"] / max(1, st["pairs"])
+    diff = torch.cat([(a.double() - b.double()).abs() for a, b in zip(outs, ref_outs)])
+    max_diff = float(diff.max().item())
+    n_same = int((diff == 0).sum().item())
+    # the fractional term in double precision (RobustMeshGwn<double, int64_grid>) on the first meshes: mixed vs FP64
+    frac_err = 0.0
+    for v, i, b, q in wl[:6]:
+        r64 = ag.CudaRobustMeshGwn(disp, v.astype(np.float64), i, b.astype(np.float64), precision="int64_grid")
+        q64 = q.astype(np.float64)
+        fr = {}
+        for mode in ("exact", "mixed"):
+            disp.set_robust_precision(mode)
+            o_, c_, f_ = np.empty(len(q64)), np.empty(len(q64), np.int32), np.empty(len(q64))
+            r64.evaluate(q64, o_, c_, f_)
+            fr[mode] = f_
+        frac_err = max(frac_err, float(np.abs(fr["exact"] - fr["mixed"]).max()))
+        r64.close()
+    disp.set_robust_precision("exact")
+    # the CPU oracle (the reference's RobustMeshGwn rule) on a few queries of the first meshes, against plain
     o = _oracle()
     worst, n_diff = 0.0, 0
-    for (v, i, b, q), out in zip(wl[:8], outs[:8]):
+    for (v, i, b, q), out in zip(wl[:8], ref_outs[:8]):
         pick = np.random.default_rng(5).choice(len(q), size=min(len(q), 200), replace=False)
         gw, _, _ = o.robust_eval("int64_grid", v, i, b, q[pick])
         got = out.cpu().numpy()[pick]
         worst = max(worst, float(np.abs(got.astype(np.float64) - gw.astype(np.float64)).max()))
         n_diff += int(np.sum(got != gw))
-
     v0, i0, b0, q0 = wl[0]
     rate, m = _cpu_sample_rate(lambda m: o.robust_eval("int64_grid", v0, i0, b0, q0[:m]), len(q0), args.cpu_seconds)
     for x in meshes:
@@ -485,10 +516,15 @@ def run_batch(args, ag, torch, stream, disp, timed):
                        "pair_units": tuned["pairs"], "items": tuned["items"], "tuned": tuned["config"],
                        "tune_seconds": tune_s},
             "plain": {"value": Q / (ms_loop * 1e-3), "ms_per_step": ms_loop,
-                      "form": "one agwn_robust_eval call per mesh (two launches each)"},
+                      "form": "exact FP64 fractional term, one agwn_robust_eval call per mesh"},
+            "exact_batched": {"value": Q / (ms_exact_batch * 1e-3), "ms_per_step": ms_exact_batch,
+                              "bit_identical_to_per_mesh": bool(exact_batch_same)},
             "chosen_over_plain": ms_loop / ms,
-            "accuracy": {"bit_identical_to_per_mesh": bool(same),
-                         "sample_max_abs_err_vs_cpu_oracle": worst, "sample_values_not_identical": n_diff,
+            "fp64_pair_fraction": fp64_frac,
+            "accuracy": {"max_abs_diff_chosen_vs_plain": max_diff,
+                         "max_abs_err_fractional_term_f64_first6_meshes": frac_err,
+                         "identical_values": n_same, "values": int(diff.numel()),
+                         "sample_plain_max_abs_err_vs_cpu_oracle": worst, "sample_plain_values_not_identical": n_diff,
                          "sample_size": 8 * 200},
             "cpu_baseline": {"value": rate, "unit": "queries/s", "cores": os.cpu_count(), "kind": "port",
                              "sample": f"first {m} queries of mesh 0 ({len(b0)} segments), RobustMeshGwn rule"}}

@@ -85,6 +85,12 @@ public:
     }
 
     void set_precision(precision p) { set_option(AGWN_OPT_FRAC_MODE, double(int(p))); }
+    // Robust evaluator under int64_grid: exact (the reference's FP64 fractional term, default) or mixed (FP32
+    // pairs under a first-order error bound, the others in FP64); integer counts are the same either way.
+    void set_robust_precision(precision p)
+    {
+        set_option(AGWN_OPT_ROBUST_MODE, p == precision::mixed ? AGWN_ROBUST_MIXED : AGWN_ROBUST_EXACT);
+    }
     void set_option(int option, double value) { check(agwn_context_set_option(m_ctx, option, value), "set_option"); }
     [[nodiscard]] double option(int option) const
     {

@@ -78,7 +78,18 @@ enum agwn_option
     AGWN_OPT_SEG_TILE = 5,
     /* Mixed mode: a pair whose first-order FP32 error bound exceeds this many radians is evaluated in FP64.
        Default 3e-8. */
-    AGWN_OPT_MIXED_TERM_ERR = 6
+    AGWN_OPT_MIXED_TERM_ERR = 6,
+    /* Robust evaluator, int64_grid policy: AGWN_ROBUST_EXACT (default, the reference's FP64 fractional term) or
+       AGWN_ROBUST_MIXED (FP32 pairs on the exact integer differences under a first-order error estimate, the
+       others -- num == 0 branches, ill-conditioned or large differences -- in FP64; counts unchanged). */
+    AGWN_OPT_ROBUST_MODE = 7,
+    /* Robust mixed mode: the per-pair estimate above which a pair is evaluated in FP64, radians.  Default 1e-7. */
+    AGWN_OPT_ROBUST_TERM_ERR = 8
+};
+enum agwn_robust_mode
+{
+    AGWN_ROBUST_EXACT = 0,
+    AGWN_ROBUST_MIXED = 1
 };
 enum agwn_frac_mode
 {

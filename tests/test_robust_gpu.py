@@ -100,3 +100,55 @@ def test_robust_empty_and_device_inputs(gwn, disp):
         gwn.eval_gwnr_mesh_batch_robust(d, r, torch.from_numpy(q).to(dev), out)
         d.synchronize()
         assert np.array_equal(out.cpu().numpy(), g)
+
+
+@pytest.mark.parametrize("dt,tol", [(np.float64, 1e-7), (np.float32, 2e-7)])
+def test_robust_mixed_int64_grid_matches_exact(gwn, disp, dt, tol):
+    """The FP32-pair form of the int64_grid fractional term: counts identical, fractional term within the bar."""
+    rng = np.random.default_rng(17)
+    for kind, ntri, holes in [("icosphere", 2000, 4), ("torus", 5000, 9)]:
+        v, i = synth.noisy_mesh(kind, ntri, holes, rng)
+        b = synth.boundary_segments(v, i)
+        q = np.concatenate([synth.grid_queries(v.min(0), v.max(0), 24),
+                            v[rng.integers(len(v), size=3000)] + rng.normal(0, 1e-4, (3000, 3))]).astype(dt)
+        r = gwn.CudaRobustMeshGwn(disp, v.astype(dt), i, b.astype(dt), precision="int64_grid")
+        outs = {}
+        for mode in ("exact", "mixed"):
+            disp.set_robust_precision(mode)
+            o, c, f = np.empty(len(q), dt), np.empty(len(q), np.int32), np.empty(len(q), dt)
+            r.evaluate(q, o, c, f)
+            outs[mode] = (o, c, f)
+        disp.set_robust_precision("exact")
+        assert np.array_equal(outs["exact"][1], outs["mixed"][1])
+        d = np.abs(outs["exact"][2].astype(np.float64) - outs["mixed"][2].astype(np.float64))
+        assert d.max() <= tol, (kind, d.max())
+        r.close()
+
+
+def test_robust_mixed_batch_equals_per_mesh(gwn, disp):
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(23)
+    meshes, pos, outs, refs = [], [], [], []
+    disp.set_robust_precision("mixed")
+    for kind, ntri, holes, side in [("icosphere", 1500, 3, 20), ("torus", 2500, 6, 14), ("torus", 700, 2, 9)]:
+        v, i = synth.noisy_mesh(kind, ntri, holes, rng)
+        b = synth.boundary_segments(v, i)
+        q = synth.grid_queries(v.min(0), v.max(0), side).astype(np.float32)
+        r = gwn.CudaRobustMeshGwn(disp, v.astype(np.float32), i, b.astype(np.float32))
+        ref = np.empty(len(q), np.float32)
+        r.evaluate(q, ref)
+        meshes.append(r)
+        refs.append(ref)
+        pos.append(torch.from_numpy(q).cuda())
+        outs.append(torch.empty(len(q), dtype=torch.float32, device="cuda"))
+    batch = gwn.CudaRobustBatch(disp, meshes, pos, outs)
+    for cfg in [(128, 1, 256, 64), (256, 2, 512, 64)]:
+        batch.set_config(*cfg)
+        batch.run(graph=True)
+        torch.cuda.synchronize()
+        for o, ref in zip(outs, refs):
+            assert np.array_equal(o.cpu().numpy(), ref)
+    disp.set_robust_precision("exact")
+    batch.close()
+    for r in meshes:
+        r.close()
