@@ -184,6 +184,14 @@ class CudaDispatcher:
             raise ValueError("robust precision must be 'exact' or 'mixed'")
         self.set_option(_lib.OPT_ROBUST_MODE, modes[precision])
 
+    def set_param_precision(self, precision: str):
+        """Parametric integrator: "exact" (default; FP64 in the reference's operation order, bit for bit) or
+        "mixed" (double-float arithmetic on the FP32 pipe, about 44 significant bits, same tree rule)."""
+        modes = {"exact": _lib.PARAM_EXACT, "mixed": _lib.PARAM_MIXED}
+        if precision not in modes:
+            raise ValueError("parametric precision must be 'exact' or 'mixed'")
+        self.set_option(_lib.OPT_PARAM_MODE, modes[precision])
+
     def set_robust_term_err(self, radians: float):
         """Robust mixed mode: per-pair error estimate above which a pair is evaluated in FP64 (default 1e-7)."""
         self.set_option(_lib.OPT_ROBUST_TERM_ERR, float(radians))

@@ -122,6 +122,7 @@ struct Context
     double mixed_term_err = 3e-8;
     int robust_mode = AGWN_ROBUST_EXACT;
     double robust_term_err = 1e-7;
+    int param_mode = AGWN_PARAM_EXACT;
     int queries_per_thread = 2;
     int frac_block = 128;
     int seg_tile = 512;

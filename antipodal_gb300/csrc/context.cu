@@ -340,6 +340,10 @@ int agwn_context_set_option(agwn_context* ctx, int option, double value)
         AGWN_CHECK_ARG(std::isfinite(value) && value > 0.0 && value <= 1.0, "term error bound must be in (0, 1]");
         ctx->robust_term_err = value;
         return AGWN_OK;
+    case AGWN_OPT_PARAM_MODE:
+        AGWN_CHECK_ARG(value == AGWN_PARAM_EXACT || value == AGWN_PARAM_MIXED, "parametric mode must be 0 or 1");
+        ctx->param_mode = int(value);
+        return AGWN_OK;
     default:
         return fail(AGWN_ERR_INVALID, "unknown option %d", option);
     }
@@ -373,6 +377,9 @@ int agwn_context_get_option(agwn_context* ctx, int option, double* value)
         return AGWN_OK;
     case AGWN_OPT_ROBUST_TERM_ERR:
         *value = ctx->robust_term_err;
+        return AGWN_OK;
+    case AGWN_OPT_PARAM_MODE:
+        *value = ctx->param_mode;
         return AGWN_OK;
     case AGWN_OPT_MIXED_TERM_ERR:
         *value = ctx->mixed_term_err;

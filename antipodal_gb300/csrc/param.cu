@@ -15,6 +15,7 @@
 // produce the same leaves and the same value; a larger s only refines further.
 
 #include "agwn_internal.cuh"
+#include "df32.cuh"
 #include "tma.cuh"
 
 #include <cmath>
@@ -151,6 +152,125 @@ __device__ __forceinline__ double gk15_panel(const double* c, ev3<rd> p, ev3<rd>
     return ik.v;
 }
 
+// ---- double-float form ----------------------------------------------------------------------------------------
+// The same integrand and panel rule in double-float arithmetic (df32.cuh, ~44 significant bits on the FP32 pipe):
+// the curve's control points relative to the query, the Bernstein basis and its derivative in closed form, the
+// normalisation and w - d_eta as above.  Not bit-identical to the reference (the value differs in the last ~1e-13
+// relative, and a panel whose |Ik - Ig| sits at the tolerance can be decided the other way); the tree rule, the
+// tolerances and the summation order are the plain integrator's.
+struct alignas(16) CurveDF
+{
+    df c[12];
+};
+
+constexpr float hi_of(double d)
+{
+    return float(d);
+}
+constexpr float lo_of(double d)
+{
+    return float(d - double(float(d)));
+}
+#define AGWN_DF(d) {hi_of(d), lo_of(d)}
+__constant__ df kGkXdf[8] = {AGWN_DF(0.0),
+                             AGWN_DF(0.9914553711208126),
+                             AGWN_DF(0.9491079123427585),
+                             AGWN_DF(0.8648644233597691),
+                             AGWN_DF(0.7415311855993945),
+                             AGWN_DF(0.5860872354676911),
+                             AGWN_DF(0.4058451513773972),
+                             AGWN_DF(0.2077849550078985)};
+__constant__ df kGkWkdf[8] = {AGWN_DF(0.2094821410847278), AGWN_DF(0.0229353220105292), AGWN_DF(0.0630920926299786),
+                              AGWN_DF(0.1047900103222502), AGWN_DF(0.1406532597155259), AGWN_DF(0.1690047266392679),
+                              AGWN_DF(0.1903505780647854), AGWN_DF(0.2044329400752989)};
+__constant__ df kGkWgdf[4] = {AGWN_DF(0.4179591836734694), AGWN_DF(0.1294849661688697), AGWN_DF(0.2797053914892767),
+                              AGWN_DF(0.3818300505051189)};
+#undef AGWN_DF
+
+__device__ __forceinline__ df df_mulf(df a, float f)
+{
+    df const p = two_prod(a.hi, f);
+    return fast_two_sum(p.hi, __fmaf_rn(a.lo, f, p.lo));
+}
+
+// w(t) - d_eta(t) with cp = the curve's control points minus the query.
+__device__ __forceinline__ df integrand_df(const df (&cp)[12], df3 x0, df t)
+{
+    df const u = df_make(1.f) - t;
+    df const uu = u * u, tt = t * t, ut = u * t;
+    df const b0 = uu * u, b1 = df_mulf(uu * t, 3.f), b2 = df_mulf(ut * t, 3.f), b3 = tt * t;
+    df const uu3 = df_mulf(uu, 3.f), tt3 = df_mulf(tt, 3.f), ut6 = df_mulf(ut, 6.f);
+    df const d0 = df_neg(uu3), d1 = uu3 - ut6, d2 = ut6 - tt3, d3 = tt3;
+    df3 r, dr;
+    r.x = b0 * cp[0] + b1 * cp[3] + b2 * cp[6] + b3 * cp[9];
+    r.y = b0 * cp[1] + b1 * cp[4] + b2 * cp[7] + b3 * cp[10];
+    r.z = b0 * cp[2] + b1 * cp[5] + b2 * cp[8] + b3 * cp[11];
+    dr.x = d0 * cp[0] + d1 * cp[3] + d2 * cp[6] + d3 * cp[9];
+    dr.y = d0 * cp[1] + d1 * cp[4] + d2 * cp[7] + d3 * cp[10];
+    dr.z = d0 * cp[2] + d1 * cp[5] + d2 * cp[8] + d3 * cp[11];
+    df const s = df_sqrt(dot(r, r));
+    df const inv_s = df_make(1.f) / s;
+    df const s1 = dot(r, dr) * inv_s; // (2 r.dr) * (0.5 / s)
+    df3 const G = r * inv_s;
+    df3 const Gp = (dr - G * s1) * inv_s;
+    df const a = dot(x0, G), ap = dot(x0, Gp);
+    df3 const X = x0 - G * a;
+    df3 const Gap = G * ap, Gpa = Gp * a;
+    df3 const Xp{df_neg(Gap.x + Gpa.x), df_neg(Gap.y + Gpa.y), df_neg(Gap.z + Gpa.z)};
+    df const d_eta = dot(G, cross(X, Xp)) / dot(X, X);
+    // x1 = -x0, so x1 (x1 . G) = x0 (x0 . G)
+    df3 const v = G - x0 * a, vp = Gp - x0 * ap;
+    df const w = df_neg(dot(x0, cross(v, vp))) / dot(v, v);
+    return w - d_eta;
+}
+
+__device__ __forceinline__ double gk15_panel_df(const df (&cp)[12], df3 x0, int depth, uint32_t j, float* err)
+{
+    float const scale = ldexpf(1.f, -depth);
+    float const h = 0.5f * scale;
+    df const cc = two_sum(float(j) * scale, h); // both exact: the centre (j + 1/2) 2^-depth
+    df const f0 = integrand_df(cp, x0, cc);
+    df fm[8], fp[8];
+#pragma unroll 1
+    for (int k = 1; k <= 7; ++k)
+    {
+        df const dx = df_scale(kGkXdf[k], h);
+        fm[k] = integrand_df(cp, x0, cc - dx);
+        fp[k] = integrand_df(cp, x0, cc + dx);
+    }
+    df ig = kGkWgdf[0] * f0;
+    df ik = kGkWkdf[0] * f0;
+    ik = ik + kGkWkdf[1] * (fm[1] + fp[1]);
+    {
+        df const s2 = fm[2] + fp[2];
+        ik = ik + kGkWkdf[2] * s2;
+        ig = ig + kGkWgdf[1] * s2;
+    }
+    ik = ik + kGkWkdf[3] * (fm[3] + fp[3]);
+    {
+        df const s4 = fm[4] + fp[4];
+        ik = ik + kGkWkdf[4] * s4;
+        ig = ig + kGkWgdf[2] * s4;
+    }
+    ik = ik + kGkWkdf[5] * (fm[5] + fp[5]);
+    {
+        df const s6 = fm[6] + fp[6];
+        ik = ik + kGkWkdf[6] * s6;
+        ig = ig + kGkWgdf[3] * s6;
+    }
+    ik = ik + kGkWkdf[7] * (fm[7] + fp[7]);
+    df const diff = df_scale(ik - ig, h);
+    *err = fabsf(diff.hi + diff.lo);
+    return df_to(df_scale(ik, h));
+}
+
+__global__ void k_curves_df(const double* __restrict__ curves, int64_t n_curves, CurveDF* __restrict__ out)
+{
+    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < 12 * n_curves;
+         i += int64_t(gridDim.x) * blockDim.x)
+        out[i / 12].c[i % 12] = df_from(curves[i]);
+}
+
 // out[q] = (sum over curves of the curve integral) / (4 pi).
 //
 // The cost of one (query, curve) integral is heavy-tailed: a query whose line along x0 passes close to a curve
@@ -168,6 +288,7 @@ __device__ __forceinline__ double gk15_panel(const double* c, ev3<rd> p, ev3<rd>
 // start_depth: per (query, curve), row-major [n][n_curves], nullable = all 0.  stats (nullable): per (query,
 // curve) packed as leaves | shallowest leaf depth << 16 | deepest leaf depth << 24.  nodes_total (nullable):
 // panels evaluated per query.  pair_vals: gridDim.x * kParamBlock * tile doubles.
+template <bool DF>
 __global__ void __launch_bounds__(kParamBlock) k_param_gk15(const double* __restrict__ pos, int64_t n,
                                                             double* __restrict__ out, double x0x, double x0y,
                                                             double x0z, const Bez* __restrict__ curves,
@@ -184,6 +305,7 @@ __global__ void __launch_bounds__(kParamBlock) k_param_gk15(const double* __rest
     Bez* const buf = reinterpret_cast<Bez*>(smem);
     double* const slab = pair_vals + size_t(blockIdx.x) * kParamBlock * tile;
     ev3<rd> const x0{rd(x0x), rd(x0y), rd(x0z)};
+    df3 const x0df{df_from(x0x), df_from(x0y), df_from(x0z)};
     int64_t const n_blocks_q = (n + kParamBlock - 1) / kParamBlock;
     int const n_tiles = int((n_curves + tile - 1) / tile);
     unsigned const lane = threadIdx.x & 31u;
@@ -227,6 +349,7 @@ __global__ void __launch_bounds__(kParamBlock) k_param_gk15(const double* __rest
             int k = 0, ql = 0, s = 0, d = 0, leaves = 0, dmin = 0, dmax = 0, pnodes = 0;
             uint32_t j = 0;
             ev3<rd> p{};
+            df cp[DF ? 12 : 1]; // DF: this pair's control points minus its query
             double pending[kParamMaxDepth + 1];
             for (;;)
             {
@@ -248,6 +371,14 @@ __global__ void __launch_bounds__(kParamBlock) k_param_gk15(const double* __rest
                             ql = mine - k * nq;
                             int64_t const q = q0 + ql;
                             p = ev3<rd>{rd(pos[3 * q]), rd(pos[3 * q + 1]), rd(pos[3 * q + 2])};
+                            if constexpr (DF)
+                            {
+                                df const pd[3] = {df_from(p.x.v), df_from(p.y.v), df_from(p.z.v)};
+                                CurveDF const& cv = reinterpret_cast<const CurveDF*>(buf)[k];
+#pragma unroll
+                                for (int e = 0; e < 12; ++e)
+                                    cp[e] = cv.c[e] - pd[e % 3];
+                            }
                             s = start_depth ? min(int(start_depth[q * n_curves + c0 + k]), max_depth) : 0;
                             d = s;
                             j = 0;
@@ -265,7 +396,15 @@ __global__ void __launch_bounds__(kParamBlock) k_param_gk15(const double* __rest
                 if (pi < 0)
                     continue;
                 double err;
-                double v = gk15_panel(buf[k].c, p, x0, d, j, &err);
+                double v;
+                if constexpr (DF)
+                {
+                    float e32;
+                    v = gk15_panel_df(cp, x0df, d, j, &e32);
+                    err = double(e32);
+                }
+                else
+                    v = gk15_panel(buf[k].c, p, x0, d, j, &err);
                 ++pnodes;
                 if (!(d >= max_depth || (d >= min_depth && err <= tol_at[d])))
                 {
@@ -322,6 +461,7 @@ int param_run(Context& ctx, const double* d_pos, int64_t n, double* d_out, const
               int64_t n_curves, int min_depth, int max_depth, double tol, const uint8_t* d_start, uint32_t* d_stats,
               int32_t* d_nodes)
 {
+    bool const dfm = ctx.param_mode == AGWN_PARAM_MIXED;
     if (n == 0)
         return AGWN_OK;
     if (n_curves == 0)
@@ -331,11 +471,13 @@ int param_run(Context& ctx, const double* d_pos, int64_t n, double* d_out, const
             AGWN_TRY_CUDA(cudaMemsetAsync(d_nodes, 0, sizeof(int32_t) * n, ctx.stream));
         return AGWN_OK;
     }
+    static_assert(sizeof(CurveDF) == sizeof(Bez), "both curve forms stage through the same tile");
     int const tile = int(std::min<int64_t>(kParamTileMax, n_curves));
     size_t const smem = size_t(tile) * sizeof(Bez);
-    AGWN_TRY_CUDA(cudaFuncSetAttribute(k_param_gk15, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+    auto const kern = dfm ? k_param_gk15<true> : k_param_gk15<false>;
+    AGWN_TRY_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
     int per_sm = 0;
-    AGWN_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_param_gk15, kParamBlock, smem));
+    AGWN_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kParamBlock, smem));
     if (per_sm < 1)
         return fail(AGWN_ERR_UNSUPPORTED, "parametric kernel does not fit on an SM");
     int64_t const n_blocks_q = (n + kParamBlock - 1) / kParamBlock;
@@ -343,11 +485,21 @@ int param_run(Context& ctx, const double* d_pos, int64_t n, double* d_out, const
     double* pair_vals = nullptr;
     AGWN_TRY(ctx.scratch_reserve(S_SEGS_RAW, sizeof(double) * size_t(grid) * kParamBlock * tile,
                                  reinterpret_cast<void**>(&pair_vals)));
+    const void* tile_src = d_curves;
+    if (dfm)
+    {
+        void* cdf = nullptr;
+        AGWN_TRY(ctx.scratch_reserve(S_FRAME, sizeof(CurveDF) * size_t(n_curves), &cdf));
+        AGWN_TRY(ctx.launch_begin(AGWN_K_OTHER));
+        k_curves_df<<<int(std::min<int64_t>(div_up(12 * n_curves, 256), 4 * ctx.sm_count)), 256, 0, ctx.stream>>>(
+            d_curves, n_curves, static_cast<CurveDF*>(cdf));
+        AGWN_TRY(ctx.launch_end(AGWN_K_OTHER));
+        tile_src = cdf;
+    }
     AGWN_TRY(ctx.launch_begin(AGWN_K_PARAMETRIC));
-    k_param_gk15<<<grid, kParamBlock, smem, ctx.stream>>>(d_pos, n, d_out, x0[0], x0[1], x0[2],
-                                                         reinterpret_cast<const Bez*>(d_curves), n_curves, tile,
-                                                         min_depth, max_depth, tol, d_start, d_stats, d_nodes,
-                                                         pair_vals, ctx.d_flags);
+    kern<<<grid, kParamBlock, smem, ctx.stream>>>(d_pos, n, d_out, x0[0], x0[1], x0[2],
+                                                 reinterpret_cast<const Bez*>(tile_src), n_curves, tile, min_depth,
+                                                 max_depth, tol, d_start, d_stats, d_nodes, pair_vals, ctx.d_flags);
     return ctx.launch_end(AGWN_K_PARAMETRIC);
 }
 } // namespace agwn

@@ -84,7 +84,16 @@ enum agwn_option
        others -- num == 0 branches, ill-conditioned or large differences -- in FP64; counts unchanged). */
     AGWN_OPT_ROBUST_MODE = 7,
     /* Robust mixed mode: the per-pair estimate above which a pair is evaluated in FP64, radians.  Default 1e-7. */
-    AGWN_OPT_ROBUST_TERM_ERR = 8
+    AGWN_OPT_ROBUST_TERM_ERR = 8,
+    /* Parametric integrator arithmetic: AGWN_PARAM_EXACT (default, FP64 with the reference's operation order, bit
+       for bit) or AGWN_PARAM_MIXED (double-float on the FP32 pipe, ~44 significant bits; the same tree rule,
+       tolerances and summation order). */
+    AGWN_OPT_PARAM_MODE = 9
+};
+enum agwn_param_mode
+{
+    AGWN_PARAM_EXACT = 0,
+    AGWN_PARAM_MIXED = 1
 };
 enum agwn_robust_mode
 {

@@ -141,3 +141,34 @@ def test_param_device_tensors(gwn, disp):
     gwn.eval_gwnr_parametric_batch_fractional(disp, qd, out, x0, cd, cfg)
     torch.cuda.synchronize()
     assert np.array_equal(out.cpu().numpy(), host)
+
+
+@pytest.mark.parametrize("tol", [1e-10, 1e-6])
+def test_param_double_float_form_agrees_with_plain(gwn, disp, tol):
+    """The double-float (FP32-pipe) integrator: the same tree rule in ~44-bit arithmetic.  Its values stay within
+    the integrator's own error scale of the plain FP64 ones, and nearly every pair builds the same tree."""
+    curves, q, x0 = patches(41, 6, 400)
+    cfg = gwn.IntegrateConfig(0, 10, tol)
+    st_e = np.empty((len(q), len(curves)), np.uint32)
+    exact = run(gwn, disp, q, x0, curves, cfg, pair_stats=st_e)
+    disp.set_param_precision("mixed")
+    try:
+        st_m = np.empty_like(st_e)
+        mixed = run(gwn, disp, q, x0, curves, cfg, pair_stats=st_m)
+    finally:
+        disp.set_param_precision("exact")
+    # leaves forced at max_depth carry error estimates above tol, so no partition bound holds there: the bar is
+    # the product's 1e-7 against FP64, with margin; typical pairs agree to ~1e-13
+    d = np.abs(mixed - exact)
+    assert d.max() <= 1e-8, d.max()
+    assert np.median(d) <= 1e-12
+    assert np.mean(st_m == st_e) > 0.99
+    # on straight-line curves too (the golden line-curve cube)
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "reference_golden.npz"))
+    disp.set_param_precision("mixed")
+    try:
+        got = run(gwn, disp, g["param_lines_queries"], synth.unit_x0(), g["param_lines_curves"],
+                  gwn.IntegrateConfig(0, 10, 1e-6))
+    finally:
+        disp.set_param_precision("exact")
+    assert np.abs(got - g["param_lines_out"]).max() <= 1e-9
