@@ -31,9 +31,13 @@ struct Frame32
 // float (u, v) coordinate (the query's, rotated in float, and the vertices', rounded from FP64).  An edge function
 // e = du*rv - dv*ru then errs by at most 3*delta*(|du| + |dv| + |ru| + |rv|); the margin takes 8*delta.  The exact
 // Moller-Trumbore test decides every leaf that passes.
+// Leaf data: 3 float4 per leaf, (u_a, v_a, u_b, v_b), (u_c, v_c, w_a, w_b), (w_c, 0, 0, 0): the triangle's corners
+// in the ray frame, rounded to float.
+constexpr int kLeafF4 = 3;
+
 __device__ __forceinline__ bool may_hit(const float4* __restrict__ leaf_uv, int leaf, float u, float v, float m8)
 {
-    float4 const a = leaf_uv[2 * leaf], b = leaf_uv[2 * leaf + 1];
+    float4 const a = leaf_uv[kLeafF4 * leaf], b = leaf_uv[kLeafF4 * leaf + 1];
     float const pu[3] = {a.x, a.z, b.x}, pv[3] = {a.y, a.w, b.y};
     bool pos = false, neg = false;
 #pragma unroll
@@ -47,6 +51,55 @@ __device__ __forceinline__ bool may_hit(const float4* __restrict__ leaf_uv, int 
         neg |= e < -m;
     }
     return !(pos && neg);
+}
+
+// The companion of may_hit that decides a leaf in float when it can: 1 or -1 (the ray certainly crosses the
+// triangle, with that orientation), 0 (it certainly does not), 2 (undecided: run the exact test).  Inside: every
+// edge function beyond its may_hit margin, all with one sign (that sign is the projected orientation, and the frame
+// is right-handed, so it is the sign of the triangle normal along the ray).  In front or behind: the plane's depth
+// at (u, v) minus the query's, (e1 dw_a + e2 dw_b + e0 dw_c) / E with E = e0 + e1 + e2, against the bound that the
+// edge functions' errors (3 delta (|du| + |dv| + |ru| + |rv|) each, delta = m8 / 8) and the depths' (2 delta each)
+// carry through that quotient, doubled.  delta is 1e-6 of the coordinate scale, far above the rounding of either
+// this float evaluation or the exact test, so a decided leaf gets the exact test's answer; only points within
+// that margin of an edge, a vertex or the plane go to the exact test.
+__device__ __forceinline__ int certain_leaf(const float4* __restrict__ leaf_uv, int leaf, float u, float v, float w,
+                                            float m8)
+{
+    float4 const a = leaf_uv[kLeafF4 * leaf], b = leaf_uv[kLeafF4 * leaf + 1], c = leaf_uv[kLeafF4 * leaf + 2];
+    float const pu[3] = {a.x, a.z, b.x}, pv[3] = {a.y, a.w, b.y};
+    float const dw[3] = {b.z - w, b.w - w, c.x - w}; // depths of a, b, c relative to the query
+    float e[3], err[3];
+    bool pos = true, neg = true;
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+    {
+        int const k1 = (k + 1) % 3;
+        float const du = pu[k1] - pu[k], dv = pv[k1] - pv[k], ru = u - pu[k], rv = v - pv[k];
+        float const sabs = fabsf(du) + fabsf(dv) + fabsf(ru) + fabsf(rv);
+        e[k] = du * rv - dv * ru;
+        err[k] = 0.375f * m8 * sabs;
+        pos &= e[k] > m8 * sabs;
+        neg &= e[k] < -m8 * sabs;
+    }
+    if (!(pos || neg))
+        return 2;
+    // e[k] is the weight of the vertex opposite edge k: e0 -> c, e1 -> a, e2 -> b
+    float const E = e[0] + e[1] + e[2];
+    float const errE = err[0] + err[1] + err[2];
+    float const N = e[1] * dw[0] + e[2] * dw[1] + e[0] * dw[2];
+    float const two_delta = 0.25f * m8;
+    float const errN = err[1] * fabsf(dw[0]) + err[2] * fabsf(dw[1]) + err[0] * fabsf(dw[2]) +
+                       two_delta * (fabsf(e[0]) + fabsf(e[1]) + fabsf(e[2]));
+    float const aE = fabsf(E);
+    if (!(aE > 2.f * errE))
+        return 2;
+    float const depth = N / E;
+    float const bound = 2.f * (errN + fabsf(depth) * errE) / (aE - errE);
+    if (depth > bound)
+        return pos ? 1 : -1;
+    if (depth < -bound)
+        return 0;
+    return 2;
 }
 
 // Walks the hierarchy for the query point (u, v) and depth w, calling emit(leaf) for every leaf whose box the ray

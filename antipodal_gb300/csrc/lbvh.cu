@@ -23,6 +23,8 @@
 #include "gwn_kernels.cuh"
 #include "hier.cuh"
 
+#include <type_traits>
+
 #include <algorithm>
 #include <atomic>
 #include <cmath>
@@ -326,15 +328,16 @@ __global__ void k_leaves(const T* __restrict__ tri_in, const unsigned* __restric
             tri[9 * l + k] = tri_in[9 * int64_t(t) + k];
         for (int k = 0; k < 6; ++k)
             leaf_box[6 * l + k] = box[6 * int64_t(t) + k];
+        float* const o = leaf_uv + 4 * kLeafF4 * l; // layout: see kLeafF4 (hier.cuh)
         for (int v = 0; v < 3; ++v)
         {
             double const x = double(tri_in[9 * int64_t(t) + 3 * v]), y = double(tri_in[9 * int64_t(t) + 3 * v + 1]),
                          z = double(tri_in[9 * int64_t(t) + 3 * v + 2]);
-            leaf_uv[8 * l + 2 * v] = float(f.r[0] * x + f.r[1] * y + f.r[2] * z);
-            leaf_uv[8 * l + 2 * v + 1] = float(f.r[3] * x + f.r[4] * y + f.r[5] * z);
+            o[2 * v] = float(f.r[0] * x + f.r[1] * y + f.r[2] * z);
+            o[2 * v + 1] = float(f.r[3] * x + f.r[4] * y + f.r[5] * z);
+            o[6 + v] = float(f.r[6] * x + f.r[7] * y + f.r[8] * z);
         }
-        leaf_uv[8 * l + 6] = 0.f;
-        leaf_uv[8 * l + 7] = 0.f;
+        o[9] = o[10] = o[11] = 0.f;
     }
 }
 
@@ -462,6 +465,19 @@ __global__ void __launch_bounds__(kTravBlock) k_traverse(const BvhNode* __restri
             float const qmax = fmaxf(fmaxf(fabsf(ox), fabsf(oy)), fabsf(oz));
             float const tol = (qmax + scene_scale) * 3.8146973e-6f + 1e-30f; // 2^-18 of the coordinate scale
             float const m8 = 8.0f * 1e-6f * (qmax + scene_scale);            // 8 * delta of may_hit
+            // Double input: most candidates are decided in float by certain_leaf, whose margins are ~1e9 times the
+            // FP64 test's rounding; the rest take NaiveIntersector's exact test.  Float input always takes the exact
+            // test: its own rounding is not small enough against the margin for very thin triangles.
+            auto const decide = [&](int leaf) -> int
+            {
+                if constexpr (std::is_same_v<T, double>)
+                {
+                    int const c = certain_leaf(leaf_uv, leaf, u, v, w, m8);
+                    if (c != 2)
+                        return c;
+                }
+                return leaf_test<T>(tri, leaf, p, dir);
+            };
             int cand[kCand];
             int nc = 0;
             bool const ok = hier_walk(nodes, leaf_uv, u, v, w, tol, m8,
@@ -470,7 +486,7 @@ __global__ void __launch_bounds__(kTravBlock) k_traverse(const BvhNode* __restri
                                           if (nc == kCand)
                                           {
                                               for (int j = 0; j < kCand; ++j)
-                                                  sum += leaf_test<T>(tri, cand[j], p, dir);
+                                                  sum += decide(cand[j]);
                                               nc = 0;
                                           }
                                           cand[nc++] = leaf;
@@ -478,7 +494,7 @@ __global__ void __launch_bounds__(kTravBlock) k_traverse(const BvhNode* __restri
             if (!ok)
                 atomicOr(flags + FLAG_STACK, 1);
             for (int j = 0; j < nc; ++j)
-                sum += leaf_test<T>(tri, cand[j], p, dir);
+                sum += decide(cand[j]);
         }
         counts[i] = sum;
     }
@@ -625,7 +641,7 @@ int build_hier(Context& ctx, const T* tri_in, int64_t n_tri, const double* dir, 
     AGWN_TRY_CUDA(cudaStreamSynchronize(st)); // the buffers may still be read by queued traversals
     AGWN_TRY(out.tri.reserve(sizeof(T) * 9 * std::max<int64_t>(1, n_tri)));
     AGWN_TRY(out.nodes.reserve(sizeof(BvhNode) * std::max<int64_t>(1, n_tri - 1)));
-    AGWN_TRY(out.leaf_uv.reserve(sizeof(float) * 8 * std::max<int64_t>(1, n_tri)));
+    AGWN_TRY(out.leaf_uv.reserve(sizeof(float4) * kLeafF4 * std::max<int64_t>(1, n_tri)));
     T* tri = static_cast<T*>(out.tri.ptr);
     int32_t depth = n_tri > 0 ? 1 : 0;
     unsigned scale_bits = 0;
