@@ -115,6 +115,10 @@ struct Context
     DevBuf scratch[S_COUNT];
     int sm_count = 0;
     RayCache ray_cache;
+    // host-array pipeline (mesh batch): upload and download streams and their events, created on first use
+    cudaStream_t copy_in = nullptr, copy_out = nullptr;
+    cudaEvent_t pipe_ev[6] = {};
+    int ensure_pipeline();
 
     // options
     int frac_mode = AGWN_FRAC_EXACT;

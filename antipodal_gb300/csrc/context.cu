@@ -145,6 +145,18 @@ bool is_device_pointer(const void* p)
     return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
+int Context::ensure_pipeline()
+{
+    if (!copy_in)
+        AGWN_TRY_CUDA(cudaStreamCreateWithFlags(&copy_in, cudaStreamNonBlocking));
+    if (!copy_out)
+        AGWN_TRY_CUDA(cudaStreamCreateWithFlags(&copy_out, cudaStreamNonBlocking));
+    for (cudaEvent_t& e : pipe_ev)
+        if (!e)
+            AGWN_TRY_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    return AGWN_OK;
+}
+
 int stage_in(Context& ctx, const void* src, size_t bytes, int slot, const void** dev)
 {
     if (bytes == 0 || is_device_pointer(src))
@@ -285,6 +297,13 @@ int agwn_context_destroy(agwn_context* ctx)
         cudaFree(ctx->d_counters);
     if (ctx->h_flags)
         cudaFreeHost(ctx->h_flags);
+    for (cudaEvent_t e : ctx->pipe_ev)
+        if (e)
+            cudaEventDestroy(e);
+    if (ctx->copy_in)
+        cudaStreamDestroy(ctx->copy_in);
+    if (ctx->copy_out)
+        cudaStreamDestroy(ctx->copy_out);
     if (ctx->own_stream && ctx->stream)
         cudaStreamDestroy(ctx->stream);
     delete ctx;

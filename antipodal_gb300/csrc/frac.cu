@@ -30,6 +30,8 @@
 //              The FP64 terms and the compensated FP32 sum are combined in FP64.
 
 #include "agwn_internal.cuh"
+
+#include <algorithm>
 #include "frac_kernels.cuh"
 #include "gwn_kernels.cuh"
 #include "tma.cuh"
@@ -163,6 +165,56 @@ template int fractional_run<float>(Context&, const float*, int64_t, float*, cons
 // --------------------------------------------------------------------------------------------------------------
 namespace
 {
+// Host queries and host results: the batch runs in chunks through two device buffers, so that uploading chunk
+// i + 1 and downloading chunk i - 1 (each on its own copy stream) overlap the kernels of chunk i on the context's
+// stream.  Events order every reuse of a buffer: an upload waits until the kernels of the chunk two back have read
+// its buffer, and the kernels wait until that chunk's results have left theirs.
+template <class T>
+int mesh_batch_pipelined(Context& ctx, const agwn_bvh* bvh, const T* positions, int64_t n, T* out, const T* x0,
+                         const T* dseg, int64_t n_seg, bool want_frac)
+{
+    AGWN_TRY(ctx.ensure_pipeline());
+    int64_t chunk = std::max<int64_t>(int64_t(1) << 20, (n + 7) / 8);
+    chunk = (chunk + 1023) / 1024 * 1024;
+    void *qbuf = nullptr, *obuf = nullptr;
+    int32_t* dcounts = nullptr;
+    AGWN_TRY(ctx.scratch_reserve(S_QUERIES, 2 * sizeof(T) * 3 * size_t(chunk), &qbuf));
+    AGWN_TRY(ctx.scratch_reserve(S_OUT, 2 * sizeof(T) * size_t(chunk), &obuf));
+    bool const with_int = bvh && bvh->n_tri > 0;
+    if (with_int)
+        AGWN_TRY(ctx.scratch_reserve(S_COUNTS, sizeof(int32_t) * size_t(chunk), reinterpret_cast<void**>(&dcounts)));
+    cudaEvent_t* const up = ctx.pipe_ev;       // [b]: chunk uploaded into buffer b
+    cudaEvent_t* const done = ctx.pipe_ev + 2; // [b]: kernels on buffer b finished
+    cudaEvent_t* const down = ctx.pipe_ev + 4; // [b]: results of buffer b downloaded
+    // the copy streams start after everything already queued on the context stream (the staged boundary)
+    AGWN_TRY_CUDA(cudaEventRecord(done[0], ctx.stream));
+    AGWN_TRY_CUDA(cudaStreamWaitEvent(ctx.copy_in, done[0], 0));
+    int64_t const n_chunks = (n + chunk - 1) / chunk;
+    for (int64_t i = 0; i < n_chunks; ++i)
+    {
+        int const b = int(i & 1);
+        int64_t const q0 = i * chunk, m = std::min(chunk, n - q0);
+        T* const qb = static_cast<T*>(qbuf) + size_t(b) * 3 * chunk;
+        T* const ob = static_cast<T*>(obuf) + size_t(b) * chunk;
+        if (i >= 2)
+            AGWN_TRY_CUDA(cudaStreamWaitEvent(ctx.copy_in, done[b], 0));
+        AGWN_TRY_CUDA(cudaMemcpyAsync(qb, positions + 3 * q0, sizeof(T) * 3 * m, cudaMemcpyHostToDevice, ctx.copy_in));
+        AGWN_TRY_CUDA(cudaEventRecord(up[b], ctx.copy_in));
+        AGWN_TRY_CUDA(cudaStreamWaitEvent(ctx.stream, up[b], 0));
+        if (i >= 2)
+            AGWN_TRY_CUDA(cudaStreamWaitEvent(ctx.stream, down[b], 0));
+        if (with_int)
+            AGWN_TRY(integer_run<T>(ctx, *bvh, qb, m, dcounts, x0));
+        AGWN_TRY(fractional_run<T>(ctx, qb, m, ob, with_int ? dcounts : nullptr, x0, dseg, want_frac ? n_seg : 0));
+        AGWN_TRY_CUDA(cudaEventRecord(done[b], ctx.stream));
+        AGWN_TRY_CUDA(cudaStreamWaitEvent(ctx.copy_out, done[b], 0));
+        AGWN_TRY_CUDA(cudaMemcpyAsync(out + q0, ob, sizeof(T) * m, cudaMemcpyDeviceToHost, ctx.copy_out));
+        AGWN_TRY_CUDA(cudaEventRecord(down[b], ctx.copy_out));
+    }
+    AGWN_TRY_CUDA(cudaStreamSynchronize(ctx.copy_out));
+    return ctx.check_flags();
+}
+
 template <class T>
 int mesh_batch(agwn_context* ctx, const agwn_bvh* bvh, const T* positions, int64_t n, T* out, const T* x0,
                const T* boundary, int64_t n_seg, bool want_frac)
@@ -184,6 +236,12 @@ int mesh_batch(agwn_context* ctx, const agwn_bvh* bvh, const T* positions, int64
     const void* dseg = nullptr;
     void* dout = nullptr;
     bool host_out = false;
+    if (n >= (int64_t(1) << 21) && !is_device_pointer(positions) && !is_device_pointer(out))
+    {
+        AGWN_TRY(stage_in(*ctx, boundary, sizeof(T) * 7 * n_seg, S_MISC0, &dseg));
+        return mesh_batch_pipelined<T>(*ctx, bvh, positions, n, out, x0, static_cast<const T*>(dseg), n_seg,
+                                       want_frac);
+    }
     AGWN_TRY(stage_in(*ctx, positions, sizeof(T) * 3 * n, S_QUERIES, &dpos));
     AGWN_TRY(stage_in(*ctx, boundary, sizeof(T) * 7 * n_seg, S_MISC0, &dseg));
     AGWN_TRY(stage_out(*ctx, out, sizeof(T) * n, S_OUT, &dout, &host_out));

@@ -214,3 +214,30 @@ def test_own_atan2_against_cuda_and_fp64(gwn, disp):
     err_cuda = np.abs(ref - exact) / ulp
     assert np.max(err_ours) <= 6.0, np.max(err_ours)
     assert np.max(err_cuda) <= 6.0
+
+
+def test_host_arrays_pipelined_equal_device_arrays(gwn):
+    """Host queries and results of 2^21 or more run through the chunked upload/compute/download pipeline; the values
+    must equal the device-array call's bit for bit, in both precisions of the fractional term."""
+    torch = pytest.importorskip("torch")
+    verts, idx, bnd, q, x0 = synth.open_icosphere(seed=2, level=4, grid=128)
+    assert len(q) >= 1 << 21
+    s = torch.cuda.Stream()
+    disp = gwn.CudaDispatcher(stream=s)
+    isect = gwn.CudaIntersector(disp, verts, idx)
+    for prec in ("exact", "mixed"):
+        disp.set_precision(prec)
+        qd = torch.from_numpy(q).cuda()
+        od = torch.empty(len(q), dtype=torch.float64, device="cuda")
+        gwn.eval_gwnr_mesh_batch(disp, isect, qd, od, x0, torch.from_numpy(bnd).cuda())
+        disp.synchronize()
+        qh = torch.from_numpy(q).pin_memory().numpy()
+        oh = torch.empty(len(q), dtype=torch.float64).pin_memory().numpy()
+        gwn.eval_gwnr_mesh_batch(disp, isect, qh, oh, x0, bnd)
+        assert np.array_equal(oh, od.cpu().numpy()), prec
+        # pageable host memory takes the same path
+        op = np.empty(len(q))
+        gwn.eval_gwnr_mesh_batch(disp, isect, q, op, x0, bnd)
+        assert np.array_equal(op, oh)
+    isect.close()
+    disp.close()
