@@ -17,7 +17,7 @@ struct alignas(16) SegX
 {
     T p0x, p0y, p0z, p1x, p1y, p1z, w, pad;
 };
-// Mixed-mode segment: a = (P0_hi, w), b = (P1 - P0, tau * |p1 - p0|), c = (P0_lo, index as bits).
+// Mixed-mode segment: a = (P0_hi, w), b = (P1 - P0, (tau * |p1 - p0|)^2), c = (P0_lo, index as bits).
 struct alignas(16) SegM
 {
     float4 a, b, c;
@@ -265,7 +265,7 @@ __global__ void __launch_bounds__(1024) k_prep_mixed(const double* __restrict__ 
         float const len = float(sqrt(ex * ex + ey * ey + ez * ez));
         SegM m;
         m.a = make_float4(hi[0], hi[1], hi[2], float(w[6]));
-        m.b = make_float4(dv[0], dv[1], dv[2], tau * len);
+        m.b = make_float4(dv[0], dv[1], dv[2], (tau * len) * (tau * len)); // near test on squared lengths
         m.c = make_float4(lo[0], lo[1], lo[2], __int_as_float(int(s)));
         out[s] = m;
         out64[s] = SegX<double>{w[0], w[1], w[2], w[3], w[4], w[5], w[6], 0.0};
@@ -503,8 +503,10 @@ __global__ void __launch_bounds__(256, mixed_min_blocks<K>()) k_frac_mixed(const
                     float const an = fabsf(num_s), ad = fabsf(den_s);
                     float const inv = __fdividef(1.f, fmaxf(fmaxf(an, ad), 1e-37f));
                     float const an1 = an * inv, ad1 = ad * inv;
-                    bool const need = fminf(l0, l1) < B.w || !(q0 > 0.f && q1 > 0.f) || !(nn + ad < INFINITY) ||
-                                      kEpsBound * fmaf(sn, ad1, sd * an1) * inv > term_err ||
+                    // near: min(|v0|, |v1|)^2 < (tau |P1 - P0|)^2 (also catches |v| = 0, where l is NaN); an infinity
+                    // or NaN anywhere makes the bound NaN, which the negated comparison sends to FP64 as well
+                    bool const need = fminf(q0, q1) < B.w ||
+                                      !(kEpsBound * fmaf(sn, ad1, sd * an1) * inv <= term_err) ||
                                       (den_s < 0.f && an <= kEpsBound * sn);
                     unsigned const m = __ballot_sync(0xffffffffu, need);
                     if (m)
