@@ -405,12 +405,20 @@ def eval_gwnr_mesh_batch_integer_bruteforce(dispatcher: CudaDispatcher, vertices
     del x
 
 
-def build_boundary_segments(vertices, indices) -> np.ndarray:
-    """Open boundary as (s, 7) [pos0, pos1, weight] rows, the rule of build_boundary_segments
-    (src/antipodal/math/common.hh:123-174), ordered by (lo, hi) vertex index.  Host-side (numpy)."""
-    from .synth import boundary_segments
-    v = np.asarray(vertices)
-    return boundary_segments(v, np.asarray(indices, np.int32)).astype(v.dtype)
+def build_boundary_segments(dispatcher: CudaDispatcher, vertices, indices):
+    """build_boundary_segments (src/antipodal/math/common.hh:123-174) on the device: the open boundary as (s, 7)
+    [pos0, pos1, weight] rows in ascending (lo, hi) vertex order.  Returns a numpy array for host vertices and a
+    CUDA tensor for CUDA vertices."""
+    dt, kind = _float_kind(vertices)
+    v = _View(vertices, dt, 3, "vertices")
+    i = _View(indices, np.int32, None, "indices")
+    fn = getattr(library(), f"agwn_build_boundary_segments_{kind}")
+    cnt = C.c_int64()
+    _check(fn(dispatcher.handle, v.ptr, v.n, i.ptr, i.n, None, 0, C.byref(cnt)), "build_boundary_segments")
+    out = _empty_like_input(vertices, (cnt.value, 7), dt)
+    o = _View(out, dt, None, "out", writable=True)
+    _check(fn(dispatcher.handle, v.ptr, v.n, i.ptr, i.n, o.ptr, cnt.value, C.byref(cnt)), "build_boundary_segments")
+    return out
 
 
 class CudaRobustBatch:

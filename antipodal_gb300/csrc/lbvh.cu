@@ -22,6 +22,7 @@
 #include "agwn_internal.cuh"
 #include "gwn_kernels.cuh"
 #include "hier.cuh"
+#include "radix.cuh"
 
 #include <type_traits>
 
@@ -163,101 +164,7 @@ __global__ void k_morton2(const float* __restrict__ cen, int64_t n_tri, const un
     }
 }
 
-// ---- stable LSD radix sort, 8 bits per pass -----------------------------------------------------------------
-constexpr int kRsBlock = 256;
-constexpr int kRsIpt = 8;
-constexpr int kRsTile = kRsBlock * kRsIpt;
 
-__global__ void __launch_bounds__(kRsBlock) k_rs_hist(const unsigned* __restrict__ keys, int64_t n, int shift,
-                                                      unsigned* __restrict__ hist, int n_blocks)
-{
-    __shared__ unsigned cnt[256];
-    cnt[threadIdx.x] = 0;
-    __syncthreads();
-    int64_t const base = int64_t(blockIdx.x) * kRsTile;
-    for (int r = 0; r < kRsIpt; ++r)
-    {
-        int64_t const i = base + r * kRsBlock + threadIdx.x;
-        if (i < n)
-            atomicAdd(&cnt[(keys[i] >> shift) & 255u], 1u);
-    }
-    __syncthreads();
-    hist[int64_t(threadIdx.x) * n_blocks + blockIdx.x] = cnt[threadIdx.x];
-}
-
-// Exclusive scan of m counters in one block of 1024 threads.
-__global__ void __launch_bounds__(1024) k_rs_scan(unsigned* __restrict__ hist, int64_t m)
-{
-    __shared__ unsigned part[1024];
-    int64_t const per = (m + 1023) / 1024;
-    int64_t const b = per * threadIdx.x;
-    int64_t const e = min(b + per, m);
-    unsigned s = 0;
-    for (int64_t i = b; i < e; ++i)
-        s += hist[i];
-    part[threadIdx.x] = s;
-    __syncthreads();
-    for (int o = 1; o < 1024; o <<= 1)
-    {
-        unsigned const v = threadIdx.x >= unsigned(o) ? part[threadIdx.x - o] : 0u;
-        __syncthreads();
-        part[threadIdx.x] += v;
-        __syncthreads();
-    }
-    unsigned run = threadIdx.x ? part[threadIdx.x - 1] : 0u;
-    for (int64_t i = b; i < e; ++i)
-    {
-        unsigned const v = hist[i];
-        hist[i] = run;
-        run += v;
-    }
-}
-
-__global__ void __launch_bounds__(kRsBlock) k_rs_scatter(const unsigned* __restrict__ kin,
-                                                         const unsigned* __restrict__ vin, int64_t n, int shift,
-                                                         const unsigned* __restrict__ hist, int n_blocks,
-                                                         unsigned* __restrict__ kout, unsigned* __restrict__ vout)
-{
-    constexpr int W = kRsBlock / 32;
-    __shared__ unsigned base[256];
-    __shared__ unsigned wcnt[W][256];
-    base[threadIdx.x] = hist[int64_t(threadIdx.x) * n_blocks + blockIdx.x];
-    for (int w = 0; w < W; ++w)
-        wcnt[w][threadIdx.x] = 0;
-    __syncthreads();
-    int const lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    unsigned const lt = (1u << lane) - 1u;
-    int64_t const tile0 = int64_t(blockIdx.x) * kRsTile;
-    for (int r = 0; r < kRsIpt; ++r)
-    {
-        int64_t const i = tile0 + r * kRsBlock + threadIdx.x;
-        bool const valid = i < n;
-        unsigned const key = valid ? kin[i] : 0u;
-        unsigned const val = valid ? vin[i] : 0u;
-        unsigned const d = valid ? ((key >> shift) & 255u) : 256u;
-        unsigned const peers = __match_any_sync(0xffffffffu, d);
-        unsigned const rank = __popc(peers & lt);
-        bool const leader = (peers & lt) == 0;
-        if (valid && leader)
-            wcnt[warp][d] = __popc(peers);
-        __syncthreads();
-        if (valid)
-        {
-            unsigned pos = base[d] + rank;
-            for (int w = 0; w < warp; ++w)
-                pos += wcnt[w][d];
-            kout[pos] = key;
-            vout[pos] = val;
-        }
-        __syncthreads();
-        if (valid && leader)
-        {
-            atomicAdd(&base[d], unsigned(__popc(peers))); // several warps may hold the same digit
-            wcnt[warp][d] = 0;
-        }
-        __syncthreads();
-    }
-}
 
 // ---- Karras hierarchy ---------------------------------------------------------------------------------------
 __device__ __forceinline__ int delta(const unsigned* keys, int n, int i, int j)

@@ -488,6 +488,37 @@ void eval_gwnr_mesh_batch(cuda::CudaDispatcher& dispatcher, cuda::CudaIntersecto
                     "eval_gwnr_mesh_batch");
 }
 
+// common.hh:123-174 on the GPU: the open boundary, rows in ascending (lo, hi) vertex order (the reference emits
+// the same rows in hash-map order).
+template <class T>
+[[nodiscard]] std::vector<weighted_segment3<T>> build_boundary_segments(cuda::CudaDispatcher& dispatcher,
+                                                                        std::span<vec3<T> const> vertices,
+                                                                        std::span<int const> indices)
+{
+    static_assert(sizeof(weighted_segment3<T>) == 7 * sizeof(T));
+    auto const* v = cuda::detail::raw(vertices);
+    auto const* i = reinterpret_cast<std::int32_t const*>(indices.data());
+    auto run = [&](weighted_segment3<T>* out, std::int64_t cap, std::int64_t* n)
+    {
+        if constexpr (std::is_same_v<T, double>)
+            cuda::check(agwn_build_boundary_segments_f64(dispatcher.handle(), v, std::int64_t(vertices.size()), i,
+                                                         std::int64_t(indices.size()),
+                                                         reinterpret_cast<double*>(out), cap, n),
+                        "build_boundary_segments");
+        else
+            cuda::check(agwn_build_boundary_segments_f32(dispatcher.handle(), v, std::int64_t(vertices.size()), i,
+                                                         std::int64_t(indices.size()),
+                                                         reinterpret_cast<float*>(out), cap, n),
+                        "build_boundary_segments");
+    };
+    std::int64_t n = 0;
+    run(nullptr, 0, &n);
+    std::vector<weighted_segment3<T>> out(static_cast<std::size_t>(n));
+    if (n > 0)
+        run(out.data(), n, &n);
+    return out;
+}
+
 // gwn_mesh_robust.hh:441-456 on the GPU: out_wnrs[i] = robust.eval(positions[i]).
 template <class T, class Precision>
 void eval_gwnr_mesh_batch_robust(cuda::CudaDispatcher&, cuda::CudaRobustMeshGwn<T, Precision> const& robust,

@@ -200,6 +200,20 @@ int agwn_robust_eval_f64(agwn_context* ctx, const agwn_robust* robust, const dou
 int agwn_robust_eval_f32(agwn_context* ctx, const agwn_robust* robust, const float* positions, int64_t n,
                          float* out_gwn, int32_t* out_counts, float* out_frac);
 
+/* ---- open boundary of a mesh ------------------------------------------------------------------------------
+ * Replaces build_boundary_segments (src/antipodal/math/common.hh:123-174) on the device: every triangle edge
+ * u -> v adds +1 (u < v) or -1 to its undirected edge {min, max}; edges with a non-zero net count become
+ * weighted_segment3 rows (7 scalars) directed lo -> hi for a positive count and hi -> lo otherwise, weight |count|.
+ * The reference emits in hash-map order; these rows come in ascending (lo, hi) order.  *n_segments receives the
+ * number of rows; min(*n_segments, capacity) of them are written to out (host or device, may be NULL to query
+ * the count).  An index outside [0, n_vertices) is rejected with AGWN_ERR_INVALID. */
+int agwn_build_boundary_segments_f64(agwn_context* ctx, const double* vertices, int64_t n_vertices,
+                                     const int32_t* indices, int64_t n_indices, double* out, int64_t capacity,
+                                     int64_t* n_segments);
+int agwn_build_boundary_segments_f32(agwn_context* ctx, const float* vertices, int64_t n_vertices,
+                                     const int32_t* indices, int64_t n_indices, float* out, int64_t capacity,
+                                     int64_t* n_segments);
+
 /* ---- many robust meshes in one persistent launch ----------------------------------------------------------
  * No single reference counterpart: the result equals calling eval_gwnr_mesh_batch_robust
  * (src/antipodal/gwn_mesh_robust.hh:441-456) once per mesh -- out_i[j] = meshes[i].eval(positions_i[j]) --

@@ -118,6 +118,8 @@ void run(cuda::CudaDispatcher& d, cuda::CudaIntersector<double> const& i, std::v
     cuda::CudaRobustBatch<double, robust::int128_grid> batch{d, jobs};
     batch.tune();
     batch.run();
+    auto const segs = build_boundary_segments(d, std::span<dvec3 const>{p}, std::span<int const>{});
+    (void)segs;
     // the reference's CPU path still works alongside
     PoolDispatcher pool{2};
     NaiveIntersector<double> naive{std::span<dvec3 const>{p}, std::span<int const>{}};
