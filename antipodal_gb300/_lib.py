@@ -64,6 +64,8 @@ SIGNATURES = {
     "agwn_probe_atan2": (_I, [_P, _P, _P, _I64, _P, _P]),
     "agwn_probe_fp64_peak": (_I, [_P, _P]),
     "agwn_param_batch_fractional_bezier3_f64": (_I, [_P, _P, _I64, _P, _P, _P, _I64, _I, _I, _D, _P, _P, _P]),
+    "agwn_robust_eval_grid_f64": (_I, [_P, _P, _P, _P, _I64, _I64, _I64, _P, _P, _P]),
+    "agwn_robust_eval_grid_f32": (_I, [_P, _P, _P, _P, _I64, _I64, _I64, _P, _P, _P]),
     "agwn_build_boundary_segments_f64": (_I, [_P, _P, _I64, _P, _I64, _P, _I64, _P]),
     "agwn_build_boundary_segments_f32": (_I, [_P, _P, _I64, _P, _I64, _P, _I64, _P]),
     "agwn_batch_create": (_I, [_P, _P, C.c_int32, _P, _P, _P, _P, _PP]),

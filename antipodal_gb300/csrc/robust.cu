@@ -152,12 +152,15 @@ int robust_build(Context& ctx, const T* vertices, int64_t nv, const int32_t* ind
 }
 
 template <class T, class P>
-int robust_run(Context& ctx, const Robust& r, const T* d_pos, int64_t n, T* d_out, int32_t* d_counts, T* d_frac)
+int robust_run(Context& ctx, const Robust& r, const T* d_pos, int64_t n, T* d_out, int32_t* d_counts, T* d_frac,
+               bool counts_ready = false)
 {
     using C = typename P::C;
     Quant qz{{r.center[0], r.center[1], r.center[2]}, r.scale};
     cudaStream_t const st = ctx.stream;
-    if (r.n_tri == 0)
+    if (counts_ready)
+        ;
+    else if (r.n_tri == 0)
         AGWN_TRY_CUDA(cudaMemsetAsync(d_counts, 0, sizeof(int32_t) * n, st));
     else
     {
@@ -279,6 +282,229 @@ int robust_eval(agwn_context* ctx, const agwn_robust* r, const T* positions, int
     bool const sync = dpos != positions || h_out || h_cnt || h_fr;
     return sync ? ctx->check_flags() : AGWN_OK;
 }
+// ---- RobustMeshGwn::eval over an axis-aligned grid ------------------------------------------------------------
+// Cell (ix, iy, iz) is the point (T(s_x + ix h_x), T(s_y + iy h_y), T(s_z + iz h_z)), each coordinate computed in
+// double, unfused, then rounded to T; h > 0.  The integer term needs no traversal: the -x crossing rule
+// (robust_crossing) decides inclusion and the hit depth hx from the point's (y, z) alone, so for a column of cells
+// (fixed iy, iz) a triangle either crosses none of them or crosses exactly those whose predicate x is >= hx, which
+// -- x being monotone in ix -- are ix >= ix0.  The rasterizer adds the crossing's sign at (ix0, iy, iz) for every
+// (triangle, column) and a prefix sum along x turns that into every cell's count, equal to robust_crossing summed
+// over the triangles at that cell.  Columns a triangle can cover come from binary searches of its predicate-space
+// box over the monotone grid coordinates.  The fractional term is the evaluator's own, on the materialised cells.
+// The reference's OpenGL evaluator (gwn_mesh_opengl.hh:198-351) rasterizes the same way in float with ceil
+// snapping; these counts are exact.
+
+template <class T>
+__device__ __forceinline__ T grid_coord(double s, double h, int64_t i)
+{
+    return T(__dadd_rn(s, __dmul_rn(double(i), h)));
+}
+
+// The predicate coordinate of grid index i along axis k (quantize, per axis).
+template <class T, class P>
+__device__ __forceinline__ typename P::C grid_pred(double s, double h, int64_t i, int k, Quant const& qz)
+{
+    double const v = double(grid_coord<T>(s, h, i));
+    if constexpr (P::grid)
+    {
+        constexpr double max_q = double(1ll << (P::bits + 10));
+        double const t = __dmul_rn(__dsub_rn(v, qz.c[k]), qz.s);
+        double const cl = t < -max_q ? -max_q : (max_q < t ? max_q : t);
+        return typename P::C(llround(cl));
+    }
+    else
+        return v;
+}
+
+// First index in [0, n) whose predicate coordinate, seen as a double as robust_crossing compares it, is >= v
+// (strict: > v), or n.  The coordinate is monotone in the index and so is its double, so the search is exact.
+template <class T, class P>
+__device__ __forceinline__ int64_t grid_first(double s, double h, int64_t n, int k, Quant const& qz, double v,
+                                              bool strict)
+{
+    int64_t lo = 0, hi = n;
+    while (lo < hi)
+    {
+        int64_t const mid = (lo + hi) >> 1;
+        double const c = P::cdbl(grid_pred<T, P>(s, h, mid, k, qz));
+        if (strict ? c > v : c >= v)
+            hi = mid;
+        else
+            lo = mid + 1;
+    }
+    return lo;
+}
+
+struct GridSpec
+{
+    double s[3], h[3];
+    int64_t n[3];
+};
+
+template <class T>
+__global__ void k_grid_positions(GridSpec g, T* __restrict__ pos)
+{
+    int64_t const total = g.n[0] * g.n[1] * g.n[2];
+    for (int64_t c = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; c < total; c += int64_t(gridDim.x) * blockDim.x)
+    {
+        int64_t const ix = c % g.n[0], iy = (c / g.n[0]) % g.n[1], iz = c / (g.n[0] * g.n[1]);
+        pos[3 * c] = grid_coord<T>(g.s[0], g.h[0], ix);
+        pos[3 * c + 1] = grid_coord<T>(g.s[1], g.h[1], iy);
+        pos[3 * c + 2] = grid_coord<T>(g.s[2], g.h[2], iz);
+    }
+}
+
+template <class T, class P>
+__global__ void k_grid_raster(const typename P::C* __restrict__ tri, int64_t n_tri, Quant qz, GridSpec g,
+                              int32_t* __restrict__ counts)
+{
+    using C = typename P::C;
+    for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; t < n_tri; t += int64_t(gridDim.x) * blockDim.x)
+    {
+        const C* const v = tri + 9 * t;
+        qv3<C> const a{v[0], v[1], v[2]}, b{v[3], v[4], v[5]}, c{v[6], v[7], v[8]};
+        double const y0 = fmin(fmin(P::cdbl(a.y), P::cdbl(b.y)), P::cdbl(c.y));
+        double const y1 = fmax(fmax(P::cdbl(a.y), P::cdbl(b.y)), P::cdbl(c.y));
+        double const z0 = fmin(fmin(P::cdbl(a.z), P::cdbl(b.z)), P::cdbl(c.z));
+        double const z1 = fmax(fmax(P::cdbl(a.z), P::cdbl(b.z)), P::cdbl(c.z));
+        int64_t const iy0 = grid_first<T, P>(g.s[1], g.h[1], g.n[1], 1, qz, y0, false);
+        int64_t const iy1 = grid_first<T, P>(g.s[1], g.h[1], g.n[1], 1, qz, y1, true);
+        int64_t const iz0 = grid_first<T, P>(g.s[2], g.h[2], g.n[2], 2, qz, z0, false);
+        int64_t const iz1 = grid_first<T, P>(g.s[2], g.h[2], g.n[2], 2, qz, z1, true);
+        for (int64_t iz = iz0; iz < iz1; ++iz)
+        {
+            C const qzc = grid_pred<T, P>(g.s[2], g.h[2], iz, 2, qz);
+            for (int64_t iy = iy0; iy < iy1; ++iy)
+            {
+                qv3<C> const q{C(0), grid_pred<T, P>(g.s[1], g.h[1], iy, 1, qz), qzc};
+                int const e01 = edge_sign<P>(q, a, b);
+                int const e12 = edge_sign<P>(q, b, c);
+                int const e20 = edge_sign<P>(q, c, a);
+                if (e01 == 0 || e01 != e12 || e01 != e20)
+                    continue;
+                // the hit depth of robust_crossing, with the same operations
+                double const w0 = P::dbl(edge_det<P>(q, b, c));
+                double const w1 = P::dbl(edge_det<P>(q, c, a));
+                double const w2 = P::dbl(edge_det<P>(q, a, b));
+                rd const hx = (rd(w0) * rd(P::cdbl(a.x)) + rd(w1) * rd(P::cdbl(b.x)) + rd(w2) * rd(P::cdbl(c.x))) /
+                              (rd(w0) + rd(w1) + rd(w2));
+                int64_t const ix0 = grid_first<T, P>(g.s[0], g.h[0], g.n[0], 0, qz, hx.v, false);
+                if (ix0 < g.n[0])
+                    atomicAdd(counts + (iz * g.n[1] + iy) * g.n[0] + ix0, -e01);
+            }
+        }
+    }
+}
+
+// Inclusive prefix sum along x of every (y, z) row: one warp per row, 32 cells per step.
+__global__ void k_grid_prefix(int32_t* __restrict__ counts, int64_t nx, int64_t rows)
+{
+    int const lane = threadIdx.x & 31;
+    for (int64_t r = (blockIdx.x * int64_t(blockDim.x) + threadIdx.x) >> 5; r < rows;
+         r += (int64_t(gridDim.x) * blockDim.x) >> 5)
+    {
+        int32_t* const row = counts + r * nx;
+        int carry = 0;
+        for (int64_t x0 = 0; x0 < nx; x0 += 32)
+        {
+            int64_t const x = x0 + lane;
+            int v = x < nx ? row[x] : 0;
+            for (int o = 1; o < 32; o <<= 1)
+            {
+                int const y = __shfl_up_sync(0xffffffffu, v, o);
+                if (lane >= o)
+                    v += y;
+            }
+            v += carry;
+            if (x < nx)
+                row[x] = v;
+            carry = __shfl_sync(0xffffffffu, v, 31);
+        }
+    }
+}
+
+template <class T, class P>
+int robust_grid_counts(Context& ctx, const Robust& r, GridSpec const& g, int32_t* d_counts)
+{
+    using C = typename P::C;
+    int64_t const cells = g.n[0] * g.n[1] * g.n[2];
+    AGWN_TRY_CUDA(cudaMemsetAsync(d_counts, 0, sizeof(int32_t) * cells, ctx.stream));
+    if (r.n_tri == 0)
+        return AGWN_OK;
+    Quant const qz{{r.center[0], r.center[1], r.center[2]}, r.scale};
+    AGWN_TRY(ctx.launch_begin(AGWN_K_ROBUST));
+    k_grid_raster<T, P><<<int(std::min<int64_t>(div_up(r.n_tri, 128), 16 * ctx.sm_count)), 128, 0, ctx.stream>>>(
+        static_cast<const C*>(r.tri), r.n_tri, qz, g, d_counts);
+    AGWN_TRY(ctx.launch_end(AGWN_K_ROBUST));
+    int64_t const rows = g.n[1] * g.n[2];
+    AGWN_TRY(ctx.launch_begin(AGWN_K_OTHER));
+    k_grid_prefix<<<int(std::min<int64_t>(div_up(rows * 32, 256), 16 * ctx.sm_count)), 256, 0, ctx.stream>>>(
+        d_counts, g.n[0], rows);
+    return ctx.launch_end(AGWN_K_OTHER);
+}
+
+template <class T>
+int robust_eval_grid(agwn_context* ctx, const agwn_robust* r, const double* start, const double* spacing, int64_t nx,
+                     int64_t ny, int64_t nz, T* out, int32_t* out_counts, T* out_frac)
+{
+    AGWN_CHECK_ARG(ctx && r && start && spacing, "null argument");
+    AGWN_CHECK_ARG(nx >= 0 && ny >= 0 && nz >= 0, "negative grid size");
+    AGWN_CHECK_ARG(r->scalar_bytes == int(sizeof(T)), "evaluator precision does not match the output");
+    for (int k = 0; k < 3; ++k)
+        AGWN_CHECK_ARG(std::isfinite(start[k]) && std::isfinite(spacing[k]) && spacing[k] > 0,
+                       "grid start must be finite and spacing positive");
+    clear_message();
+    AGWN_TRY_CUDA(cudaSetDevice(ctx->device));
+    int64_t const cells = nx * ny * nz;
+    if (cells == 0)
+        return AGWN_OK;
+    AGWN_CHECK_ARG(out, "null output");
+    AGWN_CHECK_ARG(nx < (int64_t(1) << 31) && ny < (int64_t(1) << 31) && nz < (int64_t(1) << 31) &&
+                       cells < (int64_t(1) << 40),
+                   "grid too large");
+    GridSpec g{{start[0], start[1], start[2]}, {spacing[0], spacing[1], spacing[2]}, {nx, ny, nz}};
+    void *dpos = nullptr, *dout = nullptr, *dcnt = nullptr, *dfr = nullptr;
+    bool h_out = false, h_cnt = false, h_fr = false;
+    AGWN_TRY(ctx->scratch_reserve(S_QUERIES, sizeof(T) * 3 * size_t(cells), &dpos));
+    AGWN_TRY(stage_out(*ctx, out, sizeof(T) * cells, S_OUT, &dout, &h_out));
+    if (out_counts)
+        AGWN_TRY(stage_out(*ctx, out_counts, sizeof(int32_t) * cells, S_COUNTS, &dcnt, &h_cnt));
+    else
+        AGWN_TRY(ctx->scratch_reserve(S_COUNTS, sizeof(int32_t) * cells, &dcnt));
+    if (out_frac)
+        AGWN_TRY(stage_out(*ctx, out_frac, sizeof(T) * cells, S_MISC3, &dfr, &h_fr));
+    AGWN_TRY(ctx->launch_begin(AGWN_K_OTHER));
+    k_grid_positions<T><<<int(std::min<int64_t>(div_up(cells, 256), 16 * ctx->sm_count)), 256, 0, ctx->stream>>>(
+        g, static_cast<T*>(dpos));
+    AGWN_TRY(ctx->launch_end(AGWN_K_OTHER));
+    const T* p = static_cast<const T*>(dpos);
+    T* o = static_cast<T*>(dout);
+    int32_t* c = static_cast<int32_t*>(dcnt);
+    T* fr = static_cast<T*>(dfr);
+    switch (r->policy)
+    {
+    case 0:
+        AGWN_TRY((robust_grid_counts<T, P64>(*ctx, *r, g, c)));
+        AGWN_TRY((robust_run<T, P64>(*ctx, *r, p, cells, o, c, fr, true)));
+        break;
+    case 1:
+        AGWN_TRY((robust_grid_counts<T, P128>(*ctx, *r, g, c)));
+        AGWN_TRY((robust_run<T, P128>(*ctx, *r, p, cells, o, c, fr, true)));
+        break;
+    default:
+        AGWN_TRY((robust_grid_counts<T, PF>(*ctx, *r, g, c)));
+        AGWN_TRY((robust_run<T, PF>(*ctx, *r, p, cells, o, c, fr, true)));
+        break;
+    }
+    if (h_out)
+        AGWN_TRY_CUDA(cudaMemcpyAsync(out, dout, sizeof(T) * cells, cudaMemcpyDeviceToHost, ctx->stream));
+    if (h_cnt)
+        AGWN_TRY_CUDA(cudaMemcpyAsync(out_counts, dcnt, sizeof(int32_t) * cells, cudaMemcpyDeviceToHost, ctx->stream));
+    if (h_fr)
+        AGWN_TRY_CUDA(cudaMemcpyAsync(out_frac, dfr, sizeof(T) * cells, cudaMemcpyDeviceToHost, ctx->stream));
+    return (h_out || h_cnt || h_fr) ? ctx->check_flags() : AGWN_OK;
+}
+
 } // namespace
 } // namespace agwn
 
@@ -329,5 +555,17 @@ int agwn_robust_eval_f32(agwn_context* ctx, const agwn_robust* r, const float* p
                          int32_t* out_counts, float* out_frac)
 {
     return robust_eval<float>(ctx, r, positions, n, out_gwn, out_counts, out_frac);
+}
+
+int agwn_robust_eval_grid_f64(agwn_context* ctx, const agwn_robust* r, const double* start, const double* spacing,
+                              int64_t nx, int64_t ny, int64_t nz, double* out_gwn, int32_t* out_counts,
+                              double* out_frac)
+{
+    return robust_eval_grid<double>(ctx, r, start, spacing, nx, ny, nz, out_gwn, out_counts, out_frac);
+}
+int agwn_robust_eval_grid_f32(agwn_context* ctx, const agwn_robust* r, const double* start, const double* spacing,
+                              int64_t nx, int64_t ny, int64_t nz, float* out_gwn, int32_t* out_counts, float* out_frac)
+{
+    return robust_eval_grid<float>(ctx, r, start, spacing, nx, ny, nz, out_gwn, out_counts, out_frac);
 }
 } // extern "C"

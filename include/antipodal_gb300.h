@@ -200,6 +200,19 @@ int agwn_robust_eval_f64(agwn_context* ctx, const agwn_robust* robust, const dou
 int agwn_robust_eval_f32(agwn_context* ctx, const agwn_robust* robust, const float* positions, int64_t n,
                          float* out_gwn, int32_t* out_counts, float* out_frac);
 
+/* RobustMeshGwn::eval over an axis-aligned grid, without query arrays or a hierarchy walk.  Cell (ix, iy, iz),
+ * stored at ((iz * ny) + iy) * nx + ix, is the point (T(start[0] + ix * spacing[0]), T(start[1] + iy * spacing[1]),
+ * T(start[2] + iz * spacing[2])), each coordinate computed in double without fused multiply-add and rounded to the
+ * evaluator's scalar type; spacing > 0.  The integer term is rasterized per (y, z) column with the evaluator's exact
+ * -x crossing rule and prefix-summed along x, so every output equals agwn_robust_eval_* at that point (counts bit
+ * for bit).  The reference's OpenGL grid evaluator (gwn_mesh_opengl.hh:519) does the same in float; this one is
+ * exact.  out_counts / out_frac may be NULL. */
+int agwn_robust_eval_grid_f64(agwn_context* ctx, const agwn_robust* robust, const double* start, const double* spacing,
+                              int64_t nx, int64_t ny, int64_t nz, double* out_gwn, int32_t* out_counts,
+                              double* out_frac);
+int agwn_robust_eval_grid_f32(agwn_context* ctx, const agwn_robust* robust, const double* start, const double* spacing,
+                              int64_t nx, int64_t ny, int64_t nz, float* out_gwn, int32_t* out_counts, float* out_frac);
+
 /* ---- open boundary of a mesh ------------------------------------------------------------------------------
  * Replaces build_boundary_segments (src/antipodal/math/common.hh:123-174) on the device: every triangle edge
  * u -> v adds +1 (u < v) or -1 to its undirected edge {min, max}; edges with a non-zero net count become
