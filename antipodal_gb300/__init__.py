@@ -604,9 +604,17 @@ def eval_gwnr_parametric_batch_fractional(dispatcher: CudaDispatcher, positions,
     _, xp = x = _vec3(x0, np.float64)
     if learned:  # propose and integrate in one call; the start depths stay in device scratch
         fn = library().agwn_param_batch_fractional_learned_bezier3_f64
-        _check(fn(dispatcher.handle, integrator.handle, p.ptr, p.n, o.ptr, xp, c.ptr, c.n, integrator.n_classes,
-                  cfg.min_depth, cfg.max_depth, cfg.tol, integrator.alpha, st.ptr if st else None,
-                  nd.ptr if nd else None), "eval_gwnr_parametric_batch_fractional")
+        panel = integrator.panel
+        if panel is not None:
+            _check(library().agwn_param_set_panel_network(dispatcher.handle, panel.handle, panel.alpha),
+                   "agwn_param_set_panel_network")
+        try:
+            _check(fn(dispatcher.handle, integrator.handle, p.ptr, p.n, o.ptr, xp, c.ptr, c.n, integrator.n_classes,
+                      cfg.min_depth, cfg.max_depth, cfg.tol, integrator.alpha, st.ptr if st else None,
+                      nd.ptr if nd else None), "eval_gwnr_parametric_batch_fractional")
+        finally:
+            if panel is not None:
+                library().agwn_param_set_panel_network(dispatcher.handle, None, C.c_float(0.5))
     else:
         fn = library().agwn_param_batch_fractional_bezier3_f64
         _check(fn(dispatcher.handle, p.ptr, p.n, o.ptr, xp, c.ptr, c.n, cfg.min_depth, cfg.max_depth, cfg.tol,
@@ -627,13 +635,14 @@ class LearnedGK15Proposal:
     tree; it never skips the error test).
     """
 
-    FORMAT = 1
+    FORMAT = 2
 
     def __init__(self, dispatcher: CudaDispatcher, seed: int = 0, n_classes: int = 11, alpha: float = 0.02,
                  params=None):
         self.dispatcher = dispatcher
         self.n_classes = int(n_classes)
         self.alpha = float(alpha)
+        self.panel = None  # optional per-panel network (2 classes; its alpha is the skip threshold beta)
         h = C.c_void_p()
         _check(library().agwn_mlp_create(dispatcher.handle, int(seed) & 0xFFFFFFFFFFFFFFFF, C.byref(h)),
                "agwn_mlp_create")
@@ -664,14 +673,54 @@ class LearnedGK15Proposal:
 
     def save(self, path):
         """Write the FP32 weights and the decision settings (the only state the proposal has) to an .npz file."""
-        np.savez(path, params=self.params, n_classes=self.n_classes, alpha=self.alpha, format=self.FORMAT)
+        extra = {}
+        if self.panel is not None:
+            extra = {"panel_params": self.panel.params, "panel_beta": self.panel.alpha}
+        np.savez(path, params=self.params, n_classes=self.n_classes, alpha=self.alpha, format=self.FORMAT, **extra)
 
     @classmethod
     def load(cls, dispatcher: CudaDispatcher, path):
         z = np.load(path)
-        if int(z["format"]) != cls.FORMAT:
+        if int(z["format"]) not in (1, cls.FORMAT):
             raise ValueError(f"{path}: unsupported format {int(z['format'])}")
-        return cls(dispatcher, n_classes=int(z["n_classes"]), alpha=float(z["alpha"]), params=z["params"])
+        net = cls(dispatcher, n_classes=int(z["n_classes"]), alpha=float(z["alpha"]), params=z["params"])
+        if "panel_params" in z.files:
+            net.panel = cls(dispatcher, n_classes=2, alpha=float(z["panel_beta"]), params=z["panel_params"])
+        return net
+
+    # -- the per-panel network ----------------------------------------------------------------------------------
+    def panel_data(self, positions, x0, curves, cfg: IntegrateConfig, capacity: int = 4_000_000):
+        """Features and labels (accepted or split) of the panels the integrator evaluates (in the dispatcher's
+        parametric arithmetic), up to ``capacity`` of them."""
+        p = _View(positions, np.float64, 3, "positions")
+        c = _View(curves, np.float64, 12, "curves")
+        log = _empty_like_input(positions, (int(capacity), 2), np.int32)  # uint32 words, same bits
+        lv = _View(log, np.int32, None, "log", writable=True)
+        _, xp = x = _vec3(x0, np.float64)
+        cnt = C.c_int64()
+        _check(library().agwn_param_panel_log_bezier3_f64(self.dispatcher.handle, p.ptr, p.n, xp, c.ptr, c.n,
+                                                          cfg.min_depth, cfg.max_depth, cfg.tol, lv.ptr,
+                                                          int(capacity), C.byref(cnt)), "agwn_param_panel_log")
+        m = min(cnt.value, int(capacity))
+        feats = _empty_like_input(positions, (m, 12), np.float32)
+        labels = _empty_like_input(positions, (m,), np.uint8)
+        fv = _View(feats, np.float32, None, "features", writable=True)
+        lb = _View(labels, np.uint8, None, "labels", writable=True)
+        if m:
+            _check(library().agwn_param_panel_features_bezier3_f64(self.dispatcher.handle, p.ptr, p.n, xp, c.ptr, c.n,
+                                                                   cfg.tol, lv.ptr, m, fv.ptr, lb.ptr),
+                   "agwn_param_panel_features")
+        del x
+        return feats, labels
+
+    def fit_panels(self, positions, x0, curves, cfg: IntegrateConfig, beta: float = 0.02, capacity: int = 4_000_000,
+                   seed: int = 7, **train_kw):
+        """Train the per-panel network (split or accept) on the integrator's own panels; returns the loss history."""
+        feats, labels = self.panel_data(positions, x0, curves, cfg, capacity)
+        if self.panel is None:
+            self.panel = LearnedGK15Proposal(self.dispatcher, seed=seed, n_classes=2, alpha=beta)
+        self.panel.alpha = float(beta)
+        return self.panel.train(feats, labels, **train_kw)
 
     # -- data ---------------------------------------------------------------------------------------------------
     def features(self, positions, x0, curves, tol: float):
@@ -744,6 +793,9 @@ class LearnedGK15Proposal:
         return out
 
     def close(self):
+        if getattr(self, "panel", None) is not None:
+            self.panel.close()
+            self.panel = None
         if getattr(self, "_h", None) is not None:
             library().agwn_mlp_destroy(self._h)
             self._h = None

@@ -127,6 +127,8 @@ struct Context
     int robust_mode = AGWN_ROBUST_EXACT;
     double robust_term_err = 1e-7;
     int param_mode = AGWN_PARAM_EXACT;
+    const agwn_mlp* panel_mlp = nullptr; // the per-panel network of the double-float integrator (or none)
+    float panel_beta = 0.02f;
     int queries_per_thread = 2;
     int frac_block = 128;
     int seg_tile = 512;
@@ -162,7 +164,10 @@ int stage_out(Context& ctx, void* dst, size_t bytes, int slot, void** dev, bool*
 // Device-side runners behind the parametric entry points; all pointers are device memory of the context's GPU.
 int param_run(Context& ctx, const double* d_pos, int64_t n, double* d_out, const double* x0, const double* d_curves,
               int64_t n_curves, int min_depth, int max_depth, double tol, const uint8_t* d_start, uint32_t* d_stats,
-              int32_t* d_nodes);
+              int32_t* d_nodes, uint32_t* d_panel_log = nullptr, unsigned long long* d_log_count = nullptr,
+              long long log_cap = 0);
+// The device copies of a network's weights (BF16 layouts) and FP32 parameters.
+void mlp_device_weights(const agwn_mlp* mlp, const void** bf16_weights, const float** params);
 int mlp_propose_run(Context& ctx, const agwn_mlp* mlp, const double* d_pos, int64_t n, const double* x0,
                     const double* d_curves, int64_t n_curves, int n_classes, int min_depth, int max_depth, double tol,
                     float alpha, uint8_t* d_start, float* d_logits);

@@ -12,7 +12,7 @@
 // and output gradients transposed through shared memory.  Training is Adam on FP32 master weights; each step's
 // two launches are captured once in a CUDA graph and replayed.
 
-#include "agwn_internal.cuh"
+#include "mlp.cuh"
 
 #include <cuda_bf16.h>
 
@@ -23,262 +23,33 @@ namespace agwn
 {
 namespace
 {
-constexpr int kF = 12;  // features
-constexpr int kFP = 16; // padded input width
-constexpr int kH = 64;  // hidden width
-constexpr int kC = 16;  // output width (classes, <= 16)
-
-// FP32 parameter blob: W1t[kH][kFP], b1[kH], W2t[kH][kH], b2[kH], W3t[kC][kH], b3[kC] (W*t = [out][in])
-constexpr int kOffW1 = 0;
-constexpr int kOffB1 = kOffW1 + kH * kFP;
-constexpr int kOffW2 = kOffB1 + kH;
-constexpr int kOffB2 = kOffW2 + kH * kH;
-constexpr int kOffW3 = kOffB2 + kH;
-constexpr int kOffB3 = kOffW3 + kC * kH;
-constexpr int kParams = kOffB3 + kC;
-
-// BF16 weight copies: the forward layouts ([out][in], pairs along `in`) and the backward ones ([in][out], pairs
-// along `out`), in this order.
-constexpr int kBW1t = 0;
-constexpr int kBW2t = kBW1t + kH * kFP;
-constexpr int kBW3t = kBW2t + kH * kH;
-constexpr int kBW2n = kBW3t + kC * kH;
-constexpr int kBW3n = kBW2n + kH * kH;
-constexpr int kBWCount = kBW3n + kH * kC;
-
-// Shared-memory row strides in 32-bit words, padded so that a fragment load (8 rows x 4 words) hits 32 banks.
-constexpr int kS16 = 12; // rows of 16 bf16
-constexpr int kS64 = 36; // rows of 64 bf16
-
-constexpr int kChunk = 128;           // training samples per block pass (8 warps x 16)
-constexpr int kSA = kChunk / 2 + 4;   // words per transposed activation row (128 bf16 + padding)
-constexpr int kActRows = kFP + 4 * kH + kC; // X, H1, H2, dZ1, dZ2, dZ3
-
-__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi)
+// Features and labels of logged panels: entry = (pair index, (depth << 25) | (j << 1) | accepted).
+__global__ void k_panel_features(const double* __restrict__ pos, float x0x, float x0y, float x0z,
+                                 const double* __restrict__ curves, int64_t n_curves, float log10_tol,
+                                 const uint32_t* __restrict__ log, int64_t n_entries, float* __restrict__ feats,
+                                 uint8_t* __restrict__ labels)
 {
-    __nv_bfloat162 const v = __floats2bfloat162_rn(lo, hi);
-    return *reinterpret_cast<const uint32_t*>(&v);
-}
-
-__device__ __forceinline__ void mma_bf16(float (&d)[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3,
-                                         uint32_t b0, uint32_t b1)
-{
-    asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-                 "{%0,%1,%2,%3};\n"
-                 : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-                 : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
-}
-
-// Shared-memory copy of the BF16 weights (padded rows) and the FP32 biases.
-struct WeightsSmem
-{
-    uint32_t w1t[kH * kS16];
-    uint32_t w2t[kH * kS64];
-    uint32_t w3t[kC * kS64];
-    uint32_t w2n[kH * kS64];
-    uint32_t w3n[kH * kS16];
-    float b1[kH], b2[kH], b3[kC];
-};
-
-__device__ void load_weights(WeightsSmem& s, const __nv_bfloat16* wb, const float* params, bool backward)
-{
-    auto copy = [&](uint32_t* dst, int off, int rows, int cols, int stride)
+    float3 const x0 = make_float3(x0x, x0y, x0z);
+    for (int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; e < n_entries;
+         e += int64_t(gridDim.x) * blockDim.x)
     {
-        const uint32_t* src = reinterpret_cast<const uint32_t*>(wb + off);
-        int const wpr = cols / 2;
-        for (int e = threadIdx.x; e < rows * wpr; e += blockDim.x)
-            dst[(e / wpr) * stride + e % wpr] = src[e];
-    };
-    copy(s.w1t, kBW1t, kH, kFP, kS16);
-    copy(s.w2t, kBW2t, kH, kH, kS64);
-    copy(s.w3t, kBW3t, kC, kH, kS64);
-    if (backward)
-    {
-        copy(s.w2n, kBW2n, kH, kH, kS64);
-        copy(s.w3n, kBW3n, kH, kC, kS16);
+        int64_t const pair = log[2 * e];
+        uint32_t const w = log[2 * e + 1];
+        int const d = int(w >> 25);
+        uint32_t const j = (w >> 1) & 0xffffffu;
+        int64_t const q = pair / n_curves, c = pair - q * n_curves;
+        float cp[12];
+#pragma unroll
+        for (int i = 0; i < 12; ++i)
+            cp[i] = float(curves[12 * c + i] - pos[3 * q + i % 3]);
+        float f[kF];
+        panel_features(cp, d, j, x0, log10_tol, f);
+#pragma unroll
+        for (int i = 0; i < kF; ++i)
+            feats[e * kF + i] = f[i];
+        if (labels)
+            labels[e] = uint8_t(w & 1u);
     }
-    for (int e = threadIdx.x; e < kH; e += blockDim.x)
-    {
-        s.b1[e] = params[kOffB1 + e];
-        s.b2[e] = params[kOffB2 + e];
-    }
-    for (int e = threadIdx.x; e < kC; e += blockDim.x)
-        s.b3[e] = params[kOffB3 + e];
-}
-
-// Forward pass of one m16 tile of samples; a0 is the input fragment (16 samples x 16 features).
-// z1, z2: pre-activations of the hidden layers, z3: logits, all as m16n8 accumulator fragments.
-__device__ __forceinline__ void mlp_forward(const WeightsSmem& s, const uint32_t (&a0)[4], float (&z1)[8][4],
-                                            float (&z2)[8][4], float (&z3)[2][4])
-{
-    int const lane = threadIdx.x & 31, g = lane >> 2, tig = lane & 3;
-#pragma unroll
-    for (int nt = 0; nt < 8; ++nt)
-    {
-        int const n0 = nt * 8 + tig * 2;
-        z1[nt][0] = z1[nt][2] = s.b1[n0];
-        z1[nt][1] = z1[nt][3] = s.b1[n0 + 1];
-        uint32_t const* w = s.w1t + (nt * 8 + g) * kS16;
-        mma_bf16(z1[nt], a0[0], a0[1], a0[2], a0[3], w[tig], w[4 + tig]);
-    }
-    uint32_t a1[4][4];
-#pragma unroll
-    for (int kt = 0; kt < 4; ++kt)
-    {
-        a1[kt][0] = pack_bf16(fmaxf(z1[2 * kt][0], 0.f), fmaxf(z1[2 * kt][1], 0.f));
-        a1[kt][1] = pack_bf16(fmaxf(z1[2 * kt][2], 0.f), fmaxf(z1[2 * kt][3], 0.f));
-        a1[kt][2] = pack_bf16(fmaxf(z1[2 * kt + 1][0], 0.f), fmaxf(z1[2 * kt + 1][1], 0.f));
-        a1[kt][3] = pack_bf16(fmaxf(z1[2 * kt + 1][2], 0.f), fmaxf(z1[2 * kt + 1][3], 0.f));
-    }
-#pragma unroll
-    for (int nt = 0; nt < 8; ++nt)
-    {
-        int const n0 = nt * 8 + tig * 2;
-        z2[nt][0] = z2[nt][2] = s.b2[n0];
-        z2[nt][1] = z2[nt][3] = s.b2[n0 + 1];
-        uint32_t const* w = s.w2t + (nt * 8 + g) * kS64;
-#pragma unroll
-        for (int kt = 0; kt < 4; ++kt)
-            mma_bf16(z2[nt], a1[kt][0], a1[kt][1], a1[kt][2], a1[kt][3], w[kt * 8 + tig], w[kt * 8 + 4 + tig]);
-    }
-    uint32_t a2[4][4];
-#pragma unroll
-    for (int kt = 0; kt < 4; ++kt)
-    {
-        a2[kt][0] = pack_bf16(fmaxf(z2[2 * kt][0], 0.f), fmaxf(z2[2 * kt][1], 0.f));
-        a2[kt][1] = pack_bf16(fmaxf(z2[2 * kt][2], 0.f), fmaxf(z2[2 * kt][3], 0.f));
-        a2[kt][2] = pack_bf16(fmaxf(z2[2 * kt + 1][0], 0.f), fmaxf(z2[2 * kt + 1][1], 0.f));
-        a2[kt][3] = pack_bf16(fmaxf(z2[2 * kt + 1][2], 0.f), fmaxf(z2[2 * kt + 1][3], 0.f));
-    }
-#pragma unroll
-    for (int nt = 0; nt < 2; ++nt)
-    {
-        int const n0 = nt * 8 + tig * 2;
-        z3[nt][0] = z3[nt][2] = s.b3[n0];
-        z3[nt][1] = z3[nt][3] = s.b3[n0 + 1];
-        uint32_t const* w = s.w3t + (nt * 8 + g) * kS64;
-#pragma unroll
-        for (int kt = 0; kt < 4; ++kt)
-            mma_bf16(z3[nt], a2[kt][0], a2[kt][1], a2[kt][2], a2[kt][3], w[kt * 8 + tig], w[kt * 8 + 4 + tig]);
-    }
-}
-
-// ---- features ------------------------------------------------------------------------------------------------
-
-__device__ __forceinline__ float3 f3sub(float3 a, float3 b)
-{
-    return make_float3(a.x - b.x, a.y - b.y, a.z - b.z);
-}
-__device__ __forceinline__ float f3dot(float3 a, float3 b)
-{
-    return a.x * b.x + a.y * b.y + a.z * b.z;
-}
-__device__ __forceinline__ float f3len(float3 a)
-{
-    return sqrtf(f3dot(a, a));
-}
-__device__ __forceinline__ float f3angle(float3 a, float3 b)
-{
-    float3 const c = make_float3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
-    return atan2f(f3len(c), f3dot(a, b));
-}
-// distance from the origin to segment [a, b], and the segment parameter of the nearest point
-__device__ __forceinline__ float seg_dist0(float3 a, float3 b, float* tpar)
-{
-    float3 const e = f3sub(b, a);
-    float const ee = f3dot(e, e);
-    float t = ee > 0.f ? -f3dot(a, e) / ee : 0.f;
-    t = fminf(fmaxf(t, 0.f), 1.f);
-    *tpar = t;
-    return f3len(make_float3(a.x + t * e.x, a.y + t * e.y, a.z + t * e.z));
-}
-__device__ __forceinline__ float flog2(float v)
-{
-    return log2f(fmaxf(v, 1e-30f)) * 0.125f;
-}
-
-// The 12 features of a (query, curve) pair, from the control polygon r_i = c_i - p (relative to the query):
-//  0 log2(polygon distance / L)   1 log2(nearest control point / L)   2 log2(farthest control point / L)
-//  3 log2(L)                      4 chord / L                         5 control-point offset from the chord / L
-//  6 polygon turning / pi         7 angle the polygon subtends at p / pi
-//  8 log2(distance of the polygon from the line p + t x0, / L)   9 log2(that distance / polygon distance)
-// 10 axial cosine of the polygon point nearest that line      11 log10(tol) / 10
-// (logs are /8; L = polygon length).  The integrand is steep where the curve passes close to p and where it
-// passes close to the line through p along x0, where w and d_eta change fast.
-__device__ void pair_features(const double* c, double px, double py, double pz, float3 x0, float tol_feat,
-                              float* f)
-{
-    float3 r[4];
-#pragma unroll
-    for (int i = 0; i < 4; ++i)
-        r[i] = make_float3(float(c[3 * i] - px), float(c[3 * i + 1] - py), float(c[3 * i + 2] - pz));
-    float L = 0.f;
-    float3 e[3];
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-    {
-        e[i] = f3sub(r[i + 1], r[i]);
-        L += f3len(e[i]);
-    }
-    L = fmaxf(L, 1e-30f);
-    float dpoly = 3e38f, t;
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-        dpoly = fminf(dpoly, seg_dist0(r[i], r[i + 1], &t));
-    float nmin = 3e38f, nmax = 0.f;
-#pragma unroll
-    for (int i = 0; i < 4; ++i)
-    {
-        float const n = f3len(r[i]);
-        nmin = fminf(nmin, n);
-        nmax = fmaxf(nmax, n);
-    }
-    float3 const ch = f3sub(r[3], r[0]);
-    float const chord = f3len(ch);
-    float flat = 0.f;
-#pragma unroll
-    for (int i = 1; i <= 2; ++i)
-    {
-        float3 const a = f3sub(r[0], r[i]), b = f3sub(r[3], r[i]);
-        flat = fmaxf(flat, seg_dist0(a, b, &t));
-    }
-    float const turning = f3angle(e[0], e[1]) + f3angle(e[1], e[2]);
-    float const subt = f3angle(r[0], r[1]) + f3angle(r[1], r[2]) + f3angle(r[2], r[3]);
-    float3 u[4];
-#pragma unroll
-    for (int i = 0; i < 4; ++i)
-    {
-        float const a = f3dot(r[i], x0);
-        u[i] = make_float3(r[i].x - a * x0.x, r[i].y - a * x0.y, r[i].z - a * x0.z);
-    }
-    float dline = 3e38f, axial = 0.f;
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-    {
-        float const d = seg_dist0(u[i], u[i + 1], &t);
-        if (d < dline)
-        {
-            dline = d;
-            float3 const q = make_float3(r[i].x + t * e[i].x, r[i].y + t * e[i].y, r[i].z + t * e[i].z);
-            axial = f3dot(q, x0) / fmaxf(f3len(q), 1e-30f);
-        }
-    }
-    float const kInvPi = 0.31830988618379067f;
-    f[0] = flog2(dpoly / L);
-    f[1] = flog2(nmin / L);
-    f[2] = flog2(nmax / L);
-    f[3] = flog2(L);
-    f[4] = chord / L;
-    f[5] = flat / L;
-    f[6] = turning * kInvPi;
-    f[7] = subt * kInvPi;
-    f[8] = flog2(dline / L);
-    f[9] = flog2(fmaxf(dline, 1e-30f) / fmaxf(dpoly, 1e-30f));
-    f[10] = axial;
-    f[11] = tol_feat;
-#pragma unroll
-    for (int i = 0; i < kF; ++i)
-        f[i] = fminf(fmaxf(f[i], -8.f), 8.f);
 }
 
 __global__ void k_features(const double* __restrict__ pos, int64_t n, float x0x, float x0y, float x0z,
@@ -347,7 +118,7 @@ __global__ void __launch_bounds__(kInferWarps * 32) k_propose(const __nv_bfloat1
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     InferSmem& s = *reinterpret_cast<InferSmem*>(smem_raw);
-    load_weights(s.w, wb, params, false);
+    load_weights(s.w, wb, params);
     __syncthreads();
     int const warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, tig = lane & 3;
     float3 const x0 = make_float3(x0x, x0y, x0z);
@@ -415,6 +186,7 @@ __global__ void __launch_bounds__(kInferWarps * 32) k_propose(const __nv_bfloat1
 struct TrainSmem
 {
     WeightsSmem w;
+    BackWeightsSmem wback;
     uint32_t act[kActRows][kSA]; // transposed BF16 tiles [feature][sample] of X, H1, H2, dZ1, dZ2, dZ3
     float db[kH + kH + kC];
     float loss;
@@ -450,7 +222,8 @@ __global__ void __launch_bounds__(256, 1) k_mlp_grad(const __nv_bfloat16* __rest
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     TrainSmem& s = *reinterpret_cast<TrainSmem*>(smem_raw);
-    load_weights(s.w, wb, params, true);
+    load_weights(s.w, wb, params);
+    load_back_weights(s.wback, wb);
     for (int e = threadIdx.x; e < kH + kH + kC; e += blockDim.x)
         s.db[e] = 0.f;
     if (threadIdx.x == 0)
@@ -546,7 +319,7 @@ __global__ void __launch_bounds__(256, 1) k_mlp_grad(const __nv_bfloat16* __rest
             for (int nt = 0; nt < 8; ++nt)
             {
                 dz2[nt][0] = dz2[nt][1] = dz2[nt][2] = dz2[nt][3] = 0.f;
-                uint32_t const* w = s.w.w3n + (nt * 8 + g) * kS16;
+                uint32_t const* w = s.wback.w3n + (nt * 8 + g) * kS16;
                 mma_bf16(dz2[nt], b0, b1, b2, b3, w[tig], w[4 + tig]);
 #pragma unroll
                 for (int e = 0; e < 4; ++e)
@@ -569,7 +342,7 @@ __global__ void __launch_bounds__(256, 1) k_mlp_grad(const __nv_bfloat16* __rest
             for (int nt = 0; nt < 8; ++nt)
             {
                 dz1[nt][0] = dz1[nt][1] = dz1[nt][2] = dz1[nt][3] = 0.f;
-                uint32_t const* w = s.w.w2n + (nt * 8 + g) * kS64;
+                uint32_t const* w = s.wback.w2n + (nt * 8 + g) * kS64;
 #pragma unroll
                 for (int kt = 0; kt < 4; ++kt)
                     mma_bf16(dz1[nt], a[kt][0], a[kt][1], a[kt][2], a[kt][3], w[kt * 8 + tig], w[kt * 8 + 4 + tig]);
@@ -1031,6 +804,12 @@ extern "C" int agwn_mlp_train(agwn_context* ctx, agwn_mlp* mlp, const float* fea
 
 namespace agwn
 {
+void mlp_device_weights(const agwn_mlp* mlp, const void** bf16_weights, const float** params)
+{
+    *bf16_weights = mlp->wb.ptr;
+    *params = static_cast<const float*>(mlp->params.ptr);
+}
+
 int mlp_propose_run(Context& ctx, const agwn_mlp* mlp, const double* d_pos, int64_t n, const double* x0,
                     const double* d_curves, int64_t n_curves, int n_classes, int min_depth, int max_depth, double tol,
                     float alpha, uint8_t* d_start, float* d_logits)
@@ -1090,4 +869,39 @@ extern "C" int agwn_param_propose_depth_bezier3_f64(agwn_context* ctx, const agw
         AGWN_TRY_CUDA(cudaMemcpyAsync(logits, dlog, sizeof(float) * kC * total, cudaMemcpyDeviceToHost, ctx->stream));
     bool const sync = h_sd || h_log || dpos != positions || dcur != curves;
     return sync ? ctx->check_flags() : AGWN_OK;
+}
+
+extern "C" int agwn_param_panel_features_bezier3_f64(agwn_context* ctx, const double* positions, int64_t n,
+                                                     const double* x0, const double* curves, int64_t n_curves,
+                                                     double tol, const uint32_t* log, int64_t n_entries,
+                                                     float* features, uint8_t* labels)
+{
+    AGWN_CHECK_ARG(ctx && x0 && n >= 0 && n_curves > 0 && n_entries >= 0, "bad arguments");
+    AGWN_CHECK_ARG(n_entries == 0 || (positions && curves && log && features), "null array");
+    AGWN_CHECK_ARG(std::isfinite(tol) && tol > 0, "tol must be finite and > 0");
+    clear_message();
+    AGWN_TRY_CUDA(cudaSetDevice(ctx->device));
+    if (n_entries == 0)
+        return AGWN_OK;
+    const void *dpos = nullptr, *dcur = nullptr, *dlog = nullptr;
+    void *dfeat = nullptr, *dlab = nullptr;
+    bool h_feat = false, h_lab = false;
+    AGWN_TRY(stage_in(*ctx, positions, sizeof(double) * 3 * n, S_QUERIES, &dpos));
+    AGWN_TRY(stage_in(*ctx, curves, sizeof(double) * 12 * n_curves, S_MISC0, &dcur));
+    AGWN_TRY(stage_in(*ctx, log, sizeof(uint32_t) * 2 * size_t(n_entries), S_SEGS, &dlog));
+    AGWN_TRY(stage_out(*ctx, features, sizeof(float) * kF * size_t(n_entries), S_MISC1, &dfeat, &h_feat));
+    if (labels)
+        AGWN_TRY(stage_out(*ctx, labels, size_t(n_entries), S_MISC2, &dlab, &h_lab));
+    AGWN_TRY(ctx->launch_begin(AGWN_K_OTHER));
+    k_panel_features<<<int(std::min<int64_t>(div_up(n_entries, 256), 8 * ctx->sm_count)), 256, 0, ctx->stream>>>(
+        static_cast<const double*>(dpos), float(x0[0]), float(x0[1]), float(x0[2]), static_cast<const double*>(dcur),
+        n_curves, float(std::log10(tol)), static_cast<const uint32_t*>(dlog), n_entries, static_cast<float*>(dfeat),
+        static_cast<uint8_t*>(dlab));
+    AGWN_TRY(ctx->launch_end(AGWN_K_OTHER));
+    if (h_feat)
+        AGWN_TRY_CUDA(cudaMemcpyAsync(features, dfeat, sizeof(float) * kF * size_t(n_entries), cudaMemcpyDeviceToHost,
+                                      ctx->stream));
+    if (h_lab)
+        AGWN_TRY_CUDA(cudaMemcpyAsync(labels, dlab, size_t(n_entries), cudaMemcpyDeviceToHost, ctx->stream));
+    return ctx->check_flags();
 }

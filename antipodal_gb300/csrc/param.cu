@@ -16,6 +16,7 @@
 
 #include "agwn_internal.cuh"
 #include "df32.cuh"
+#include "mlp.cuh"
 #include "tma.cuh"
 
 #include <cmath>
@@ -288,6 +289,34 @@ __global__ void k_curves_df(const double* __restrict__ curves, int64_t n_curves,
 // start_depth: per (query, curve), row-major [n][n_curves], nullable = all 0.  stats (nullable): per (query,
 // curve) packed as leaves | shallowest leaf depth << 16 | deepest leaf depth << 24.  nodes_total (nullable):
 // panels evaluated per query.  pair_vals: gridDim.x * kParamBlock * tile doubles.
+// Optional work of the integrator kernel.
+//   panel_log: training data for the per-panel network, 2 words per evaluated panel below max_depth -- the pair's
+//     index (query * n_curves + curve) and (depth << 25) | (j << 1) | accepted; entries past log_cap are counted,
+//     not written.
+//   pwb / pparams (double-float kernel only): the per-panel network.  Before a panel below max_depth is evaluated
+//     the warp runs the network on its lanes' panels; a panel whose predicted chance of being accepted is below
+//     beta (logit margin < skip_logit) is split without evaluation.  Every evaluated panel is still accepted or split
+//     by the plain error test.
+struct ParamExtras
+{
+    uint32_t* panel_log;
+    unsigned long long* log_count;
+    long long log_cap;
+    const __nv_bfloat16* pwb;
+    const float* pparams;
+    float skip_logit;
+    float log10_tol;
+    unsigned long long* skip_count;
+};
+
+// The per-panel network's shared memory, after the curve tile.
+struct PanelSmem
+{
+    WeightsSmem w;
+    uint32_t feat[kParamBlock / 32][32][kS16 - 4 + 1];
+    float logit[kParamBlock / 32][32][2];
+};
+
 template <bool DF>
 __global__ void __launch_bounds__(kParamBlock) k_param_gk15(const double* __restrict__ pos, int64_t n,
                                                             double* __restrict__ out, double x0x, double x0y,
@@ -296,13 +325,17 @@ __global__ void __launch_bounds__(kParamBlock) k_param_gk15(const double* __rest
                                                             double tol, const uint8_t* __restrict__ start_depth,
                                                             uint32_t* __restrict__ stats,
                                                             int32_t* __restrict__ nodes_total,
-                                                            double* __restrict__ pair_vals, int* flags)
+                                                            double* __restrict__ pair_vals, int* flags,
+                                                            ParamExtras ex)
 {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ __align__(8) uint64_t bar;
     __shared__ int s_next;
     __shared__ int s_nodes[kParamBlock];
     Bez* const buf = reinterpret_cast<Bez*>(smem);
+    PanelSmem* const ps = reinterpret_cast<PanelSmem*>(smem + size_t(tile) * sizeof(Bez));
+    bool const use_panel = DF && ex.pwb != nullptr;
+    unsigned long long skips = 0;
     double* const slab = pair_vals + size_t(blockIdx.x) * kParamBlock * tile;
     ev3<rd> const x0{rd(x0x), rd(x0y), rd(x0z)};
     df3 const x0df{df_from(x0x), df_from(x0y), df_from(x0z)};
@@ -314,6 +347,10 @@ __global__ void __launch_bounds__(kParamBlock) k_param_gk15(const double* __rest
     tol_at[0] = tol;
     for (int l = 1; l <= kParamMaxDepth; ++l)
         tol_at[l] = __dmul_rn(tol_at[l - 1], 0.5);
+    if (use_panel)
+        load_weights(ps->w, ex.pwb, ex.pparams);
+    float3 const x0f = make_float3(float(x0x), float(x0y), float(x0z));
+    int const warp = int(threadIdx.x >> 5);
     if (threadIdx.x == 0)
     {
         mbar_init(&bar, 1);
@@ -393,6 +430,65 @@ __global__ void __launch_bounds__(kParamBlock) k_param_gk15(const double* __rest
                 }
                 if (!__any_sync(0xffffffffu, pi >= 0))
                     break;
+                if constexpr (DF)
+                {
+                    // the per-panel network: up to four rounds of "split it without evaluating", all lanes together
+                    for (int round = 0; use_panel && round < 4; ++round)
+                    {
+                        bool const cand = pi >= 0 && d < max_depth;
+                        float f[kF];
+                        if (cand)
+                        {
+                            float cpf[12];
+#pragma unroll
+                            for (int e = 0; e < 12; ++e)
+                                cpf[e] = cp[e].hi;
+                            panel_features(cpf, d, j, x0f, ex.log10_tol, f);
+                        }
+                        else
+                        {
+#pragma unroll
+                            for (int e = 0; e < kF; ++e)
+                                f[e] = 0.f;
+                        }
+                        uint32_t* const row = ps->feat[warp][lane];
+#pragma unroll
+                        for (int e = 0; e < kF / 2; ++e)
+                            row[e] = pack_bf16(f[2 * e], f[2 * e + 1]);
+                        row[6] = 0u;
+                        row[7] = 0u;
+                        __syncwarp();
+                        int const g = int(lane >> 2), tig = int(lane & 3u);
+#pragma unroll
+                        for (int mt = 0; mt < 2; ++mt)
+                        {
+                            uint32_t a0[4] = {ps->feat[warp][mt * 16 + g][tig], ps->feat[warp][mt * 16 + g + 8][tig],
+                                              ps->feat[warp][mt * 16 + g][4 + tig],
+                                              ps->feat[warp][mt * 16 + g + 8][4 + tig]};
+                            float z1[8][4], z2[8][4], z3[2][4];
+                            mlp_forward(ps->w, a0, z1, z2, z3);
+                            if (tig == 0) // columns 0 and 1: the split and accept logits
+                            {
+                                ps->logit[warp][mt * 16 + g][0] = z3[0][0];
+                                ps->logit[warp][mt * 16 + g][1] = z3[0][1];
+                                ps->logit[warp][mt * 16 + g + 8][0] = z3[0][2];
+                                ps->logit[warp][mt * 16 + g + 8][1] = z3[0][3];
+                            }
+                        }
+                        __syncwarp();
+                        bool const skip =
+                            cand && (ps->logit[warp][lane][1] - ps->logit[warp][lane][0]) < ex.skip_logit;
+                        __syncwarp();
+                        if (!__any_sync(0xffffffffu, skip))
+                            break;
+                        if (skip)
+                        {
+                            ++d; // split without evaluating: left child next
+                            j <<= 1;
+                            ++skips;
+                        }
+                    }
+                }
                 if (pi < 0)
                     continue;
                 double err;
@@ -406,7 +502,17 @@ __global__ void __launch_bounds__(kParamBlock) k_param_gk15(const double* __rest
                 else
                     v = gk15_panel(buf[k].c, p, x0, d, j, &err);
                 ++pnodes;
-                if (!(d >= max_depth || (d >= min_depth && err <= tol_at[d])))
+                bool const accept = d >= max_depth || (d >= min_depth && err <= tol_at[d]);
+                if (ex.panel_log && d < max_depth)
+                {
+                    unsigned long long const slot = atomicAdd(ex.log_count, 1ull);
+                    if ((long long)slot < ex.log_cap)
+                    {
+                        ex.panel_log[2 * slot] = uint32_t((q0 + ql) * n_curves + c0 + k);
+                        ex.panel_log[2 * slot + 1] = (uint32_t(d) << 25) | (j << 1) | (accept ? 1u : 0u);
+                    }
+                }
+                if (!accept)
                 {
                     ++d; // split: left child next
                     j <<= 1;
@@ -454,14 +560,31 @@ __global__ void __launch_bounds__(kParamBlock) k_param_gk15(const double* __rest
                 nodes_total[i] = s_nodes[threadIdx.x];
         }
     }
+    if (ex.skip_count && skips)
+        atomicAdd(ex.skip_count, skips);
 }
 } // namespace
 
 int param_run(Context& ctx, const double* d_pos, int64_t n, double* d_out, const double* x0, const double* d_curves,
               int64_t n_curves, int min_depth, int max_depth, double tol, const uint8_t* d_start, uint32_t* d_stats,
-              int32_t* d_nodes)
+              int32_t* d_nodes, uint32_t* d_panel_log, unsigned long long* d_log_count, long long log_cap)
 {
     bool const dfm = ctx.param_mode == AGWN_PARAM_MIXED;
+    bool const panel = dfm && ctx.panel_mlp && tol > 0;
+    ParamExtras ex{};
+    ex.panel_log = d_panel_log;
+    ex.log_count = d_log_count;
+    ex.log_cap = log_cap;
+    if (panel)
+    {
+        const void* wb = nullptr;
+        mlp_device_weights(ctx.panel_mlp, &wb, &ex.pparams);
+        ex.pwb = static_cast<const __nv_bfloat16*>(wb);
+        double const b = std::min(std::max(double(ctx.panel_beta), 1e-9), 1.0 - 1e-9);
+        ex.skip_logit = float(std::log(b / (1.0 - b)));
+        ex.log10_tol = float(std::log10(tol));
+        ex.skip_count = ctx.timing ? reinterpret_cast<unsigned long long*>(ctx.d_counters + 2) : nullptr;
+    }
     if (n == 0)
         return AGWN_OK;
     if (n_curves == 0)
@@ -472,8 +595,9 @@ int param_run(Context& ctx, const double* d_pos, int64_t n, double* d_out, const
         return AGWN_OK;
     }
     static_assert(sizeof(CurveDF) == sizeof(Bez), "both curve forms stage through the same tile");
-    int const tile = int(std::min<int64_t>(kParamTileMax, n_curves));
-    size_t const smem = size_t(tile) * sizeof(Bez);
+    // with the per-panel network a smaller tile keeps two blocks per SM
+    int const tile = int(std::min<int64_t>(panel ? 768 : kParamTileMax, n_curves));
+    size_t const smem = size_t(tile) * sizeof(Bez) + (panel ? sizeof(PanelSmem) : 0);
     auto const kern = dfm ? k_param_gk15<true> : k_param_gk15<false>;
     AGWN_TRY_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
     int per_sm = 0;
@@ -499,7 +623,8 @@ int param_run(Context& ctx, const double* d_pos, int64_t n, double* d_out, const
     AGWN_TRY(ctx.launch_begin(AGWN_K_PARAMETRIC));
     kern<<<grid, kParamBlock, smem, ctx.stream>>>(d_pos, n, d_out, x0[0], x0[1], x0[2],
                                                  reinterpret_cast<const Bez*>(tile_src), n_curves, tile, min_depth,
-                                                 max_depth, tol, d_start, d_stats, d_nodes, pair_vals, ctx.d_flags);
+                                                 max_depth, tol, d_start, d_stats, d_nodes, pair_vals, ctx.d_flags,
+                                                 ex);
     return ctx.launch_end(AGWN_K_PARAMETRIC);
 }
 } // namespace agwn
@@ -593,4 +718,64 @@ extern "C" int agwn_param_batch_fractional_learned_bezier3_f64(agwn_context* ctx
     AGWN_CHECK_ARG(mlp, "null network");
     return param_entry(ctx, mlp, n_classes, alpha, positions, n, out, x0, curves, n_curves, min_depth, max_depth, tol,
                        nullptr, pair_stats, nodes_per_query);
+}
+
+extern "C" int agwn_param_set_panel_network(agwn_context* ctx, const agwn_mlp* mlp, float beta)
+{
+    AGWN_CHECK_ARG(ctx, "null context");
+    AGWN_CHECK_ARG(beta > 0.f && beta < 1.f, "beta must be in (0, 1)");
+    clear_message();
+    ctx->panel_mlp = mlp;
+    ctx->panel_beta = beta;
+    return AGWN_OK;
+}
+
+extern "C" int agwn_param_panel_log_bezier3_f64(agwn_context* ctx, const double* positions, int64_t n,
+                                                const double* x0, const double* curves, int64_t n_curves,
+                                                int min_depth, int max_depth, double tol, uint32_t* log,
+                                                int64_t capacity, int64_t* n_entries)
+{
+    AGWN_CHECK_ARG(ctx && x0 && n_entries && capacity >= 0 && (capacity == 0 || log), "bad arguments");
+    AGWN_CHECK_ARG(n >= 0 && n_curves >= 0 && (n == 0 || positions) && (n_curves == 0 || curves), "bad arguments");
+    AGWN_CHECK_ARG(n * n_curves < (int64_t(1) << 32), "the log indexes (query, curve) pairs in 32 bits");
+    AGWN_CHECK_ARG(min_depth >= 0 && max_depth >= 0 && max_depth <= kParamMaxDepth, "bad depths");
+    AGWN_CHECK_ARG(std::isfinite(tol) && tol >= 0, "tol must be finite and >= 0");
+    clear_message();
+    AGWN_TRY_CUDA(cudaSetDevice(ctx->device));
+    *n_entries = 0;
+    if (n == 0 || n_curves == 0)
+        return AGWN_OK;
+    const void *dpos = nullptr, *dcur = nullptr;
+    void *dout = nullptr, *dlog = nullptr, *dcnt = nullptr;
+    bool h_log = false;
+    AGWN_TRY(stage_in(*ctx, positions, sizeof(double) * 3 * n, S_QUERIES, &dpos));
+    AGWN_TRY(stage_in(*ctx, curves, sizeof(double) * 12 * n_curves, S_MISC0, &dcur));
+    if (reinterpret_cast<uintptr_t>(dcur) % 16 != 0)
+    {
+        void* aligned = nullptr;
+        AGWN_TRY(ctx->scratch_reserve(S_SEGS, sizeof(double) * 12 * n_curves, &aligned));
+        AGWN_TRY_CUDA(cudaMemcpyAsync(aligned, dcur, sizeof(double) * 12 * n_curves, cudaMemcpyDeviceToDevice,
+                                      ctx->stream));
+        dcur = aligned;
+    }
+    AGWN_TRY(ctx->scratch_reserve(S_OUT, sizeof(double) * n, &dout));
+    if (capacity > 0)
+        AGWN_TRY(stage_out(*ctx, log, sizeof(uint32_t) * 2 * size_t(capacity), S_MISC2, &dlog, &h_log));
+    AGWN_TRY(ctx->scratch_reserve(S_MISC3, sizeof(unsigned long long), &dcnt));
+    AGWN_TRY_CUDA(cudaMemsetAsync(dcnt, 0, sizeof(unsigned long long), ctx->stream));
+    AGWN_TRY(param_run(*ctx, static_cast<const double*>(dpos), n, static_cast<double*>(dout), x0,
+                       static_cast<const double*>(dcur), n_curves, min_depth, max_depth, tol, nullptr, nullptr,
+                       nullptr, static_cast<uint32_t*>(dlog), static_cast<unsigned long long*>(dcnt), capacity));
+    unsigned long long cnt = 0;
+    AGWN_TRY_CUDA(cudaMemcpyAsync(&cnt, dcnt, sizeof(cnt), cudaMemcpyDeviceToHost, ctx->stream));
+    AGWN_TRY(ctx->check_flags());
+    *n_entries = int64_t(cnt);
+    if (h_log)
+    {
+        int64_t const rows = std::min<int64_t>(int64_t(cnt), capacity);
+        AGWN_TRY_CUDA(cudaMemcpyAsync(log, dlog, sizeof(uint32_t) * 2 * size_t(rows), cudaMemcpyDeviceToHost,
+                                      ctx->stream));
+        AGWN_TRY(ctx->check_flags());
+    }
+    return AGWN_OK;
 }

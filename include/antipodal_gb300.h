@@ -305,6 +305,22 @@ int agwn_param_propose_depth_bezier3_f64(agwn_context* ctx, const agwn_mlp* mlp,
                                          int min_depth, int max_depth, double tol, float alpha,
                                          uint8_t* start_depth, float* logits);
 
+/* The per-panel network of the double-float integrator (AGWN_PARAM_MIXED): before a panel below max_depth is
+ * evaluated, the warp runs `mlp` (2 classes: split, accept) on its lanes' panels -- features of the panel's piece
+ * of the curve -- and splits without evaluating those whose predicted chance of acceptance is below beta.  Every
+ * evaluated panel is still accepted or split by the plain error test.  NULL turns it off.  The context keeps the
+ * pointer: the network must outlive its use. */
+int agwn_param_set_panel_network(agwn_context* ctx, const agwn_mlp* mlp, float beta);
+/* Training data for it: runs the integrator (in the context's arithmetic) and logs every evaluated panel below
+ * max_depth as 2 words, the pair's index (query * n_curves + curve, below 2^32) and
+ * (depth << 25) | (j << 1) | accepted.  *n_entries = panels logged; min(*n_entries, capacity) are written. */
+int agwn_param_panel_log_bezier3_f64(agwn_context* ctx, const double* positions, int64_t n, const double* x0,
+                                     const double* curves, int64_t n_curves, int min_depth, int max_depth, double tol,
+                                     uint32_t* log, int64_t capacity, int64_t* n_entries);
+/* The 12 features of logged panels ([n_entries][12] floats) and their labels (accepted, nullable). */
+int agwn_param_panel_features_bezier3_f64(agwn_context* ctx, const double* positions, int64_t n, const double* x0,
+                                          const double* curves, int64_t n_curves, double tol, const uint32_t* log,
+                                          int64_t n_entries, float* features, uint8_t* labels);
 /* agwn_param_batch_fractional_bezier3_f64 with start depths proposed by `mlp` in the same call (kept in device
  * scratch): the learned form of eval_gwnr_parametric_batch_fractional. */
 int agwn_param_batch_fractional_learned_bezier3_f64(agwn_context* ctx, const agwn_mlp* mlp, const double* positions,

@@ -181,3 +181,60 @@ def test_errors(gwn, disp):
     net.n_classes = 17
     with pytest.raises(gwn.GwnError):
         net.loss_grad(f, lab)
+
+
+def test_panel_log_counts_the_plain_tree(gwn, disp):
+    """Every split panel of the plain tree is logged once: split entries = sum over pairs of (leaves - 1)."""
+    curves, q, x0 = patch_pairs(41, 8, 200)
+    cfg = gwn.IntegrateConfig(0, 10, 1e-10)
+    st = np.empty((len(q), len(curves)), np.uint32)
+    out = np.empty(len(q))
+    gwn.eval_gwnr_parametric_batch_fractional(disp, q, out, x0, curves, cfg, pair_stats=st)
+    lv, _, dmax = gwn.unpack_pair_stats(st)
+    net = gwn.LearnedGK15Proposal(disp, seed=2)
+    feats, labels = net.panel_data(q, x0, curves, cfg, capacity=2_000_000)
+    assert np.isfinite(feats).all()
+    assert int((labels == 0).sum()) == int((lv - 1).sum())
+    # accepted entries: the leaves above max_depth (forced leaves at max_depth are not logged)
+    assert int(labels.sum()) <= int(lv.sum())
+    net.close()
+
+
+def test_panel_network_skips_panels_at_equal_accuracy(gwn, trained):
+    disp, net, cfg, _ = trained
+    tc, tq, tx = patch_pairs(21, 64, 300)
+    disp.set_param_precision("mixed")
+    try:
+        hist = net.fit_panels(tq, tx, tc, cfg, beta=0.02, capacity=3_000_000, steps=800, batch=8192, lr=2e-3)
+        assert hist[-100:].mean() < 0.8 * hist[:20].mean()
+        curves, q, x0 = patch_pairs(22, 48, 300)  # held out
+        n = len(q)
+        base, nb = np.empty(n), np.empty(n, np.int32)
+        gwn.eval_gwnr_parametric_batch_fractional(disp, q, base, x0, curves, cfg, nodes_per_query=nb)
+        got, ng = np.empty(n), np.empty(n, np.int32)
+        gwn.eval_gwnr_parametric_batch_fractional(disp, q, got, x0, curves, cfg, integrator=net, nodes_per_query=ng)
+        panel, start_only = net.panel, None
+        net.panel = None
+        try:
+            start_only = np.empty(n, np.int32)
+            gwn.eval_gwnr_parametric_batch_fractional(disp, q, np.empty(n), x0, curves, cfg, integrator=net,
+                                                      nodes_per_query=start_only)
+        finally:
+            net.panel = panel
+        print(f"panels: plain {nb.sum()}, start depth only {start_only.sum()}, start depth + panel net {ng.sum()}")
+        assert ng.sum() < start_only.sum() < nb.sum()
+        assert np.abs(got - base).max() <= 1e-8
+    finally:
+        disp.set_param_precision("exact")
+
+
+def test_panel_network_save_load(gwn, trained, tmp_path):
+    disp, net, cfg, _ = trained
+    if net.panel is None:
+        pytest.skip("the panel network is trained by the previous test")
+    path = tmp_path / "p.npz"
+    net.save(path)
+    back = gwn.LearnedGK15Proposal.load(disp, path)
+    assert back.panel is not None and np.array_equal(back.panel.params, net.panel.params)
+    assert back.panel.alpha == net.panel.alpha
+    back.close()
