@@ -13,9 +13,11 @@
 //  * exact  -- the reference formula in the input precision with unfused, correctly rounded operations
 //              (rd/rf), summed in segment order: the same values as the CPU reference up to atan2's last bit.
 //  * mixed  -- double input only.  Queries and segments are moved to a frame where x1 is +z and centred on the
-//              boundary; query and segment start are held as float pairs hi + lo and the segment vector
-//              d = P1 - P0 is rounded from FP64.  A pair (query, segment) is evaluated in FP32 from
-//              v0 = (P0_hi - Q_hi) + (P0_lo - Q_lo) and v1 = v0 + d:
+//              boundary; queries and boundary vertices are held as float pairs hi + lo and the segment vector
+//              d = P1 - P0 is rounded from FP64.  The boundary is walked as chains of segments that share
+//              vertices (k_prep_mixed), so v = (P_hi - Q_hi) + (P_lo - Q_lo), |v| and the half-angle form of each
+//              vertex are computed once for the two segments that meet there.  A pair (query, segment) is
+//              evaluated in FP32 from v0, v1 and d:
 //                num = v0.x*d.y - v0.y*d.x  (no cancellation for a far segment: d is accurate on its own),
 //                den = (l0 + z0)(l1 + z1) + v0.x*v1.x + v0.y*v1.y  with l + z = (x^2 + y^2)/(l - z) for z < 0
 //              and atan2f, summed with TwoSum compensation.  Each term is then accurate to about eps32 times its
@@ -118,16 +120,24 @@ int fractional_run(Context& ctx, const T* d_pos, int64_t n, T* d_out, const int3
         double const x0n = x0d[0] * x0d[0] + x0d[1] * x0d[1] + x0d[2] * x0d[2];
         AGWN_CHECK_ARG(x0n > 0 && std::isfinite(x0n), "mixed mode needs a finite nonzero x0");
         Rot const rot = make_rotation(x0d);
+        // the entry stream holds between n_seg + 1 and 2 n_seg entries; the tile (even) and the buffers are sized
+        // for the most, the kernel reads the count k_prep_mixed wrote
+        int64_t const max_entries = 2 * n_seg;
+        int const etile = int(std::min<int64_t>(ctx.seg_tile, max_entries));
+        int const ebuf = max_entries > etile ? 2 : 1;
+        int64_t const n_order = 2 * std::min<int64_t>(n_seg, kChainMax);
         SegM* seg = nullptr;
         SegX<double>* seg64 = nullptr;
         Frame* frame = nullptr;
-        AGWN_TRY(ctx.scratch_reserve(S_SEGS, sizeof(SegM) * n_seg, reinterpret_cast<void**>(&seg)));
+        AGWN_TRY(ctx.scratch_reserve(S_SEGS, sizeof(SegM) * max_entries + sizeof(int) * n_order,
+                                     reinterpret_cast<void**>(&seg)));
+        int* const order = reinterpret_cast<int*>(seg + max_entries);
         AGWN_TRY(ctx.scratch_reserve(S_SEGS_RAW, sizeof(SegX<double>) * n_seg, reinterpret_cast<void**>(&seg64)));
         AGWN_TRY(ctx.scratch_reserve(S_FRAME, sizeof(Frame), reinterpret_cast<void**>(&frame)));
         AGWN_TRY(ctx.launch_begin(AGWN_K_OTHER));
-        k_prep_mixed<<<1, 1024, 0, ctx.stream>>>(raw, n_seg, rot, float(ctx.mixed_tau), frame, seg, seg64);
+        k_prep_mixed<<<1, 1024, 0, ctx.stream>>>(raw, n_seg, rot, float(ctx.mixed_tau), frame, seg, seg64, order);
         AGWN_TRY(ctx.launch_end(AGWN_K_OTHER));
-        size_t const smem = size_t(nbuf) * tile * sizeof(SegM);
+        size_t const smem = size_t(ebuf) * etile * sizeof(SegM);
         float const tau = float(ctx.mixed_tau);
         auto launch = [&](auto kern) -> int
         {
@@ -137,7 +147,7 @@ int fractional_run(Context& ctx, const T* d_pos, int64_t n, T* d_out, const int3
             kern<<<grid, block, smem, ctx.stream>>>(reinterpret_cast<const double*>(d_pos), n,
                                                     reinterpret_cast<double*>(d_out), d_counts, x0d[0], x0d[1], x0d[2],
                                                     rot, frame, tau, float(ctx.mixed_term_err), seg, seg64, n_seg,
-                                                    tile, ctx.d_flags,
+                                                    etile, ctx.d_flags,
                                                     ctx.d_counters, ctx.timing);
             return ctx.launch_end(AGWN_K_FRACTIONAL);
         };

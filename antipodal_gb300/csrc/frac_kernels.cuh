@@ -6,6 +6,7 @@
 #include "agwn_internal.cuh"
 #include "tma.cuh"
 
+#include <climits>
 #include <cmath>
 
 namespace agwn
@@ -17,7 +18,11 @@ struct alignas(16) SegX
 {
     T p0x, p0y, p0z, p1x, p1y, p1z, w, pad;
 };
-// Mixed-mode segment: a = (P0_hi, w), b = (P1 - P0, (tau * |p1 - p0|)^2), c = (P0_lo, index as bits).
+// Mixed-mode boundary entry: a vertex and the segment that ends at it, in chain order (k_prep_mixed).
+//   segment entry: a = (P1_hi, w), b = (P1 - P0, near2), c = (P1_lo, segment index as bits);
+//   chain start:   a = (P0_hi, 0), b = (0, 0, 0, near2), c = (P0_lo, -1 as bits).
+// P0 of a segment entry is the vertex of the entry before it.  near2 = (tau * L)^2 with L the longer of the (one or
+// two) segments of the chain that meet at the vertex.
 struct alignas(16) SegM
 {
     float4 a, b, c;
@@ -29,6 +34,7 @@ struct Rot
 struct Frame
 {
     double c[3];
+    long long n_entries; // boundary entries written by k_prep_mixed
 };
 
 template <class T>
@@ -198,12 +204,32 @@ __global__ void __launch_bounds__(256) k_frac_exact(const T* __restrict__ pos, i
 // mixed form
 // --------------------------------------------------------------------------------------------------------------
 
-// One block: bounding-box centre of all endpoints, then each segment moved into the x1 = +z frame around it.
+// Boundaries of up to this many segments are put in chain order; larger ones take one chain per segment.
+constexpr int kChainMax = 4096;
+
+__device__ __forceinline__ float seg_length(const double* w)
+{
+    double const ex = w[3] - w[0], ey = w[4] - w[1], ez = w[5] - w[2];
+    return float(sqrt(ex * ex + ey * ey + ez * ez));
+}
+
+// One block.  (1) The bounding-box centre of all endpoints.  (2) Chains: segment t follows segment s when
+// P0(t) == P1(s) exactly (all three doubles), each t following at most one s (the lowest-numbered), so the links form
+// disjoint open chains and closed loops.  (3) The entry stream: per chain a start entry (its first segment's P0)
+// and then one entry per segment (its P1), open chains from their first segment and closed loops from their
+// lowest-numbered segment, each vertex moved into the x1 = +z frame around the centre.  Chained vertices are the
+// same doubles, so every segment sees the same P0 and P1 as in a stream of one chain per segment; chaining only
+// lets the fractional kernel share the per-vertex work of consecutive segments.  order: 2 * min(n_seg, kChainMax)
+// ints of scratch.
 __global__ void __launch_bounds__(1024) k_prep_mixed(const double* __restrict__ raw, int64_t n_seg, Rot rot,
                                                      float tau, Frame* __restrict__ frame, SegM* __restrict__ out,
-                                                     SegX<double>* __restrict__ out64)
+                                                     SegX<double>* __restrict__ out64, int* __restrict__ order)
 {
     __shared__ double red[2][3][32];
+    __shared__ double centre[3];
+    __shared__ int s_succ[kChainMax], s_pred[kChainMax];
+    __shared__ unsigned char s_seen[kChainMax];
+    __shared__ int s_entries;
     double mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
     for (int64_t s = threadIdx.x; s < n_seg; s += blockDim.x)
     {
@@ -228,8 +254,14 @@ __global__ void __launch_bounds__(1024) k_prep_mixed(const double* __restrict__ 
             red[1][k][warp] = mx[k];
         }
     }
+    bool const chain = n_seg <= kChainMax;
+    int const ns = chain ? int(n_seg) : 0;
+    for (int s = threadIdx.x; s < ns; s += blockDim.x)
+    {
+        s_pred[s] = INT_MAX;
+        s_seen[s] = 0;
+    }
     __syncthreads();
-    __shared__ double centre[3];
     if (threadIdx.x < 3)
     {
         int const k = threadIdx.x;
@@ -242,32 +274,122 @@ __global__ void __launch_bounds__(1024) k_prep_mixed(const double* __restrict__ 
         centre[k] = (n_seg > 0) ? 0.5 * (a + b) : 0.0;
         frame->c[k] = centre[k];
     }
+    // (2) every thread scans all segments for the first one starting where its segment ends (a broadcast read)
+    for (int s = threadIdx.x; s < ns; s += blockDim.x)
+    {
+        const double* w = raw + 7 * size_t(s);
+        double const ex = w[3], ey = w[4], ez = w[5];
+        int next = -1;
+        for (int t = 0; t < ns; ++t)
+        {
+            const double* u = raw + 7 * size_t(t);
+            if (u[0] == ex && u[1] == ey && u[2] == ez && t != s)
+            {
+                next = t;
+                break;
+            }
+        }
+        s_succ[s] = next;
+        if (next >= 0)
+            atomicMin(&s_pred[next], s);
+    }
+    __syncthreads();
+    for (int s = threadIdx.x; s < ns; s += blockDim.x)
+    {
+        int const t = s_succ[s];
+        if (t >= 0 && s_pred[t] != s)
+            s_succ[s] = -1; // t follows a lower-numbered segment
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+        int m = 0;
+        if (chain)
+        {
+            // pass 0: open chains from their heads (no predecessor); pass 1: what is left lies on closed loops
+            for (int pass = 0; pass < 2; ++pass)
+                for (int s = 0; s < ns; ++s)
+                {
+                    if (s_seen[s] || (pass == 0 && s_pred[s] != INT_MAX))
+                        continue;
+                    order[m++] = ~s;
+                    for (int cur = s; cur >= 0 && !s_seen[cur]; cur = s_succ[cur])
+                    {
+                        s_seen[cur] = 1;
+                        order[m++] = cur;
+                    }
+                }
+        }
+        else
+            m = int(2 * n_seg);
+        s_entries = m;
+        frame->n_entries = m;
+    }
     __syncthreads();
     double const cx = centre[0], cy = centre[1], cz = centre[2];
-    for (int64_t s = threadIdx.x; s < n_seg; s += blockDim.x)
+    auto rotated = [&](const double* pt, double (&P)[3])
     {
-        const double* w = raw + 7 * s;
-        double P[2][3];
-        for (int e = 0; e < 2; ++e)
+        double const dx = pt[0] - cx, dy = pt[1] - cy, dz = pt[2] - cz;
+        for (int r = 0; r < 3; ++r)
+            P[r] = rot.m[3 * r] * dx + rot.m[3 * r + 1] * dy + rot.m[3 * r + 2] * dz;
+    };
+    int const m = s_entries;
+    for (int e = threadIdx.x; e < m; e += blockDim.x)
+    {
+        int s;
+        bool start;
+        if (chain)
         {
-            double const dx = w[3 * e] - cx, dy = w[3 * e + 1] - cy, dz = w[3 * e + 2] - cz;
-            for (int r = 0; r < 3; ++r)
-                P[e][r] = rot.m[3 * r] * dx + rot.m[3 * r + 1] * dy + rot.m[3 * r + 2] * dz;
+            int const o = order[e];
+            start = o < 0;
+            s = start ? ~o : o;
         }
+        else
+        {
+            s = e >> 1;
+            start = (e & 1) == 0;
+        }
+        const double* w = raw + 7 * size_t(s);
+        double P0[3], P1[3];
+        rotated(w, P0);
+        rotated(w + 3, P1);
+        double const* V = start ? P0 : P1;
         float hi[3], lo[3], dv[3];
         for (int r = 0; r < 3; ++r)
         {
-            hi[r] = __double2float_rn(P[0][r]);
-            lo[r] = __double2float_rn(P[0][r] - double(hi[r]));
-            dv[r] = __double2float_rn(P[1][r] - P[0][r]);
+            hi[r] = __double2float_rn(V[r]);
+            lo[r] = __double2float_rn(V[r] - double(hi[r]));
+            dv[r] = __double2float_rn(P1[r] - P0[r]);
         }
-        double const ex = w[3] - w[0], ey = w[4] - w[1], ez = w[5] - w[2];
-        float const len = float(sqrt(ex * ex + ey * ey + ez * ez));
-        SegM m;
-        m.a = make_float4(hi[0], hi[1], hi[2], float(w[6]));
-        m.b = make_float4(dv[0], dv[1], dv[2], (tau * len) * (tau * len)); // near test on squared lengths
-        m.c = make_float4(lo[0], lo[1], lo[2], __int_as_float(int(s)));
-        out[s] = m;
+        // the segments meeting at this vertex: the entry's own (unless a start) and the next entry's (unless a start)
+        int next = -1;
+        if (e + 1 < m)
+        {
+            if (chain)
+                next = order[e + 1];
+            else
+                next = (e & 1) == 0 ? s : -1;
+        }
+        float const L = fmaxf(start ? 0.f : seg_length(w), next >= 0 ? seg_length(raw + 7 * size_t(next)) : 0.f);
+        float const near2 = (tau * L) * (tau * L);
+        SegM mm;
+        if (start)
+        {
+            mm.a = make_float4(hi[0], hi[1], hi[2], 0.f);
+            mm.b = make_float4(0.f, 0.f, 0.f, near2);
+            mm.c = make_float4(lo[0], lo[1], lo[2], __int_as_float(-1));
+        }
+        else
+        {
+            mm.a = make_float4(hi[0], hi[1], hi[2], float(w[6]));
+            mm.b = make_float4(dv[0], dv[1], dv[2], near2);
+            mm.c = make_float4(lo[0], lo[1], lo[2], __int_as_float(s));
+        }
+        out[e] = mm;
+    }
+    for (int64_t s = threadIdx.x; s < n_seg; s += blockDim.x)
+    {
+        const double* w = raw + 7 * s;
         out64[s] = SegX<double>{w[0], w[1], w[2], w[3], w[4], w[5], w[6], 0.0};
     }
 }
@@ -321,7 +443,7 @@ __device__ __forceinline__ float atan2_fast(float y, float x)
 template <int K>
 struct Fp64Queue
 {
-    static constexpr unsigned kCap = 64u * K; // > 31 left over + 32 * K added per segment
+    static constexpr unsigned kCap = 128u * K; // > 31 left over + 2 * 32 * K added per pair of entries
     uint32_t* e;                              // kCap entries of this warp
     double* res;                              // 32 results of this warp
     unsigned head = 0, tail = 0;              // warp-uniform counters
@@ -362,6 +484,13 @@ __device__ __forceinline__ void fp64_flush(Fp64Queue<K>& q, unsigned c, int lane
     q.head += c;
 }
 
+// Per-vertex quantities of one boundary vertex relative to one query (frame coordinates): v = vertex - query and
+// the half-angle form (n, |d|) of l + z, l = |v|, with the near flag in the sign of d.
+struct VState
+{
+    float x, y, z, n, d;
+};
+
 // Blocks per SM the mixed kernel is compiled for: registers per thread scale with the queries per thread.
 template <int K>
 constexpr int mixed_min_blocks()
@@ -385,14 +514,16 @@ __global__ void __launch_bounds__(256, mixed_min_blocks<K>()) k_frac_mixed(const
     __shared__ uint32_t q_entries[8][Fp64Queue<K>::kCap];
     __shared__ double q_results[8][32];
 
+    // the entry stream (chain starts and segments, k_prep_mixed) is what the tiles walk
+    int64_t const n_entries = frame->n_entries;
     TilePipe<SegM> pipe;
-    pipe.n_tiles = int((n_seg + tile - 1) / tile);
+    pipe.n_tiles = int((n_entries + tile - 1) / tile);
     pipe.single = pipe.n_tiles == 1;
     pipe.buf[0] = reinterpret_cast<SegM*>(smem);
     pipe.buf[1] = pipe.buf[0] + (pipe.single ? 0 : tile);
     pipe.bar = bars;
     pipe.gseg = seg;
-    pipe.n_seg = n_seg;
+    pipe.n_seg = n_entries;
     pipe.tile = tile;
 
     int64_t const per_tile = int64_t(blockDim.x) * K;
@@ -433,6 +564,8 @@ __global__ void __launch_bounds__(256, mixed_min_blocks<K>()) k_frac_mixed(const
         float qhx[K], qhy[K], qhz[K], qlx[K], qly[K], qlz[K];
         float acc[K], comp[K];
         double acc64[K];
+        // per-vertex state of the two most recent entries, in alternation (even entries write st0, odd ones st1)
+        VState st0[K], st1[K];
 #pragma unroll
         for (int k = 0; k < K; ++k)
         {
@@ -452,7 +585,73 @@ __global__ void __launch_bounds__(256, mixed_min_blocks<K>()) k_frac_mixed(const
             acc[k] = 0.f;
             comp[k] = 0.f;
             acc64[k] = 0.0;
+            st0[k] = VState{};
+            st1[k] = VState{};
         }
+        // One entry: its vertex relative to each query (into cv), then the pair term of the segment from the
+        // previous entry's vertex (pv) to this one.  With may_start false (both entries of the pair are segments,
+        // the common case) the body has no branches: the queue push is a predicated store and a term taken to FP64
+        // adds an exact zero to the TwoSum, so the compiler schedules consecutive entries together.  With may_start
+        // true a chain start skips the pair term.
+        auto step = [&](SegM const& ent, VState (&pv)[K], VState (&cv)[K], bool may_start)
+        {
+            float4 const A = ent.a, B = ent.b, C = ent.c;
+            int const sidx = __float_as_int(C.w);
+#pragma unroll
+            for (int k = 0; k < K; ++k)
+            {
+                VState& c = cv[k];
+                c.x = (A.x - qhx[k]) + (C.x - qlx[k]);
+                c.y = (A.y - qhy[k]) + (C.y - qly[k]);
+                c.z = (A.z - qhz[k]) + (C.z - qlz[k]);
+                float const r = c.x * c.x + c.y * c.y;
+                float const q = r + c.z * c.z;
+                float const l = q * rsqrtf(q);
+                // l + z = n / d with (n, d) = (l + z, 1) for z >= 0 and (x^2 + y^2, l - z) for z < 0, free of
+                // cancellation.  d > 0 (or NaN); its sign bit carries "near": |v|^2 < near2.
+                c.n = c.z >= 0.f ? l + c.z : r;
+                float const d = c.z >= 0.f ? 1.f : l - c.z;
+                c.d = q < B.w ? -d : d;
+            }
+            if (may_start && sidx < 0)
+                return;
+#pragma unroll
+            for (int k = 0; k < K; ++k)
+            {
+                VState const& v0 = pv[k];
+                VState const& v1 = cv[k];
+                // num from the segment vector B (accurate on its own, no cancellation for a far segment)
+                float const ta = v0.x * B.y, tb = v0.y * B.x;
+                float const num = ta - tb;
+                // scaling num and den by the positive D = d0 * d1 leaves the angle unchanged and removes both
+                // divisions: den * D = n0 * n1 + (v0.x*v1.x + v0.y*v1.y) * D
+                float const D = fabsf(v0.d) * fabsf(v1.d), nn = v0.n * v1.n;
+                float const pxy = v0.x * v1.x, pyy = v0.y * v1.y;
+                float const num_s = num * D;
+                float const den_s = fmaf(pxy + pyy, D, nn);
+                // first-order rounding bounds: num errs by about eps * sn and den by about eps * sd, so the angle
+                // errs by at most eps * (sn * |den| + sd * |num|) / (num^2 + den^2).  With both divided by
+                // M = max(|num|, |den|) (one reciprocal, reused by atan2) that is <= eps * (sn * ad1 + sd * an1) / M.
+                float const sn = (fabsf(ta) + fabsf(tb)) * D;
+                float const sd = fmaf(fabsf(pxy) + fabsf(pyy), D, nn);
+                float const an = fabsf(num_s), ad = fabsf(den_s);
+                float const inv = __fdividef(1.f, fmaxf(fmaxf(an, ad), 1e-37f));
+                float const an1 = an * inv, ad1 = ad * inv;
+                // near: either end within tau times its longest segment (the sign bits of d); |v| = 0 makes l, and
+                // so the bound, NaN, and an infinity or NaN anywhere does the same: the negated comparison sends
+                // those to FP64 as well
+                bool const need = (__float_as_int(v0.d) | __float_as_int(v1.d)) < 0 ||
+                                  !(kEpsBound * fmaf(sn, ad1, sd * an1) * inv <= term_err) ||
+                                  (den_s < 0.f && an <= kEpsBound * sn);
+                unsigned const mq = __ballot_sync(0xffffffffu, need);
+                if (need)
+                    fq.e[(fq.tail + __popc(mq & lt)) & (Fp64Queue<K>::kCap - 1)] =
+                        (uint32_t(sidx) << 8) | (uint32_t(lane) << 3) | uint32_t(k);
+                fq.tail += __popc(mq);
+                float const t = A.w * atan2_scaled(num_s, den_s, ad1, an1);
+                two_sum_acc(acc[k], comp[k], need ? 0.f : t);
+            }
+        };
         for (int st = 0; st < pipe.n_tiles; ++st)
         {
             int const b = it & 1;
@@ -467,62 +666,27 @@ __global__ void __launch_bounds__(256, mixed_min_blocks<K>()) k_frac_mixed(const
                 return;
             SegM const* sb = pipe.buf[b];
             int const cnt = pipe.tile_count(st);
-            uint32_t const sg0 = uint32_t(st) * uint32_t(tile);
-            for (int s = 0; s < cnt; ++s)
+            // tiles start at even positions of the stream (the tile is even), so the alternation runs across them;
+            // only the last tile can end on an odd count
+            int s = 0;
+            for (; s + 1 < cnt; s += 2)
             {
-                float4 const A = sb[s].a, B = sb[s].b, C = sb[s].c;
-#pragma unroll
-                for (int k = 0; k < K; ++k)
+                if ((__float_as_int(sb[s].c.w) | __float_as_int(sb[s + 1].c.w)) >= 0)
                 {
-                    float const v0x = (A.x - qhx[k]) + (C.x - qlx[k]);
-                    float const v0y = (A.y - qhy[k]) + (C.y - qly[k]);
-                    float const v0z = (A.z - qhz[k]) + (C.z - qlz[k]);
-                    float const v1x = v0x + B.x, v1y = v0y + B.y, v1z = v0z + B.z;
-                    float const ta = v0x * B.y, tb = v0y * B.x;
-                    float const num = ta - tb;
-                    float const r0 = v0x * v0x + v0y * v0y;
-                    float const r1 = v1x * v1x + v1y * v1y;
-                    float const q0 = r0 + v0z * v0z;
-                    float const q1 = r1 + v1z * v1z;
-                    float const l0 = q0 * rsqrtf(q0);
-                    float const l1 = q1 * rsqrtf(q1);
-                    // l + z = n / d with (n, d) = (l + z, 1) for z >= 0 and (x^2 + y^2, l - z) for z < 0, free of
-                    // cancellation.  Scaling num and den by the positive D = d0 * d1 leaves the angle unchanged and
-                    // removes both divisions: den * D = n0 * n1 + (v0.x*v1.x + v0.y*v1.y) * D.
-                    float const n0 = v0z >= 0.f ? l0 + v0z : r0, d0 = v0z >= 0.f ? 1.f : l0 - v0z;
-                    float const n1 = v1z >= 0.f ? l1 + v1z : r1, d1 = v1z >= 0.f ? 1.f : l1 - v1z;
-                    float const D = d0 * d1, nn = n0 * n1;
-                    float const pxy = v0x * v1x, pyy = v0y * v1y;
-                    float const num_s = num * D;
-                    float const den_s = fmaf(pxy + pyy, D, nn);
-                    // first-order rounding bounds: num errs by about eps * sn and den by about eps * sd, so the angle
-                    // errs by at most eps * (sn * |den| + sd * |num|) / (num^2 + den^2).  With both divided by
-                    // M = max(|num|, |den|) (one reciprocal, reused by atan2) that is <= eps * (sn * ad1 + sd * an1) / M.
-                    float const sn = (fabsf(ta) + fabsf(tb)) * D;
-                    float const sd = fmaf(fabsf(pxy) + fabsf(pyy), D, nn);
-                    float const an = fabsf(num_s), ad = fabsf(den_s);
-                    float const inv = __fdividef(1.f, fmaxf(fmaxf(an, ad), 1e-37f));
-                    float const an1 = an * inv, ad1 = ad * inv;
-                    // near: min(|v0|, |v1|)^2 < (tau |P1 - P0|)^2 (also catches |v| = 0, where l is NaN); an infinity
-                    // or NaN anywhere makes the bound NaN, which the negated comparison sends to FP64 as well
-                    bool const need = fminf(q0, q1) < B.w ||
-                                      !(kEpsBound * fmaf(sn, ad1, sd * an1) * inv <= term_err) ||
-                                      (den_s < 0.f && an <= kEpsBound * sn);
-                    unsigned const m = __ballot_sync(0xffffffffu, need);
-                    if (m)
-                    {
-                        if (need)
-                            fq.e[(fq.tail + __popc(m & lt)) & (Fp64Queue<K>::kCap - 1)] =
-                                ((sg0 + uint32_t(s)) << 8) | (uint32_t(lane) << 3) | uint32_t(k);
-                        fq.tail += __popc(m);
-                    }
-                    if (!need)
-                        two_sum_acc(acc[k], comp[k], A.w * atan2_scaled(num_s, den_s, ad1, an1));
+                    step(sb[s], st1, st0, false);
+                    step(sb[s + 1], st0, st1, false);
                 }
-                // drain full batches: at most 31 + 32 * K entries stay queued, below the ring's capacity
+                else
+                {
+                    step(sb[s], st1, st0, true);
+                    step(sb[s + 1], st0, st1, true);
+                }
+                // drain full batches: at most 31 + 2 * 32 * K entries stay queued, below the ring's capacity
                 while (fq.tail - fq.head >= 32)
                     fp64_flush<K>(fq, 32, lane, warp, tile_base, pos, n, seg64, x1, acc64);
             }
+            if (s < cnt)
+                step(sb[s], st1, st0, true);
             if (!pipe.single)
             {
                 __syncthreads();

@@ -9,7 +9,7 @@
 //
 // agwn_mesh_batch_fractional_mixed_noalloc_f64 runs the same two kernels as agwn_mesh_batch_fractional_f64 in
 // the mixed mode, but its scratch -- the prepared boundary, the frame and the error flags -- lives in one
-// file-scope static __device__ array of fixed size (kNoAllocMaxSegments segments, about 0.9 MB), created when
+// file-scope static __device__ array of fixed size (kNoAllocMaxSegments segments, about 1.3 MB), created when
 // the library is loaded and held by every GPU that loads it until the process exits.  The caller passes the
 // inputs and the output in memory it already owns.  Nothing here calls cudaMalloc, cudaFree or any other
 // allocating routine.
@@ -31,7 +31,8 @@ constexpr int kMaxDevices = 64;
 
 struct NoAllocScratch
 {
-    SegM seg[kNoAllocMaxSegments];
+    SegM seg[2 * kNoAllocMaxSegments]; // the boundary entry stream: at most two entries per segment
+    int order[2 * kChainMax];
     SegX<double> seg64[kNoAllocMaxSegments];
     Frame frame;
     int flags[FLAG_COUNT];
@@ -121,11 +122,12 @@ extern "C" int agwn_mesh_batch_fractional_mixed_noalloc_f64(void* stream, const 
     Context defaults; // option defaults only (no resources)
     Rot const rot = make_rotation(x0);
     k_prep_mixed<<<1, 1024, 0, st>>>(boundary, n_segments, rot, float(defaults.mixed_tau), &scr->frame, scr->seg,
-                                     scr->seg64);
+                                     scr->seg64, scr->order);
     AGWN_TRY_CUDA(cudaGetLastError());
 
-    int const tile = int(std::min<int64_t>(kNoAllocTile, n_segments));
-    int const n_tiles = int((n_segments + tile - 1) / tile);
+    int64_t const max_entries = 2 * n_segments;
+    int const tile = int(std::min<int64_t>(kNoAllocTile, max_entries));
+    int const n_tiles = int((max_entries + tile - 1) / tile);
     size_t const smem = size_t(n_tiles == 1 ? 1 : 2) * tile * sizeof(SegM);
     auto kern = k_frac_mixed<kNoAllocK>;
     AGWN_TRY_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
