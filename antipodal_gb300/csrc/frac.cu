@@ -59,45 +59,99 @@ int launch_persistent(Context& ctx, Kern kernel, int block, size_t smem, int64_t
 }
 } // namespace
 
+namespace
+{
+// A boundary prepared for the fractional kernels (device scratch of the context), reusable by any number of
+// launches on the same context stream until the next preparation.
 template <class T>
-int fractional_run(Context& ctx, const T* d_pos, int64_t n, T* d_out, const int32_t* d_counts, const T* x0_host,
-                   const T* d_seg_raw, int64_t n_seg)
+struct FracPlan
+{
+    int64_t n_seg = 0;
+    bool mixed = false;
+    int tile = 0;     // segments (exact) or entries (mixed) per shared-memory tile
+    int nbuf = 1;     // shared-memory buffers
+    T x0[3] = {};
+    double x0d[3] = {};
+    Rot rot{};
+    SegX<T>* seg = nullptr;     // exact form
+    SegM* segm = nullptr;       // mixed form: the entry stream
+    SegX<double>* seg64 = nullptr;
+    Frame* frame = nullptr;
+};
+
+template <class T>
+int fractional_prepare(Context& ctx, const T* x0_host, const T* d_seg_raw, int64_t n_seg, FracPlan<T>* plan)
+{
+    FracPlan<T>& p = *plan;
+    p = FracPlan<T>{};
+    p.n_seg = n_seg;
+    for (int k = 0; k < 3; ++k)
+    {
+        p.x0[k] = x0_host[k];
+        p.x0d[k] = double(x0_host[k]);
+    }
+    if (n_seg == 0)
+        return AGWN_OK;
+    AGWN_CHECK_ARG(n_seg < (int64_t(1) << 31), "at most 2^31 - 1 boundary segments");
+    p.mixed = ctx.frac_mode == AGWN_FRAC_MIXED && sizeof(T) == 8;
+    if (!p.mixed)
+    {
+        p.tile = int(std::min<int64_t>(ctx.seg_tile, n_seg));
+        p.nbuf = n_seg > p.tile ? 2 : 1;
+        AGWN_TRY(ctx.scratch_reserve(S_SEGS, sizeof(SegX<T>) * n_seg, reinterpret_cast<void**>(&p.seg)));
+        AGWN_TRY(ctx.launch_begin(AGWN_K_OTHER));
+        k_prep_exact<T><<<std::min<int64_t>(div_up(n_seg, 256), 4 * ctx.sm_count), 256, 0, ctx.stream>>>(
+            d_seg_raw, n_seg, p.seg);
+        return ctx.launch_end(AGWN_K_OTHER);
+    }
+    AGWN_CHECK_ARG(n_seg < (int64_t(1) << 24), "the mixed form takes at most 2^24 - 1 boundary segments");
+    double const x0n = p.x0d[0] * p.x0d[0] + p.x0d[1] * p.x0d[1] + p.x0d[2] * p.x0d[2];
+    AGWN_CHECK_ARG(x0n > 0 && std::isfinite(x0n), "mixed mode needs a finite nonzero x0");
+    p.rot = make_rotation(p.x0d);
+    // the entry stream holds between n_seg + 1 and 2 n_seg entries; the tile (even) and the buffers are sized for
+    // the most, the kernel reads the count k_prep_mixed wrote
+    int64_t const max_entries = 2 * n_seg;
+    p.tile = int(std::min<int64_t>(ctx.seg_tile, max_entries));
+    p.nbuf = max_entries > p.tile ? 2 : 1;
+    int64_t const n_order = chain_scratch_ints(n_seg);
+    AGWN_TRY(ctx.scratch_reserve(S_SEGS, sizeof(SegM) * max_entries + sizeof(int) * n_order,
+                                 reinterpret_cast<void**>(&p.segm)));
+    int* const order = reinterpret_cast<int*>(p.segm + max_entries);
+    AGWN_TRY(ctx.scratch_reserve(S_SEGS_RAW, sizeof(SegX<double>) * n_seg, reinterpret_cast<void**>(&p.seg64)));
+    AGWN_TRY(ctx.scratch_reserve(S_FRAME, sizeof(Frame), reinterpret_cast<void**>(&p.frame)));
+    AGWN_TRY(ctx.launch_begin(AGWN_K_OTHER));
+    k_prep_mixed<<<1, 1024, 0, ctx.stream>>>(reinterpret_cast<const double*>(d_seg_raw), n_seg, p.rot,
+                                             float(ctx.mixed_tau), p.frame, p.segm, p.seg64, order);
+    return ctx.launch_end(AGWN_K_OTHER);
+}
+
+template <class T>
+int fractional_launch(Context& ctx, const FracPlan<T>& p, const T* d_pos, int64_t n, T* d_out,
+                      const int32_t* d_counts)
 {
     if (n == 0)
         return AGWN_OK;
-    if (n_seg == 0)
+    if (p.n_seg == 0)
     {
         AGWN_TRY(ctx.launch_begin(AGWN_K_FRACTIONAL));
         k_fill_counts<T><<<std::min<int64_t>(div_up(n, 256), 4 * ctx.sm_count), 256, 0, ctx.stream>>>(d_out, d_counts,
                                                                                                       n);
         return ctx.launch_end(AGWN_K_FRACTIONAL);
     }
-    AGWN_CHECK_ARG(n_seg < (int64_t(1) << 31), "at most 2^31 - 1 boundary segments");
     int const K = ctx.queries_per_thread;
     int const block = ctx.frac_block;
     int64_t const per_tile = int64_t(block) * K;
     int64_t const n_qtiles = (n + per_tile - 1) / per_tile;
-    int const tile = int(std::min<int64_t>(ctx.seg_tile, n_seg));
-    int const n_tiles = int((n_seg + tile - 1) / tile);
-    int const nbuf = n_tiles == 1 ? 1 : 2;
-    bool const mixed = ctx.frac_mode == AGWN_FRAC_MIXED && sizeof(T) == 8;
-
-    if (!mixed)
+    if (!p.mixed)
     {
-        SegX<T>* seg = nullptr;
-        AGWN_TRY(ctx.scratch_reserve(S_SEGS, sizeof(SegX<T>) * n_seg, reinterpret_cast<void**>(&seg)));
-        AGWN_TRY(ctx.launch_begin(AGWN_K_OTHER));
-        k_prep_exact<T><<<std::min<int64_t>(div_up(n_seg, 256), 4 * ctx.sm_count), 256, 0, ctx.stream>>>(d_seg_raw,
-                                                                                                        n_seg, seg);
-        AGWN_TRY(ctx.launch_end(AGWN_K_OTHER));
-        size_t const smem = size_t(nbuf) * tile * sizeof(SegX<T>);
+        size_t const smem = size_t(p.nbuf) * p.tile * sizeof(SegX<T>);
         auto launch = [&](auto kern) -> int
         {
             int grid = 0;
             AGWN_TRY(launch_persistent(ctx, kern, block, smem, n_qtiles, &grid));
             AGWN_TRY(ctx.launch_begin(AGWN_K_FRACTIONAL));
-            kern<<<grid, block, smem, ctx.stream>>>(d_pos, n, d_out, d_counts, x0_host[0], x0_host[1], x0_host[2], seg,
-                                                    n_seg, tile, ctx.d_flags);
+            kern<<<grid, block, smem, ctx.stream>>>(d_pos, n, d_out, d_counts, p.x0[0], p.x0[1], p.x0[2], p.seg,
+                                                    p.n_seg, p.tile, ctx.d_flags);
             return ctx.launch_end(AGWN_K_FRACTIONAL);
         };
         switch (K)
@@ -112,57 +166,42 @@ int fractional_run(Context& ctx, const T* d_pos, int64_t n, T* d_out, const int3
             return launch(k_frac_exact<T, 8>);
         }
     }
-    else
+    size_t const smem = size_t(p.nbuf) * p.tile * sizeof(SegM);
+    float const tau = float(ctx.mixed_tau);
+    auto launch = [&](auto kern) -> int
     {
-        AGWN_CHECK_ARG(n_seg < (int64_t(1) << 24), "the mixed form takes at most 2^24 - 1 boundary segments");
-        const double* raw = reinterpret_cast<const double*>(d_seg_raw);
-        double x0d[3] = {double(x0_host[0]), double(x0_host[1]), double(x0_host[2])};
-        double const x0n = x0d[0] * x0d[0] + x0d[1] * x0d[1] + x0d[2] * x0d[2];
-        AGWN_CHECK_ARG(x0n > 0 && std::isfinite(x0n), "mixed mode needs a finite nonzero x0");
-        Rot const rot = make_rotation(x0d);
-        // the entry stream holds between n_seg + 1 and 2 n_seg entries; the tile (even) and the buffers are sized
-        // for the most, the kernel reads the count k_prep_mixed wrote
-        int64_t const max_entries = 2 * n_seg;
-        int const etile = int(std::min<int64_t>(ctx.seg_tile, max_entries));
-        int const ebuf = max_entries > etile ? 2 : 1;
-        int64_t const n_order = 2 * std::min<int64_t>(n_seg, kChainMax);
-        SegM* seg = nullptr;
-        SegX<double>* seg64 = nullptr;
-        Frame* frame = nullptr;
-        AGWN_TRY(ctx.scratch_reserve(S_SEGS, sizeof(SegM) * max_entries + sizeof(int) * n_order,
-                                     reinterpret_cast<void**>(&seg)));
-        int* const order = reinterpret_cast<int*>(seg + max_entries);
-        AGWN_TRY(ctx.scratch_reserve(S_SEGS_RAW, sizeof(SegX<double>) * n_seg, reinterpret_cast<void**>(&seg64)));
-        AGWN_TRY(ctx.scratch_reserve(S_FRAME, sizeof(Frame), reinterpret_cast<void**>(&frame)));
-        AGWN_TRY(ctx.launch_begin(AGWN_K_OTHER));
-        k_prep_mixed<<<1, 1024, 0, ctx.stream>>>(raw, n_seg, rot, float(ctx.mixed_tau), frame, seg, seg64, order);
-        AGWN_TRY(ctx.launch_end(AGWN_K_OTHER));
-        size_t const smem = size_t(ebuf) * etile * sizeof(SegM);
-        float const tau = float(ctx.mixed_tau);
-        auto launch = [&](auto kern) -> int
-        {
-            int grid = 0;
-            AGWN_TRY(launch_persistent(ctx, kern, block, smem, n_qtiles, &grid));
-            AGWN_TRY(ctx.launch_begin(AGWN_K_FRACTIONAL));
-            kern<<<grid, block, smem, ctx.stream>>>(reinterpret_cast<const double*>(d_pos), n,
-                                                    reinterpret_cast<double*>(d_out), d_counts, x0d[0], x0d[1], x0d[2],
-                                                    rot, frame, tau, float(ctx.mixed_term_err), seg, seg64, n_seg,
-                                                    etile, ctx.d_flags,
-                                                    ctx.d_counters, ctx.timing);
-            return ctx.launch_end(AGWN_K_FRACTIONAL);
-        };
-        switch (K)
-        {
-        case 1:
-            return launch(k_frac_mixed<1>);
-        case 2:
-            return launch(k_frac_mixed<2>);
-        case 4:
-            return launch(k_frac_mixed<4>);
-        default:
-            return launch(k_frac_mixed<8>);
-        }
+        int grid = 0;
+        AGWN_TRY(launch_persistent(ctx, kern, block, smem, n_qtiles, &grid));
+        AGWN_TRY(ctx.launch_begin(AGWN_K_FRACTIONAL));
+        kern<<<grid, block, smem, ctx.stream>>>(reinterpret_cast<const double*>(d_pos), n,
+                                                reinterpret_cast<double*>(d_out), d_counts, p.x0d[0], p.x0d[1],
+                                                p.x0d[2], p.rot, p.frame, tau, float(ctx.mixed_term_err), p.segm,
+                                                p.seg64, p.n_seg, p.tile, ctx.d_flags, ctx.d_counters, ctx.timing);
+        return ctx.launch_end(AGWN_K_FRACTIONAL);
+    };
+    switch (K)
+    {
+    case 1:
+        return launch(k_frac_mixed<1>);
+    case 2:
+        return launch(k_frac_mixed<2>);
+    case 4:
+        return launch(k_frac_mixed<4>);
+    default:
+        return launch(k_frac_mixed<8>);
     }
+}
+} // namespace
+
+template <class T>
+int fractional_run(Context& ctx, const T* d_pos, int64_t n, T* d_out, const int32_t* d_counts, const T* x0_host,
+                   const T* d_seg_raw, int64_t n_seg)
+{
+    if (n == 0)
+        return AGWN_OK;
+    FracPlan<T> plan;
+    AGWN_TRY(fractional_prepare<T>(ctx, x0_host, d_seg_raw, n_seg, &plan));
+    return fractional_launch<T>(ctx, plan, d_pos, n, d_out, d_counts);
 }
 
 template int fractional_run<double>(Context&, const double*, int64_t, double*, const int32_t*, const double*,
@@ -196,9 +235,12 @@ int mesh_batch_pipelined(Context& ctx, const agwn_bvh* bvh, const T* positions, 
     cudaEvent_t* const up = ctx.pipe_ev;       // [b]: chunk uploaded into buffer b
     cudaEvent_t* const done = ctx.pipe_ev + 2; // [b]: kernels on buffer b finished
     cudaEvent_t* const down = ctx.pipe_ev + 4; // [b]: results of buffer b downloaded
-    // the copy streams start after everything already queued on the context stream (the staged boundary)
+    // the copy streams start after everything already queued on the context stream (the staged boundary); the
+    // boundary is prepared once, while the first chunk uploads, and serves every chunk
     AGWN_TRY_CUDA(cudaEventRecord(done[0], ctx.stream));
     AGWN_TRY_CUDA(cudaStreamWaitEvent(ctx.copy_in, done[0], 0));
+    FracPlan<T> plan;
+    AGWN_TRY(fractional_prepare<T>(ctx, x0, dseg, want_frac ? n_seg : 0, &plan));
     int64_t const n_chunks = (n + chunk - 1) / chunk;
     for (int64_t i = 0; i < n_chunks; ++i)
     {
@@ -215,7 +257,7 @@ int mesh_batch_pipelined(Context& ctx, const agwn_bvh* bvh, const T* positions, 
             AGWN_TRY_CUDA(cudaStreamWaitEvent(ctx.stream, down[b], 0));
         if (with_int)
             AGWN_TRY(integer_run<T>(ctx, *bvh, qb, m, dcounts, x0));
-        AGWN_TRY(fractional_run<T>(ctx, qb, m, ob, with_int ? dcounts : nullptr, x0, dseg, want_frac ? n_seg : 0));
+        AGWN_TRY(fractional_launch<T>(ctx, plan, qb, m, ob, with_int ? dcounts : nullptr));
         AGWN_TRY_CUDA(cudaEventRecord(done[b], ctx.stream));
         AGWN_TRY_CUDA(cudaStreamWaitEvent(ctx.copy_out, done[b], 0));
         AGWN_TRY_CUDA(cudaMemcpyAsync(out + q0, ob, sizeof(T) * m, cudaMemcpyDeviceToHost, ctx.copy_out));

@@ -207,6 +207,28 @@ __global__ void __launch_bounds__(256) k_frac_exact(const T* __restrict__ pos, i
 // Boundaries of up to this many segments are put in chain order; larger ones take one chain per segment.
 constexpr int kChainMax = 4096;
 
+__host__ __device__ constexpr int chain_table_size(int64_t n_seg)
+{
+    int t = 64;
+    while (t < 2 * n_seg && t < 2 * kChainMax)
+        t <<= 1;
+    return t;
+}
+__host__ __device__ constexpr int64_t chain_scratch_ints(int64_t n_seg)
+{
+    return n_seg <= kChainMax ? 4 * n_seg + chain_table_size(n_seg) : 0;
+}
+
+// Hash of a point for the link table; +0.0 folds -0.0 into +0.0, which compares equal to it.
+__device__ __forceinline__ uint32_t point_hash(double x, double y, double z)
+{
+    uint64_t const a = uint64_t(__double_as_longlong(x + 0.0)), b = uint64_t(__double_as_longlong(y + 0.0)),
+                   c = uint64_t(__double_as_longlong(z + 0.0));
+    uint64_t h = a * 0x9E3779B97F4A7C15ull ^ b * 0xC2B2AE3D27D4EB4Full ^ c * 0x165667B19E3779F9ull;
+    h ^= h >> 29;
+    return uint32_t(h) ^ uint32_t(h >> 32);
+}
+
 __device__ __forceinline__ float seg_length(const double* w)
 {
     double const ex = w[3] - w[0], ey = w[4] - w[1], ez = w[5] - w[2];
@@ -219,8 +241,11 @@ __device__ __forceinline__ float seg_length(const double* w)
 // and then one entry per segment (its P1), open chains from their first segment and closed loops from their
 // lowest-numbered segment, each vertex moved into the x1 = +z frame around the centre.  Chained vertices are the
 // same doubles, so every segment sees the same P0 and P1 as in a stream of one chain per segment; chaining only
-// lets the fractional kernel share the per-vertex work of consecutive segments.  order: 2 * min(n_seg, kChainMax)
-// ints of scratch.
+// lets the fractional kernel share the per-vertex work of consecutive segments.  A vertex's near threshold takes
+// the longer of the segments that meet it in its chain, the last and first segments of a closed loop included, so
+// on a boundary where no more than two segments meet at a vertex it does not depend on the input order.
+// order: chain_scratch_ints(n_seg) ints of scratch (the stream order, each entry's loop-closing neighbour, and an
+// open-addressing hash table of segment starts that finds the links in O(n_seg)).
 __global__ void __launch_bounds__(1024) k_prep_mixed(const double* __restrict__ raw, int64_t n_seg, Rot rot,
                                                      float tau, Frame* __restrict__ frame, SegM* __restrict__ out,
                                                      SegX<double>* __restrict__ out64, int* __restrict__ order)
@@ -256,11 +281,18 @@ __global__ void __launch_bounds__(1024) k_prep_mixed(const double* __restrict__ 
     }
     bool const chain = n_seg <= kChainMax;
     int const ns = chain ? int(n_seg) : 0;
+    int* const wrap = order + 2 * ns; // per entry: the segment that closes its loop at this vertex, or -1
+    int* const table = order + 4 * ns;
+    int const tmask = chain_table_size(ns) - 1;
     for (int s = threadIdx.x; s < ns; s += blockDim.x)
     {
         s_pred[s] = INT_MAX;
         s_seen[s] = 0;
+        wrap[2 * s] = -1;
+        wrap[2 * s + 1] = -1;
     }
+    for (int h = threadIdx.x; chain && h <= tmask; h += blockDim.x)
+        table[h] = -1;
     __syncthreads();
     if (threadIdx.x < 3)
     {
@@ -274,20 +306,30 @@ __global__ void __launch_bounds__(1024) k_prep_mixed(const double* __restrict__ 
         centre[k] = (n_seg > 0) ? 0.5 * (a + b) : 0.0;
         frame->c[k] = centre[k];
     }
-    // (2) every thread scans all segments for the first one starting where its segment ends (a broadcast read)
+    __syncthreads();
+    // (2) segment starts into the table (linear probing; at least half of it stays empty), then every segment looks
+    // up the lowest-numbered other segment that starts where it ends
+    for (int t = threadIdx.x; t < ns; t += blockDim.x)
+    {
+        const double* u = raw + 7 * size_t(t);
+        uint32_t h = point_hash(u[0], u[1], u[2]) & uint32_t(tmask);
+        while (atomicCAS(&table[h], -1, t) != -1)
+            h = (h + 1) & uint32_t(tmask);
+    }
+    __syncthreads();
     for (int s = threadIdx.x; s < ns; s += blockDim.x)
     {
         const double* w = raw + 7 * size_t(s);
         double const ex = w[3], ey = w[4], ez = w[5];
         int next = -1;
-        for (int t = 0; t < ns; ++t)
+        for (uint32_t h = point_hash(ex, ey, ez) & uint32_t(tmask);; h = (h + 1) & uint32_t(tmask))
         {
-            const double* u = raw + 7 * size_t(t);
-            if (u[0] == ex && u[1] == ey && u[2] == ez && t != s)
-            {
-                next = t;
+            int const t = __ldcg(&table[h]); // written by atomics: read from L2
+            if (t < 0)
                 break;
-            }
+            const double* u = raw + 7 * size_t(t);
+            if (u[0] == ex && u[1] == ey && u[2] == ez && t != s && (next < 0 || t < next))
+                next = t;
         }
         s_succ[s] = next;
         if (next >= 0)
@@ -312,11 +354,20 @@ __global__ void __launch_bounds__(1024) k_prep_mixed(const double* __restrict__ 
                 {
                     if (s_seen[s] || (pass == 0 && s_pred[s] != INT_MAX))
                         continue;
+                    int const first = m;
                     order[m++] = ~s;
+                    int last = s;
                     for (int cur = s; cur >= 0 && !s_seen[cur]; cur = s_succ[cur])
                     {
                         s_seen[cur] = 1;
                         order[m++] = cur;
+                        last = cur;
+                    }
+                    if (pass == 1)
+                    {
+                        // a closed loop: its last segment ends at the start vertex
+                        wrap[first] = last;
+                        wrap[m - 1] = s;
                     }
                 }
         }
@@ -326,6 +377,12 @@ __global__ void __launch_bounds__(1024) k_prep_mixed(const double* __restrict__ 
         frame->n_entries = m;
     }
     __syncthreads();
+    // the links are done: s_pred now holds each segment's length
+    float* const s_len = reinterpret_cast<float*>(s_pred);
+    for (int s = threadIdx.x; s < ns; s += blockDim.x)
+        s_len[s] = seg_length(raw + 7 * size_t(s));
+    __syncthreads();
+    auto len_of = [&](int s) { return chain ? s_len[s] : seg_length(raw + 7 * size_t(s)); };
     double const cx = centre[0], cy = centre[1], cz = centre[2];
     auto rotated = [&](const double* pt, double (&P)[3])
     {
@@ -370,7 +427,9 @@ __global__ void __launch_bounds__(1024) k_prep_mixed(const double* __restrict__ 
             else
                 next = (e & 1) == 0 ? s : -1;
         }
-        float const L = fmaxf(start ? 0.f : seg_length(w), next >= 0 ? seg_length(raw + 7 * size_t(next)) : 0.f);
+        int const closing = chain ? wrap[e] : -1;
+        float const L = fmaxf(fmaxf(start ? 0.f : len_of(s), next >= 0 ? len_of(next) : 0.f),
+                              closing >= 0 ? len_of(closing) : 0.f);
         float const near2 = (tau * L) * (tau * L);
         SegM mm;
         if (start)

@@ -32,7 +32,7 @@ constexpr int kMaxDevices = 64;
 struct NoAllocScratch
 {
     SegM seg[2 * kNoAllocMaxSegments]; // the boundary entry stream: at most two entries per segment
-    int order[2 * kChainMax];
+    int order[chain_scratch_ints(kChainMax)];
     SegX<double> seg64[kNoAllocMaxSegments];
     Frame frame;
     int flags[FLAG_COUNT];

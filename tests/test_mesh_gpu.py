@@ -241,3 +241,76 @@ def test_host_arrays_pipelined_equal_device_arrays(gwn):
         assert np.array_equal(op, oh)
     isect.close()
     disp.close()
+
+
+def _polyline(rng, n, closed, centre=(0.0, 0.0, 0.0), radius=1.0):
+    t = np.sort(rng.uniform(0, 2 * np.pi, size=n))
+    v = np.stack([np.cos(t), np.sin(t), 0.3 * np.sin(3 * t)], axis=1) * radius + np.asarray(centre)
+    v = v + rng.normal(0, 0.01, size=v.shape)
+    nxt = np.roll(v, -1, axis=0)
+    segs = np.concatenate([v, nxt, np.ones((n, 1))], axis=1)
+    return segs if closed else segs[:-1]
+
+
+def _check_mixed(gwn, oracle, q, x0, segs, seg_tile=512, qpt=2):
+    ref = oracle.frac_batch(q, x0, segs)
+    with gwn.CudaDispatcher(precision="mixed", queries_per_thread=qpt, seg_tile=seg_tile) as d:
+        out = np.empty(len(q))
+        gwn.eval_gwnr_mesh_batch_fractional(d, q, out, x0, segs)
+    assert np.abs(out - ref).max() <= TOL_MIXED, np.abs(out - ref).max()
+    return out
+
+
+def test_mixed_boundary_chains_any_order(gwn, oracle):
+    """The mixed kernel walks the boundary as chains of segments that share endpoints (found by exact equality,
+    whatever the input order).  On loops and open chains where at most two segments meet at a vertex every pair is
+    evaluated and routed (FP32 or FP64) the same way in any order, so any order agrees with itself up to summation
+    order.  Where more segments meet at a vertex (or duplicates and zero-length segments sit there), the linking
+    decides which neighbour sets a vertex's near threshold, so a few pairs may be routed differently: still within
+    the mixed tolerance of the oracle."""
+    rng = np.random.default_rng(11)
+    x0 = synth.unit_x0()
+    q = rng.uniform(-1.6, 1.6, size=(2001, 3))
+    loop_a = _polyline(rng, 97, True)
+    loop_b = _polyline(rng, 40, True, centre=(0.3, -0.2, 0.4), radius=0.5)
+    open_c = _polyline(rng, 31, False, centre=(-0.2, 0.5, -0.3), radius=0.7)
+    manifold = np.concatenate([loop_a, loop_b, open_c])
+    base = _check_mixed(gwn, oracle, q, x0, manifold)
+    for seed in range(3):
+        perm = np.random.default_rng(seed).permutation(len(manifold))
+        got = _check_mixed(gwn, oracle, q, x0, manifold[perm])
+        assert np.abs(got - base).max() <= 1e-12
+    # two more segments leave and re-enter a vertex of loop_a: four segments meet there
+    p = loop_a[10, :3]
+    extra = np.array([np.r_[p, p + [0.2, 0.1, 0.0], 1.0], np.r_[p + [0.2, 0.1, 0.0], p, 1.0]])
+    dup = loop_b[:3].copy()  # the same segments twice
+    zero = np.array([np.r_[p, p, 2.0], np.r_[p, p, 1.0]])  # zero-length segments at a shared vertex
+    rev = open_c[5:9][:, [3, 4, 5, 0, 1, 2, 6]]  # reversed copies: they chain among themselves only
+    segs = np.concatenate([manifold, extra, dup, zero, rev])
+    base = _check_mixed(gwn, oracle, q, x0, segs)
+    for seed in range(3):
+        perm = np.random.default_rng(seed).permutation(len(segs))
+        got = _check_mixed(gwn, oracle, q, x0, segs[perm])
+        assert np.abs(got - base).max() <= TOL_MIXED
+
+
+@pytest.mark.parametrize("n_seg,seg_tile,qpt", [(101, 32, 2), (101, 64, 1), (255, 32, 4), (63, 32, 8)])
+def test_mixed_chains_across_tiles(gwn, oracle, n_seg, seg_tile, qpt):
+    # chains longer than a tile, odd entry counts, several chains per tile, every queries-per-thread variant
+    rng = np.random.default_rng(n_seg + seg_tile)
+    x0 = synth.unit_x0()
+    q = rng.uniform(-1.6, 1.6, size=(1500, 3))
+    segs = np.concatenate([_polyline(rng, n_seg, True), _polyline(rng, 17, False, centre=(0.1, 0.1, 0.1), radius=0.3),
+                           _polyline(rng, 8, True, centre=(-0.3, 0.0, 0.2), radius=0.2)])
+    _check_mixed(gwn, oracle, q, x0, segs, seg_tile=seg_tile, qpt=qpt)
+
+
+@pytest.mark.parametrize("n_seg", [4096, 4097])
+def test_mixed_chain_limit(gwn, oracle, n_seg):
+    # up to 4096 segments the boundary is chained; above, every segment is a chain of its own
+    rng = np.random.default_rng(n_seg)
+    x0 = synth.unit_x0()
+    q = rng.uniform(-1.6, 1.6, size=(1200, 3))
+    segs = _polyline(rng, n_seg, True)
+    _check_mixed(gwn, oracle, q, x0, segs)
+
