@@ -481,6 +481,14 @@ __device__ __forceinline__ float atan_unit(float t)
     p = fmaf(p, s, 0.9999999847657755f);
     return t * p;
 }
+// atan2(y, x) given t = min(|x|, |y|) / max(|x|, |y|) and swap = |y| > |x|.
+__device__ __forceinline__ float atan2_unit(float y, float x, float t, bool swap)
+{
+    float a = atan_unit(t);
+    a = swap ? 1.5707963267948966f - a : a;
+    a = x < 0.f ? 3.141592653589793f - a : a;
+    return copysignf(a, y);
+}
 // atan2(y, x) given |x| and |y| already divided by max(|x|, |y|) (so the larger is 1).
 __device__ __forceinline__ float atan2_scaled(float y, float x, float ax1, float ay1)
 {
@@ -502,7 +510,7 @@ __device__ __forceinline__ float atan2_fast(float y, float x)
 template <int K>
 struct Fp64Queue
 {
-    static constexpr unsigned kCap = 128u * K; // > 31 left over + 2 * 32 * K added per pair of entries
+    static constexpr unsigned kCap = 128u * K; // > 31 left over + 2 * 32 * K pushed per pair of entries
     uint32_t* e;                              // kCap entries of this warp
     double* res;                              // 32 results of this warp
     unsigned head = 0, tail = 0;              // warp-uniform counters
@@ -544,7 +552,7 @@ __device__ __forceinline__ void fp64_flush(Fp64Queue<K>& q, unsigned c, int lane
 }
 
 // Per-vertex quantities of one boundary vertex relative to one query (frame coordinates): v = vertex - query and
-// the half-angle form (n, |d|) of l + z, l = |v|, with the near flag in the sign of d.
+// the half-angle form (n, d) of l + z, l = |v|; d is NaN at a near vertex.
 struct VState
 {
     float x, y, z, n, d;
@@ -647,12 +655,14 @@ __global__ void __launch_bounds__(256, mixed_min_blocks<K>()) k_frac_mixed(const
             st0[k] = VState{};
             st1[k] = VState{};
         }
+        // Pairs that go to FP64 are marked in a bit mask (bit slot * K + k) while two entries are evaluated, and
+        // pushed to the warp's queue afterwards behind one warp-uniform branch that is rarely taken.
+        uint32_t nb = 0;
         // One entry: its vertex relative to each query (into cv), then the pair term of the segment from the
         // previous entry's vertex (pv) to this one.  With may_start false (both entries of the pair are segments,
-        // the common case) the body has no branches: the queue push is a predicated store and a term taken to FP64
-        // adds an exact zero to the TwoSum, so the compiler schedules consecutive entries together.  With may_start
-        // true a chain start skips the pair term.
-        auto step = [&](SegM const& ent, VState (&pv)[K], VState (&cv)[K], bool may_start)
+        // the common case) the body has no branches: a term taken to FP64 adds an exact zero to the TwoSum, so the
+        // compiler schedules consecutive entries together.  With may_start true a chain start skips the pair term.
+        auto step = [&](SegM const& ent, VState (&pv)[K], VState (&cv)[K], bool may_start, int slot)
         {
             float4 const A = ent.a, B = ent.b, C = ent.c;
             int const sidx = __float_as_int(C.w);
@@ -667,10 +677,11 @@ __global__ void __launch_bounds__(256, mixed_min_blocks<K>()) k_frac_mixed(const
                 float const q = r + c.z * c.z;
                 float const l = q * rsqrtf(q);
                 // l + z = n / d with (n, d) = (l + z, 1) for z >= 0 and (x^2 + y^2, l - z) for z < 0, free of
-                // cancellation.  d > 0 (or NaN); its sign bit carries "near": |v|^2 < near2.
+                // cancellation.  d > 0, or NaN for a near vertex (|v|^2 < near2): the NaN makes the error bound of
+                // both segments at this vertex NaN, which sends them to FP64
                 c.n = c.z >= 0.f ? l + c.z : r;
                 float const d = c.z >= 0.f ? 1.f : l - c.z;
-                c.d = q < B.w ? -d : d;
+                c.d = q < B.w ? __int_as_float(0x7fffffff) : d;
             }
             if (may_start && sidx < 0)
                 return;
@@ -684,32 +695,53 @@ __global__ void __launch_bounds__(256, mixed_min_blocks<K>()) k_frac_mixed(const
                 float const num = ta - tb;
                 // scaling num and den by the positive D = d0 * d1 leaves the angle unchanged and removes both
                 // divisions: den * D = n0 * n1 + (v0.x*v1.x + v0.y*v1.y) * D
-                float const D = fabsf(v0.d) * fabsf(v1.d), nn = v0.n * v1.n;
+                float const D = v0.d * v1.d, nn = v0.n * v1.n;
                 float const pxy = v0.x * v1.x, pyy = v0.y * v1.y;
                 float const num_s = num * D;
                 float const den_s = fmaf(pxy + pyy, D, nn);
                 // first-order rounding bounds: num errs by about eps * sn and den by about eps * sd, so the angle
-                // errs by at most eps * (sn * |den| + sd * |num|) / (num^2 + den^2).  With both divided by
-                // M = max(|num|, |den|) (one reciprocal, reused by atan2) that is <= eps * (sn * ad1 + sd * an1) / M.
+                // errs by at most eps * (sn * |den| + sd * |num|) / (num^2 + den^2) <= eps * (sn * ad1 + sd * an1) / M
+                // with M = max(|num|, |den|) and an1, ad1 the two divided by M: one of them is 1, the other is the
+                // ratio t that atan2 takes as well
                 float const sn = (fabsf(ta) + fabsf(tb)) * D;
                 float const sd = fmaf(fabsf(pxy) + fabsf(pyy), D, nn);
                 float const an = fabsf(num_s), ad = fabsf(den_s);
-                float const inv = __fdividef(1.f, fmaxf(fmaxf(an, ad), 1e-37f));
-                float const an1 = an * inv, ad1 = ad * inv;
-                // near: either end within tau times its longest segment (the sign bits of d); |v| = 0 makes l, and
-                // so the bound, NaN, and an infinity or NaN anywhere does the same: the negated comparison sends
-                // those to FP64 as well
-                bool const need = (__float_as_int(v0.d) | __float_as_int(v1.d)) < 0 ||
-                                  !(kEpsBound * fmaf(sn, ad1, sd * an1) * inv <= term_err) ||
-                                  (den_s < 0.f && an <= kEpsBound * sn);
-                unsigned const mq = __ballot_sync(0xffffffffu, need);
-                if (need)
-                    fq.e[(fq.tail + __popc(mq & lt)) & (Fp64Queue<K>::kCap - 1)] =
-                        (uint32_t(sidx) << 8) | (uint32_t(lane) << 3) | uint32_t(k);
-                fq.tail += __popc(mq);
-                float const t = A.w * atan2_scaled(num_s, den_s, ad1, an1);
-                two_sum_acc(acc[k], comp[k], need ? 0.f : t);
+                bool const swap = an > ad;
+                float const inv = __fdividef(1.f, fmaxf(swap ? an : ad, 1e-37f));
+                float const t = fminf(an, ad) * inv;
+                float const bound = kEpsBound * fmaf(swap ? sn : sd, t, swap ? sd : sn) * inv;
+                // a NaN or infinity anywhere (a near vertex, |v| = 0, overflow) makes the bound NaN, which the negated
+                // comparison sends to FP64; so does a branch (den < 0) decided within the rounding of num
+                bool const need = !(bound <= term_err) || (den_s < 0.f && an <= kEpsBound * sn);
+                nb |= need ? (1u << (slot * K + k)) : 0u;
+                float const term = A.w * atan2_unit(num_s, den_s, t, swap);
+                two_sum_acc(acc[k], comp[k], need ? 0.f : term);
             }
+        };
+        // the marked pairs of `count` entries from sb[s0] into the queue, then full batches drained: at most
+        // 31 + 2 * 32 * K entries stay queued, below the ring's capacity
+        auto push = [&](SegM const* sb, int s0, int count)
+        {
+#pragma unroll
+            for (int e = 0; e < 2; ++e)
+            {
+                if (e >= count)
+                    break;
+                uint32_t const sidx = uint32_t(__float_as_int(sb[s0 + e].c.w));
+#pragma unroll
+                for (int k = 0; k < K; ++k)
+                {
+                    bool const nd = (nb >> (e * K + k)) & 1u;
+                    unsigned const mq = __ballot_sync(0xffffffffu, nd);
+                    if (nd)
+                        fq.e[(fq.tail + __popc(mq & lt)) & (Fp64Queue<K>::kCap - 1)] =
+                            (sidx << 8) | (uint32_t(lane) << 3) | uint32_t(k);
+                    fq.tail += __popc(mq);
+                }
+            }
+            nb = 0;
+            while (fq.tail - fq.head >= 32)
+                fp64_flush<K>(fq, 32, lane, warp, tile_base, pos, n, seg64, x1, acc64);
         };
         for (int st = 0; st < pipe.n_tiles; ++st)
         {
@@ -732,20 +764,23 @@ __global__ void __launch_bounds__(256, mixed_min_blocks<K>()) k_frac_mixed(const
             {
                 if ((__float_as_int(sb[s].c.w) | __float_as_int(sb[s + 1].c.w)) >= 0)
                 {
-                    step(sb[s], st1, st0, false);
-                    step(sb[s + 1], st0, st1, false);
+                    step(sb[s], st1, st0, false, 0);
+                    step(sb[s + 1], st0, st1, false, 1);
                 }
                 else
                 {
-                    step(sb[s], st1, st0, true);
-                    step(sb[s + 1], st0, st1, true);
+                    step(sb[s], st1, st0, true, 0);
+                    step(sb[s + 1], st0, st1, true, 1);
                 }
-                // drain full batches: at most 31 + 2 * 32 * K entries stay queued, below the ring's capacity
-                while (fq.tail - fq.head >= 32)
-                    fp64_flush<K>(fq, 32, lane, warp, tile_base, pos, n, seg64, x1, acc64);
+                if (__any_sync(0xffffffffu, nb != 0))
+                    push(sb, s, 2);
             }
             if (s < cnt)
-                step(sb[s], st1, st0, true);
+            {
+                step(sb[s], st1, st0, true, 0);
+                if (__any_sync(0xffffffffu, nb != 0))
+                    push(sb, s, 1);
+            }
             if (!pipe.single)
             {
                 __syncthreads();
