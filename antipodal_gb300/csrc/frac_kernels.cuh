@@ -615,8 +615,9 @@ __global__ void __launch_bounds__(256, mixed_min_blocks<K>()) k_frac_mixed(const
         centre[threadIdx.x] = frame->c[threadIdx.x];
     __syncthreads();
 
-    // Rounding bound per FP32 operation chain (4 eps32).
+    // Rounding bound per FP32 operation chain (4 eps32), and the term error bound in its units.
     constexpr float kEpsBound = 4.0f * 5.9604645e-8f;
+    float const te_units = term_err / kEpsBound;
     double const two_pi = 2.0 * kPi<double>;
     ev3<rd> const x1{rd(-x0x), rd(-x0y), rd(-x0z)};
     Fp64Queue<K> fq;
@@ -709,10 +710,10 @@ __global__ void __launch_bounds__(256, mixed_min_blocks<K>()) k_frac_mixed(const
                 bool const swap = an > ad;
                 float const inv = __fdividef(1.f, fmaxf(swap ? an : ad, 1e-37f));
                 float const t = fminf(an, ad) * inv;
-                float const bound = kEpsBound * fmaf(swap ? sn : sd, t, swap ? sd : sn) * inv;
+                float const bound = fmaf(swap ? sn : sd, t, swap ? sd : sn) * inv; // in units of kEpsBound
                 // a NaN or infinity anywhere (a near vertex, |v| = 0, overflow) makes the bound NaN, which the negated
-                // comparison sends to FP64; so does a branch (den < 0) decided within the rounding of num
-                bool const need = !(bound <= term_err) || (den_s < 0.f && an <= kEpsBound * sn);
+                // comparison sends to FP64; so does a branch (den <= 0) decided within the rounding of num
+                bool const need = !(bound <= te_units) || fmaxf(den_s, fmaf(-kEpsBound, sn, an)) <= 0.f;
                 nb |= need ? (1u << (slot * K + k)) : 0u;
                 float const term = A.w * atan2_unit(num_s, den_s, t, swap);
                 two_sum_acc(acc[k], comp[k], need ? 0.f : term);
