@@ -747,15 +747,17 @@ __global__ void __launch_bounds__(256, mixed_min_blocks<K>()) k_frac_mixed(const
         for (int st = 0; st < pipe.n_tiles; ++st)
         {
             int const b = it & 1;
+            // a single tile stays in shared memory for every query tile: only the first waits for it, and the warps
+            // then run their query tiles without meeting at a barrier
             if (!pipe.single || j == 0)
             {
                 bool ok = mbar_wait_bounded(&bars[b], unsigned((it >> 1) & 1), flags, 2);
                 if (!ok)
                     abort_cta = 1;
+                __syncthreads();
+                if (abort_cta)
+                    return;
             }
-            __syncthreads();
-            if (abort_cta)
-                return;
             SegM const* sb = pipe.buf[b];
             int const cnt = pipe.tile_count(st);
             // tiles start at even positions of the stream (the tile is even), so the alternation runs across them;
