@@ -94,6 +94,26 @@ struct Hier
     }
 };
 
+// A uniform grid over the (u, v) plane of a ray-frame hierarchy: per cell (CSR), the leaves whose (u, v) box,
+// widened by `margin`, overlaps the cell (lbvh.cu).
+struct CellGrid
+{
+    DevBuf offsets; // n_cells + 1 unsigned
+    DevBuf list;    // leaf indices
+    int gu = 0, gv = 0;
+    float umin = 0, vmin = 0, umax = 0, vmax = 0, inv_u = 0, inv_v = 0;
+    float margin = 0;  // the widening of every leaf's box
+    float tol_max = 0; // queries whose own tolerance exceeds this take the hierarchy walk
+    int64_t entries = 0;
+    bool valid = false;
+    void release()
+    {
+        offsets.release();
+        list.release();
+        valid = false;
+    }
+};
+
 // The hierarchy of one intersector along one direction, cached per context.  Keyed by the intersector's
 // generation number and the direction's bits.
 struct RayCache
@@ -102,6 +122,7 @@ struct RayCache
     double dir[3] = {0, 0, 0};
     int scalar_bytes = 0;
     Hier h;
+    CellGrid cells; // built on first use, invalid whenever h is rebuilt
 };
 
 struct Context
@@ -129,6 +150,7 @@ struct Context
     int param_mode = AGWN_PARAM_EXACT;
     const agwn_mlp* panel_mlp = nullptr; // the per-panel network of the double-float integrator (or none)
     float panel_beta = 0.02f;
+    int integer_cells = 1;
     int queries_per_thread = 2;
     int frac_block = 128;
     int seg_tile = 512;

@@ -284,6 +284,7 @@ int agwn_context_destroy(agwn_context* ctx)
     for (auto& b : ctx->scratch)
         b.release();
     ctx->ray_cache.h.release();
+    ctx->ray_cache.cells.release();
     for (int i = 0; i < Context::kMaxPending; ++i)
     {
         if (ctx->ev_begin[i])
@@ -363,6 +364,10 @@ int agwn_context_set_option(agwn_context* ctx, int option, double value)
         AGWN_CHECK_ARG(value == AGWN_PARAM_EXACT || value == AGWN_PARAM_MIXED, "parametric mode must be 0 or 1");
         ctx->param_mode = int(value);
         return AGWN_OK;
+    case AGWN_OPT_INTEGER_CELLS:
+        AGWN_CHECK_ARG(value == 0 || value == 1, "integer cells must be 0 or 1");
+        ctx->integer_cells = int(value);
+        return AGWN_OK;
     default:
         return fail(AGWN_ERR_INVALID, "unknown option %d", option);
     }
@@ -402,6 +407,9 @@ int agwn_context_get_option(agwn_context* ctx, int option, double* value)
         return AGWN_OK;
     case AGWN_OPT_MIXED_TERM_ERR:
         *value = ctx->mixed_term_err;
+        return AGWN_OK;
+    case AGWN_OPT_INTEGER_CELLS:
+        *value = ctx->integer_cells;
         return AGWN_OK;
     default:
         return fail(AGWN_ERR_INVALID, "unknown option %d", option);

@@ -407,6 +407,182 @@ __global__ void __launch_bounds__(kTravBlock) k_traverse(const BvhNode* __restri
     }
 }
 
+// ---- integer term through a grid of cells --------------------------------------------------------------------
+// Every ray of a batch has the same direction, so in the ray frame a ray is a point (u, v) and a depth w.  A uniform
+// grid over (u, v) lists, per cell, the leaves whose (u, v) box widened by `margin` overlaps the cell; a ray reads
+// its cell's list instead of walking the hierarchy.  The leaves it then considers are a superset of the walk's (a
+// listed leaf whose box the point misses by more than the walk's tolerance is one the exact test answers 0 for),
+// and they go through the same conditions -- top of the leaf above the query's depth, may_hit -- and the same
+// decision, so the counts are the walk's.  Neighbouring rays share cells, so the lists and leaves are read
+// coherently, and there is no stack.
+struct CellView
+{
+    const unsigned* offsets;
+    const int* list;
+    int gu, gv;
+    float umin, vmin, umax, vmax, inv_u, inv_v;
+    float tol_max;
+};
+
+// Cell column / row of a coordinate: monotone in x, so a point inside a widened box maps into the box's cells.
+__device__ __forceinline__ int cell_of(float x, float lo, float inv, int g)
+{
+    int const i = int(floorf((x - lo) * inv));
+    return i < 0 ? 0 : (i >= g ? g - 1 : i);
+}
+
+// Order-preserving encodings of floats as unsigned (for atomic min / max).
+__device__ __forceinline__ unsigned f2o(float x)
+{
+    unsigned const b = __float_as_uint(x);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+float o2f(unsigned o)
+{
+    unsigned const b = (o & 0x80000000u) ? (o & 0x7FFFFFFFu) : ~o;
+    float f;
+    std::memcpy(&f, &b, sizeof(f));
+    return f;
+}
+
+// (u, v) box of a leaf from its float corners; false for a box with a NaN (never listed, as the walk never
+// reaches it)
+__device__ __forceinline__ bool leaf_box_uv(const float4* __restrict__ leaf_uv, int64_t l, float margin, float& u0,
+                                            float& v0, float& u1, float& v1)
+{
+    float4 const a = leaf_uv[kLeafF4 * l], b = leaf_uv[kLeafF4 * l + 1];
+    u0 = fminf(fminf(a.x, a.z), b.x) - margin;
+    u1 = fmaxf(fmaxf(a.x, a.z), b.x) + margin;
+    v0 = fminf(fminf(a.y, a.w), b.y) - margin;
+    v1 = fmaxf(fmaxf(a.y, a.w), b.y) + margin;
+    bool const nan = isnan(a.x) || isnan(a.y) || isnan(a.z) || isnan(a.w) || isnan(b.x) || isnan(b.y);
+    return !nan && u0 <= u1 && v0 <= v1;
+}
+
+// ext: min u, min v, max u, max v of the widened boxes, order-encoded
+__global__ void k_cell_extent(const float4* __restrict__ leaf_uv, int64_t n, float margin, unsigned* ext)
+{
+    unsigned mn[2] = {0xFFFFFFFFu, 0xFFFFFFFFu}, mx[2] = {0u, 0u};
+    for (int64_t l = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; l < n; l += int64_t(gridDim.x) * blockDim.x)
+    {
+        float u0, v0, u1, v1;
+        if (!leaf_box_uv(leaf_uv, l, margin, u0, v0, u1, v1))
+            continue;
+        mn[0] = min(mn[0], f2o(u0));
+        mn[1] = min(mn[1], f2o(v0));
+        mx[0] = max(mx[0], f2o(u1));
+        mx[1] = max(mx[1], f2o(v1));
+    }
+    for (int k = 0; k < 2; ++k)
+        for (int o = 16; o > 0; o >>= 1)
+        {
+            mn[k] = min(mn[k], __shfl_xor_sync(0xffffffffu, mn[k], o));
+            mx[k] = max(mx[k], __shfl_xor_sync(0xffffffffu, mx[k], o));
+        }
+    if ((threadIdx.x & 31) == 0)
+        for (int k = 0; k < 2; ++k)
+        {
+            atomicMin(ext + k, mn[k]);
+            atomicMax(ext + 2 + k, mx[k]);
+        }
+}
+
+// counts[c] += 1 for every cell c of every leaf (cursor == nullptr), or the leaf written at its slot of each of
+// its cells (cursor: a copy of the offsets)
+__global__ void k_cell_bin(const float4* __restrict__ leaf_uv, int64_t n, float margin, CellView g,
+                           unsigned* __restrict__ counts, unsigned long long* __restrict__ total,
+                           unsigned* __restrict__ cursor, int* __restrict__ list)
+{
+    for (int64_t l = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; l < n; l += int64_t(gridDim.x) * blockDim.x)
+    {
+        float u0, v0, u1, v1;
+        if (!leaf_box_uv(leaf_uv, l, margin, u0, v0, u1, v1))
+            continue;
+        int const iu0 = cell_of(u0, g.umin, g.inv_u, g.gu), iu1 = cell_of(u1, g.umin, g.inv_u, g.gu);
+        int const iv0 = cell_of(v0, g.vmin, g.inv_v, g.gv), iv1 = cell_of(v1, g.vmin, g.inv_v, g.gv);
+        if (total)
+            atomicAdd(total, (unsigned long long)(iu1 - iu0 + 1) * (unsigned long long)(iv1 - iv0 + 1));
+        for (int iv = iv0; iv <= iv1; ++iv)
+            for (int iu = iu0; iu <= iu1; ++iu)
+            {
+                int64_t const c = int64_t(iv) * g.gu + iu;
+                if (cursor)
+                    list[atomicAdd(cursor + c, 1u)] = int(l);
+                else
+                    atomicAdd(counts + c, 1u);
+            }
+    }
+}
+
+template <class T>
+__global__ void __launch_bounds__(kTravBlock) k_cells(const BvhNode* __restrict__ nodes, const T* __restrict__ tri,
+                                                      const float4* __restrict__ leaf_uv, float scene_scale,
+                                                      Frame32 f, CellView g, const T* __restrict__ pos, int64_t n,
+                                                      int32_t* __restrict__ counts, T dx, T dy, T dz, int* flags)
+{
+    using S = typename exact_of<T>::type;
+    ev3<S> const dir{S(dx), S(dy), S(dz)};
+    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+    {
+        T const px = pos[3 * i], py = pos[3 * i + 1], pz = pos[3 * i + 2];
+        ev3<S> const p{S(px), S(py), S(pz)};
+        float const ox = float(px), oy = float(py), oz = float(pz);
+        float const u = f.r[0] * ox + f.r[1] * oy + f.r[2] * oz;
+        float const v = f.r[3] * ox + f.r[4] * oy + f.r[5] * oz;
+        float const w = f.r[6] * ox + f.r[7] * oy + f.r[8] * oz;
+        float const qmax = fmaxf(fmaxf(fabsf(ox), fabsf(oy)), fabsf(oz));
+        float const tol = (qmax + scene_scale) * 3.8146973e-6f + 1e-30f; // as in k_traverse
+        float const m8 = 8.0f * 1e-6f * (qmax + scene_scale);
+        auto const decide = [&](int leaf) -> int
+        {
+            if constexpr (std::is_same_v<T, double>)
+            {
+                int const c = certain_leaf(leaf_uv, leaf, u, v, w, m8);
+                if (c != 2)
+                    return c;
+            }
+            return leaf_test<T>(tri, leaf, p, dir);
+        };
+        int sum = 0;
+        int cand[kCand];
+        int nc = 0;
+        auto const consider = [&](int leaf)
+        {
+            if (nc == kCand)
+            {
+                for (int j = 0; j < kCand; ++j)
+                    sum += decide(cand[j]);
+                nc = 0;
+            }
+            cand[nc++] = leaf;
+        };
+        if (tol <= g.tol_max)
+        {
+            // outside the grid no widened box reaches the point: no leaf can be hit
+            if (u >= g.umin && u <= g.umax && v >= g.vmin && v <= g.vmax)
+            {
+                int64_t const c =
+                    int64_t(cell_of(v, g.vmin, g.inv_v, g.gv)) * g.gu + cell_of(u, g.umin, g.inv_u, g.gu);
+                unsigned const b = g.offsets[c], e = g.offsets[c + 1];
+                float const wq = w - tol;
+                for (unsigned j = b; j < e; ++j)
+                {
+                    int const leaf = g.list[j];
+                    float4 const lb = leaf_uv[kLeafF4 * leaf + 1];
+                    float const wc = leaf_uv[kLeafF4 * leaf + 2].x;
+                    if (fmaxf(fmaxf(lb.z, lb.w), wc) >= wq && may_hit(leaf_uv, leaf, u, v, m8))
+                        consider(leaf);
+                }
+            }
+        }
+        else if (!hier_walk(nodes, leaf_uv, u, v, w, tol, m8, consider))
+            atomicOr(flags + FLAG_STACK, 1);
+        for (int j = 0; j < nc; ++j)
+            sum += decide(cand[j]);
+        counts[i] = sum;
+    }
+}
+
 template <class T>
 __global__ void __launch_bounds__(128) k_bruteforce(const T* __restrict__ verts, const int32_t* __restrict__ idx,
                                                     int64_t n_tri, const T* __restrict__ pos, int64_t n,
@@ -646,6 +822,7 @@ int ray_hierarchy(Context& ctx, const Bvh& bvh, const T* dir_host)
         std::memcmp(rc.dir, dir, sizeof(dir)) == 0)
         return AGWN_OK;
     rc.generation = 0; // invalid until the build completes
+    rc.cells.valid = false;
     AGWN_TRY(build_hier<T>(ctx, static_cast<const T*>(bvh.tri), bvh.n_tri, dir, rc.h, nullptr));
     std::memcpy(rc.dir, dir, sizeof(dir));
     rc.scalar_bytes = bvh.scalar_bytes;
@@ -654,6 +831,84 @@ int ray_hierarchy(Context& ctx, const Bvh& bvh, const T* dir_host)
     return AGWN_OK;
 }
 } // namespace
+
+// The cell grid of the cached hierarchy (its leaves' float (u, v) corners), about two cells per leaf over the
+// widened boxes' extent.  Leaf boxes are widened by 4 * 2^-18 of the scene scale; a query takes the grid while its
+// own tolerance (qmax + scene) * 2^-18 stays below 3.5 * 2^-18 of the scene scale (qmax <= 2.5 * scene), which
+// leaves room for the one-ulp difference between the corners and the walk's outward-rounded boxes.
+static int build_cells(Context& ctx, const Hier& h, float scene_scale, CellGrid& g)
+{
+    g.valid = false;
+    int64_t const n = h.n_tri;
+    if (n < 2 || !(scene_scale > 0.f) || !std::isfinite(scene_scale))
+        return AGWN_OK;
+    cudaStream_t const st = ctx.stream;
+    float const margin = 4.f * scene_scale * 3.8146973e-6f;
+    const float4* leaf_uv = static_cast<const float4*>(h.leaf_uv.ptr);
+    Tmp ext; // 4 order-encoded extents, then the 64-bit entry count
+    AGWN_TRY(ext.alloc(sizeof(unsigned) * 6));
+    unsigned const init[6] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0u, 0u, 0u, 0u};
+    AGWN_TRY_CUDA(cudaMemcpyAsync(ext.p, init, sizeof(init), cudaMemcpyHostToDevice, st));
+    auto* const total64 = reinterpret_cast<unsigned long long*>(ext.as<unsigned>() + 4);
+    int const gl = std::min(div_up(n, 256), 8 * ctx.sm_count);
+    AGWN_TRY(ctx.launch_begin(AGWN_K_OTHER));
+    k_cell_extent<<<gl, 256, 0, st>>>(leaf_uv, n, margin, ext.as<unsigned>());
+    AGWN_TRY(ctx.launch_end(AGWN_K_OTHER));
+    unsigned back[4];
+    AGWN_TRY_CUDA(cudaMemcpyAsync(back, ext.p, sizeof(back), cudaMemcpyDeviceToHost, st));
+    AGWN_TRY_CUDA(cudaStreamSynchronize(st));
+    if (back[0] == 0xFFFFFFFFu)
+        return AGWN_OK; // no leaf with a finite box: keep the walk
+    CellView v{};
+    v.umin = o2f(back[0]);
+    v.vmin = o2f(back[1]);
+    v.umax = o2f(back[2]);
+    v.vmax = o2f(back[3]);
+    double const W = double(v.umax) - double(v.umin), H = double(v.vmax) - double(v.vmin);
+    if (!(W > 0) || !(H > 0) || !std::isfinite(W) || !std::isfinite(H))
+        return AGWN_OK;
+    double const target = double(std::min<int64_t>(std::max<int64_t>(2 * n, 1024), int64_t(1) << 22));
+    double const side = std::sqrt(W * H / target);
+    v.gu = int(std::min(4096.0, std::max(1.0, std::ceil(W / side))));
+    v.gv = int(std::min(4096.0, std::max(1.0, std::ceil(H / side))));
+    v.inv_u = float(double(v.gu) / W);
+    v.inv_v = float(double(v.gv) / H);
+    int64_t const n_cells = int64_t(v.gu) * v.gv;
+    AGWN_TRY(g.offsets.reserve(sizeof(unsigned) * (n_cells + 1)));
+    unsigned* const off = static_cast<unsigned*>(g.offsets.ptr);
+    AGWN_TRY_CUDA(cudaMemsetAsync(off, 0, sizeof(unsigned) * (n_cells + 1), st));
+    AGWN_TRY(ctx.launch_begin(AGWN_K_OTHER));
+    k_cell_bin<<<gl, 256, 0, st>>>(leaf_uv, n, margin, v, off, total64, nullptr, nullptr);
+    k_rs_scan<<<1, 1024, 0, st>>>(off, n_cells + 1);
+    AGWN_TRY(ctx.launch_end(AGWN_K_OTHER));
+    unsigned long long total = 0;
+    AGWN_TRY_CUDA(cudaMemcpyAsync(&total, total64, sizeof(total), cudaMemcpyDeviceToHost, st));
+    AGWN_TRY_CUDA(cudaStreamSynchronize(st));
+    if (total >= (1ull << 31))
+        return AGWN_OK; // the lists would not fit 32-bit offsets: keep the walk
+    AGWN_TRY(g.list.reserve(sizeof(int) * std::max<unsigned long long>(1, total)));
+    Tmp cursor;
+    AGWN_TRY(cursor.alloc(sizeof(unsigned) * n_cells));
+    AGWN_TRY_CUDA(cudaMemcpyAsync(cursor.p, off, sizeof(unsigned) * n_cells, cudaMemcpyDeviceToDevice, st));
+    AGWN_TRY(ctx.launch_begin(AGWN_K_OTHER));
+    k_cell_bin<<<gl, 256, 0, st>>>(leaf_uv, n, margin, v, nullptr, nullptr, cursor.as<unsigned>(),
+                                   static_cast<int*>(g.list.ptr));
+    AGWN_TRY(ctx.launch_end(AGWN_K_OTHER));
+    AGWN_TRY_CUDA(cudaStreamSynchronize(st)); // the cursor is freed on return
+    g.gu = v.gu;
+    g.gv = v.gv;
+    g.umin = v.umin;
+    g.vmin = v.vmin;
+    g.umax = v.umax;
+    g.vmax = v.vmax;
+    g.inv_u = v.inv_u;
+    g.inv_v = v.inv_v;
+    g.margin = margin;
+    g.tol_max = 3.5f * scene_scale * 3.8146973e-6f;
+    g.entries = int64_t(total);
+    g.valid = true;
+    return AGWN_OK;
+}
 
 template <class T>
 int integer_run(Context& ctx, const Bvh& bvh, const T* d_pos, int64_t n, int32_t* d_counts, const T* dir_host)
@@ -671,6 +926,21 @@ int integer_run(Context& ctx, const Bvh& bvh, const T* d_pos, int64_t n, int32_t
         f.r[k] = ctx.ray_cache.h.frame[k];
     int const block = kTravBlock;
     int const grid = int(std::min<int64_t>(div_up(n, block), int64_t(ctx.sm_count) * 16));
+    CellGrid& cg = ctx.ray_cache.cells;
+    if (ctx.integer_cells && bvh.n_tri > 1 && !cg.valid)
+        AGWN_TRY(build_cells(ctx, ctx.ray_cache.h, float(bvh.scene_scale), cg));
+    if (ctx.integer_cells && bvh.n_tri > 1 && cg.valid)
+    {
+        CellView v{static_cast<const unsigned*>(cg.offsets.ptr), static_cast<const int*>(cg.list.ptr), cg.gu, cg.gv,
+                   cg.umin, cg.vmin, cg.umax, cg.vmax, cg.inv_u, cg.inv_v, cg.tol_max};
+        AGWN_TRY(ctx.launch_begin(AGWN_K_INTEGER));
+        k_cells<T><<<grid, block, 0, ctx.stream>>>(static_cast<const BvhNode*>(ctx.ray_cache.h.nodes.ptr),
+                                                  static_cast<const T*>(ctx.ray_cache.h.tri.ptr),
+                                                  static_cast<const float4*>(ctx.ray_cache.h.leaf_uv.ptr),
+                                                  float(bvh.scene_scale), f, v, d_pos, n, d_counts, dir_host[0],
+                                                  dir_host[1], dir_host[2], ctx.d_flags);
+        return ctx.launch_end(AGWN_K_INTEGER);
+    }
     AGWN_TRY(ctx.launch_begin(AGWN_K_INTEGER));
     k_traverse<T><<<grid, block, 0, ctx.stream>>>(static_cast<const BvhNode*>(ctx.ray_cache.h.nodes.ptr),
                                                   static_cast<const T*>(ctx.ray_cache.h.tri.ptr),

@@ -88,7 +88,11 @@ enum agwn_option
     /* Parametric integrator arithmetic: AGWN_PARAM_EXACT (default, FP64 with the reference's operation order, bit
        for bit) or AGWN_PARAM_MIXED (double-float on the FP32 pipe, ~44 significant bits; the same tree rule,
        tolerances and summation order). */
-    AGWN_OPT_PARAM_MODE = 9
+    AGWN_OPT_PARAM_MODE = 9,
+    /* Integer term of the mesh functions (intersector of more than one triangle): 1 (default) looks up each ray's
+       candidate triangles in a uniform grid over the plane across the ray direction, built once per (intersector,
+       direction) and cached with the hierarchy; 0 walks the hierarchy for every ray.  Counts are the same. */
+    AGWN_OPT_INTEGER_CELLS = 10
 };
 enum agwn_param_mode
 {

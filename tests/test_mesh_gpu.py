@@ -314,3 +314,37 @@ def test_mixed_chain_limit(gwn, oracle, n_seg):
     segs = _polyline(rng, n_seg, True)
     _check_mixed(gwn, oracle, q, x0, segs)
 
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_integer_cells_equal_the_walk_and_the_oracle(gwn, oracle, dtype):
+    """The integer term looks up each ray's candidate triangles in a uniform grid over the plane across the ray
+    (default) or walks the hierarchy (option 0): the same counts, equal to the scan of every triangle.  Queries on
+    a grid through the mesh, far outside it (a tolerance above the grid's widening: those take the walk inside the
+    grid kernel), beyond the grid's extent, on vertices and edges; two directions, switched back and forth so the
+    grid is rebuilt with the hierarchy."""
+    from antipodal_gb300 import _lib
+    verts, idx, _, _, _ = synth.open_icosphere(seed=4, level=4, grid=0)
+    verts = verts.astype(dtype)
+    rng = np.random.default_rng(4)
+    g = synth.grid_queries(verts.min(0), verts.max(0), 24, 1.2)
+    far = rng.uniform(-40, 40, size=(2000, 3))
+    outside = rng.uniform(-1, 1, size=(500, 3)) + np.array([3.0, -3.0, 0.5])
+    on_vertex = verts[rng.integers(0, len(verts), size=500)].astype(np.float64)
+    tri = idx.reshape(-1, 3)[rng.integers(0, len(idx) // 3, size=500)]
+    on_edge = 0.5 * (verts[tri[:, 0]].astype(np.float64) + verts[tri[:, 1]])
+    q = np.concatenate([g, far, outside, on_vertex, on_edge]).astype(dtype)
+    with gwn.CudaDispatcher() as d:
+        isect = gwn.CudaIntersector(d, verts, idx)
+        for x0 in [synth.unit_x0(), [0.0, 0.0, 1.0], synth.unit_x0()]:
+            x0 = np.asarray(x0, dtype)
+            ref = oracle.int_naive(q, x0, verts, idx)
+            got = {}
+            for cells in (1, 0):
+                d.set_option(_lib.OPT_INTEGER_CELLS, cells)
+                c = np.empty(len(q), np.int32)
+                gwn.eval_gwnr_mesh_batch_integer(d, isect, q, c, x0)
+                got[cells] = c
+            assert np.array_equal(got[1], got[0]), np.flatnonzero(got[1] != got[0])[:10]
+            assert np.array_equal(got[1], ref), np.flatnonzero(got[1] != ref)[:10]
+        isect.close()
