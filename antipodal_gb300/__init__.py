@@ -176,9 +176,11 @@ class CudaDispatcher:
         return v.value
 
     def set_robust_precision(self, precision: str):
-        """Robust evaluator under int64_grid: "exact" (default; the reference's FP64 fractional term) or "mixed"
-        (FP32 pairs on the exact integer differences under a first-order error estimate, the others in FP64).
-        Counts are unchanged."""
+        """Robust evaluator's fractional term: "exact" (default; the reference's FP64 arithmetic) or "mixed".  Under
+        int64_grid, mixed evaluates FP32 pairs on the exact integer differences under a first-order error estimate
+        (term bound: the robust term error option); under exact_float with double queries it runs the mesh
+        functions' mixed kernel along -x (term bound: the mixed term error option).  The pairs turned down take the
+        evaluator's own FP64 rule.  Counts are unchanged; int128_grid stays exact."""
         modes = {"exact": _lib.ROBUST_EXACT, "mixed": _lib.ROBUST_MIXED}
         if precision not in modes:
             raise ValueError("robust precision must be 'exact' or 'mixed'")

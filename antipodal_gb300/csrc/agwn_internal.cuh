@@ -214,7 +214,7 @@ struct rd
 {
     double v;
     rd() = default;
-    __device__ __forceinline__ constexpr rd(double x) : v(x) {}
+    __host__ __device__ __forceinline__ constexpr rd(double x) : v(x) {}
     __device__ __forceinline__ friend rd operator+(rd a, rd b) { return rd(__dadd_rn(a.v, b.v)); }
     __device__ __forceinline__ friend rd operator-(rd a, rd b) { return rd(__dsub_rn(a.v, b.v)); }
     __device__ __forceinline__ friend rd operator*(rd a, rd b) { return rd(__dmul_rn(a.v, b.v)); }

@@ -36,6 +36,7 @@
 #include <algorithm>
 #include "frac_kernels.cuh"
 #include "gwn_kernels.cuh"
+#include "robust.cuh"
 #include "tma.cuh"
 
 #include <cmath>
@@ -79,8 +80,10 @@ struct FracPlan
     Frame* frame = nullptr;
 };
 
+// force_mixed: the mixed form whatever the context's fractional mode (double only).
 template <class T>
-int fractional_prepare(Context& ctx, const T* x0_host, const T* d_seg_raw, int64_t n_seg, FracPlan<T>* plan)
+int fractional_prepare(Context& ctx, const T* x0_host, const T* d_seg_raw, int64_t n_seg, FracPlan<T>* plan,
+                       bool force_mixed = false)
 {
     FracPlan<T>& p = *plan;
     p = FracPlan<T>{};
@@ -93,7 +96,7 @@ int fractional_prepare(Context& ctx, const T* x0_host, const T* d_seg_raw, int64
     if (n_seg == 0)
         return AGWN_OK;
     AGWN_CHECK_ARG(n_seg < (int64_t(1) << 31), "at most 2^31 - 1 boundary segments");
-    p.mixed = ctx.frac_mode == AGWN_FRAC_MIXED && sizeof(T) == 8;
+    p.mixed = (force_mixed || ctx.frac_mode == AGWN_FRAC_MIXED) && sizeof(T) == 8;
     if (!p.mixed)
     {
         p.tile = int(std::min<int64_t>(ctx.seg_tile, n_seg));
@@ -124,6 +127,10 @@ int fractional_prepare(Context& ctx, const T* x0_host, const T* d_seg_raw, int64
                                              float(ctx.mixed_tau), p.frame, p.segm, p.seg64, order);
     return ctx.launch_end(AGWN_K_OTHER);
 }
+
+template <class T, class FB>
+int fractional_launch_mixed(Context& ctx, const FracPlan<T>& p, const double* d_pos, int64_t n, double* d_out,
+                            const int32_t* d_counts, FB fb);
 
 template <class T>
 int fractional_launch(Context& ctx, const FracPlan<T>& p, const T* d_pos, int64_t n, T* d_out,
@@ -166,6 +173,19 @@ int fractional_launch(Context& ctx, const FracPlan<T>& p, const T* d_pos, int64_
             return launch(k_frac_exact<T, 8>);
         }
     }
+    ev3<rd> const x1{rd(-p.x0d[0]), rd(-p.x0d[1]), rd(-p.x0d[2])};
+    return fractional_launch_mixed(ctx, p, reinterpret_cast<const double*>(d_pos), n, reinterpret_cast<double*>(d_out),
+                                   d_counts, MeshFallback{p.seg64, x1});
+}
+
+// The mixed kernel over a prepared plan, with the FP64 rule fb for the pairs it turns down.
+template <class T, class FB>
+int fractional_launch_mixed(Context& ctx, const FracPlan<T>& p, const double* d_pos, int64_t n, double* d_out,
+                            const int32_t* d_counts, FB fb)
+{
+    int const K = ctx.queries_per_thread;
+    int const block = ctx.frac_block;
+    int64_t const n_qtiles = (n + int64_t(block) * K - 1) / (int64_t(block) * K);
     size_t const smem = size_t(p.nbuf) * p.tile * sizeof(SegM);
     float const tau = float(ctx.mixed_tau);
     auto launch = [&](auto kern) -> int
@@ -173,24 +193,37 @@ int fractional_launch(Context& ctx, const FracPlan<T>& p, const T* d_pos, int64_
         int grid = 0;
         AGWN_TRY(launch_persistent(ctx, kern, block, smem, n_qtiles, &grid));
         AGWN_TRY(ctx.launch_begin(AGWN_K_FRACTIONAL));
-        kern<<<grid, block, smem, ctx.stream>>>(reinterpret_cast<const double*>(d_pos), n,
-                                                reinterpret_cast<double*>(d_out), d_counts, p.x0d[0], p.x0d[1],
-                                                p.x0d[2], p.rot, p.frame, tau, float(ctx.mixed_term_err), p.segm,
-                                                p.seg64, p.n_seg, p.tile, ctx.d_flags, ctx.d_counters, ctx.timing);
+        kern<<<grid, block, smem, ctx.stream>>>(d_pos, n, d_out, d_counts, p.rot, p.frame, tau,
+                                                float(ctx.mixed_term_err), p.segm, fb, p.n_seg, p.tile, ctx.d_flags,
+                                                ctx.d_counters, ctx.timing);
         return ctx.launch_end(AGWN_K_FRACTIONAL);
     };
     switch (K)
     {
     case 1:
-        return launch(k_frac_mixed<1>);
+        return launch(k_frac_mixed<1, FB>);
     case 2:
-        return launch(k_frac_mixed<2>);
+        return launch(k_frac_mixed<2, FB>);
     case 4:
-        return launch(k_frac_mixed<4>);
+        return launch(k_frac_mixed<4, FB>);
     default:
-        return launch(k_frac_mixed<8>);
+        return launch(k_frac_mixed<8, FB>);
     }
 }
+
+// The robust evaluator's FP64 rule (exact_float policy) for a pair the mixed kernel turns down: the reference's
+// per-segment branches (gwn_mesh_robust.hh:272-321) on the query's own doubles and the evaluator's swapped segment,
+// so the branch of every pair near the ray is the reference's exact decision.
+struct RobustFallbackPF
+{
+    const RSeg<double>* seg;
+    __device__ __forceinline__ double operator()(const double* __restrict__ pos, int64_t i, uint32_t s) const
+    {
+        RSeg<double> const g = seg[s];
+        qv3<double> const q{pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]};
+        return __dmul_rn(g.w, robust_contrib<PF>(q, g));
+    }
+};
 } // namespace
 
 template <class T>
@@ -208,6 +241,22 @@ template int fractional_run<double>(Context&, const double*, int64_t, double*, c
                                     const double*, int64_t);
 template int fractional_run<float>(Context&, const float*, int64_t, float*, const int32_t*, const float*, const float*,
                                    int64_t);
+
+int frac_mixed_robust_pf(Context& ctx, const double* d_pos, int64_t n, double* d_out, const int32_t* d_counts,
+                         const double* d_raw, int64_t n_seg, const void* rseg)
+{
+    if (n == 0)
+        return AGWN_OK;
+    // the robust term along the -x ray is the mesh term with x0 = -x on the unswapped segments (x1 = +x: the same
+    // numerator and l + x denominator)
+    double const x0[3] = {-1.0, 0.0, 0.0};
+    FracPlan<double> plan;
+    AGWN_TRY(fractional_prepare<double>(ctx, x0, d_raw, n_seg, &plan, true));
+    if (n_seg == 0)
+        return fractional_launch<double>(ctx, plan, d_pos, n, d_out, d_counts);
+    return fractional_launch_mixed(ctx, plan, d_pos, n, d_out, d_counts,
+                                   RobustFallbackPF{static_cast<const RSeg<double>*>(rseg)});
+}
 
 // --------------------------------------------------------------------------------------------------------------
 // C ABI: mesh batch functions

@@ -516,10 +516,28 @@ struct Fp64Queue
     unsigned head = 0, tail = 0;              // warp-uniform counters
 };
 
-template <int K>
+// The FP64 rule of the mesh functions for a pair the FP32 path turns down: the reference formula on the original
+// doubles, times the weight.
+struct MeshFallback
+{
+    const SegX<double>* seg64;
+    ev3<rd> x1;
+    __device__ __forceinline__ double operator()(const double* __restrict__ pos, int64_t i, uint32_t s) const
+    {
+        SegX<double> const g = seg64[s];
+        ev3<rd> const p{rd(pos[3 * i]), rd(pos[3 * i + 1]), rd(pos[3 * i + 2])};
+        ev3<rd> const v0 = ev3<rd>{rd(g.p0x), rd(g.p0y), rd(g.p0z)} - p;
+        ev3<rd> const v1 = ev3<rd>{rd(g.p1x), rd(g.p1y), rd(g.p1z)} - p;
+        return (rd(g.w) * rd(vos_exact(x1, v0, v1))).v;
+    }
+};
+
+// Evaluates up to 32 queued pairs, one per lane, with the FP64 rule fb(pos, query, segment), and adds each result
+// to its owner's accumulator.
+template <int K, class FB>
 __device__ __forceinline__ void fp64_flush(Fp64Queue<K>& q, unsigned c, int lane, int warp, int64_t tile_base,
-                                           const double* __restrict__ pos, int64_t n,
-                                           const SegX<double>* __restrict__ seg64, ev3<rd> x1, double (&acc64)[K])
+                                           const double* __restrict__ pos, int64_t n, FB const& fb,
+                                           double (&acc64)[K])
 {
     __syncwarp();
     if (unsigned(lane) < c)
@@ -528,11 +546,7 @@ __device__ __forceinline__ void fp64_flush(Fp64Queue<K>& q, unsigned c, int lane
         int const owner = (e >> 3) & 31, kk = e & 7;
         int64_t i = tile_base + int64_t(kk) * blockDim.x + warp * 32 + owner;
         i = i < n ? i : n - 1;
-        SegX<double> const g = seg64[e >> 8];
-        ev3<rd> const p{rd(pos[3 * i]), rd(pos[3 * i + 1]), rd(pos[3 * i + 2])};
-        ev3<rd> const v0 = ev3<rd>{rd(g.p0x), rd(g.p0y), rd(g.p0z)} - p;
-        ev3<rd> const v1 = ev3<rd>{rd(g.p1x), rd(g.p1y), rd(g.p1z)} - p;
-        q.res[lane] = (rd(g.w) * rd(vos_exact(x1, v0, v1))).v;
+        q.res[lane] = fb(pos, i, e >> 8);
     }
     __syncwarp();
     for (unsigned j = 0; j < c; ++j)
@@ -565,13 +579,12 @@ constexpr int mixed_min_blocks()
     return K >= 8 ? 1 : (K >= 4 ? 2 : (K >= 2 ? 3 : 4));
 }
 
-template <int K>
-__global__ void __launch_bounds__(256, mixed_min_blocks<K>()) k_frac_mixed(const double* __restrict__ pos, int64_t n, double* __restrict__ out,
-                                                    const int32_t* __restrict__ counts, double x0x, double x0y,
-                                                    double x0z, Rot rot, const Frame* __restrict__ frame, float tau,
-                                                    float term_err, const SegM* __restrict__ seg,
-                                                    const SegX<double>* __restrict__ seg64, int64_t n_seg, int tile,
-                                                    int* flags, long long* counters, int count_pairs)
+// fb: the FP64 rule for the pairs the FP32 path turns down (MeshFallback, or the robust evaluator's).
+template <int K, class FB>
+__global__ void __launch_bounds__(256, mixed_min_blocks<K>())
+    k_frac_mixed(const double* __restrict__ pos, int64_t n, double* __restrict__ out, const int32_t* __restrict__ counts,
+                 Rot rot, const Frame* __restrict__ frame, float tau, float term_err, const SegM* __restrict__ seg,
+                 FB fb, int64_t n_seg, int tile, int* flags, long long* counters, int count_pairs)
 {
     (void)tau;
     extern __shared__ __align__(128) unsigned char smem[];
@@ -619,7 +632,6 @@ __global__ void __launch_bounds__(256, mixed_min_blocks<K>()) k_frac_mixed(const
     constexpr float kEpsBound = 4.0f * 5.9604645e-8f;
     float const te_units = term_err / kEpsBound;
     double const two_pi = 2.0 * kPi<double>;
-    ev3<rd> const x1{rd(-x0x), rd(-x0y), rd(-x0z)};
     Fp64Queue<K> fq;
     fq.e = q_entries[warp];
     fq.res = q_results[warp];
@@ -742,7 +754,7 @@ __global__ void __launch_bounds__(256, mixed_min_blocks<K>()) k_frac_mixed(const
             }
             nb = 0;
             while (fq.tail - fq.head >= 32)
-                fp64_flush<K>(fq, 32, lane, warp, tile_base, pos, n, seg64, x1, acc64);
+                fp64_flush<K>(fq, 32, lane, warp, tile_base, pos, n, fb, acc64);
         };
         for (int st = 0; st < pipe.n_tiles; ++st)
         {
@@ -795,7 +807,7 @@ __global__ void __launch_bounds__(256, mixed_min_blocks<K>()) k_frac_mixed(const
         while (fq.tail != fq.head)
         {
             unsigned const c = min(32u, fq.tail - fq.head);
-            fp64_flush<K>(fq, c, lane, warp, tile_base, pos, n, seg64, x1, acc64);
+            fp64_flush<K>(fq, c, lane, warp, tile_base, pos, n, fb, acc64);
         }
 #pragma unroll
         for (int k = 0; k < K; ++k)

@@ -23,6 +23,13 @@ template <class T>
 int fractional_run(Context& ctx, const T* d_pos, int64_t n, T* d_out, const int32_t* d_counts, const T* x0_host,
                    const T* d_seg_raw, int64_t n_seg);
 
+// The robust evaluator's fractional term under the exact_float policy in mixed precision (frac.cu): the mesh
+// functions' mixed kernel along the -x ray over the raw segments d_raw (7 doubles each, the evaluator's input
+// orientation), with the robust FP64 rule for the pairs it turns down (rseg: the evaluator's RSeg<double> array,
+// same order).  out = fractional term + counts (counts may be null).
+int frac_mixed_robust_pf(Context& ctx, const double* d_pos, int64_t n, double* d_out, const int32_t* d_counts,
+                         const double* d_raw, int64_t n_seg, const void* rseg);
+
 // Integer term over a BVH for `n` device-resident queries.
 template <class T>
 int integer_run(Context& ctx, const Bvh& bvh, const T* d_pos, int64_t n, int32_t* d_counts, const T* dir_host);

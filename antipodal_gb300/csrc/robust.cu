@@ -151,6 +151,29 @@ int robust_build(Context& ctx, const T* vertices, int64_t nv, const int32_t* ind
     return AGWN_OK;
 }
 
+// The evaluator's swapped exact_float segments back in input orientation, 7 doubles each (pos0, pos1, w).
+__global__ void k_rseg_raw(const RSeg<double>* __restrict__ seg, int64_t n_seg, double* __restrict__ raw)
+{
+    for (int64_t s = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; s < n_seg; s += int64_t(gridDim.x) * blockDim.x)
+    {
+        RSeg<double> const g = seg[s];
+        double* const o = raw + 7 * s;
+        for (int k = 0; k < 3; ++k)
+        {
+            o[k] = g.p1[k];
+            o[3 + k] = g.p0[k];
+        }
+        o[6] = g.w;
+    }
+}
+
+__global__ void k_frac_plus_counts(const double* __restrict__ frac, const int32_t* __restrict__ counts,
+                                   double* __restrict__ out, int64_t n)
+{
+    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+        out[i] = frac[i] + double(counts[i]);
+}
+
 template <class T, class P>
 int robust_run(Context& ctx, const Robust& r, const T* d_pos, int64_t n, T* d_out, int32_t* d_counts, T* d_frac,
                bool counts_ready = false)
@@ -176,6 +199,26 @@ int robust_run(Context& ctx, const Robust& r, const T* d_pos, int64_t n, T* d_ou
         AGWN_TRY(ctx.launch_end(AGWN_K_ROBUST));
     }
     using Seg = RSeg<C>;
+    if constexpr (std::is_same_v<P, PF> && std::is_same_v<T, double>)
+    {
+        // mixed exact_float: the mesh functions' mixed kernel with the robust FP64 rule (frac.cu)
+        if (ctx.robust_mode == AGWN_ROBUST_MIXED && r.n_seg > 0 && r.n_seg < (int64_t(1) << 24))
+        {
+            double* raw = nullptr;
+            AGWN_TRY(ctx.scratch_reserve(S_MISC2, sizeof(double) * 7 * size_t(r.n_seg), reinterpret_cast<void**>(&raw)));
+            AGWN_TRY(ctx.launch_begin(AGWN_K_OTHER));
+            k_rseg_raw<<<int(std::min<int64_t>(div_up(r.n_seg, 256), 4 * ctx.sm_count)), 256, 0, st>>>(
+                static_cast<const RSeg<double>*>(r.seg), r.n_seg, raw);
+            AGWN_TRY(ctx.launch_end(AGWN_K_OTHER));
+            if (!d_frac)
+                return frac_mixed_robust_pf(ctx, d_pos, n, d_out, d_counts, raw, r.n_seg, r.seg);
+            AGWN_TRY(frac_mixed_robust_pf(ctx, d_pos, n, d_frac, nullptr, raw, r.n_seg, r.seg));
+            AGWN_TRY(ctx.launch_begin(AGWN_K_OTHER));
+            k_frac_plus_counts<<<int(std::min<int64_t>(div_up(n, 256), 8 * ctx.sm_count)), 256, 0, st>>>(
+                d_frac, d_counts, d_out, n);
+            return ctx.launch_end(AGWN_K_OTHER);
+        }
+    }
     int const tile = int(std::max<int64_t>(1, std::min<int64_t>(ctx.seg_tile, r.n_seg)));
     int const n_tiles = int((r.n_seg + tile - 1) / tile);
     // the mixed form (int64_grid only) adds the tiles' FP32 weights after two segment buffers

@@ -79,9 +79,12 @@ enum agwn_option
     /* Mixed mode: a pair whose first-order FP32 error bound exceeds this many radians is evaluated in FP64.
        Default 3e-8. */
     AGWN_OPT_MIXED_TERM_ERR = 6,
-    /* Robust evaluator, int64_grid policy: AGWN_ROBUST_EXACT (default, the reference's FP64 fractional term) or
-       AGWN_ROBUST_MIXED (FP32 pairs on the exact integer differences under a first-order error estimate, the
-       others -- num == 0 branches, ill-conditioned or large differences -- in FP64; counts unchanged). */
+    /* Robust evaluator's fractional term: AGWN_ROBUST_EXACT (default, the reference's FP64 arithmetic) or
+       AGWN_ROBUST_MIXED.  int64_grid: FP32 pairs on the exact integer differences under a first-order error
+       estimate (AGWN_OPT_ROBUST_TERM_ERR), the others -- num == 0 branches, ill-conditioned or large differences --
+       in FP64.  exact_float with double queries: the mesh functions' mixed kernel along -x (AGWN_OPT_MIXED_TERM_ERR)
+       with the evaluator's FP64 rule, exact branches included, for the pairs it turns down.  Counts unchanged;
+       int128_grid and the multi-mesh batch's exact_float meshes stay exact. */
     AGWN_OPT_ROBUST_MODE = 7,
     /* Robust mixed mode: the per-pair estimate above which a pair is evaluated in FP64, radians.  Default 1e-7. */
     AGWN_OPT_ROBUST_TERM_ERR = 8,

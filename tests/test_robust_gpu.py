@@ -152,3 +152,41 @@ def test_robust_mixed_batch_equals_per_mesh(gwn, disp):
     batch.close()
     for r in meshes:
         r.close()
+
+
+def test_robust_mixed_exact_float_matches_exact(gwn, disp):
+    """exact_float with double queries in mixed mode: the mesh functions' mixed kernel along -x, with the robust
+    evaluator's FP64 rule (its exact branches) for the pairs it turns down.  Counts identical; fractional term and
+    GWN within 1e-7 of the exact (FP64) form -- on grid points, on points 1e-9..1e-3 off the surface, and on points
+    whose -x ray runs exactly through a boundary vertex (the reference's special branches)."""
+    rng = np.random.default_rng(29)
+    for kind, ntri, holes in [("torus", 6000, 7), ("icosphere", 3000, 3)]:
+        v, i = synth.noisy_mesh(kind, ntri, holes, rng)
+        b = synth.boundary_segments(v, i)
+        tri = v[i.reshape(-1, 3)]
+        pick = tri[rng.integers(len(tri), size=3000)]
+        bary = rng.dirichlet([1, 1, 1], size=3000)
+        n = np.cross(pick[:, 1] - pick[:, 0], pick[:, 2] - pick[:, 0])
+        n /= np.linalg.norm(n, axis=1, keepdims=True)
+        off = (bary[:, :, None] * pick).sum(1) + n * (10.0 ** rng.uniform(-9, -3, 3000) * rng.choice([-1, 1], 3000))[:, None]
+        on_ray = b[rng.integers(len(b), size=500), :3] + np.stack([rng.uniform(0.01, 2, 500), np.zeros(500),
+                                                                   np.zeros(500)], axis=1)
+        q = np.concatenate([synth.grid_queries(v.min(0), v.max(0), 20), off, on_ray]).astype(np.float64)
+        r = gwn.CudaRobustMeshGwn(disp, v, i, b, precision="exact_float")
+        outs = {}
+        try:
+            for mode in ("exact", "mixed"):
+                disp.set_robust_precision(mode)
+                o, c, f = np.empty(len(q)), np.empty(len(q), np.int32), np.empty(len(q))
+                r.evaluate(q, o, c, f)
+                o2 = np.empty(len(q))
+                r.evaluate(q, o2)  # without the separate outputs: the other launch path
+                assert np.array_equal(o, o2)
+                outs[mode] = (o, c, f)
+        finally:
+            disp.set_robust_precision("exact")
+            r.close()
+        assert np.array_equal(outs["exact"][1], outs["mixed"][1])
+        for k in (0, 2):
+            d = np.abs(outs["exact"][k] - outs["mixed"][k])
+            assert d.max() <= 1e-7, (kind, k, d.max())
