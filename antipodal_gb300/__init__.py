@@ -114,13 +114,14 @@ class CudaDispatcher:
     ``precision`` "exact" (the reference's arithmetic, the default) or "mixed" (FP32 pairs with TwoSum
     accumulation and FP64 near / ill-conditioned / branch-cut pairs; double inputs), ``tau`` (mixed mode
     near-pair ratio), ``term_err`` (mixed mode per-pair FP32 error bound, radians),
-    ``queries_per_thread``, ``block`` and ``seg_tile`` (kernel shape), ``timing`` (CUDA-event kernel timing).
+    ``queries_per_thread``, ``block`` (0: automatic) and ``seg_tile`` (kernel shape), ``timing`` (CUDA-event
+    kernel timing).
     Like PoolDispatcher it runs one job at a time.  ``parallel_for`` is not provided: arbitrary host callables
     have no device form here, and the library has no CPU fallback.
     """
 
     def __init__(self, device: int = 0, stream=None, precision: str = "exact", tau: float = 4.0,
-                 term_err: float = 3e-8, queries_per_thread: int = 2, block: int = 128, seg_tile: int = 512,
+                 term_err: float = 3e-8, queries_per_thread: int = 2, block: int = 0, seg_tile: int = 512,
                  timing: bool = False):
         lib = library()
         handle = None

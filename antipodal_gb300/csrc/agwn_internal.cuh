@@ -152,7 +152,7 @@ struct Context
     float panel_beta = 0.02f;
     int integer_cells = 1;
     int queries_per_thread = 2;
-    int frac_block = 128;
+    int frac_block = 0; // 0: chosen per launch (frac.cu)
     int seg_tile = 512;
     int timing = 0;
 

@@ -336,8 +336,8 @@ int agwn_context_set_option(agwn_context* ctx, int option, double value)
         ctx->queries_per_thread = int(value);
         return AGWN_OK;
     case AGWN_OPT_FRAC_BLOCK:
-        AGWN_CHECK_ARG(value >= 64 && value <= 256 && std::fmod(value, 32.0) == 0.0,
-                       "block must be a multiple of 32 in [64, 256]");
+        AGWN_CHECK_ARG(value == 0 || (value >= 64 && value <= 256 && std::fmod(value, 32.0) == 0.0),
+                       "block must be 0 (automatic) or a multiple of 32 in [64, 256]");
         ctx->frac_block = int(value);
         return AGWN_OK;
     case AGWN_OPT_TIMING:

@@ -521,8 +521,8 @@ struct Fp64Queue
 struct MeshFallback
 {
     const SegX<double>* seg64;
-    ev3<rd> x1;
-    __device__ __forceinline__ double operator()(const double* __restrict__ pos, int64_t i, uint32_t s) const
+    __device__ __forceinline__ double operator()(const double* __restrict__ pos, int64_t i, uint32_t s,
+                                                 ev3<rd> x1) const
     {
         SegX<double> const g = seg64[s];
         ev3<rd> const p{rd(pos[3 * i]), rd(pos[3 * i + 1]), rd(pos[3 * i + 2])};
@@ -532,11 +532,11 @@ struct MeshFallback
     }
 };
 
-// Evaluates up to 32 queued pairs, one per lane, with the FP64 rule fb(pos, query, segment), and adds each result
-// to its owner's accumulator.
+// Evaluates up to 32 queued pairs, one per lane, with the FP64 rule fb(pos, query, segment, x1), and adds each
+// result to its owner's accumulator.
 template <int K, class FB>
 __device__ __forceinline__ void fp64_flush(Fp64Queue<K>& q, unsigned c, int lane, int warp, int64_t tile_base,
-                                           const double* __restrict__ pos, int64_t n, FB const& fb,
+                                           const double* __restrict__ pos, int64_t n, FB fb, ev3<rd> x1,
                                            double (&acc64)[K])
 {
     __syncwarp();
@@ -546,7 +546,7 @@ __device__ __forceinline__ void fp64_flush(Fp64Queue<K>& q, unsigned c, int lane
         int const owner = (e >> 3) & 31, kk = e & 7;
         int64_t i = tile_base + int64_t(kk) * blockDim.x + warp * 32 + owner;
         i = i < n ? i : n - 1;
-        q.res[lane] = fb(pos, i, e >> 8);
+        q.res[lane] = fb(pos, i, e >> 8, x1);
     }
     __syncwarp();
     for (unsigned j = 0; j < c; ++j)
@@ -583,8 +583,9 @@ constexpr int mixed_min_blocks()
 template <int K, class FB>
 __global__ void __launch_bounds__(256, mixed_min_blocks<K>())
     k_frac_mixed(const double* __restrict__ pos, int64_t n, double* __restrict__ out, const int32_t* __restrict__ counts,
-                 Rot rot, const Frame* __restrict__ frame, float tau, float term_err, const SegM* __restrict__ seg,
-                 FB fb, int64_t n_seg, int tile, int* flags, long long* counters, int count_pairs)
+                 double x0x, double x0y, double x0z, Rot rot, const Frame* __restrict__ frame, float tau,
+                 float term_err, const SegM* __restrict__ seg, FB fb, int64_t n_seg, int tile, int* flags,
+                 long long* counters, int count_pairs)
 {
     (void)tau;
     extern __shared__ __align__(128) unsigned char smem[];
@@ -632,6 +633,7 @@ __global__ void __launch_bounds__(256, mixed_min_blocks<K>())
     constexpr float kEpsBound = 4.0f * 5.9604645e-8f;
     float const te_units = term_err / kEpsBound;
     double const two_pi = 2.0 * kPi<double>;
+    ev3<rd> const x1{rd(-x0x), rd(-x0y), rd(-x0z)};
     Fp64Queue<K> fq;
     fq.e = q_entries[warp];
     fq.res = q_results[warp];
@@ -731,8 +733,8 @@ __global__ void __launch_bounds__(256, mixed_min_blocks<K>())
                 two_sum_acc(acc[k], comp[k], need ? 0.f : term);
             }
         };
-        // the marked pairs of `count` entries from sb[s0] into the queue, then full batches drained: at most
-        // 31 + 2 * 32 * K entries stay queued, below the ring's capacity
+        // the marked pairs of `count` entries from sb[s0] into the queue (the caller then drains full batches: at
+        // most 31 + 2 * 32 * K entries stay queued, below the ring's capacity)
         auto push = [&](SegM const* sb, int s0, int count)
         {
 #pragma unroll
@@ -753,8 +755,6 @@ __global__ void __launch_bounds__(256, mixed_min_blocks<K>())
                 }
             }
             nb = 0;
-            while (fq.tail - fq.head >= 32)
-                fp64_flush<K>(fq, 32, lane, warp, tile_base, pos, n, fb, acc64);
         };
         for (int st = 0; st < pipe.n_tiles; ++st)
         {
@@ -788,13 +788,21 @@ __global__ void __launch_bounds__(256, mixed_min_blocks<K>())
                     step(sb[s + 1], st0, st1, true, 1);
                 }
                 if (__any_sync(0xffffffffu, nb != 0))
+                {
                     push(sb, s, 2);
+                    while (fq.tail - fq.head >= 32)
+                        fp64_flush<K>(fq, 32, lane, warp, tile_base, pos, n, fb, x1, acc64);
+                }
             }
             if (s < cnt)
             {
                 step(sb[s], st1, st0, true, 0);
                 if (__any_sync(0xffffffffu, nb != 0))
+                {
                     push(sb, s, 1);
+                    while (fq.tail - fq.head >= 32)
+                        fp64_flush<K>(fq, 32, lane, warp, tile_base, pos, n, fb, x1, acc64);
+                }
             }
             if (!pipe.single)
             {
@@ -807,7 +815,7 @@ __global__ void __launch_bounds__(256, mixed_min_blocks<K>())
         while (fq.tail != fq.head)
         {
             unsigned const c = min(32u, fq.tail - fq.head);
-            fp64_flush<K>(fq, c, lane, warp, tile_base, pos, n, fb, acc64);
+            fp64_flush<K>(fq, c, lane, warp, tile_base, pos, n, fb, x1, acc64);
         }
 #pragma unroll
         for (int k = 0; k < K; ++k)

@@ -154,6 +154,53 @@ __device__ __forceinline__ bool hier_walk(const BvhNode* __restrict__ nodes, con
     }
 }
 
+// A cell grid (CellGrid, agwn_internal.cuh) as the kernels read it.
+struct CellView
+{
+    const unsigned* offsets;
+    const int* list;
+    int gu, gv;
+    float umin, vmin, umax, vmax, inv_u, inv_v;
+    float tol_max;
+};
+inline CellView cell_view(const CellGrid& g)
+{
+    return CellView{static_cast<const unsigned*>(g.offsets.ptr), static_cast<const int*>(g.list.ptr), g.gu, g.gv,
+                    g.umin, g.vmin, g.umax, g.vmax, g.inv_u, g.inv_v, g.tol_max};
+}
+
+// Cell column / row of a coordinate: monotone in x, so a point inside a widened box maps into the box's cells.
+__device__ __forceinline__ int cell_of(float x, float lo, float inv, int g)
+{
+    int const i = int(floorf((x - lo) * inv));
+    return i < 0 ? 0 : (i >= g ? g - 1 : i);
+}
+
+// The leaves listed in the cell of a query's (u, v) point that the walk's leaf conditions admit (the top of the
+// leaf above the query's depth, may_hit), passed to emit; a query outside the grid's extent has none.  The caller
+// takes the hierarchy walk instead when the query's tolerance exceeds g.tol_max.
+template <class Emit>
+__device__ __forceinline__ void cell_candidates(CellView const& g, const float4* __restrict__ leaf_uv, float u, float v,
+                                                float w, float tol, float m8, Emit&& emit)
+{
+    if (!(u >= g.umin && u <= g.umax && v >= g.vmin && v <= g.vmax))
+        return;
+    int64_t const c = int64_t(cell_of(v, g.vmin, g.inv_v, g.gv)) * g.gu + cell_of(u, g.umin, g.inv_u, g.gu);
+    unsigned const b = g.offsets[c], e = g.offsets[c + 1];
+    float const wq = w - tol;
+    for (unsigned j = b; j < e; ++j)
+    {
+        int const leaf = g.list[j];
+        float4 const lb = leaf_uv[kLeafF4 * leaf + 1];
+        float const wc = leaf_uv[kLeafF4 * leaf + 2].x;
+        if (fmaxf(fmaxf(lb.z, lb.w), wc) >= wq && may_hit(leaf_uv, leaf, u, v, m8))
+            emit(leaf);
+    }
+}
+
+// Builds the cell grid of hierarchy h (lbvh.cu); leaves g invalid when a grid does not apply.
+int build_cells(Context& ctx, const Hier& h, float scene_scale, CellGrid& g);
+
 // Orthonormal frame whose third row is dir / |dir|.
 Frame64 ray_frame(const double* dir);
 

@@ -415,22 +415,6 @@ __global__ void __launch_bounds__(kTravBlock) k_traverse(const BvhNode* __restri
 // and they go through the same conditions -- top of the leaf above the query's depth, may_hit -- and the same
 // decision, so the counts are the walk's.  Neighbouring rays share cells, so the lists and leaves are read
 // coherently, and there is no stack.
-struct CellView
-{
-    const unsigned* offsets;
-    const int* list;
-    int gu, gv;
-    float umin, vmin, umax, vmax, inv_u, inv_v;
-    float tol_max;
-};
-
-// Cell column / row of a coordinate: monotone in x, so a point inside a widened box maps into the box's cells.
-__device__ __forceinline__ int cell_of(float x, float lo, float inv, int g)
-{
-    int const i = int(floorf((x - lo) * inv));
-    return i < 0 ? 0 : (i >= g ? g - 1 : i);
-}
-
 // Order-preserving encodings of floats as unsigned (for atomic min / max).
 __device__ __forceinline__ unsigned f2o(float x)
 {
@@ -557,24 +541,7 @@ __global__ void __launch_bounds__(kTravBlock) k_cells(const BvhNode* __restrict_
             cand[nc++] = leaf;
         };
         if (tol <= g.tol_max)
-        {
-            // outside the grid no widened box reaches the point: no leaf can be hit
-            if (u >= g.umin && u <= g.umax && v >= g.vmin && v <= g.vmax)
-            {
-                int64_t const c =
-                    int64_t(cell_of(v, g.vmin, g.inv_v, g.gv)) * g.gu + cell_of(u, g.umin, g.inv_u, g.gu);
-                unsigned const b = g.offsets[c], e = g.offsets[c + 1];
-                float const wq = w - tol;
-                for (unsigned j = b; j < e; ++j)
-                {
-                    int const leaf = g.list[j];
-                    float4 const lb = leaf_uv[kLeafF4 * leaf + 1];
-                    float const wc = leaf_uv[kLeafF4 * leaf + 2].x;
-                    if (fmaxf(fmaxf(lb.z, lb.w), wc) >= wq && may_hit(leaf_uv, leaf, u, v, m8))
-                        consider(leaf);
-                }
-            }
-        }
+            cell_candidates(g, leaf_uv, u, v, w, tol, m8, consider);
         else if (!hier_walk(nodes, leaf_uv, u, v, w, tol, m8, consider))
             atomicOr(flags + FLAG_STACK, 1);
         for (int j = 0; j < nc; ++j)
@@ -836,7 +803,7 @@ int ray_hierarchy(Context& ctx, const Bvh& bvh, const T* dir_host)
 // widened boxes' extent.  Leaf boxes are widened by 4 * 2^-18 of the scene scale; a query takes the grid while its
 // own tolerance (qmax + scene) * 2^-18 stays below 3.5 * 2^-18 of the scene scale (qmax <= 2.5 * scene), which
 // leaves room for the one-ulp difference between the corners and the walk's outward-rounded boxes.
-static int build_cells(Context& ctx, const Hier& h, float scene_scale, CellGrid& g)
+int build_cells(Context& ctx, const Hier& h, float scene_scale, CellGrid& g)
 {
     g.valid = false;
     int64_t const n = h.n_tri;
@@ -931,8 +898,7 @@ int integer_run(Context& ctx, const Bvh& bvh, const T* d_pos, int64_t n, int32_t
         AGWN_TRY(build_cells(ctx, ctx.ray_cache.h, float(bvh.scene_scale), cg));
     if (ctx.integer_cells && bvh.n_tri > 1 && cg.valid)
     {
-        CellView v{static_cast<const unsigned*>(cg.offsets.ptr), static_cast<const int*>(cg.list.ptr), cg.gu, cg.gv,
-                   cg.umin, cg.vmin, cg.umax, cg.vmax, cg.inv_u, cg.inv_v, cg.tol_max};
+        CellView const v = cell_view(cg);
         AGWN_TRY(ctx.launch_begin(AGWN_K_INTEGER));
         k_cells<T><<<grid, block, 0, ctx.stream>>>(static_cast<const BvhNode*>(ctx.ray_cache.h.nodes.ptr),
                                                   static_cast<const T*>(ctx.ray_cache.h.tri.ptr),

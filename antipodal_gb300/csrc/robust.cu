@@ -57,6 +57,7 @@ void robust_free(Robust* r)
     if (r->seg)
         cudaFree(r->seg);
     r->tri = r->seg = nullptr;
+    r->cells.release();
     r->hier.release();
 }
 
@@ -191,12 +192,26 @@ int robust_run(Context& ctx, const Robust& r, const T* d_pos, int64_t n, T* d_ou
         for (int k = 0; k < 9; ++k)
             f.r[k] = r.hier.frame[k];
         int const grid = int(std::min<int64_t>(div_up(n, kRobBlock), int64_t(ctx.sm_count) * 16));
+        if (ctx.integer_cells && r.n_tri > 1 && !r.cells.valid)
+            AGWN_TRY(build_cells(ctx, r.hier, float(r.hier.scale), r.cells));
+        if (ctx.integer_cells && r.n_tri > 1 && r.cells.valid)
+        {
+            AGWN_TRY(ctx.launch_begin(AGWN_K_ROBUST));
+            k_robust_cells<T, P><<<grid, kRobBlock, 0, st>>>(
+                static_cast<const BvhNode*>(r.hier.nodes.ptr), static_cast<const C*>(r.tri),
+                static_cast<const float4*>(r.hier.leaf_uv.ptr), float(r.hier.scale), f, cell_view(r.cells), qz, d_pos,
+                n, d_counts, ctx.d_flags);
+            AGWN_TRY(ctx.launch_end(AGWN_K_ROBUST));
+        }
+        else
+        {
         AGWN_TRY(ctx.launch_begin(AGWN_K_ROBUST));
         k_robust_count<T, P><<<grid, kRobBlock, 0, st>>>(
             static_cast<const BvhNode*>(r.hier.nodes.ptr), static_cast<const C*>(r.tri),
             static_cast<const float4*>(r.hier.leaf_uv.ptr), r.n_tri, float(r.hier.scale), f, qz, d_pos, n, d_counts,
             ctx.d_flags);
         AGWN_TRY(ctx.launch_end(AGWN_K_ROBUST));
+        }
     }
     using Seg = RSeg<C>;
     if constexpr (std::is_same_v<P, PF> && std::is_same_v<T, double>)

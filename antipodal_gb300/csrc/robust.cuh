@@ -428,6 +428,50 @@ __global__ void __launch_bounds__(kRobBlock) k_robust_count(const BvhNode* __res
     }
 }
 
+// k_robust_count with the candidate leaves read from the cell grid of the evaluator's hierarchy (the walk for
+// queries beyond the grid's tolerance): the same leaves decided by the same exact predicate, the same counts.
+template <class T, class P>
+__global__ void __launch_bounds__(kRobBlock) k_robust_cells(const BvhNode* __restrict__ nodes,
+                                                            const typename P::C* __restrict__ tri,
+                                                            const float4* __restrict__ leaf_uv, float scene_scale,
+                                                            Frame32 f, CellView g, Quant qz,
+                                                            const T* __restrict__ pos, int64_t n,
+                                                            int32_t* __restrict__ counts, int* flags)
+{
+    using C = typename P::C;
+    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+    {
+        qv3<C> const q = quantize<P>(double(pos[3 * i]), double(pos[3 * i + 1]), double(pos[3 * i + 2]), qz);
+        float const ox = float(P::cdbl(q.x)), oy = float(P::cdbl(q.y)), oz = float(P::cdbl(q.z));
+        float const u = f.r[0] * ox + f.r[1] * oy + f.r[2] * oz;
+        float const v = f.r[3] * ox + f.r[4] * oy + f.r[5] * oz;
+        float const w = f.r[6] * ox + f.r[7] * oy + f.r[8] * oz;
+        float const qmax = fmaxf(fmaxf(fabsf(ox), fabsf(oy)), fabsf(oz));
+        float const tol = (qmax + scene_scale) * 3.8146973e-6f + 1e-30f;
+        float const m8 = 8.0f * 1e-6f * (qmax + scene_scale);
+        int sum = 0;
+        int cand[kRobCand];
+        int nc = 0;
+        auto const consider = [&](int leaf)
+        {
+            if (nc == kRobCand)
+            {
+                for (int j = 0; j < kRobCand; ++j)
+                    sum += robust_crossing<P>(q, tri + 9 * int64_t(cand[j]));
+                nc = 0;
+            }
+            cand[nc++] = leaf;
+        };
+        if (tol <= g.tol_max)
+            cell_candidates(g, leaf_uv, u, v, w, tol, m8, consider);
+        else if (!hier_walk(nodes, leaf_uv, u, v, w, tol, m8, consider))
+            atomicOr(flags + FLAG_STACK, 1);
+        for (int j = 0; j < nc; ++j)
+            sum += robust_crossing<P>(q, tri + 9 * int64_t(cand[j]));
+        counts[i] = sum;
+    }
+}
+
 template <class P>
 __device__ __forceinline__ double l_plus_x(qv3<typename P::C> v, double l)
 {

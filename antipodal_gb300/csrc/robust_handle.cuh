@@ -18,6 +18,7 @@ struct Robust
     void* tri = nullptr; // predicate triangles in leaf order
     void* seg = nullptr; // quantised, swapped boundary segments
     Hier hier;
+    mutable CellGrid cells; // the integer term's cell grid over hier, built on first use
 };
 } // namespace agwn
 

@@ -584,7 +584,10 @@ def run_robust(args, ag, torch, stream, disp, timed):
               "queries_over_1e-7": int((d > 1e-7).sum().item()),
               "counts_identical_to_exact": bool(torch.equal(cnt, exact["cnt"])),
               "sample_max_abs_err_vs_cpu_oracle": float(np.abs(out.cpu().numpy()[pick] - exact["gw"]).max()),
-              "fp64_pair_fraction": st["fp64_pairs"] / max(1, st["pairs"])}
+              "fp64_pair_fraction": st["fp64_pairs"] / max(1, st["pairs"]),
+              "kernels_ms_per_step": {"counts (robust predicates)": st["kernel_ms"]["robust"],
+                                      "fractional (mixed)": st["kernel_ms"]["fractional"],
+                                      "other": st["kernel_ms"]["other"]}}
     r.close()
     rate, m = _cpu_sample_rate(lambda m: o.robust_eval("exact_float", v, i, b, q[:m]), Q, args.cpu_seconds)
     return {"metric": METRIC, "value": chosen["value"], "unit": "queries/s", "ms_per_step": ms,

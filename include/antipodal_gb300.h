@@ -70,7 +70,8 @@ enum agwn_option
     AGWN_OPT_MIXED_TAU = 1,
     /* Queries owned by each thread in the fractional kernels (1, 2, 4 or 8).  Default 2. */
     AGWN_OPT_QUERIES_PER_THREAD = 2,
-    /* Threads per block of the fractional kernels (64..256, a multiple of 32).  Default 128. */
+    /* Threads per block of the fractional kernels (64..256, a multiple of 32), or 0 (default): 128, and 256 for the
+       mixed kernel when the boundary spans more than one segment tile (more queries share each staged tile). */
     AGWN_OPT_FRAC_BLOCK = 3,
     /* Record CUDA events around the library's kernels and accumulate their device time (0/1).  Default 0. */
     AGWN_OPT_TIMING = 4,

@@ -190,3 +190,28 @@ def test_robust_mixed_exact_float_matches_exact(gwn, disp):
         for k in (0, 2):
             d = np.abs(outs["exact"][k] - outs["mixed"][k])
             assert d.max() <= 1e-7, (kind, k, d.max())
+
+
+@pytest.mark.parametrize("pol", ["int64_grid", "int128_grid", "exact_float"])
+def test_robust_counts_cells_equal_the_walk(gwn, pol):
+    """The robust counts with candidate leaves from the cell grid (default) and from the hierarchy walk (option 0):
+    identical, on grid points, points on vertices and edges, points near the surface and far away."""
+    from antipodal_gb300 import _lib
+    rng = np.random.default_rng(31)
+    v, i = synth.noisy_mesh("torus", 4000, 5, rng)
+    b = synth.boundary_segments(v, i)
+    tri = i.reshape(-1, 3)[rng.integers(len(i) // 3, size=400)]
+    q = np.concatenate([synth.grid_queries(v.min(0), v.max(0), 22), v[rng.integers(len(v), size=400)],
+                        0.5 * (v[tri[:, 0]] + v[tri[:, 1]]), v[rng.integers(len(v), size=400)] + rng.normal(0, 1e-7, (400, 3)),
+                        rng.uniform(-30, 30, size=(400, 3))])
+    with gwn.CudaDispatcher() as d:
+        r = gwn.CudaRobustMeshGwn(d, v, i, b, precision=pol)
+        got = {}
+        for cells in (1, 0):
+            d.set_option(_lib.OPT_INTEGER_CELLS, cells)
+            o, c = np.empty(len(q)), np.empty(len(q), np.int32)
+            r.evaluate(q, o, c)
+            got[cells] = (o, c)
+        r.close()
+    assert np.array_equal(got[1][1], got[0][1])
+    assert np.array_equal(got[1][0], got[0][0])
