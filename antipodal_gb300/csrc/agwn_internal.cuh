@@ -138,7 +138,8 @@ struct Context
     RayCache ray_cache;
     // host-array pipeline (mesh batch): upload and download streams and their events, created on first use
     cudaStream_t copy_in = nullptr, copy_out = nullptr;
-    cudaEvent_t pipe_ev[6] = {};
+    cudaStream_t compute2 = nullptr; // the host-array pipeline runs alternate chunks' kernels here
+    cudaEvent_t pipe_ev[8] = {};
     int ensure_pipeline();
 
     // options

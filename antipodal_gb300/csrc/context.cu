@@ -151,6 +151,8 @@ int Context::ensure_pipeline()
         AGWN_TRY_CUDA(cudaStreamCreateWithFlags(&copy_in, cudaStreamNonBlocking));
     if (!copy_out)
         AGWN_TRY_CUDA(cudaStreamCreateWithFlags(&copy_out, cudaStreamNonBlocking));
+    if (!compute2)
+        AGWN_TRY_CUDA(cudaStreamCreateWithFlags(&compute2, cudaStreamNonBlocking));
     for (cudaEvent_t& e : pipe_ev)
         if (!e)
             AGWN_TRY_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
@@ -305,6 +307,8 @@ int agwn_context_destroy(agwn_context* ctx)
         cudaStreamDestroy(ctx->copy_in);
     if (ctx->copy_out)
         cudaStreamDestroy(ctx->copy_out);
+    if (ctx->compute2)
+        cudaStreamDestroy(ctx->compute2);
     if (ctx->own_stream && ctx->stream)
         cudaStreamDestroy(ctx->stream);
     delete ctx;

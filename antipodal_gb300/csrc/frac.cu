@@ -282,37 +282,63 @@ int mesh_batch_pipelined(Context& ctx, const agwn_bvh* bvh, const T* positions, 
     AGWN_TRY(ctx.scratch_reserve(S_OUT, 2 * sizeof(T) * size_t(chunk), &obuf));
     bool const with_int = bvh && bvh->n_tri > 0;
     if (with_int)
-        AGWN_TRY(ctx.scratch_reserve(S_COUNTS, sizeof(int32_t) * size_t(chunk), reinterpret_cast<void**>(&dcounts)));
+        AGWN_TRY(ctx.scratch_reserve(S_COUNTS, 2 * sizeof(int32_t) * size_t(chunk),
+                                     reinterpret_cast<void**>(&dcounts)));
     cudaEvent_t* const up = ctx.pipe_ev;       // [b]: chunk uploaded into buffer b
     cudaEvent_t* const done = ctx.pipe_ev + 2; // [b]: kernels on buffer b finished
     cudaEvent_t* const down = ctx.pipe_ev + 4; // [b]: results of buffer b downloaded
-    // the copy streams start after everything already queued on the context stream (the staged boundary); the
-    // boundary is prepared once, while the first chunk uploads, and serves every chunk
-    AGWN_TRY_CUDA(cudaEventRecord(done[0], ctx.stream));
+    cudaEvent_t const ready = ctx.pipe_ev[6];  // the staged boundary and its preparation
+    cudaEvent_t const joined = ctx.pipe_ev[7]; // the second compute stream's last kernels
+    // The kernels of chunk i run on compute stream i & 1 (the context's stream and a second one), so the next
+    // chunk's kernels fill the SMs that the end of the current chunk's fractional kernel leaves idle.
+    cudaStream_t const main = ctx.stream;
+    cudaStream_t const cs[2] = {main, ctx.compute2};
+    // the boundary is prepared once, while the first chunk uploads, and serves every chunk
+    AGWN_TRY_CUDA(cudaEventRecord(done[0], main));
     AGWN_TRY_CUDA(cudaStreamWaitEvent(ctx.copy_in, done[0], 0));
     FracPlan<T> plan;
     AGWN_TRY(fractional_prepare<T>(ctx, x0, dseg, want_frac ? n_seg : 0, &plan));
+    if (with_int && n >= 1)
+        AGWN_TRY(integer_prepare<T>(ctx, *bvh, x0)); // the hierarchy and its cell grid, built on the main stream
+    AGWN_TRY_CUDA(cudaEventRecord(ready, main));
+    AGWN_TRY_CUDA(cudaStreamWaitEvent(cs[1], ready, 0));
     int64_t const n_chunks = (n + chunk - 1) / chunk;
-    for (int64_t i = 0; i < n_chunks; ++i)
+    int rc = AGWN_OK;
+    for (int64_t i = 0; i < n_chunks && rc == AGWN_OK; ++i)
     {
         int const b = int(i & 1);
         int64_t const q0 = i * chunk, m = std::min(chunk, n - q0);
         T* const qb = static_cast<T*>(qbuf) + size_t(b) * 3 * chunk;
         T* const ob = static_cast<T*>(obuf) + size_t(b) * chunk;
+        int32_t* const cb = with_int ? dcounts + size_t(b) * chunk : nullptr;
         if (i >= 2)
             AGWN_TRY_CUDA(cudaStreamWaitEvent(ctx.copy_in, done[b], 0));
         AGWN_TRY_CUDA(cudaMemcpyAsync(qb, positions + 3 * q0, sizeof(T) * 3 * m, cudaMemcpyHostToDevice, ctx.copy_in));
         AGWN_TRY_CUDA(cudaEventRecord(up[b], ctx.copy_in));
-        AGWN_TRY_CUDA(cudaStreamWaitEvent(ctx.stream, up[b], 0));
+        AGWN_TRY_CUDA(cudaStreamWaitEvent(cs[b], up[b], 0));
         if (i >= 2)
-            AGWN_TRY_CUDA(cudaStreamWaitEvent(ctx.stream, down[b], 0));
+            AGWN_TRY_CUDA(cudaStreamWaitEvent(cs[b], down[b], 0));
+        ctx.stream = cs[b]; // the launches below go to this chunk's compute stream
         if (with_int)
-            AGWN_TRY(integer_run<T>(ctx, *bvh, qb, m, dcounts, x0));
-        AGWN_TRY(fractional_launch<T>(ctx, plan, qb, m, ob, with_int ? dcounts : nullptr));
-        AGWN_TRY_CUDA(cudaEventRecord(done[b], ctx.stream));
+            rc = integer_run<T>(ctx, *bvh, qb, m, cb, x0);
+        if (rc == AGWN_OK)
+            rc = fractional_launch<T>(ctx, plan, qb, m, ob, cb);
+        ctx.stream = main;
+        if (rc != AGWN_OK)
+            break;
+        AGWN_TRY_CUDA(cudaEventRecord(done[b], cs[b]));
         AGWN_TRY_CUDA(cudaStreamWaitEvent(ctx.copy_out, done[b], 0));
         AGWN_TRY_CUDA(cudaMemcpyAsync(out + q0, ob, sizeof(T) * m, cudaMemcpyDeviceToHost, ctx.copy_out));
         AGWN_TRY_CUDA(cudaEventRecord(down[b], ctx.copy_out));
+    }
+    // the main stream continues after everything of the second one
+    AGWN_TRY_CUDA(cudaEventRecord(joined, cs[1]));
+    AGWN_TRY_CUDA(cudaStreamWaitEvent(main, joined, 0));
+    if (rc != AGWN_OK)
+    {
+        cudaStreamSynchronize(ctx.copy_out);
+        cudaStreamSynchronize(main);
+        return rc;
     }
     AGWN_TRY_CUDA(cudaStreamSynchronize(ctx.copy_out));
     return ctx.check_flags();

@@ -33,6 +33,9 @@ int frac_mixed_robust_pf(Context& ctx, const double* d_pos, int64_t n, double* d
 // Integer term over a BVH for `n` device-resident queries.
 template <class T>
 int integer_run(Context& ctx, const Bvh& bvh, const T* d_pos, int64_t n, int32_t* d_counts, const T* dir_host);
+// The hierarchy along dir_host and its cell grid (when enabled), built on ctx.stream unless cached.
+template <class T>
+int integer_prepare(Context& ctx, const Bvh& bvh, const T* dir_host);
 } // namespace agwn
 
 struct agwn_bvh : agwn::Bvh

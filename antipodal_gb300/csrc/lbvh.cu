@@ -878,6 +878,21 @@ int build_cells(Context& ctx, const Hier& h, float scene_scale, CellGrid& g)
 }
 
 template <class T>
+int integer_prepare(Context& ctx, const Bvh& bvh, const T* dir_host)
+{
+    if (bvh.n_tri == 0)
+        return AGWN_OK;
+    AGWN_TRY(ray_hierarchy<T>(ctx, bvh, dir_host));
+    CellGrid& cg = ctx.ray_cache.cells;
+    if (ctx.integer_cells && bvh.n_tri > 1 && !cg.valid)
+        AGWN_TRY(build_cells(ctx, ctx.ray_cache.h, float(bvh.scene_scale), cg));
+    return AGWN_OK;
+}
+
+template int integer_prepare<double>(Context&, const Bvh&, const double*);
+template int integer_prepare<float>(Context&, const Bvh&, const float*);
+
+template <class T>
 int integer_run(Context& ctx, const Bvh& bvh, const T* d_pos, int64_t n, int32_t* d_counts, const T* dir_host)
 {
     if (n == 0)
@@ -887,15 +902,13 @@ int integer_run(Context& ctx, const Bvh& bvh, const T* d_pos, int64_t n, int32_t
         AGWN_TRY_CUDA(cudaMemsetAsync(d_counts, 0, sizeof(int32_t) * n, ctx.stream));
         return AGWN_OK;
     }
-    AGWN_TRY(ray_hierarchy<T>(ctx, bvh, dir_host));
+    AGWN_TRY(integer_prepare<T>(ctx, bvh, dir_host));
     Frame32 f;
     for (int k = 0; k < 9; ++k)
         f.r[k] = ctx.ray_cache.h.frame[k];
     int const block = kTravBlock;
     int const grid = int(std::min<int64_t>(div_up(n, block), int64_t(ctx.sm_count) * 16));
     CellGrid& cg = ctx.ray_cache.cells;
-    if (ctx.integer_cells && bvh.n_tri > 1 && !cg.valid)
-        AGWN_TRY(build_cells(ctx, ctx.ray_cache.h, float(bvh.scene_scale), cg));
     if (ctx.integer_cells && bvh.n_tri > 1 && cg.valid)
     {
         CellView const v = cell_view(cg);
