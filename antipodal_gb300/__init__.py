@@ -115,14 +115,15 @@ class CudaDispatcher:
     accumulation and FP64 near / ill-conditioned / branch-cut pairs; double inputs), ``tau`` (mixed mode
     near-pair ratio), ``term_err`` (mixed mode per-pair FP32 error bound, radians),
     ``queries_per_thread``, ``block`` (0: automatic) and ``seg_tile`` (kernel shape), ``timing`` (CUDA-event
-    kernel timing).
+    kernel timing), ``mixed_min_pairs`` (below this many (query, segment) pairs per call the mixed modes run the
+    exact kernels; None keeps the library default, 2^20).
     Like PoolDispatcher it runs one job at a time.  ``parallel_for`` is not provided: arbitrary host callables
     have no device form here, and the library has no CPU fallback.
     """
 
     def __init__(self, device: int = 0, stream=None, precision: str = "exact", tau: float = 4.0,
                  term_err: float = 3e-8, queries_per_thread: int = 2, block: int = 0, seg_tile: int = 512,
-                 timing: bool = False):
+                 timing: bool = False, mixed_min_pairs: float | None = None):
         lib = library()
         handle = None
         if stream is not None:
@@ -140,6 +141,8 @@ class CudaDispatcher:
         self.set_option(_lib.OPT_FRAC_BLOCK, block)
         self.set_option(_lib.OPT_SEG_TILE, seg_tile)
         self.set_option(_lib.OPT_TIMING, 1 if timing else 0)
+        if mixed_min_pairs is not None:
+            self.set_option(_lib.OPT_MIXED_MIN_PAIRS, mixed_min_pairs)
 
     @property
     def handle(self):

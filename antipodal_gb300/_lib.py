@@ -20,7 +20,8 @@ STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA runtime error", 3: "out of de
           4: "BVH traversal stack exhausted", 5: "device wait timed out", 6: "unsupported", 7: "no CUDA device"}
 
 OPT_FRAC_MODE, OPT_MIXED_TAU, OPT_QUERIES_PER_THREAD, OPT_FRAC_BLOCK, OPT_TIMING, OPT_SEG_TILE, \
-    OPT_MIXED_TERM_ERR, OPT_ROBUST_MODE, OPT_ROBUST_TERM_ERR, OPT_PARAM_MODE, OPT_INTEGER_CELLS = range(11)
+    OPT_MIXED_TERM_ERR, OPT_ROBUST_MODE, OPT_ROBUST_TERM_ERR, OPT_PARAM_MODE, OPT_INTEGER_CELLS, \
+    OPT_MIXED_MIN_PAIRS = range(12)
 ROBUST_EXACT, ROBUST_MIXED = 0, 1
 PARAM_EXACT, PARAM_MIXED = 0, 1
 FRAC_EXACT, FRAC_MIXED = 0, 1

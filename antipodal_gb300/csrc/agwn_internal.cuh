@@ -152,6 +152,7 @@ struct Context
     const agwn_mlp* panel_mlp = nullptr; // the per-panel network of the double-float integrator (or none)
     float panel_beta = 0.02f;
     int integer_cells = 1;
+    double mixed_min_pairs = double(1 << 20);
     int queries_per_thread = 2;
     int frac_block = 0; // 0: chosen per launch (frac.cu)
     int seg_tile = 512;

@@ -372,6 +372,10 @@ int agwn_context_set_option(agwn_context* ctx, int option, double value)
         AGWN_CHECK_ARG(value == 0 || value == 1, "integer cells must be 0 or 1");
         ctx->integer_cells = int(value);
         return AGWN_OK;
+    case AGWN_OPT_MIXED_MIN_PAIRS:
+        AGWN_CHECK_ARG(std::isfinite(value) && value >= 0.0, "mixed minimum pairs must be finite and >= 0");
+        ctx->mixed_min_pairs = value;
+        return AGWN_OK;
     default:
         return fail(AGWN_ERR_INVALID, "unknown option %d", option);
     }
@@ -414,6 +418,9 @@ int agwn_context_get_option(agwn_context* ctx, int option, double* value)
         return AGWN_OK;
     case AGWN_OPT_INTEGER_CELLS:
         *value = ctx->integer_cells;
+        return AGWN_OK;
+    case AGWN_OPT_MIXED_MIN_PAIRS:
+        *value = ctx->mixed_min_pairs;
         return AGWN_OK;
     default:
         return fail(AGWN_ERR_INVALID, "unknown option %d", option);

@@ -80,10 +80,13 @@ struct FracPlan
     Frame* frame = nullptr;
 };
 
-// force_mixed: the mixed form whatever the context's fractional mode (double only).
+// n_queries: the queries the plan will serve.  Below ctx.mixed_min_pairs (query, segment) pairs the mixed mode runs
+// the exact kernels: its one-block boundary preparation would cost more than the FP64 pairs it saves (a 4-segment
+// boundary with 1e5 queries: 0.21 ms mixed, 0.17 ms exact), and the exact form is the more accurate one.
+// force_mixed: the mixed form whatever the context's fractional mode and the size (double only).
 template <class T>
-int fractional_prepare(Context& ctx, const T* x0_host, const T* d_seg_raw, int64_t n_seg, FracPlan<T>* plan,
-                       bool force_mixed = false)
+int fractional_prepare(Context& ctx, const T* x0_host, const T* d_seg_raw, int64_t n_seg, int64_t n_queries,
+                       FracPlan<T>* plan, bool force_mixed = false)
 {
     FracPlan<T>& p = *plan;
     p = FracPlan<T>{};
@@ -96,7 +99,8 @@ int fractional_prepare(Context& ctx, const T* x0_host, const T* d_seg_raw, int64
     if (n_seg == 0)
         return AGWN_OK;
     AGWN_CHECK_ARG(n_seg < (int64_t(1) << 31), "at most 2^31 - 1 boundary segments");
-    p.mixed = (force_mixed || ctx.frac_mode == AGWN_FRAC_MIXED) && sizeof(T) == 8;
+    p.mixed = (force_mixed || (ctx.frac_mode == AGWN_FRAC_MIXED && double(n_queries) * double(n_seg) >= ctx.mixed_min_pairs)) &&
+              sizeof(T) == 8;
     if (!p.mixed)
     {
         p.tile = int(std::min<int64_t>(ctx.seg_tile, n_seg));
@@ -235,7 +239,7 @@ int fractional_run(Context& ctx, const T* d_pos, int64_t n, T* d_out, const int3
     if (n == 0)
         return AGWN_OK;
     FracPlan<T> plan;
-    AGWN_TRY(fractional_prepare<T>(ctx, x0_host, d_seg_raw, n_seg, &plan));
+    AGWN_TRY(fractional_prepare<T>(ctx, x0_host, d_seg_raw, n_seg, n, &plan));
     return fractional_launch<T>(ctx, plan, d_pos, n, d_out, d_counts);
 }
 
@@ -253,7 +257,7 @@ int frac_mixed_robust_pf(Context& ctx, const double* d_pos, int64_t n, double* d
     // numerator and l + x denominator)
     double const x0[3] = {-1.0, 0.0, 0.0};
     FracPlan<double> plan;
-    AGWN_TRY(fractional_prepare<double>(ctx, x0, d_raw, n_seg, &plan, true));
+    AGWN_TRY(fractional_prepare<double>(ctx, x0, d_raw, n_seg, n, &plan, true));
     if (n_seg == 0)
         return fractional_launch<double>(ctx, plan, d_pos, n, d_out, d_counts);
     return fractional_launch_mixed(ctx, plan, d_pos, n, d_out, d_counts,
@@ -297,7 +301,7 @@ int mesh_batch_pipelined(Context& ctx, const agwn_bvh* bvh, const T* positions, 
     AGWN_TRY_CUDA(cudaEventRecord(done[0], main));
     AGWN_TRY_CUDA(cudaStreamWaitEvent(ctx.copy_in, done[0], 0));
     FracPlan<T> plan;
-    AGWN_TRY(fractional_prepare<T>(ctx, x0, dseg, want_frac ? n_seg : 0, &plan));
+    AGWN_TRY(fractional_prepare<T>(ctx, x0, dseg, want_frac ? n_seg : 0, n, &plan));
     if (with_int && n >= 1)
         AGWN_TRY(integer_prepare<T>(ctx, *bvh, x0)); // the hierarchy and its cell grid, built on the main stream
     AGWN_TRY_CUDA(cudaEventRecord(ready, main));

@@ -217,7 +217,9 @@ int robust_run(Context& ctx, const Robust& r, const T* d_pos, int64_t n, T* d_ou
     if constexpr (std::is_same_v<P, PF> && std::is_same_v<T, double>)
     {
         // mixed exact_float: the mesh functions' mixed kernel with the robust FP64 rule (frac.cu)
-        if (ctx.robust_mode == AGWN_ROBUST_MIXED && r.n_seg > 0 && r.n_seg < (int64_t(1) << 24))
+        // (below ctx.mixed_min_pairs pairs the exact kernel is the faster one, as for the mesh functions)
+        if (ctx.robust_mode == AGWN_ROBUST_MIXED && r.n_seg > 0 && r.n_seg < (int64_t(1) << 24) &&
+            double(n) * double(r.n_seg) >= ctx.mixed_min_pairs)
         {
             double* raw = nullptr;
             AGWN_TRY(ctx.scratch_reserve(S_MISC2, sizeof(double) * 7 * size_t(r.n_seg), reinterpret_cast<void**>(&raw)));

@@ -96,7 +96,11 @@ enum agwn_option
     /* Integer term of the mesh functions (intersector of more than one triangle): 1 (default) looks up each ray's
        candidate triangles in a uniform grid over the plane across the ray direction, built once per (intersector,
        direction) and cached with the hierarchy; 0 walks the hierarchy for every ray.  Counts are the same. */
-    AGWN_OPT_INTEGER_CELLS = 10
+    AGWN_OPT_INTEGER_CELLS = 10,
+    /* Mixed modes (mesh, and the robust evaluator's exact_float): below this many (query, segment) pairs in one
+       call the exact FP64 kernels run instead, which are the faster ones there (the mixed form's boundary
+       preparation costs more than the FP64 pairs it saves).  Default 2^20; 0 always runs the mixed form. */
+    AGWN_OPT_MIXED_MIN_PAIRS = 11
 };
 enum agwn_param_mode
 {

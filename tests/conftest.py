@@ -39,6 +39,7 @@ def gwn():
 
 @pytest.fixture()
 def disp(gwn):
-    d = gwn.CudaDispatcher(device=0)
+    # the mixed kernels run at every size here (by default they start at 2^20 pairs per call)
+    d = gwn.CudaDispatcher(device=0, mixed_min_pairs=0)
     yield d
     d.close()

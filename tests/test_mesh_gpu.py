@@ -107,7 +107,7 @@ def test_segment_tiles_and_queries_per_thread(gwn, oracle, n_seg, qpt):
     segs = np.concatenate([a, a + rng.normal(0, 0.05, size=(n_seg, 3)), np.ones((n_seg, 1))], axis=1)
     x0 = synth.unit_x0()
     ref = oracle.frac_batch(q, x0, segs)
-    with gwn.CudaDispatcher(queries_per_thread=qpt, seg_tile=512) as d:
+    with gwn.CudaDispatcher(queries_per_thread=qpt, seg_tile=512, mixed_min_pairs=0) as d:
         out = np.empty(len(q))
         gwn.eval_gwnr_mesh_batch_fractional(d, q, out, x0, segs)
         np.testing.assert_allclose(out, ref, rtol=0, atol=TOL_EXACT64)
@@ -151,7 +151,7 @@ def test_device_resident_tensors(gwn, oracle):
     verts, idx, bnd, q, x0 = synth.rotated_open_cube(seed=2, n_queries=50_000)
     ref = oracle.full_naive(q, x0, verts, idx, bnd)
     dev = torch.device("cuda:0")
-    with gwn.CudaDispatcher(stream=torch.cuda.current_stream()) as d:
+    with gwn.CudaDispatcher(stream=torch.cuda.current_stream(), mixed_min_pairs=0) as d:
         tq = torch.from_numpy(q).to(dev)
         tb = torch.from_numpy(bnd).to(dev)
         tv = torch.from_numpy(verts).to(dev)
@@ -254,7 +254,7 @@ def _polyline(rng, n, closed, centre=(0.0, 0.0, 0.0), radius=1.0):
 
 def _check_mixed(gwn, oracle, q, x0, segs, seg_tile=512, qpt=2):
     ref = oracle.frac_batch(q, x0, segs)
-    with gwn.CudaDispatcher(precision="mixed", queries_per_thread=qpt, seg_tile=seg_tile) as d:
+    with gwn.CudaDispatcher(precision="mixed", queries_per_thread=qpt, seg_tile=seg_tile, mixed_min_pairs=0) as d:
         out = np.empty(len(q))
         gwn.eval_gwnr_mesh_batch_fractional(d, q, out, x0, segs)
     assert np.abs(out - ref).max() <= TOL_MIXED, np.abs(out - ref).max()
@@ -348,3 +348,24 @@ def test_integer_cells_equal_the_walk_and_the_oracle(gwn, oracle, dtype):
             assert np.array_equal(got[1], got[0]), np.flatnonzero(got[1] != got[0])[:10]
             assert np.array_equal(got[1], ref), np.flatnonzero(got[1] != ref)[:10]
         isect.close()
+
+
+def test_mixed_mode_runs_exact_kernels_below_its_minimum(gwn, oracle):
+    # below the minimum pair count (default 2^20 per call) the mixed mode runs the exact kernels: bit-identical to
+    # the exact mode; with the minimum at 0 it runs the mixed kernel (within the mixed tolerance)
+    from antipodal_gb300 import _lib
+    verts, idx, bnd, q, x0 = synth.rotated_open_cube(seed=3, n_queries=20_000)
+    with gwn.CudaDispatcher() as d:
+        assert d.get_option(_lib.OPT_MIXED_MIN_PAIRS) == float(1 << 20)
+        isect = gwn.CudaIntersector(d, verts, idx)
+        outs = {}
+        for prec, minp in (("exact", 1 << 20), ("mixed", 1 << 20), ("mixed", 0)):
+            d.set_precision(prec)
+            d.set_option(_lib.OPT_MIXED_MIN_PAIRS, minp)
+            o = np.empty(len(q))
+            gwn.eval_gwnr_mesh_batch(d, isect, q, o, x0, bnd)
+            outs[(prec, minp)] = o
+        isect.close()
+    assert np.array_equal(outs[("mixed", 1 << 20)], outs[("exact", 1 << 20)])
+    assert np.abs(outs[("mixed", 0)] - outs[("exact", 1 << 20)]).max() <= TOL_MIXED
+    assert np.abs(outs[("exact", 1 << 20)] - oracle.full_naive(q, x0, verts, idx, bnd)).max() <= TOL_EXACT64

@@ -93,7 +93,7 @@ def test_robust_empty_and_device_inputs(gwn, disp):
     g, c, _ = run(gwn, disp, "exact_float", v, i, np.zeros((0, 7)), q)
     assert np.array_equal(c, np.rint(g).astype(np.int32))
     dev = torch.device("cuda:0")
-    with gwn.CudaDispatcher(stream=torch.cuda.current_stream(dev)) as d:
+    with gwn.CudaDispatcher(stream=torch.cuda.current_stream(dev), mixed_min_pairs=0) as d:
         r = gwn.CudaRobustMeshGwn(d, torch.from_numpy(v).to(dev), torch.from_numpy(i).to(dev),
                                   torch.zeros((0, 7), dtype=torch.float64, device=dev))
         out = torch.empty(len(q), dtype=torch.float64, device=dev)

@@ -39,7 +39,7 @@ def test_noalloc_matches_regular_entry_point_on_two_calls(gwn):
     torch = pytest.importorskip("torch")
     dev = torch.device("cuda:0")
     f = _entry(gwn.library())
-    with gwn.CudaDispatcher(stream=torch.cuda.current_stream(dev), precision="mixed") as disp:
+    with gwn.CudaDispatcher(stream=torch.cuda.current_stream(dev), precision="mixed", mixed_min_pairs=0) as disp:
         for q, bnd, x0 in _inputs():
             qd = torch.from_numpy(q).to(dev)
             bd = torch.from_numpy(bnd).to(dev)
