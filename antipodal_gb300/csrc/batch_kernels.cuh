@@ -171,21 +171,9 @@ __global__ void __launch_bounds__(256) k_batch(const BMesh* __restrict__ meshes,
                     }
                     float const* const wb = wts + b * tile;
                     uint32_t const seg0 = uint32_t(int64_t(st) * tile);
-                    for (int s = 0; s < cnt_s; ++s)
-                    {
-                        Seg const sgm = sb[s];
-#pragma unroll
-                        for (int k = 0; k < K; ++k)
-                        {
-                            float th;
-                            bool const ok = robust_pair_f32<P>(q[k], sgm, term_err, &th);
-                            rq_push(fq, !ok, seg0 + uint32_t(s), lane, k);
-                            if (ok)
-                                two_sum_acc(acc[k], comp[k], wb[s] * th);
-                        }
-                        while (fq.tail - fq.head >= 32)
-                            rq_flush<P, K>(fq, 32, lane, gseg, q, half);
-                    }
+                    for (int s = 0; s < cnt_s; s += 2)
+                        robust_mixed_step<P, K>(sb, wb, s, cnt_s - s < 2 ? cnt_s - s : 2, seg0, q, term_err, acc, comp,
+                                                fq, lane, gseg, half);
                     pairs += 32ull * K * unsigned(cnt_s);
                 }
                 else

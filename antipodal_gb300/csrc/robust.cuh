@@ -537,29 +537,38 @@ __device__ __forceinline__ bool robust_pair_f32(qv3<typename P::C> q, RSeg<typen
     unsigned const lim = 1u << 25, off = 1u << 24;
     bool const small = unsigned(v0x) + off < lim && unsigned(v0y) + off < lim && unsigned(v0z) + off < lim &&
                        unsigned(v1x) + off < lim && unsigned(v1y) + off < lim && unsigned(v1z) + off < lim;
-    if (!small || (long long)v0z * v1y == (long long)v0y * v1z)
+    if (!small)
         return false;
     float const x0 = float(v0x), y0 = float(v0y), z0 = float(v0z);
     float const x1 = float(v1x), y1 = float(v1y), z1 = float(v1z);
+    // num = z0 y1 - y0 z1 by TwoProduct: for integer inputs below 2^24 it is 0 exactly when the exact value is
+    // (a nonzero exact value is at least 1 in magnitude), where the reference takes its exact branches
     float const pn = y0 * z1, en = fmaf(y0, z1, -pn);
     float const numf = fmaf(z0, y1, -pn) - en;
+    if (numf == 0.f)
+        return false;
     float const pz = z0 * z1, ez = fmaf(z0, z1, -pz);
     float const yzf = fmaf(y0, y1, pz) + ez;
     float const yz0 = fmaf(y0, y0, z0 * z0), yz1 = fmaf(y1, y1, z1 * z1);
     float const s0 = fmaf(x0, x0, yz0), s1 = fmaf(x1, x1, yz1);
     float const l0 = s0 * rsqrtf(s0), l1 = s1 * rsqrtf(s1);
-    float const a = x0 >= 0.f ? l0 + x0 : __fdividef(yz0, l0 - x0);
-    float const b = x1 >= 0.f ? l1 + x1 : __fdividef(yz1, l1 - x1);
-    float const ab = a * b;
-    float const den = ab + yzf;
-    float const an = fabsf(numf), ad = fabsf(den);
-    float const inv = __fdividef(1.f, fmaxf(an, ad));
+    // l + x = n / d with (n, d) = (l + x, 1) for x >= 0 and (y^2 + z^2, l - x) for x < 0, the reference's
+    // cancellation-free form; num and den scaled by D = d0 d1 > 0 (the angle is unchanged): den D = n0 n1 + yz D
+    float const n0 = x0 >= 0.f ? l0 + x0 : yz0, d0 = x0 >= 0.f ? 1.f : l0 - x0;
+    float const n1 = x1 >= 0.f ? l1 + x1 : yz1, d1 = x1 >= 0.f ? 1.f : l1 - x1;
+    float const D = d0 * d1, ab = n0 * n1, yzs = yzf * D;
+    float const num_s = numf * D, den_s = ab + yzs;
+    float const an = fabsf(num_s), ad = fabsf(den_s);
+    bool const swap = an > ad;
+    float const inv = __fdividef(1.f, fmaxf(swap ? an : ad, 1e-37f));
     float const an1 = an * inv, ad1 = ad * inv;
+    // the angle errs by about 4u (|num| (|ab| + |yz|) + |den| |num|) / (num^2 + den^2); in units of M = max(|num|,
+    // |den|), with the division by an1^2 + ad1^2 moved to the other side
     constexpr float k4u = 4.f * 5.9604645e-8f;
-    float const bound = k4u * fmaf(an1, (fabsf(ab) + fabsf(yzf)) * inv, ad1 * an1) / fmaf(an1, an1, ad1 * ad1);
-    if (!(bound <= term_err))
+    float const bound = k4u * fmaf(an1, (fabsf(ab) + fabsf(yzs)) * inv, ad1 * an1);
+    if (!(bound <= term_err * fmaf(an1, an1, ad1 * ad1)))
         return false;
-    *theta = atan2_scaled(numf, den, ad1, an1);
+    *theta = atan2_unit(num_s, den_s, swap ? ad1 : an1, swap);
     return true;
 }
 
@@ -577,7 +586,7 @@ __device__ __forceinline__ void tile_weights(Seg const* sb, int cnt, float* w)
 template <int K>
 struct RQueue
 {
-    static constexpr unsigned kCap = 64u * K; // > 31 left over + 32 * K appended per segment
+    static constexpr unsigned kCap = 128u * K; // > 31 left over + 2 * 32 * K appended per pair of segments
     uint32_t* e;
     double* res;
     unsigned head = 0, tail = 0; // warp-uniform
@@ -638,6 +647,50 @@ __device__ __forceinline__ void rq_flush(RQueue<K>& fq, unsigned c, int lane, co
     fq.head += c;
 }
 
+// The FP32 pairs of up to two segments (sb[s], sb[s + 1]; ne of them) with K queries: accepted terms go into the
+// TwoSum accumulators (a turned-down pair adds an exact zero), turned-down pairs are marked in a bit mask and, only
+// when a lane of the warp has one, pushed to the FP64 queue in segment order, which is then drained in full
+// batches.  k_robust_frac and the batch kernel both evaluate their pairs through this, so their sums agree bit for
+// bit.
+template <class P, int K>
+__device__ __forceinline__ void robust_mixed_step(RSeg<typename P::C> const* sb, float const* wb, int s, int ne,
+                                                  uint32_t seg0, qv3<typename P::C> const (&q)[K], float term_err,
+                                                  float (&acc)[K], float (&comp)[K], RQueue<K>& fq, int lane,
+                                                  RSeg<typename P::C> const* gseg, double (&half)[K])
+{
+    uint32_t bits = 0;
+#pragma unroll
+    for (int e = 0; e < 2; ++e)
+    {
+        if (e >= ne)
+            break;
+        RSeg<typename P::C> const sgm = sb[s + e];
+        float const w = wb[s + e];
+#pragma unroll
+        for (int k = 0; k < K; ++k)
+        {
+            float th = 0.f;
+            bool const ok = robust_pair_f32<P>(q[k], sgm, term_err, &th);
+            bits |= ok ? 0u : (1u << (e * K + k));
+            two_sum_acc(acc[k], comp[k], ok ? w * th : 0.f);
+        }
+    }
+    if (__any_sync(0xffffffffu, bits != 0u))
+    {
+#pragma unroll
+        for (int e = 0; e < 2; ++e)
+        {
+            if (e >= ne)
+                break;
+#pragma unroll
+            for (int k = 0; k < K; ++k)
+                rq_push(fq, ((bits >> (e * K + k)) & 1u) != 0u, seg0 + uint32_t(s + e), lane, k);
+        }
+        while (fq.tail - fq.head >= 32)
+            rq_flush<P, K>(fq, 32, lane, gseg, q, half);
+    }
+}
+
 // Mixed = true (int64_grid only): FP32 pairs through robust_pair_f32 with TwoSum accumulation, the others in FP64.
 template <class T, class P, bool Mixed = false>
 __global__ void __launch_bounds__(kRobBlock) k_robust_frac(const T* __restrict__ pos, int64_t n, Quant qz,
@@ -691,7 +744,7 @@ __global__ void __launch_bounds__(kRobBlock) k_robust_frac(const T* __restrict__
         int64_t const ii = i < n ? i : n - 1;
         auto const q = quantize<P>(double(pos[3 * ii]), double(pos[3 * ii + 1]), double(pos[3 * ii + 2]), qz);
         double half = 0.0;
-        float acc = 0.f, comp = 0.f;
+        float acc[1] = {0.f}, comp[1] = {0.f};
         decltype(q) qarr[1] = {q};
         double harr[1] = {0.0};
         for (int st = 0; st < pipe.n_tiles && n_seg > 0; ++st)
@@ -715,17 +768,9 @@ __global__ void __launch_bounds__(kRobBlock) k_robust_frac(const T* __restrict__
                 }
                 float const* wb = wts + b * tile;
                 uint32_t const seg0 = uint32_t(int64_t(st) * tile);
-                for (int s = 0; s < cnt; ++s)
-                {
-                    Seg const sgm = sb[s];
-                    float th;
-                    bool const ok = robust_pair_f32<P>(q, sgm, term_err, &th);
-                    rq_push(fq, !ok, seg0 + uint32_t(s), lane, 0);
-                    if (ok)
-                        two_sum_acc(acc, comp, wb[s] * th);
-                    while (fq.tail - fq.head >= 32)
-                        rq_flush<P, 1>(fq, 32, lane, seg, qarr, harr);
-                }
+                for (int s = 0; s < cnt; s += 2)
+                    robust_mixed_step<P, 1>(sb, wb, s, cnt - s < 2 ? cnt - s : 2, seg0, qarr, term_err, acc, comp, fq,
+                                            lane, seg, harr);
             }
             else
             {
@@ -747,7 +792,7 @@ __global__ void __launch_bounds__(kRobBlock) k_robust_frac(const T* __restrict__
         {
             while (fq.tail != fq.head)
                 rq_flush<P, 1>(fq, min(32u, fq.tail - fq.head), lane, seg, qarr, harr);
-            half = __dadd_rn(harr[0], __dadd_rn(double(acc), double(comp)));
+            half = __dadd_rn(harr[0], __dadd_rn(double(acc[0]), double(comp[0])));
             if (counters && lane == 0)
             {
                 atomicAdd(reinterpret_cast<unsigned long long*>(counters), (unsigned long long)fq.tail);
