@@ -72,7 +72,8 @@ enum scratch_slot
     S_MISC1 = 7,
     S_MISC2 = 8,
     S_MISC3 = 9,
-    S_COUNT = 10
+    S_PARTIAL = 10, // the parametric integrator's per-group partial sums
+    S_COUNT = 11
 };
 
 // A hierarchy over triangles in the frame of one ray direction (built by build_hier, lbvh.cu): internal nodes,

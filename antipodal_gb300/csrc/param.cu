@@ -320,8 +320,18 @@ struct PanelSmem
     float logit[kParamBlock / 32][32][2];
 };
 
-template <bool DF>
-__global__ void __launch_bounds__(kParamBlock) k_param_gk15(const double* __restrict__ pos, int64_t n,
+// DF: double-float panels.  PANEL (DF only): the per-panel network runs (its code and shared memory are compiled
+// only into this instance, so the other instances keep their registers).  n_groups > 1 (DF only): the curve tiles
+// of a query block are split into n_groups consecutive groups, one work item each, and each item writes its raw
+// partial sum to partial[g * n + i] (a later kernel adds the groups in order) and adds its panel counts to
+// nodes_total[i] (zeroed first).
+template <bool DF, bool PANEL>
+constexpr int param_min_blocks()
+{
+    return DF && !PANEL ? 6 : 1; // the double-float panels in 80 registers (no spills), six blocks per SM
+}
+template <bool DF, bool PANEL>
+__global__ void __launch_bounds__(kParamBlock, param_min_blocks<DF, PANEL>()) k_param_gk15(const double* __restrict__ pos, int64_t n,
                                                             double* __restrict__ out, double x0x, double x0y,
                                                             double x0z, const Bez* __restrict__ curves,
                                                             int64_t n_curves, int tile, int min_depth, int max_depth,
@@ -329,7 +339,7 @@ __global__ void __launch_bounds__(kParamBlock) k_param_gk15(const double* __rest
                                                             uint32_t* __restrict__ stats,
                                                             int32_t* __restrict__ nodes_total,
                                                             double* __restrict__ pair_vals, int* flags,
-                                                            ParamExtras ex)
+                                                            ParamExtras ex, int n_groups, double* __restrict__ partial)
 {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ __align__(8) uint64_t bar;
@@ -337,13 +347,15 @@ __global__ void __launch_bounds__(kParamBlock) k_param_gk15(const double* __rest
     __shared__ int s_nodes[kParamBlock];
     Bez* const buf = reinterpret_cast<Bez*>(smem);
     PanelSmem* const ps = reinterpret_cast<PanelSmem*>(smem + size_t(tile) * sizeof(Bez));
-    bool const use_panel = DF && ex.pwb != nullptr;
+    bool const use_panel = PANEL && ex.pwb != nullptr;
     unsigned long long skips = 0;
     double* const slab = pair_vals + size_t(blockIdx.x) * kParamBlock * tile;
     ev3<rd> const x0{rd(x0x), rd(x0y), rd(x0z)};
     df3 const x0df{df_from(x0x), df_from(x0y), df_from(x0z)};
     int64_t const n_blocks_q = (n + kParamBlock - 1) / kParamBlock;
     int const n_tiles = int((n_curves + tile - 1) / tile);
+    int const tiles_per_group = (n_tiles + n_groups - 1) / n_groups;
+    int64_t const n_items = n_blocks_q * n_groups;
     unsigned const lane = threadIdx.x & 31u;
     // tol * 2^-depth by repeated halving, as the recursion computes it (exact unless it reaches subnormals)
     double tol_at[kParamMaxDepth + 1];
@@ -361,13 +373,17 @@ __global__ void __launch_bounds__(kParamBlock) k_param_gk15(const double* __rest
     }
     __syncthreads();
     unsigned phase = 0;
-    for (int64_t qb = blockIdx.x; qb < n_blocks_q; qb += gridDim.x)
+    for (int64_t item = blockIdx.x; item < n_items; item += gridDim.x)
     {
+        int64_t const qb = item / n_groups;
+        int const grp = int(item - qb * n_groups);
+        int const t_begin = grp * tiles_per_group;
+        int const t_end = min(n_tiles, t_begin + tiles_per_group);
         int64_t const q0 = qb * kParamBlock;
         int const nq = int(n - q0 < kParamBlock ? n - q0 : int64_t(kParamBlock));
         rd sum = rd(0.0);
         s_nodes[threadIdx.x] = 0;
-        for (int t = 0; t < n_tiles; ++t)
+        for (int t = t_begin; t < t_end; ++t)
         {
             int64_t const c0 = int64_t(t) * tile;
             int const cnt = int(n_curves - c0 < tile ? n_curves - c0 : int64_t(tile));
@@ -436,7 +452,7 @@ __global__ void __launch_bounds__(kParamBlock) k_param_gk15(const double* __rest
                 if constexpr (DF)
                 {
                     // the per-panel network: up to four rounds of "split it without evaluating", all lanes together
-                    for (int round = 0; use_panel && round < 4; ++round)
+                    for (int round = 0; PANEL && use_panel && round < 4; ++round)
                     {
                         bool const cand = pi >= 0 && d < max_depth;
                         float f[kF];
@@ -558,13 +574,34 @@ __global__ void __launch_bounds__(kParamBlock) k_param_gk15(const double* __rest
         if (int(threadIdx.x) < nq)
         {
             int64_t const i = q0 + threadIdx.x;
-            out[i] = (sum / (rd(4.0) * rd(3.141592653589793238462643383279502884))).v;
-            if (nodes_total)
-                nodes_total[i] = s_nodes[threadIdx.x];
+            if (n_groups == 1)
+            {
+                out[i] = (sum / (rd(4.0) * rd(3.141592653589793238462643383279502884))).v;
+                if (nodes_total)
+                    nodes_total[i] = s_nodes[threadIdx.x];
+            }
+            else
+            {
+                partial[int64_t(grp) * n + i] = sum.v;
+                if (nodes_total)
+                    atomicAdd(&nodes_total[i], s_nodes[threadIdx.x]);
+            }
         }
     }
     if (ex.skip_count && skips)
         atomicAdd(ex.skip_count, skips);
+}
+
+// The groups' partial sums of each query added in group order (so in curve order by tiles), then normalised.
+__global__ void k_param_groups(const double* __restrict__ partial, int n_groups, int64_t n, double* __restrict__ out)
+{
+    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+    {
+        rd sum = rd(0.0);
+        for (int g = 0; g < n_groups; ++g)
+            sum = sum + rd(partial[int64_t(g) * n + i]);
+        out[i] = (sum / (rd(4.0) * rd(3.141592653589793238462643383279502884))).v;
+    }
 }
 } // namespace
 
@@ -598,19 +635,52 @@ int param_run(Context& ctx, const double* d_pos, int64_t n, double* d_out, const
         return AGWN_OK;
     }
     static_assert(sizeof(CurveDF) == sizeof(Bez), "both curve forms stage through the same tile");
-    int const tile = int(std::min<int64_t>(dfm ? kParamTileDF : kParamTileMax, n_curves));
-    size_t const smem = size_t(tile) * sizeof(Bez) + (panel ? sizeof(PanelSmem) : 0);
-    auto const kern = dfm ? k_param_gk15<true> : k_param_gk15<false>;
-    AGWN_TRY_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+    auto const kern = dfm ? (panel ? k_param_gk15<true, true> : k_param_gk15<true, false>) : k_param_gk15<false, false>;
+    int tile = int(std::min<int64_t>(dfm ? kParamTileDF : kParamTileMax, n_curves));
+    size_t smem = 0;
     int per_sm = 0;
-    AGWN_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kParamBlock, smem));
-    if (per_sm < 1)
-        return fail(AGWN_ERR_UNSUPPORTED, "parametric kernel does not fit on an SM");
+    auto shape = [&](int t) -> int
+    {
+        smem = size_t(t) * sizeof(Bez) + (panel ? sizeof(PanelSmem) : 0);
+        AGWN_TRY_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+        AGWN_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kParamBlock, smem));
+        if (per_sm < 1)
+            return fail(AGWN_ERR_UNSUPPORTED, "parametric kernel does not fit on an SM");
+        return AGWN_OK;
+    };
+    AGWN_TRY(shape(tile));
     int64_t const n_blocks_q = (n + kParamBlock - 1) / kParamBlock;
-    int const grid = int(std::max<int64_t>(1, std::min<int64_t>(n_blocks_q, int64_t(per_sm) * ctx.sm_count)));
+    int n_groups = 1;
+    // two waves of work items; tiles of at least 128 curves (measured: more waves or other tiles change <1%)
+    int64_t const waves = 2, min_tile = 128;
+    if (dfm && n_blocks_q < waves * int64_t(per_sm) * ctx.sm_count)
+    {
+        // Few query blocks (a sample of queries, or many curves per query): the curves of each block are split
+        // into groups of tiles, one work item each, so that every SM gets work.  Smaller tiles cost the
+        // double-float kernel nothing (measured flat from 768 down to 128 curves) and let more blocks reside.
+        int64_t const want = div_up(waves * int64_t(per_sm) * ctx.sm_count, n_blocks_q);
+        int64_t const t = div_up(div_up(n_curves, want), 32) * 32;
+        tile = int(std::max<int64_t>(std::min<int64_t>(t, tile), std::min<int64_t>(min_tile, n_curves)));
+        AGWN_TRY(shape(tile));
+        int const n_tiles = int(div_up(n_curves, tile));
+        int64_t const groups =
+            std::min<int64_t>(n_tiles, div_up(waves * int64_t(per_sm) * ctx.sm_count, n_blocks_q));
+        int const tpg = int(div_up(n_tiles, groups));
+        n_groups = int(div_up(n_tiles, tpg));
+    }
+    int64_t const n_items = n_blocks_q * n_groups;
+    int const grid = int(std::max<int64_t>(1, std::min<int64_t>(n_items, int64_t(per_sm) * ctx.sm_count)));
     double* pair_vals = nullptr;
     AGWN_TRY(ctx.scratch_reserve(S_SEGS_RAW, sizeof(double) * size_t(grid) * kParamBlock * tile,
                                  reinterpret_cast<void**>(&pair_vals)));
+    double* partial = nullptr;
+    if (n_groups > 1)
+    {
+        AGWN_TRY(ctx.scratch_reserve(S_PARTIAL, sizeof(double) * size_t(n_groups) * size_t(n),
+                                     reinterpret_cast<void**>(&partial)));
+        if (d_nodes)
+            AGWN_TRY_CUDA(cudaMemsetAsync(d_nodes, 0, sizeof(int32_t) * n, ctx.stream));
+    }
     const void* tile_src = d_curves;
     if (dfm)
     {
@@ -626,8 +696,14 @@ int param_run(Context& ctx, const double* d_pos, int64_t n, double* d_out, const
     kern<<<grid, kParamBlock, smem, ctx.stream>>>(d_pos, n, d_out, x0[0], x0[1], x0[2],
                                                  reinterpret_cast<const Bez*>(tile_src), n_curves, tile, min_depth,
                                                  max_depth, tol, d_start, d_stats, d_nodes, pair_vals, ctx.d_flags,
-                                                 ex);
-    return ctx.launch_end(AGWN_K_PARAMETRIC);
+                                                 ex, n_groups, partial);
+    AGWN_TRY(ctx.launch_end(AGWN_K_PARAMETRIC));
+    if (n_groups == 1)
+        return AGWN_OK;
+    AGWN_TRY(ctx.launch_begin(AGWN_K_OTHER));
+    k_param_groups<<<int(std::min<int64_t>(div_up(n, 256), 8 * ctx.sm_count)), 256, 0, ctx.stream>>>(partial, n_groups,
+                                                                                                     n, d_out);
+    return ctx.launch_end(AGWN_K_OTHER);
 }
 } // namespace agwn
 
