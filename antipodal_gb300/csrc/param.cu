@@ -234,35 +234,19 @@ __device__ __forceinline__ double gk15_panel_df(const df (&cp)[12], df3 x0, int 
     float const h = 0.5f * scale;
     df const cc = two_sum(float(j) * scale, h); // both exact: the centre (j + 1/2) 2^-depth
     df const f0 = integrand_df(cp, x0, cc);
-    df fm[8], fp[8];
+    // the Kronrod and Gauss sums accumulated node pair by node pair, in the order of the sums above (the same
+    // values), so no node value stays live
+    df ig = kGkWgdf[0] * f0;
+    df ik = kGkWkdf[0] * f0;
 #pragma unroll 1
     for (int k = 1; k <= 7; ++k)
     {
         df const dx = df_scale(kGkXdf[k], h);
-        fm[k] = integrand_df(cp, x0, cc - dx);
-        fp[k] = integrand_df(cp, x0, cc + dx);
+        df const s = integrand_df(cp, x0, cc - dx) + integrand_df(cp, x0, cc + dx);
+        ik = ik + kGkWkdf[k] * s;
+        if ((k & 1) == 0)
+            ig = ig + kGkWgdf[k >> 1] * s;
     }
-    df ig = kGkWgdf[0] * f0;
-    df ik = kGkWkdf[0] * f0;
-    ik = ik + kGkWkdf[1] * (fm[1] + fp[1]);
-    {
-        df const s2 = fm[2] + fp[2];
-        ik = ik + kGkWkdf[2] * s2;
-        ig = ig + kGkWgdf[1] * s2;
-    }
-    ik = ik + kGkWkdf[3] * (fm[3] + fp[3]);
-    {
-        df const s4 = fm[4] + fp[4];
-        ik = ik + kGkWkdf[4] * s4;
-        ig = ig + kGkWgdf[2] * s4;
-    }
-    ik = ik + kGkWkdf[5] * (fm[5] + fp[5]);
-    {
-        df const s6 = fm[6] + fp[6];
-        ik = ik + kGkWkdf[6] * s6;
-        ig = ig + kGkWgdf[3] * s6;
-    }
-    ik = ik + kGkWkdf[7] * (fm[7] + fp[7]);
     df const diff = df_scale(ik - ig, h);
     *err = fabsf(diff.hi + diff.lo);
     return df_to(df_scale(ik, h));
