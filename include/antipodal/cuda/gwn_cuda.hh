@@ -85,11 +85,18 @@ public:
     }
 
     void set_precision(precision p) { set_option(AGWN_OPT_FRAC_MODE, double(int(p))); }
-    // Robust evaluator under int64_grid: exact (the reference's FP64 fractional term, default) or mixed (FP32
-    // pairs under a first-order error bound, the others in FP64); integer counts are the same either way.
+    // Robust evaluator's fractional term: exact (the reference's FP64 arithmetic, default) or mixed (int64_grid:
+    // FP32 pairs under a first-order error bound; exact_float with double queries: the mesh functions' mixed kernel
+    // along -x; the other pairs by the evaluator's own FP64 rule); integer counts are the same either way.
     void set_robust_precision(precision p)
     {
         set_option(AGWN_OPT_ROBUST_MODE, p == precision::mixed ? AGWN_ROBUST_MIXED : AGWN_ROBUST_EXACT);
+    }
+    // The parametric integrator's arithmetic: exact (FP64, bit for bit the reference; default) or mixed
+    // (double-float panels on the FP32 pipe, the same tree rule).
+    void set_param_precision(precision p)
+    {
+        set_option(AGWN_OPT_PARAM_MODE, p == precision::mixed ? AGWN_PARAM_MIXED : AGWN_PARAM_EXACT);
     }
     void set_option(int option, double value) { check(agwn_context_set_option(m_ctx, option, value), "set_option"); }
     [[nodiscard]] double option(int option) const
