@@ -69,7 +69,8 @@ bool mixed_of(const agwn_batch& b, const Context& ctx)
 
 size_t smem_of(const agwn_batch& b, const BConf& c, bool mixed)
 {
-    return 2 * size_t(c.seg_tile) * (ops_of(b.policy).seg_bytes + (mixed ? sizeof(float) : 0));
+    // two tiles of segments, or of chain entries in the mixed form
+    return 2 * size_t(c.seg_tile) * std::max(ops_of(b.policy).seg_bytes, mixed ? sizeof(RChain) : size_t(0));
 }
 
 int grid_of(const agwn_batch& b, const Context& ctx, const BConf& c, int* grid)
@@ -157,6 +158,8 @@ extern "C" int agwn_batch_create(agwn_context* ctx, const agwn_robust* const* me
         m.tri = r->tri;
         m.leaf_uv = static_cast<const float4*>(r->hier.leaf_uv.ptr);
         m.seg = r->seg;
+        m.chain = r->chain;
+        m.n_entries = r->n_entries;
         m.pos = positions[i];
         m.out = out[i];
         m.counts = counts ? counts[i] : nullptr;

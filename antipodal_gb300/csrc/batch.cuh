@@ -15,7 +15,9 @@ struct BMesh
     const BvhNode* nodes;
     const void* tri; // predicate triangles in leaf order (P::C[9] each)
     const float4* leaf_uv;
-    const void* seg; // RSeg<P::C>
+    const void* seg;   // RSeg<P::C>
+    const void* chain; // int64_grid: RChain, the vertex chains of the mixed form (nullable)
+    int64_t n_entries;
     const void* pos; // n_q * 3 scalars
     void* out;       // n_q scalars
     int32_t* counts; // n_q (nullable)

@@ -51,7 +51,8 @@ __device__ __forceinline__ int batch_count(const BMesh& m, const Frame32& f, qv3
     return sum;
 }
 
-// Mixed (int64_grid only): FP32 pairs under robust_pair_f32's error bound, TwoSum-accumulated; the rest in FP64.
+// Mixed (int64_grid only): FP32 pairs on the mesh's vertex chains (robust_chain_step), TwoSum-accumulated; the rest
+// in FP64.
 template <class T, class P, int K, int kStack, bool Mixed>
 __global__ void __launch_bounds__(256) k_batch(const BMesh* __restrict__ meshes, const BItem* __restrict__ items,
                                                int n_items, int* __restrict__ head, int tile, int* flags,
@@ -59,12 +60,13 @@ __global__ void __launch_bounds__(256) k_batch(const BMesh* __restrict__ meshes,
 {
     using C = typename P::C;
     using Seg = RSeg<C>;
+    // the mixed form walks each mesh's vertex chains (RChain), the exact form its segments
+    using Elem = std::conditional_t<Mixed, RChain, Seg>;
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ __align__(8) uint64_t bars[2];
     __shared__ int s_item;
     __shared__ int abort_cta;
-    Seg* const buf[2] = {reinterpret_cast<Seg*>(smem), reinterpret_cast<Seg*>(smem) + tile};
-    float* const wts = reinterpret_cast<float*>(reinterpret_cast<Seg*>(smem) + 2 * tile); // Mixed: 2 * tile
+    Elem* const buf[2] = {reinterpret_cast<Elem*>(smem), reinterpret_cast<Elem*>(smem) + tile};
     __shared__ uint32_t q_entries[Mixed ? 8 : 1][RQueue<K>::kCap];
     __shared__ double q_results[Mixed ? 8 : 1][32];
     int const lane = threadIdx.x & 31;
@@ -101,6 +103,8 @@ __global__ void __launch_bounds__(256) k_batch(const BMesh* __restrict__ meshes,
         BMesh const& m = meshes[item.mesh];
         const Seg* const gseg = static_cast<const Seg*>(m.seg);
         int64_t const n_seg = m.n_seg;
+        const Elem* const gel = static_cast<const Elem*>(Mixed ? m.chain : m.seg);
+        int64_t const n_elem = Mixed ? m.n_entries : n_seg;
         const T* const pos = static_cast<const T*>(m.pos);
         T* const out = static_cast<T*>(m.out);
         Quant const qz{{m.qc[0], m.qc[1], m.qc[2]}, m.qs};
@@ -108,7 +112,7 @@ __global__ void __launch_bounds__(256) k_batch(const BMesh* __restrict__ meshes,
 #pragma unroll
         for (int k = 0; k < 9; ++k)
             f.r[k] = m.frame[k];
-        int const n_tiles = n_seg > 0 ? int((n_seg + tile - 1) / tile) : 0;
+        int const n_tiles = n_elem > 0 ? int((n_elem + tile - 1) / tile) : 0;
         bool const single = n_tiles == 1;
         int64_t const per_sub = int64_t(blockDim.x) * K;
         int const n_sub = int((item.q1 - item.q0 + per_sub - 1) / per_sub);
@@ -118,10 +122,10 @@ __global__ void __launch_bounds__(256) k_batch(const BMesh* __restrict__ meshes,
             unsigned const g = seq + unsigned(it);
             int const b = int(g & 1u);
             int const st = it % n_tiles;
-            int64_t const rem = n_seg - int64_t(st) * tile;
-            unsigned const bytes = unsigned(rem < tile ? rem : tile) * unsigned(sizeof(Seg));
+            int64_t const rem = n_elem - int64_t(st) * tile;
+            unsigned const bytes = unsigned(rem < tile ? rem : tile) * unsigned(sizeof(Elem));
             mbar_arrive_expect_tx(&bars[b], bytes);
-            bulk_copy_g2s(buf[b], gseg + int64_t(st) * tile, bytes, &bars[b]);
+            bulk_copy_g2s(buf[b], gel + int64_t(st) * tile, bytes, &bars[b]);
         };
         if (threadIdx.x == 0)
         {
@@ -138,6 +142,7 @@ __global__ void __launch_bounds__(256) k_batch(const BMesh* __restrict__ meshes,
             double half[K];
             float acc[K], comp[K];
             int64_t idx[K];
+            RVState st0[K] = {}, st1[K] = {};
 #pragma unroll
             for (int k = 0; k < K; ++k)
             {
@@ -159,22 +164,15 @@ __global__ void __launch_bounds__(256) k_batch(const BMesh* __restrict__ meshes,
                 __syncthreads();
                 if (abort_cta)
                     return;
-                Seg const* const sb = buf[b];
-                int64_t const rem = n_seg - int64_t(st) * tile;
+                Elem const* const sb = buf[b];
+                int64_t const rem = n_elem - int64_t(st) * tile;
                 int const cnt_s = int(rem < tile ? rem : tile);
                 if constexpr (Mixed)
                 {
-                    if (landed)
-                    {
-                        tile_weights(sb, cnt_s, wts + b * tile);
-                        __syncthreads();
-                    }
-                    float const* const wb = wts + b * tile;
-                    uint32_t const seg0 = uint32_t(int64_t(st) * tile);
+                    // tiles start at even stream positions (the tile is even): the state alternation runs across them
                     for (int s = 0; s < cnt_s; s += 2)
-                        robust_mixed_step<P, K>(sb, wb, s, cnt_s - s < 2 ? cnt_s - s : 2, seg0, q, term_err, acc, comp,
+                        robust_chain_step<P, K>(sb, s, cnt_s - s < 2 ? cnt_s - s : 2, q, st0, st1, term_err, acc, comp,
                                                 fq, lane, gseg, half);
-                    pairs += 32ull * K * unsigned(cnt_s);
                 }
                 else
                 {
@@ -195,8 +193,11 @@ __global__ void __launch_bounds__(256) k_batch(const BMesh* __restrict__ meshes,
                 }
             }
             if constexpr (Mixed)
+            {
                 while (fq.tail != fq.head)
                     rq_flush<P, K>(fq, min(32u, fq.tail - fq.head), lane, gseg, q, half);
+                pairs += 32ull * K * (unsigned long long)n_seg;
+            }
 #pragma unroll
             for (int k = 0; k < K; ++k)
                 if (idx[k] < item.q1)

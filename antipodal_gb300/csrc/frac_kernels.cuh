@@ -235,6 +235,94 @@ __device__ __forceinline__ float seg_length(const double* w)
     return float(sqrt(ex * ex + ey * ey + ez * ez));
 }
 
+// Chains of ns <= kChainMax segments by exact endpoint equality, in one block (every thread calls it): segment t
+// follows s when start(t) == end(s) (all three coordinates), each t following at most one s (the lowest-numbered),
+// so the links form disjoint open chains and closed loops.  Writes order[0..m) -- ~s: a chain start at start(s),
+// s: segment s, ending at end(s) -- open chains from their first segment, then closed loops from their
+// lowest-numbered segment, and wrap[e]: for the first and last entry of a closed loop the segment that closes it
+// at that vertex, else -1.  Returns m in every thread.  start(t), end(s): the endpoints as double3 (exact for the
+// callers' coordinates).  table: chain_table_size(ns) ints of global scratch; the s_ arrays: kChainMax each.
+template <class Start, class End>
+__device__ int block_chains(int ns, Start start, End end, int* __restrict__ order, int* __restrict__ wrap,
+                            int* __restrict__ table, int* s_succ, int* s_pred, unsigned char* s_seen, int* s_m)
+{
+    int const tmask = chain_table_size(ns) - 1;
+    for (int t = threadIdx.x; t < ns; t += blockDim.x)
+    {
+        s_pred[t] = INT_MAX;
+        s_seen[t] = 0;
+        wrap[2 * t] = -1;
+        wrap[2 * t + 1] = -1;
+    }
+    for (int h = threadIdx.x; ns > 0 && h <= tmask; h += blockDim.x)
+        table[h] = -1;
+    __syncthreads();
+    // segment starts into the table (linear probing; at least half of it stays empty), then every segment looks
+    // up the lowest-numbered other segment that starts where it ends
+    for (int t = threadIdx.x; t < ns; t += blockDim.x)
+    {
+        double3 const u = start(t);
+        uint32_t h = point_hash(u.x, u.y, u.z) & uint32_t(tmask);
+        while (atomicCAS(&table[h], -1, t) != -1)
+            h = (h + 1) & uint32_t(tmask);
+    }
+    __syncthreads();
+    for (int si = threadIdx.x; si < ns; si += blockDim.x)
+    {
+        double3 const e = end(si);
+        int next = -1;
+        for (uint32_t h = point_hash(e.x, e.y, e.z) & uint32_t(tmask);; h = (h + 1) & uint32_t(tmask))
+        {
+            int const t = __ldcg(&table[h]); // written by atomics: read from L2
+            if (t < 0)
+                break;
+            double3 const u = start(t);
+            if (u.x == e.x && u.y == e.y && u.z == e.z && t != si && (next < 0 || t < next))
+                next = t;
+        }
+        s_succ[si] = next;
+        if (next >= 0)
+            atomicMin(&s_pred[next], si);
+    }
+    __syncthreads();
+    for (int si = threadIdx.x; si < ns; si += blockDim.x)
+    {
+        int const t = s_succ[si];
+        if (t >= 0 && s_pred[t] != si)
+            s_succ[si] = -1; // t follows a lower-numbered segment
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+        int m = 0;
+        // pass 0: open chains from their heads (no predecessor); pass 1: what is left lies on closed loops
+        for (int pass = 0; pass < 2; ++pass)
+            for (int si = 0; si < ns; ++si)
+            {
+                if (s_seen[si] || (pass == 0 && s_pred[si] != INT_MAX))
+                    continue;
+                int const first = m;
+                order[m++] = ~si;
+                int last = si;
+                for (int cur = si; cur >= 0 && !s_seen[cur]; cur = s_succ[cur])
+                {
+                    s_seen[cur] = 1;
+                    order[m++] = cur;
+                    last = cur;
+                }
+                if (pass == 1)
+                {
+                    // a closed loop: its last segment ends at the start vertex
+                    wrap[first] = last;
+                    wrap[m - 1] = si;
+                }
+            }
+        *s_m = m;
+    }
+    __syncthreads();
+    return *s_m;
+}
+
 // One block.  (1) The bounding-box centre of all endpoints.  (2) Chains: segment t follows segment s when
 // P0(t) == P1(s) exactly (all three doubles), each t following at most one s (the lowest-numbered), so the links form
 // disjoint open chains and closed loops.  (3) The entry stream: per chain a start entry (its first segment's P0)
@@ -283,17 +371,7 @@ __global__ void __launch_bounds__(1024) k_prep_mixed(const double* __restrict__ 
     int const ns = chain ? int(n_seg) : 0;
     int* const wrap = order + 2 * ns; // per entry: the segment that closes its loop at this vertex, or -1
     int* const table = order + 4 * ns;
-    int const tmask = chain_table_size(ns) - 1;
-    for (int s = threadIdx.x; s < ns; s += blockDim.x)
-    {
-        s_pred[s] = INT_MAX;
-        s_seen[s] = 0;
-        wrap[2 * s] = -1;
-        wrap[2 * s + 1] = -1;
-    }
-    for (int h = threadIdx.x; chain && h <= tmask; h += blockDim.x)
-        table[h] = -1;
-    __syncthreads();
+    __syncthreads(); // the warps' bounding boxes are in red
     if (threadIdx.x < 3)
     {
         int const k = threadIdx.x;
@@ -306,77 +384,14 @@ __global__ void __launch_bounds__(1024) k_prep_mixed(const double* __restrict__ 
         centre[k] = (n_seg > 0) ? 0.5 * (a + b) : 0.0;
         frame->c[k] = centre[k];
     }
-    __syncthreads();
-    // (2) segment starts into the table (linear probing; at least half of it stays empty), then every segment looks
-    // up the lowest-numbered other segment that starts where it ends
-    for (int t = threadIdx.x; t < ns; t += blockDim.x)
-    {
-        const double* u = raw + 7 * size_t(t);
-        uint32_t h = point_hash(u[0], u[1], u[2]) & uint32_t(tmask);
-        while (atomicCAS(&table[h], -1, t) != -1)
-            h = (h + 1) & uint32_t(tmask);
-    }
-    __syncthreads();
-    for (int s = threadIdx.x; s < ns; s += blockDim.x)
-    {
-        const double* w = raw + 7 * size_t(s);
-        double const ex = w[3], ey = w[4], ez = w[5];
-        int next = -1;
-        for (uint32_t h = point_hash(ex, ey, ez) & uint32_t(tmask);; h = (h + 1) & uint32_t(tmask))
-        {
-            int const t = __ldcg(&table[h]); // written by atomics: read from L2
-            if (t < 0)
-                break;
-            const double* u = raw + 7 * size_t(t);
-            if (u[0] == ex && u[1] == ey && u[2] == ez && t != s && (next < 0 || t < next))
-                next = t;
-        }
-        s_succ[s] = next;
-        if (next >= 0)
-            atomicMin(&s_pred[next], s);
-    }
-    __syncthreads();
-    for (int s = threadIdx.x; s < ns; s += blockDim.x)
-    {
-        int const t = s_succ[s];
-        if (t >= 0 && s_pred[t] != s)
-            s_succ[s] = -1; // t follows a lower-numbered segment
-    }
-    __syncthreads();
+    // (2) the chains
+    int const mc = block_chains(
+        ns, [&](int t) { const double* u = raw + 7 * size_t(t); return make_double3(u[0], u[1], u[2]); },
+        [&](int t) { const double* u = raw + 7 * size_t(t); return make_double3(u[3], u[4], u[5]); }, order, wrap,
+        table, s_succ, s_pred, s_seen, &s_entries);
+    int const m = chain ? mc : int(2 * n_seg);
     if (threadIdx.x == 0)
-    {
-        int m = 0;
-        if (chain)
-        {
-            // pass 0: open chains from their heads (no predecessor); pass 1: what is left lies on closed loops
-            for (int pass = 0; pass < 2; ++pass)
-                for (int s = 0; s < ns; ++s)
-                {
-                    if (s_seen[s] || (pass == 0 && s_pred[s] != INT_MAX))
-                        continue;
-                    int const first = m;
-                    order[m++] = ~s;
-                    int last = s;
-                    for (int cur = s; cur >= 0 && !s_seen[cur]; cur = s_succ[cur])
-                    {
-                        s_seen[cur] = 1;
-                        order[m++] = cur;
-                        last = cur;
-                    }
-                    if (pass == 1)
-                    {
-                        // a closed loop: its last segment ends at the start vertex
-                        wrap[first] = last;
-                        wrap[m - 1] = s;
-                    }
-                }
-        }
-        else
-            m = int(2 * n_seg);
-        s_entries = m;
         frame->n_entries = m;
-    }
-    __syncthreads();
     // the links are done: s_pred now holds each segment's length
     float* const s_len = reinterpret_cast<float*>(s_pred);
     for (int s = threadIdx.x; s < ns; s += blockDim.x)
@@ -390,7 +405,6 @@ __global__ void __launch_bounds__(1024) k_prep_mixed(const double* __restrict__ 
         for (int r = 0; r < 3; ++r)
             P[r] = rot.m[3 * r] * dx + rot.m[3 * r + 1] * dy + rot.m[3 * r + 2] * dz;
     };
-    int const m = s_entries;
     for (int e = threadIdx.x; e < m; e += blockDim.x)
     {
         int s;

@@ -56,7 +56,9 @@ void robust_free(Robust* r)
         cudaFree(r->tri);
     if (r->seg)
         cudaFree(r->seg);
-    r->tri = r->seg = nullptr;
+    if (r->chain)
+        cudaFree(r->chain);
+    r->tri = r->seg = r->chain = nullptr;
     r->cells.release();
     r->hier.release();
 }
@@ -148,6 +150,24 @@ int robust_build(Context& ctx, const T* vertices, int64_t nv, const int32_t* ind
                                               static_cast<RSeg<C>*>(out->seg));
         AGWN_TRY(ctx.launch_end(AGWN_K_OTHER));
     }
+    if constexpr (std::is_same_v<P, P64>)
+        if (n_seg > 0 && n_seg < (int64_t(1) << 24))
+        {
+            // the chains of the mixed form's FP32 pairs
+            AGWN_TRY_CUDA(cudaMalloc(&out->chain, sizeof(RChain) * 2 * size_t(n_seg)));
+            RTmp order, cnt;
+            AGWN_TRY(order.alloc(sizeof(int) * std::max<int64_t>(1, chain_scratch_ints(n_seg))));
+            AGWN_TRY(cnt.alloc(sizeof(long long)));
+            AGWN_TRY(ctx.launch_begin(AGWN_K_OTHER));
+            k_robust_chain<<<1, 1024, 0, st>>>(static_cast<const RSeg<int32_t>*>(out->seg), n_seg,
+                                               static_cast<RChain*>(out->chain), static_cast<long long*>(cnt.p),
+                                               static_cast<int*>(order.p));
+            AGWN_TRY(ctx.launch_end(AGWN_K_OTHER));
+            long long m = 0;
+            AGWN_TRY_CUDA(cudaMemcpyAsync(&m, cnt.p, sizeof(m), cudaMemcpyDeviceToHost, st));
+            AGWN_TRY_CUDA(cudaStreamSynchronize(st));
+            out->n_entries = m;
+        }
     AGWN_TRY_CUDA(cudaStreamSynchronize(st));
     return AGWN_OK;
 }
@@ -236,13 +256,12 @@ int robust_run(Context& ctx, const Robust& r, const T* d_pos, int64_t n, T* d_ou
             return ctx.launch_end(AGWN_K_OTHER);
         }
     }
-    int const tile = int(std::max<int64_t>(1, std::min<int64_t>(ctx.seg_tile, r.n_seg)));
-    int const n_tiles = int((r.n_seg + tile - 1) / tile);
-    // the mixed form (int64_grid only) adds the tiles' FP32 weights after two segment buffers
-    bool const mixed =
-        std::is_same_v<P, P64> && ctx.robust_mode == AGWN_ROBUST_MIXED && r.n_seg < (int64_t(1) << 24);
-    size_t const smem = mixed ? 2 * size_t(tile) * (sizeof(Seg) + sizeof(float))
-                              : size_t(n_tiles <= 1 ? 1 : 2) * tile * sizeof(Seg);
+    // the mixed form (int64_grid only) walks the vertex chains built with the evaluator
+    bool const mixed = std::is_same_v<P, P64> && ctx.robust_mode == AGWN_ROBUST_MIXED && r.chain != nullptr;
+    int64_t const n_elem = mixed ? r.n_entries : r.n_seg;
+    int const tile = int(std::max<int64_t>(1, std::min<int64_t>(ctx.seg_tile, n_elem)));
+    int const n_tiles = int((n_elem + tile - 1) / tile);
+    size_t const smem = size_t(n_tiles <= 1 ? 1 : 2) * tile * (mixed ? sizeof(RChain) : sizeof(Seg));
     auto kern = k_robust_frac<T, P, false>;
     if constexpr (std::is_same_v<P, P64>)
         if (mixed)
@@ -255,7 +274,8 @@ int robust_run(Context& ctx, const Robust& r, const T* d_pos, int64_t n, T* d_ou
     int64_t const n_qtiles = (n + kRobBlock - 1) / kRobBlock;
     int const grid = int(std::max<int64_t>(1, std::min<int64_t>(n_qtiles, int64_t(per_sm) * ctx.sm_count)));
     AGWN_TRY(ctx.launch_begin(AGWN_K_ROBUST));
-    kern<<<grid, kRobBlock, smem, st>>>(d_pos, n, qz, static_cast<const Seg*>(r.seg), r.n_seg, tile, d_counts, d_out,
+    kern<<<grid, kRobBlock, smem, st>>>(d_pos, n, qz, static_cast<const Seg*>(r.seg), r.n_seg,
+                                        static_cast<const RChain*>(r.chain), r.n_entries, tile, d_counts, d_out,
                                         d_frac, ctx.d_flags, float(ctx.robust_term_err),
                                         ctx.timing ? ctx.d_counters : nullptr);
     return ctx.launch_end(AGWN_K_ROBUST);

@@ -378,6 +378,50 @@ __global__ void k_robust_segs(const T* __restrict__ raw, int64_t n_seg, Quant qz
     }
 }
 
+// One block: the vertex chains of an int64_grid boundary (block_chains on the RSeg endpoints), then the entries;
+// boundaries above kChainMax segments take one chain per segment.  *n_entries receives the count.  order:
+// chain_scratch_ints(n_seg) ints of scratch.
+__global__ void __launch_bounds__(1024) k_robust_chain(const RSeg<int32_t>* __restrict__ seg, int64_t n_seg,
+                                                       RChain* __restrict__ out, long long* __restrict__ n_entries,
+                                                       int* __restrict__ order)
+{
+    __shared__ int s_succ[kChainMax], s_pred[kChainMax];
+    __shared__ unsigned char s_seen[kChainMax];
+    __shared__ int s_m;
+    bool const chain = n_seg <= kChainMax;
+    int const ns = chain ? int(n_seg) : 0;
+    int const mc = block_chains(
+        ns, [&](int t) { return make_double3(seg[t].p0[0], seg[t].p0[1], seg[t].p0[2]); },
+        [&](int t) { return make_double3(seg[t].p1[0], seg[t].p1[1], seg[t].p1[2]); }, order, order + 2 * ns,
+        order + 4 * ns, s_succ, s_pred, s_seen, &s_m);
+    int const m = chain ? mc : int(2 * n_seg);
+    if (threadIdx.x == 0)
+        *n_entries = m;
+    for (int e = threadIdx.x; e < m; e += blockDim.x)
+    {
+        int si;
+        bool start;
+        if (chain)
+        {
+            int const o = order[e];
+            start = o < 0;
+            si = start ? ~o : o;
+        }
+        else
+        {
+            si = e >> 1;
+            start = (e & 1) == 0;
+        }
+        RSeg<int32_t> const g = seg[si];
+        RChain r{};
+        for (int k = 0; k < 3; ++k)
+            r.p[k] = start ? g.p0[k] : g.p1[k];
+        r.s = start ? -1 : si;
+        r.w = start ? 0.f : __double2float_rn(g.w);
+        out[e] = r;
+    }
+}
+
 // ---- evaluation -------------------------------------------------------------------------------------------------
 constexpr int kRobBlock = 128;
 constexpr int kRobCand = 8;
@@ -517,70 +561,7 @@ __device__ __forceinline__ double robust_contrib(qv3<typename P::C> q, RSeg<type
 }
 
 // ---- mixed precision (int64_grid) -------------------------------------------------------------------------------
-// The fractional term of one (query, segment) pair on the FP32 pipe, when a first-order error estimate says it is
-// close to the FP64 value.  Under int64_grid the differences v = p - q are exact integers; below 2^24 they are
-// exact floats.  The atan2 numerator num = v0.z v1.y - v0.y v1.z and y0 y1 + z0 z1 come from TwoProduct FMAs
-// (error ~2 ulp of the result), |v|, l + x (or (y^2 + z^2) / (l - x) when x < 0, the reference's cancellation-free
-// form) from an approximate rsqrt and reciprocal.  With 4 eps32 per operand chain -- the estimate of the mesh
-// kernel's mixed form -- num errs by E_n = 4u |num| and den = A B + yz by E_d = 4u (|A B| + |yz|), so the angle errs
-// by about (|num| E_d + |den| E_n) / (num^2 + den^2).  The pair stays in FP32 when that is at most term_err;
-// otherwise, when num == 0 (where the reference takes its exact branches), or when a difference is too large to
-// be exact in float, this returns false and the caller evaluates the pair in FP64 with the reference's formula.
-template <class P>
-__device__ __forceinline__ bool robust_pair_f32(qv3<typename P::C> q, RSeg<typename P::C> const& s, float term_err,
-                                                float* theta)
-{
-    static_assert(std::is_same_v<typename P::C, int32_t>, "FP32 pairs are for the int64_grid policy");
-    int32_t const v0x = s.p0[0] - q.x, v0y = s.p0[1] - q.y, v0z = s.p0[2] - q.z;
-    int32_t const v1x = s.p1[0] - q.x, v1y = s.p1[1] - q.y, v1z = s.p1[2] - q.z;
-    // all six below 2^24 in magnitude: (v + 2^24) as unsigned below 2^25
-    unsigned const lim = 1u << 25, off = 1u << 24;
-    bool const small = unsigned(v0x) + off < lim && unsigned(v0y) + off < lim && unsigned(v0z) + off < lim &&
-                       unsigned(v1x) + off < lim && unsigned(v1y) + off < lim && unsigned(v1z) + off < lim;
-    if (!small)
-        return false;
-    float const x0 = float(v0x), y0 = float(v0y), z0 = float(v0z);
-    float const x1 = float(v1x), y1 = float(v1y), z1 = float(v1z);
-    // num = z0 y1 - y0 z1 by TwoProduct: for integer inputs below 2^24 it is 0 exactly when the exact value is
-    // (a nonzero exact value is at least 1 in magnitude), where the reference takes its exact branches
-    float const pn = y0 * z1, en = fmaf(y0, z1, -pn);
-    float const numf = fmaf(z0, y1, -pn) - en;
-    if (numf == 0.f)
-        return false;
-    float const pz = z0 * z1, ez = fmaf(z0, z1, -pz);
-    float const yzf = fmaf(y0, y1, pz) + ez;
-    float const yz0 = fmaf(y0, y0, z0 * z0), yz1 = fmaf(y1, y1, z1 * z1);
-    float const s0 = fmaf(x0, x0, yz0), s1 = fmaf(x1, x1, yz1);
-    float const l0 = s0 * rsqrtf(s0), l1 = s1 * rsqrtf(s1);
-    // l + x = n / d with (n, d) = (l + x, 1) for x >= 0 and (y^2 + z^2, l - x) for x < 0, the reference's
-    // cancellation-free form; num and den scaled by D = d0 d1 > 0 (the angle is unchanged): den D = n0 n1 + yz D
-    float const n0 = x0 >= 0.f ? l0 + x0 : yz0, d0 = x0 >= 0.f ? 1.f : l0 - x0;
-    float const n1 = x1 >= 0.f ? l1 + x1 : yz1, d1 = x1 >= 0.f ? 1.f : l1 - x1;
-    float const D = d0 * d1, ab = n0 * n1, yzs = yzf * D;
-    float const num_s = numf * D, den_s = ab + yzs;
-    float const an = fabsf(num_s), ad = fabsf(den_s);
-    bool const swap = an > ad;
-    float const inv = __fdividef(1.f, fmaxf(swap ? an : ad, 1e-37f));
-    float const an1 = an * inv, ad1 = ad * inv;
-    // the angle errs by about 4u (|num| (|ab| + |yz|) + |den| |num|) / (num^2 + den^2); in units of M = max(|num|,
-    // |den|), with the division by an1^2 + ad1^2 moved to the other side
-    constexpr float k4u = 4.f * 5.9604645e-8f;
-    float const bound = k4u * fmaf(an1, (fabsf(ab) + fabsf(yzs)) * inv, ad1 * an1);
-    if (!(bound <= term_err * fmaf(an1, an1, ad1 * ad1)))
-        return false;
-    *theta = atan2_unit(num_s, den_s, swap ? ad1 : an1, swap);
-    return true;
-}
-
-// The FP32 weights of one shared-memory tile of segments, written by the block after the tile has landed.
-template <class Seg>
-__device__ __forceinline__ void tile_weights(Seg const* sb, int cnt, float* w)
-{
-    for (int s = threadIdx.x; s < cnt; s += blockDim.x)
-        w[s] = __double2float_rn(sb[s].w);
-}
-
-// Per-warp queue of the pairs robust_pair_f32 turned down, evaluated in FP64 32 at a time (one per lane), so
+// Per-warp queue of the pairs the FP32 path turned down, evaluated in FP64 32 at a time (one per lane), so
 // that the narrow FP64 pipe runs full warps instead of one diverged lane.  Entry: (segment << 8) | (lane << 3) | k,
 // with the segment's index in the mesh's boundary array (below 2^24).
 template <int K>
@@ -647,34 +628,88 @@ __device__ __forceinline__ void rq_flush(RQueue<K>& fq, unsigned c, int lane, co
     fq.head += c;
 }
 
-// The FP32 pairs of up to two segments (sb[s], sb[s + 1]; ne of them) with K queries: accepted terms go into the
-// TwoSum accumulators (a turned-down pair adds an exact zero), turned-down pairs are marked in a bit mask and, only
-// when a lane of the warp has one, pushed to the FP64 queue in segment order, which is then drained in full
-// batches.  k_robust_frac and the batch kernel both evaluate their pairs through this, so their sums agree bit for
-// bit.
+// Per-vertex quantities of one chain vertex relative to one query: v = p - q as floats (exact: below 2^24), and
+// the half-angle pair (n, d) of l + x; d is NaN when a difference is 2^24 or more (the pairs at that vertex go to
+// FP64).
+struct RVState
+{
+    float x, y, z, n, d;
+};
+
+// One chain entry with K queries: its vertex into cv, then (a segment entry) the fractional term of the segment
+// from the previous vertex pv, on the FP32 pipe, into the TwoSum accumulators -- or its bit (slot * K + k) set in
+// `bits` for FP64.  Under int64_grid the differences v = p - q are exact integers; below 2^24 they are exact
+// floats.  The atan2 numerator num = z0 y1 - y0 z1 and y0 y1 + z0 z1 come from TwoProduct FMAs (error ~2 ulp of the
+// result; num is 0 exactly when the exact value is), |v| from an approximate rsqrt, and l + x in the reference's
+// cancellation-free half-angle form (l + x, or (y^2 + z^2) / (l - x) for x < 0) with num and den scaled by the two
+// denominators (no division).  With 4 eps32 per operand chain -- the estimate of the mesh kernel's mixed form --
+// num errs by 4u |num| and den = A B + yz by 4u (|A B| + |yz|), so the angle errs by about
+// (|num| E_d + |den| E_n) / (num^2 + den^2).  The pair stays in FP32 when that is at most term_err; num == 0 (where
+// the reference takes its exact branches), a difference of 2^24 or more and ill-conditioned pairs go to FP64 with
+// the reference's formula.
+template <int K>
+__device__ __forceinline__ void robust_chain_entry(RChain const& e, qv3<int32_t> const (&q)[K], RVState (&pv)[K],
+                                                   RVState (&cv)[K], float term_err, float (&acc)[K],
+                                                   float (&comp)[K], uint32_t& bits, int slot)
+{
+    unsigned const lim = 1u << 25, off = 1u << 24;
+#pragma unroll
+    for (int k = 0; k < K; ++k)
+    {
+        int32_t const vx = e.p[0] - q[k].x, vy = e.p[1] - q[k].y, vz = e.p[2] - q[k].z;
+        bool const small = unsigned(vx) + off < lim && unsigned(vy) + off < lim && unsigned(vz) + off < lim;
+        RVState& c = cv[k];
+        c.x = float(vx);
+        c.y = float(vy);
+        c.z = float(vz);
+        float const yz = fmaf(c.y, c.y, c.z * c.z);
+        float const sq = fmaf(c.x, c.x, yz);
+        float const l = sq * rsqrtf(sq);
+        c.n = c.x >= 0.f ? l + c.x : yz;
+        float const d = c.x >= 0.f ? 1.f : l - c.x;
+        c.d = small ? d : __int_as_float(0x7fffffff);
+    }
+    if (e.s < 0)
+        return; // a chain start: its vertex only
+#pragma unroll
+    for (int k = 0; k < K; ++k)
+    {
+        RVState const& a = pv[k];
+        RVState const& b = cv[k];
+        float const pn = a.y * b.z, en = fmaf(a.y, b.z, -pn);
+        float const numf = fmaf(a.z, b.y, -pn) - en;
+        float const pz = a.z * b.z, ez = fmaf(a.z, b.z, -pz);
+        float const yzf = fmaf(a.y, b.y, pz) + ez;
+        float const D = a.d * b.d, ab = a.n * b.n, yzs = yzf * D;
+        float const num_s = numf * D, den_s = ab + yzs;
+        float const an = fabsf(num_s), ad = fabsf(den_s);
+        bool const swap = an > ad;
+        float const inv = __fdividef(1.f, fmaxf(swap ? an : ad, 1e-37f));
+        float const an1 = an * inv, ad1 = ad * inv;
+        constexpr float k4u = 4.f * 5.9604645e-8f;
+        float const bound = k4u * fmaf(an1, (fabsf(ab) + fabsf(yzs)) * inv, ad1 * an1);
+        // num == 0 (the reference's exact branches), an out-of-range difference (NaN d) or an ill-conditioned pair
+        bool const need = numf == 0.f || !(bound <= term_err * fmaf(an1, an1, ad1 * ad1));
+        bits |= need ? (1u << (slot * K + k)) : 0u;
+        float const th = atan2_unit(num_s, den_s, swap ? ad1 : an1, swap);
+        two_sum_acc(acc[k], comp[k], need ? 0.f : e.w * th);
+    }
+}
+
+// Two chain entries (sb[s], sb[s + 1]; ne of them) with K queries; entries at even positions of the stream write
+// st0, odd ones st1 (tiles start at even positions).  Pairs turned down are pushed to the FP64 queue in stream
+// order only when a lane of the warp has one; the queue is then drained in full batches.  Shared by k_robust_frac
+// and the batch kernel, so their sums agree bit for bit.
 template <class P, int K>
-__device__ __forceinline__ void robust_mixed_step(RSeg<typename P::C> const* sb, float const* wb, int s, int ne,
-                                                  uint32_t seg0, qv3<typename P::C> const (&q)[K], float term_err,
+__device__ __forceinline__ void robust_chain_step(RChain const* sb, int s, int ne, qv3<int32_t> const (&q)[K],
+                                                  RVState (&st0)[K], RVState (&st1)[K], float term_err,
                                                   float (&acc)[K], float (&comp)[K], RQueue<K>& fq, int lane,
                                                   RSeg<typename P::C> const* gseg, double (&half)[K])
 {
     uint32_t bits = 0;
-#pragma unroll
-    for (int e = 0; e < 2; ++e)
-    {
-        if (e >= ne)
-            break;
-        RSeg<typename P::C> const sgm = sb[s + e];
-        float const w = wb[s + e];
-#pragma unroll
-        for (int k = 0; k < K; ++k)
-        {
-            float th = 0.f;
-            bool const ok = robust_pair_f32<P>(q[k], sgm, term_err, &th);
-            bits |= ok ? 0u : (1u << (e * K + k));
-            two_sum_acc(acc[k], comp[k], ok ? w * th : 0.f);
-        }
-    }
+    robust_chain_entry<K>(sb[s], q, st1, st0, term_err, acc, comp, bits, 0);
+    if (ne > 1)
+        robust_chain_entry<K>(sb[s + 1], q, st0, st1, term_err, acc, comp, bits, 1);
     if (__any_sync(0xffffffffu, bits != 0u))
     {
 #pragma unroll
@@ -682,37 +717,45 @@ __device__ __forceinline__ void robust_mixed_step(RSeg<typename P::C> const* sb,
         {
             if (e >= ne)
                 break;
+            uint32_t const si = uint32_t(sb[s + e].s);
 #pragma unroll
             for (int k = 0; k < K; ++k)
-                rq_push(fq, ((bits >> (e * K + k)) & 1u) != 0u, seg0 + uint32_t(s + e), lane, k);
+                rq_push(fq, ((bits >> (e * K + k)) & 1u) != 0u, si, lane, k);
         }
         while (fq.tail - fq.head >= 32)
             rq_flush<P, K>(fq, 32, lane, gseg, q, half);
     }
 }
 
-// Mixed = true (int64_grid only): FP32 pairs through robust_pair_f32 with TwoSum accumulation, the others in FP64.
+// Mixed = true (int64_grid only): FP32 pairs on the boundary's vertex chains (robust_chain_step) with TwoSum
+// accumulation, the others in FP64.
 template <class T, class P, bool Mixed = false>
 __global__ void __launch_bounds__(kRobBlock) k_robust_frac(const T* __restrict__ pos, int64_t n, Quant qz,
                                                            const RSeg<typename P::C>* __restrict__ seg, int64_t n_seg,
+                                                           const RChain* __restrict__ chain, int64_t n_entries,
                                                            int tile, const int32_t* __restrict__ counts,
                                                            T* __restrict__ out, T* __restrict__ out_frac, int* flags,
                                                            float term_err, long long* counters)
 {
     using Seg = RSeg<typename P::C>;
+    // the mixed form walks the boundary's vertex chains (RChain), the exact form its segments
+    using Elem = std::conditional_t<Mixed, RChain, Seg>;
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ __align__(8) uint64_t bars[2];
     __shared__ int abort_cta;
-    TilePipe<Seg> pipe;
-    pipe.n_tiles = int((n_seg + tile - 1) / tile);
+    int64_t const n_elem = Mixed ? n_entries : n_seg;
+    TilePipe<Elem> pipe;
+    pipe.n_tiles = int((n_elem + tile - 1) / tile);
     pipe.single = pipe.n_tiles <= 1;
-    pipe.buf[0] = reinterpret_cast<Seg*>(smem);
+    pipe.buf[0] = reinterpret_cast<Elem*>(smem);
     pipe.buf[1] = pipe.buf[0] + (pipe.single ? 0 : tile);
     pipe.bar = bars;
-    pipe.gseg = seg;
-    pipe.n_seg = n_seg;
+    if constexpr (Mixed)
+        pipe.gseg = chain;
+    else
+        pipe.gseg = seg;
+    pipe.n_seg = n_elem;
     pipe.tile = tile;
-    float* const wts = reinterpret_cast<float*>(reinterpret_cast<Seg*>(smem) + 2 * tile); // Mixed: 2 * tile floats
     constexpr int kWarps = kRobBlock / 32;
     __shared__ uint32_t q_entries[Mixed ? kWarps : 1][RQueue<1>::kCap];
     __shared__ double q_results[Mixed ? kWarps : 1][32];
@@ -747,6 +790,7 @@ __global__ void __launch_bounds__(kRobBlock) k_robust_frac(const T* __restrict__
         float acc[1] = {0.f}, comp[1] = {0.f};
         decltype(q) qarr[1] = {q};
         double harr[1] = {0.0};
+        RVState st0[1] = {}, st1[1] = {};
         for (int st = 0; st < pipe.n_tiles && n_seg > 0; ++st)
         {
             int const b = it & 1;
@@ -757,19 +801,13 @@ __global__ void __launch_bounds__(kRobBlock) k_robust_frac(const T* __restrict__
             __syncthreads();
             if (abort_cta)
                 return;
-            Seg const* sb = pipe.buf[b];
+            Elem const* sb = pipe.buf[b];
             int const cnt = pipe.tile_count(st);
             if constexpr (Mixed)
             {
-                if (landed)
-                {
-                    tile_weights(sb, cnt, wts + b * tile);
-                    __syncthreads();
-                }
-                float const* wb = wts + b * tile;
-                uint32_t const seg0 = uint32_t(int64_t(st) * tile);
+                // tiles start at even stream positions (the tile is even), so the state alternation runs across them
                 for (int s = 0; s < cnt; s += 2)
-                    robust_mixed_step<P, 1>(sb, wb, s, cnt - s < 2 ? cnt - s : 2, seg0, qarr, term_err, acc, comp, fq,
+                    robust_chain_step<P, 1>(sb, s, cnt - s < 2 ? cnt - s : 2, qarr, st0, st1, term_err, acc, comp, fq,
                                             lane, seg, harr);
             }
             else
