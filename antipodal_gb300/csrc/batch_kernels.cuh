@@ -157,13 +157,17 @@ __global__ void __launch_bounds__(256) k_batch(const BMesh* __restrict__ meshes,
             {
                 unsigned const g = seq + unsigned(it);
                 int const b = int(g & 1u);
+                // a single tile stays in shared memory for all of the item's query sub-tiles: only the first waits for
+                // it, and the warps then run the others without meeting at a barrier
                 bool const landed = !single || sub == 0;
                 if (landed)
+                {
                     if (!mbar_wait_bounded(&bars[b], (g >> 1) & 1u, flags, 5))
                         abort_cta = 1;
-                __syncthreads();
-                if (abort_cta)
-                    return;
+                    __syncthreads();
+                    if (abort_cta)
+                        return;
+                }
                 Elem const* const sb = buf[b];
                 int64_t const rem = n_elem - int64_t(st) * tile;
                 int const cnt_s = int(rem < tile ? rem : tile);

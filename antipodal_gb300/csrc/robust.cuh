@@ -794,13 +794,17 @@ __global__ void __launch_bounds__(kRobBlock) k_robust_frac(const T* __restrict__
         for (int st = 0; st < pipe.n_tiles && n_seg > 0; ++st)
         {
             int const b = it & 1;
+            // a single tile stays in shared memory for every query tile: only the first waits for it, and the warps then
+            // run the others without meeting at a barrier
             bool const landed = !pipe.single || j == 0;
             if (landed)
+            {
                 if (!mbar_wait_bounded(&bars[b], unsigned((it >> 1) & 1), flags, 3))
                     abort_cta = 1;
-            __syncthreads();
-            if (abort_cta)
-                return;
+                __syncthreads();
+                if (abort_cta)
+                    return;
+            }
             Elem const* sb = pipe.buf[b];
             int const cnt = pipe.tile_count(st);
             if constexpr (Mixed)
