@@ -64,6 +64,10 @@ namespace
 {
 // A boundary prepared for the fractional kernels (device scratch of the context), reusable by any number of
 // launches on the same context stream until the next preparation.
+// The largest entry stream the mixed kernel stages as one shared-memory tile (57.6 KB: three 256-thread blocks per
+// SM).
+constexpr int64_t kSingleTileEntries = 1200;
+
 template <class T>
 struct FracPlan
 {
@@ -129,7 +133,22 @@ int fractional_prepare(Context& ctx, const T* x0_host, const T* d_seg_raw, int64
     AGWN_TRY(ctx.launch_begin(AGWN_K_OTHER));
     k_prep_mixed<<<1, 1024, 0, ctx.stream>>>(reinterpret_cast<const double*>(d_seg_raw), n_seg, p.rot,
                                              float(ctx.mixed_tau), p.frame, p.segm, p.seg64, order);
-    return ctx.launch_end(AGWN_K_OTHER);
+    AGWN_TRY(ctx.launch_end(AGWN_K_OTHER));
+    // The stream holds n_seg + (number of chains) entries, at most 2 n_seg.  When that bound would take several
+    // tiles but the boundary could fit one, the actual count is read back (a wait on the stream): one tile runs
+    // without block barriers (1,066 segments in 20 loops: 35.2 ms in three tiles, see the measurements).
+    if (p.nbuf > 1 && n_seg <= kSingleTileEntries)
+    {
+        long long m = 0;
+        AGWN_TRY_CUDA(cudaMemcpyAsync(&m, &p.frame->n_entries, sizeof(m), cudaMemcpyDeviceToHost, ctx.stream));
+        AGWN_TRY_CUDA(cudaStreamSynchronize(ctx.stream));
+        if (m <= kSingleTileEntries)
+        {
+            p.tile = int(m);
+            p.nbuf = 1;
+        }
+    }
+    return AGWN_OK;
 }
 
 template <class T, class FB>
@@ -189,7 +208,7 @@ int fractional_launch_mixed(Context& ctx, const FracPlan<T>& p, const double* d_
     int const K = ctx.queries_per_thread;
     // measured: one tile, 128 threads (10.2 ms against 10.6 on a 212-segment boundary); several tiles, 256 threads
     // (34.9 ms against 40.5 on 1,066 segments), since more queries share each staged tile and its barriers
-    int const block = ctx.frac_block ? ctx.frac_block : (p.nbuf > 1 ? 256 : 128);
+    int const block = ctx.frac_block ? ctx.frac_block : (p.nbuf > 1 || p.tile > 512 ? 256 : 128);
     int64_t const n_qtiles = (n + int64_t(block) * K - 1) / (int64_t(block) * K);
     size_t const smem = size_t(p.nbuf) * p.tile * sizeof(SegM);
     float const tau = float(ctx.mixed_tau);
