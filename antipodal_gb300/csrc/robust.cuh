@@ -473,7 +473,12 @@ __global__ void __launch_bounds__(kRobBlock) k_robust_count(const BvhNode* __res
 }
 
 // k_robust_count with the candidate leaves read from the cell grid of the evaluator's hierarchy (the walk for
-// queries beyond the grid's tolerance): the same leaves decided by the same exact predicate, the same counts.
+// queries beyond the grid's tolerance), and most of them decided in float.  The hierarchy's frame for the -x ray is
+// (u, v, w) = (z, y, -x), exact in double, and its leaf corners are the predicate's own coordinates, so
+// certain_leaf's edge functions are the negated (y, z) edge determinants and its "in front" is q.x >= the hit's x:
+// where it decides (all three edges, and the depth, beyond margins ~1e8 times the rounding of either
+// computation) its value is robust_crossing's, -e01 or 0.  The other leaves -- within the margin of an edge, a
+// vertex or the plane -- take robust_crossing itself.  The counts are the exact predicate's.
 template <class T, class P>
 __global__ void __launch_bounds__(kRobBlock) k_robust_cells(const BvhNode* __restrict__ nodes,
                                                             const typename P::C* __restrict__ tri,
@@ -496,12 +501,17 @@ __global__ void __launch_bounds__(kRobBlock) k_robust_cells(const BvhNode* __res
         int sum = 0;
         int cand[kRobCand];
         int nc = 0;
+        auto const decide = [&](int leaf) -> int
+        {
+            int const c = certain_leaf(leaf_uv, leaf, u, v, w, m8);
+            return c != 2 ? c : robust_crossing<P>(q, tri + 9 * int64_t(leaf));
+        };
         auto const consider = [&](int leaf)
         {
             if (nc == kRobCand)
             {
                 for (int j = 0; j < kRobCand; ++j)
-                    sum += robust_crossing<P>(q, tri + 9 * int64_t(cand[j]));
+                    sum += decide(cand[j]);
                 nc = 0;
             }
             cand[nc++] = leaf;
@@ -511,7 +521,7 @@ __global__ void __launch_bounds__(kRobBlock) k_robust_cells(const BvhNode* __res
         else if (!hier_walk(nodes, leaf_uv, u, v, w, tol, m8, consider))
             atomicOr(flags + FLAG_STACK, 1);
         for (int j = 0; j < nc; ++j)
-            sum += robust_crossing<P>(q, tri + 9 * int64_t(cand[j]));
+            sum += decide(cand[j]);
         counts[i] = sum;
     }
 }
