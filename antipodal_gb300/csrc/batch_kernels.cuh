@@ -33,13 +33,19 @@ __device__ __forceinline__ int batch_count(const BMesh& m, const Frame32& f, qv3
     int sum = 0;
     int cand[kRobCand];
     int nc = 0;
+    // most leaves are decided in float on the exact -x frame, the rest by the exact predicate (as k_robust_cells)
+    auto const decide = [&](int leaf) -> int
+    {
+        int const c = certain_leaf(m.leaf_uv, leaf, u, v, w, m8);
+        return c != 2 ? c : robust_crossing<P>(q, tri + 9 * int64_t(leaf));
+    };
     bool const ok = hier_walk<kStack>(m.nodes, m.leaf_uv, u, v, w, tol, m8,
                                       [&](int leaf)
                                       {
                                           if (nc == kRobCand)
                                           {
                                               for (int j = 0; j < kRobCand; ++j)
-                                                  sum += robust_crossing<P>(q, tri + 9 * int64_t(cand[j]));
+                                                  sum += decide(cand[j]);
                                               nc = 0;
                                           }
                                           cand[nc++] = leaf;
@@ -47,7 +53,7 @@ __device__ __forceinline__ int batch_count(const BMesh& m, const Frame32& f, qv3
     if (!ok)
         atomicOr(flags + FLAG_STACK, 1);
     for (int j = 0; j < nc; ++j)
-        sum += robust_crossing<P>(q, tri + 9 * int64_t(cand[j]));
+        sum += decide(cand[j]);
     return sum;
 }
 
