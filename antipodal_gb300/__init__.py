@@ -636,7 +636,7 @@ class LearnedGK15Proposal:
     accumulation), predicts for each (query, curve) pair the shallowest depth at which the plain integrator
     accepts a panel.  Used as ``integrator=`` of eval_gwnr_parametric_batch_fractional, it only chooses where the
     plain integrator starts evaluating; every evaluated panel is still accepted or refined by the plain error
-    test, so the plain method is both the fallback and the judge.  ``alpha`` bounds the predicted probability
+    test, so the plain method is both the fallback and the arbiter.  ``alpha`` bounds the predicted probability
     that a proposed depth overshoots the true one (an overshoot costs extra panels and refines beyond the plain
     tree; it never skips the error test).
     """

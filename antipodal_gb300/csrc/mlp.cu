@@ -2,7 +2,7 @@
 // (query, boundary curve) pair, the shallowest depth at which the plain adaptive integrator
 // (src/antipodal/math/integrate_gk15.hh:63-290) accepts a panel.  The proposal only says where the integrator
 // starts evaluating: panels above the proposed depth are split unevaluated, every evaluated panel is accepted or
-// split by the plain |Ik - Ig| <= tol 2^-depth test, so the plain method stays the judge (param.cu).  No
+// split by the plain |Ik - Ig| <= tol 2^-depth test, so the plain method decides every panel (param.cu).  No
 // counterpart in the reference.
 //
 // All three layers run on the tensor cores (mma.sync m16n8k16, BF16 operands, FP32 accumulation): inference,
