@@ -206,7 +206,7 @@ template <class T, class FB>
 int fractional_launch_mixed(Context& ctx, const FracPlan<T>& p, const double* d_pos, int64_t n, double* d_out,
                             const int32_t* d_counts, FB fb)
 {
-    int const K = ctx.queries_per_thread;
+    int const K = std::max(2, ctx.queries_per_thread); // the kernel packs its queries in pairs
     // measured: one tile, 128 threads (10.2 ms against 10.6 on a 212-segment boundary); several tiles, 256 threads
     // (34.9 ms against 40.5 on 1,066 segments), since more queries share each staged tile and its barriers
     int const block = ctx.frac_block ? ctx.frac_block : (p.nbuf > 1 || p.tile > 512 ? 256 : 128);
@@ -225,8 +225,6 @@ int fractional_launch_mixed(Context& ctx, const FracPlan<T>& p, const double* d_
     };
     switch (K)
     {
-    case 1:
-        return launch(k_frac_mixed<1, FB>);
     case 2:
         return launch(k_frac_mixed<2, FB>);
     case 4:

@@ -579,11 +579,62 @@ __device__ __forceinline__ void fp64_flush(Fp64Queue<K>& q, unsigned c, int lane
     q.head += c;
 }
 
-// Per-vertex quantities of one boundary vertex relative to one query (frame coordinates): v = vertex - query and
-// the half-angle form (n, d) of l + z, l = |v|; d is NaN at a near vertex.
-struct VState
+// Packed FP32 pairs (sm_100 and later): one instruction evaluates the same operation for two queries, each lane
+// rounded as the scalar operation would be.
+__device__ __forceinline__ float2 pk(float x)
 {
-    float x, y, z, n, d;
+    return make_float2(x, x);
+}
+__device__ __forceinline__ float2 pk_add(float2 a, float2 b)
+{
+    return __fadd2_rn(a, b);
+}
+__device__ __forceinline__ float2 pk_mul(float2 a, float2 b)
+{
+    return __fmul2_rn(a, b);
+}
+__device__ __forceinline__ float2 pk_fma(float2 a, float2 b, float2 c)
+{
+    return __ffma2_rn(a, b, c);
+}
+// a - b, rounded once (b * -1 + a)
+__device__ __forceinline__ float2 pk_sub(float2 a, float2 b)
+{
+    return __ffma2_rn(b, pk(-1.f), a);
+}
+
+// two_sum_acc on each lane of a pair
+__device__ __forceinline__ void two_sum_acc2(float2& acc, float2& comp, float2 x)
+{
+    float2 const s = pk_add(acc, x);
+    float2 const bp = pk_sub(s, acc);
+    float2 const ap = pk_sub(s, bp);
+    float2 const e = pk_add(pk_sub(acc, ap), pk_sub(x, bp));
+    acc = s;
+    comp = pk_add(comp, e);
+}
+
+// atan_unit on each lane of a pair (the same polynomial)
+__device__ __forceinline__ float2 atan_unit2(float2 t)
+{
+    float2 const s = pk_mul(t, t);
+    float2 p = pk(0.0028498897585520423f);
+    p = pk_fma(p, s, pk(-0.01606862951374933f));
+    p = pk_fma(p, s, pk(0.04269152017510156f));
+    p = pk_fma(p, s, pk(-0.07504294615760822f));
+    p = pk_fma(p, s, pk(0.10640934061441572f));
+    p = pk_fma(p, s, pk(-0.1420364447570674f));
+    p = pk_fma(p, s, pk(0.1999261939280182f));
+    p = pk_fma(p, s, pk(-0.3333307334510578f));
+    p = pk_fma(p, s, pk(0.9999999847657755f));
+    return pk_mul(t, p);
+}
+
+// Per-vertex quantities of one boundary vertex relative to two queries (frame coordinates, one lane each):
+// v = vertex - query and the half-angle form (n, d) of l + z, l = |v|; d is NaN at a near vertex.
+struct VState2
+{
+    float2 x, y, z, n, d;
 };
 
 // Blocks per SM the mixed kernel is compiled for: registers per thread scale with the queries per thread.
@@ -593,7 +644,8 @@ constexpr int mixed_min_blocks()
     return K >= 8 ? 1 : (K >= 4 ? 2 : (K >= 2 ? 3 : 4));
 }
 
-// fb: the FP64 rule for the pairs the FP32 path turns down (MeshFallback, or the robust evaluator's).
+// fb: the FP64 rule for the pairs the FP32 path turns down (MeshFallback, or the robust evaluator's).  K (even)
+// queries per thread, evaluated as K / 2 packed pairs.
 template <int K, class FB>
 __global__ void __launch_bounds__(256, mixed_min_blocks<K>())
     k_frac_mixed(const double* __restrict__ pos, int64_t n, double* __restrict__ out, const int32_t* __restrict__ counts,
@@ -602,6 +654,8 @@ __global__ void __launch_bounds__(256, mixed_min_blocks<K>())
                  long long* counters, int count_pairs)
 {
     (void)tau;
+    static_assert(K % 2 == 0, "queries per thread come in packed pairs");
+    constexpr int KP = K / 2;
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ __align__(8) uint64_t bars[2];
     __shared__ int abort_cta;
@@ -657,11 +711,13 @@ __global__ void __launch_bounds__(256, mixed_min_blocks<K>())
     {
         int64_t const tile_base = (blockIdx.x + int64_t(j) * gridDim.x) * per_tile;
         int64_t const base = tile_base + threadIdx.x;
-        float qhx[K], qhy[K], qhz[K], qlx[K], qly[K], qlz[K];
-        float acc[K], comp[K];
+        // the queries' frame coordinates as float hi + lo, negated (the vertex difference is then an add), queries
+        // 2p and 2p + 1 in the lanes of pair p
+        float2 nqhx[KP], nqhy[KP], nqhz[KP], nqlx[KP], nqly[KP], nqlz[KP];
+        float2 acc[KP], comp[KP];
         double acc64[K];
         // per-vertex state of the two most recent entries, in alternation (even entries write st0, odd ones st1)
-        VState st0[K], st1[K];
+        VState2 st0[KP], st1[KP];
 #pragma unroll
         for (int k = 0; k < K; ++k)
         {
@@ -672,17 +728,25 @@ __global__ void __launch_bounds__(256, mixed_min_blocks<K>())
             double const Qx = rot.m[0] * dx + rot.m[1] * dy + rot.m[2] * dz;
             double const Qy = rot.m[3] * dx + rot.m[4] * dy + rot.m[5] * dz;
             double const Qz = rot.m[6] * dx + rot.m[7] * dy + rot.m[8] * dz;
-            qhx[k] = __double2float_rn(Qx);
-            qhy[k] = __double2float_rn(Qy);
-            qhz[k] = __double2float_rn(Qz);
-            qlx[k] = __double2float_rn(Qx - double(qhx[k]));
-            qly[k] = __double2float_rn(Qy - double(qhy[k]));
-            qlz[k] = __double2float_rn(Qz - double(qhz[k]));
-            acc[k] = 0.f;
-            comp[k] = 0.f;
+            float const hx = __double2float_rn(Qx), hy = __double2float_rn(Qy), hz = __double2float_rn(Qz);
+            float const lx = __double2float_rn(Qx - double(hx)), ly = __double2float_rn(Qy - double(hy)),
+                        lz = __double2float_rn(Qz - double(hz));
+            auto const set = [&](float2& v, float x) { (k & 1 ? v.y : v.x) = x; };
+            set(nqhx[k / 2], -hx);
+            set(nqhy[k / 2], -hy);
+            set(nqhz[k / 2], -hz);
+            set(nqlx[k / 2], -lx);
+            set(nqly[k / 2], -ly);
+            set(nqlz[k / 2], -lz);
             acc64[k] = 0.0;
-            st0[k] = VState{};
-            st1[k] = VState{};
+        }
+#pragma unroll
+        for (int p = 0; p < KP; ++p)
+        {
+            acc[p] = pk(0.f);
+            comp[p] = pk(0.f);
+            st0[p] = VState2{};
+            st1[p] = VState2{};
         }
         // Pairs that go to FP64 are marked in a bit mask (bit slot * K + k) while two entries are evaluated, and
         // pushed to the warp's queue afterwards behind one warp-uniform branch that is rarely taken.
@@ -691,60 +755,80 @@ __global__ void __launch_bounds__(256, mixed_min_blocks<K>())
         // previous entry's vertex (pv) to this one.  With may_start false (both entries of the pair are segments,
         // the common case) the body has no branches: a term taken to FP64 adds an exact zero to the TwoSum, so the
         // compiler schedules consecutive entries together.  With may_start true a chain start skips the pair term.
-        auto step = [&](SegM const& ent, VState (&pv)[K], VState (&cv)[K], bool may_start, int slot)
+        // The arithmetic runs on packed pairs of queries; selects and comparisons per lane.
+        auto step = [&](SegM const& ent, VState2 (&pv)[KP], VState2 (&cv)[KP], bool may_start, int slot)
         {
             float4 const A = ent.a, B = ent.b, C = ent.c;
             int const sidx = __float_as_int(C.w);
+            float2 const ax = pk(A.x), ay = pk(A.y), az = pk(A.z), cx = pk(C.x), cy = pk(C.y), cz = pk(C.z);
 #pragma unroll
-            for (int k = 0; k < K; ++k)
+            for (int p = 0; p < KP; ++p)
             {
-                VState& c = cv[k];
-                c.x = (A.x - qhx[k]) + (C.x - qlx[k]);
-                c.y = (A.y - qhy[k]) + (C.y - qly[k]);
-                c.z = (A.z - qhz[k]) + (C.z - qlz[k]);
-                float const r = c.x * c.x + c.y * c.y;
-                float const q = r + c.z * c.z;
-                float const l = q * rsqrtf(q);
+                VState2& c = cv[p];
+                c.x = pk_add(pk_add(ax, nqhx[p]), pk_add(cx, nqlx[p]));
+                c.y = pk_add(pk_add(ay, nqhy[p]), pk_add(cy, nqly[p]));
+                c.z = pk_add(pk_add(az, nqhz[p]), pk_add(cz, nqlz[p]));
+                float2 const r = pk_fma(c.x, c.x, pk_mul(c.y, c.y));
+                float2 const q = pk_fma(c.z, c.z, r);
+                float2 const l = pk_mul(q, make_float2(rsqrtf(q.x), rsqrtf(q.y)));
                 // l + z = n / d with (n, d) = (l + z, 1) for z >= 0 and (x^2 + y^2, l - z) for z < 0, free of
                 // cancellation.  d > 0, or NaN for a near vertex (|v|^2 < near2): the NaN makes the error bound of
                 // both segments at this vertex NaN, which sends them to FP64
-                c.n = c.z >= 0.f ? l + c.z : r;
-                float const d = c.z >= 0.f ? 1.f : l - c.z;
-                c.d = q < B.w ? __int_as_float(0x7fffffff) : d;
+                float2 const lpz = pk_add(l, c.z), lmz = pk_sub(l, c.z);
+                float const nan = __int_as_float(0x7fffffff);
+                c.n = make_float2(c.z.x >= 0.f ? lpz.x : r.x, c.z.y >= 0.f ? lpz.y : r.y);
+                c.d = make_float2(q.x < B.w ? nan : (c.z.x >= 0.f ? 1.f : lmz.x),
+                                  q.y < B.w ? nan : (c.z.y >= 0.f ? 1.f : lmz.y));
             }
             if (may_start && sidx < 0)
                 return;
+            float2 const by = pk(B.y), nbx = pk(-B.x), w = pk(A.w);
 #pragma unroll
-            for (int k = 0; k < K; ++k)
+            for (int p = 0; p < KP; ++p)
             {
-                VState const& v0 = pv[k];
-                VState const& v1 = cv[k];
+                VState2 const& v0 = pv[p];
+                VState2 const& v1 = cv[p];
                 // num from the segment vector B (accurate on its own, no cancellation for a far segment)
-                float const ta = v0.x * B.y, tb = v0.y * B.x;
-                float const num = ta - tb;
+                float2 const ta = pk_mul(v0.x, by), tbn = pk_mul(v0.y, nbx); // v0.x * B.y and -(v0.y * B.x)
+                float2 const num = pk_add(ta, tbn);
                 // scaling num and den by the positive D = d0 * d1 leaves the angle unchanged and removes both
                 // divisions: den * D = n0 * n1 + (v0.x*v1.x + v0.y*v1.y) * D
-                float const D = v0.d * v1.d, nn = v0.n * v1.n;
-                float const pxy = v0.x * v1.x, pyy = v0.y * v1.y;
-                float const num_s = num * D;
-                float const den_s = fmaf(pxy + pyy, D, nn);
+                float2 const D = pk_mul(v0.d, v1.d), nn = pk_mul(v0.n, v1.n);
+                float2 const pxy = pk_mul(v0.x, v1.x), pyy = pk_mul(v0.y, v1.y);
+                float2 const num_s = pk_mul(num, D);
+                float2 const den_s = pk_fma(pk_add(pxy, pyy), D, nn);
                 // first-order rounding bounds: num errs by about eps * sn and den by about eps * sd, so the angle
                 // errs by at most eps * (sn * |den| + sd * |num|) / (num^2 + den^2) <= eps * (sn * ad1 + sd * an1) / M
                 // with M = max(|num|, |den|) and an1, ad1 the two divided by M: one of them is 1, the other is the
                 // ratio t that atan2 takes as well
-                float const sn = (fabsf(ta) + fabsf(tb)) * D;
-                float const sd = fmaf(fabsf(pxy) + fabsf(pyy), D, nn);
-                float const an = fabsf(num_s), ad = fabsf(den_s);
-                bool const swap = an > ad;
-                float const inv = __fdividef(1.f, fmaxf(swap ? an : ad, 1e-37f));
-                float const t = fminf(an, ad) * inv;
-                float const bound = fmaf(swap ? sn : sd, t, swap ? sd : sn) * inv; // in units of kEpsBound
+                float2 const sn =
+                    pk_mul(make_float2(fabsf(ta.x) + fabsf(tbn.x), fabsf(ta.y) + fabsf(tbn.y)), D);
+                float2 const sd =
+                    pk_fma(make_float2(fabsf(pxy.x) + fabsf(pyy.x), fabsf(pxy.y) + fabsf(pyy.y)), D, nn);
+                float2 const an = make_float2(fabsf(num_s.x), fabsf(num_s.y));
+                float2 const ad = make_float2(fabsf(den_s.x), fabsf(den_s.y));
+                bool const sw0 = an.x > ad.x, sw1 = an.y > ad.y;
+                float2 const inv = make_float2(__fdividef(1.f, fmaxf(sw0 ? an.x : ad.x, 1e-37f)),
+                                               __fdividef(1.f, fmaxf(sw1 ? an.y : ad.y, 1e-37f)));
+                float2 const t = pk_mul(make_float2(fminf(an.x, ad.x), fminf(an.y, ad.y)), inv);
+                float2 const bound = pk_mul(pk_fma(make_float2(sw0 ? sn.x : sd.x, sw1 ? sn.y : sd.y), t,
+                                                   make_float2(sw0 ? sd.x : sn.x, sw1 ? sd.y : sn.y)),
+                                            inv); // in units of kEpsBound
                 // a NaN or infinity anywhere (a near vertex, |v| = 0, overflow) makes the bound NaN, which the negated
                 // comparison sends to FP64; so does a branch (den <= 0) decided within the rounding of num
-                bool const need = !(bound <= te_units) || fmaxf(den_s, fmaf(-kEpsBound, sn, an)) <= 0.f;
-                nb |= need ? (1u << (slot * K + k)) : 0u;
-                float const term = A.w * atan2_unit(num_s, den_s, t, swap);
-                two_sum_acc(acc[k], comp[k], need ? 0.f : term);
+                float2 const margin = pk_fma(pk(-kEpsBound), sn, an);
+                bool const need0 = !(bound.x <= te_units) || fmaxf(den_s.x, margin.x) <= 0.f;
+                bool const need1 = !(bound.y <= te_units) || fmaxf(den_s.y, margin.y) <= 0.f;
+                nb |= (need0 ? (1u << (slot * K + 2 * p)) : 0u) | (need1 ? (1u << (slot * K + 2 * p + 1)) : 0u);
+                // atan2(num_s, den_s): atan(t), then the octant
+                float2 a = atan_unit2(t);
+                float2 const a_sw = pk_sub(pk(1.5707963267948966f), a);
+                a = make_float2(sw0 ? a_sw.x : a.x, sw1 ? a_sw.y : a.y);
+                float2 const a_neg = pk_sub(pk(3.141592653589793f), a);
+                a = make_float2(copysignf(den_s.x < 0.f ? a_neg.x : a.x, num_s.x),
+                                copysignf(den_s.y < 0.f ? a_neg.y : a.y, num_s.y));
+                float2 const term = pk_mul(w, a);
+                two_sum_acc2(acc[p], comp[p], make_float2(need0 ? 0.f : term.x, need1 ? 0.f : term.y));
             }
         };
         // the marked pairs of `count` entries from sb[s0] into the queue (the caller then drains full batches: at
@@ -837,7 +921,8 @@ __global__ void __launch_bounds__(256, mixed_min_blocks<K>())
             int64_t const i = base + int64_t(k) * blockDim.x;
             if (i < n)
             {
-                double v = ((double(acc[k]) + double(comp[k])) + acc64[k]) / two_pi;
+                float const ak = (k & 1) ? acc[k / 2].y : acc[k / 2].x, ck = (k & 1) ? comp[k / 2].y : comp[k / 2].x;
+                double v = ((double(ak) + double(ck)) + acc64[k]) / two_pi;
                 if (counts)
                     v += double(counts[i]);
                 out[i] = v;
