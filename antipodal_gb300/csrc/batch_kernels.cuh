@@ -146,9 +146,13 @@ __global__ void __launch_bounds__(256) k_batch(const BMesh* __restrict__ meshes,
             qv3<C> q[K];
             int cnt[K];
             double half[K];
-            float acc[K], comp[K];
+            using LV = typename RLanes<K>::V;
+            LV acc[RLanes<K>::NP], comp[RLanes<K>::NP];
             int64_t idx[K];
-            RVState st0[K] = {}, st1[K] = {};
+            RVState<LV> st0[RLanes<K>::NP] = {}, st1[RLanes<K>::NP] = {};
+#pragma unroll
+            for (int p = 0; p < RLanes<K>::NP; ++p)
+                acc[p] = comp[p] = lv_set<LV>(0.f);
 #pragma unroll
             for (int k = 0; k < K; ++k)
             {
@@ -157,7 +161,6 @@ __global__ void __launch_bounds__(256) k_batch(const BMesh* __restrict__ meshes,
                 q[k] = quantize<P>(double(pos[3 * ii]), double(pos[3 * ii + 1]), double(pos[3 * ii + 2]), qz);
                 cnt[k] = batch_count<P, kStack>(m, f, q[k], flags);
                 half[k] = 0.0;
-                acc[k] = comp[k] = 0.f;
             }
             for (int st = 0; st < n_tiles; ++st)
             {
@@ -213,7 +216,8 @@ __global__ void __launch_bounds__(256) k_batch(const BMesh* __restrict__ meshes,
                 if (idx[k] < item.q1)
                 {
                     if constexpr (Mixed)
-                        half[k] = __dadd_rn(half[k], __dadd_rn(double(acc[k]), double(comp[k])));
+                        half[k] = __dadd_rn(half[k], __dadd_rn(double(ln(acc[k / RLanes<K>::W], k % RLanes<K>::W)),
+                                                               double(ln(comp[k / RLanes<K>::W], k % RLanes<K>::W))));
                     T const fr = T(__dmul_rn(half[k], f_norm));
                     out[idx[k]] = fr + T(cnt[k]);
                     if (m.counts)

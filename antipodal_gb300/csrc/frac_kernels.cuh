@@ -6,6 +6,8 @@
 #include "agwn_internal.cuh"
 #include "tma.cuh"
 
+#include <type_traits>
+
 #include <climits>
 #include <cmath>
 
@@ -628,6 +630,91 @@ __device__ __forceinline__ float2 atan_unit2(float2 t)
     p = pk_fma(p, s, pk(-0.3333307334510578f));
     p = pk_fma(p, s, pk(0.9999999847657755f));
     return pk_mul(t, p);
+}
+
+// The same operations on a lane vector: one query (float) or a packed pair of queries (float2).  Each lane is
+// rounded as the scalar operation would be, so code written over a lane vector gives bit-identical lanes for one
+// query per thread and for two.
+__device__ __forceinline__ float lv_add(float a, float b)
+{
+    return __fadd_rn(a, b);
+}
+__device__ __forceinline__ float lv_mul(float a, float b)
+{
+    return __fmul_rn(a, b);
+}
+__device__ __forceinline__ float lv_fma(float a, float b, float c)
+{
+    return __fmaf_rn(a, b, c);
+}
+__device__ __forceinline__ float2 lv_add(float2 a, float2 b)
+{
+    return __fadd2_rn(a, b);
+}
+__device__ __forceinline__ float2 lv_mul(float2 a, float2 b)
+{
+    return __fmul2_rn(a, b);
+}
+__device__ __forceinline__ float2 lv_fma(float2 a, float2 b, float2 c)
+{
+    return __ffma2_rn(a, b, c);
+}
+template <class V>
+__device__ __forceinline__ V lv_set(float x)
+{
+    if constexpr (std::is_same_v<V, float>)
+        return x;
+    else
+        return make_float2(x, x);
+}
+// a - b, rounded once
+template <class V>
+__device__ __forceinline__ V lv_sub(V a, V b)
+{
+    return lv_fma(b, lv_set<V>(-1.f), a);
+}
+// lane h of a lane vector
+__device__ __forceinline__ float& ln(float& v, int)
+{
+    return v;
+}
+__device__ __forceinline__ float ln(float const& v, int)
+{
+    return v;
+}
+__device__ __forceinline__ float& ln(float2& v, int h)
+{
+    return h ? v.y : v.x;
+}
+__device__ __forceinline__ float ln(float2 const& v, int h)
+{
+    return h ? v.y : v.x;
+}
+template <class V>
+__device__ __forceinline__ void two_sum_lv(V& acc, V& comp, V x)
+{
+    V const s = lv_add(acc, x);
+    V const bp = lv_sub(s, acc);
+    V const ap = lv_sub(s, bp);
+    V const e = lv_add(lv_sub(acc, ap), lv_sub(x, bp));
+    acc = s;
+    comp = lv_add(comp, e);
+}
+// atan_unit on a lane vector (the same polynomial)
+template <class V>
+__device__ __forceinline__ V atan_unit_lv(V t)
+{
+    V const s = lv_mul(t, t);
+    V p = lv_set<V>(0.0028498897585520423f);
+    p = lv_fma(p, s, lv_set<V>(-0.01606862951374933f));
+    p = lv_fma(p, s, lv_set<V>(0.04269152017510156f));
+    p = lv_fma(p, s, lv_set<V>(-0.07504294615760822f));
+    p = lv_fma(p, s, lv_set<V>(0.10640934061441572f));
+    p = lv_fma(p, s, lv_set<V>(-0.1420364447570674f));
+    p = lv_fma(p, s, lv_set<V>(0.1999261939280182f));
+    p = lv_fma(p, s, lv_set<V>(-0.3333307334510578f));
+    p = lv_fma(p, s, lv_set<V>(0.9999999847657755f));
+    return lv_mul(t, p);
 }
 
 // Per-vertex quantities of one boundary vertex relative to two queries (frame coordinates, one lane each):

@@ -638,12 +638,23 @@ __device__ __forceinline__ void rq_flush(RQueue<K>& fq, unsigned c, int lane, co
     fq.head += c;
 }
 
-// Per-vertex quantities of one chain vertex relative to one query: v = p - q as floats (exact: below 2^24), and
-// the half-angle pair (n, d) of l + x; d is NaN when a difference is 2^24 or more (the pairs at that vertex go to
-// FP64).
+// The lane vectors of the chain loop: K = 1 query per thread as float, or K / 2 packed pairs (float2).
+template <int K>
+struct RLanes
+{
+    using V = std::conditional_t<K == 1, float, float2>;
+    static constexpr int W = K == 1 ? 1 : 2; // queries per lane vector
+    static constexpr int NP = K / W;         // lane vectors per thread
+    static_assert(K == 1 || K % 2 == 0, "one query per thread or packed pairs");
+};
+
+// Per-vertex quantities of one chain vertex relative to the queries of a lane vector: v = p - q as floats (exact:
+// below 2^24), and the half-angle pair (n, d) of l + x; d is NaN when a difference is 2^24 or more (the pairs at
+// that vertex go to FP64).
+template <class V>
 struct RVState
 {
-    float x, y, z, n, d;
+    V x, y, z, n, d;
 };
 
 // One chain entry with K queries: its vertex into cv, then (a segment entry) the fractional term of the segment
@@ -656,53 +667,109 @@ struct RVState
 // num errs by 4u |num| and den = A B + yz by 4u (|A B| + |yz|), so the angle errs by about
 // (|num| E_d + |den| E_n) / (num^2 + den^2).  The pair stays in FP32 when that is at most term_err; num == 0 (where
 // the reference takes its exact branches), a difference of 2^24 or more and ill-conditioned pairs go to FP64 with
-// the reference's formula.
+// the reference's formula.  The arithmetic runs on lane vectors (RLanes), so one query per thread and packed
+// pairs give the same bits; selects and comparisons per lane.
 template <int K>
-__device__ __forceinline__ void robust_chain_entry(RChain const& e, qv3<int32_t> const (&q)[K], RVState (&pv)[K],
-                                                   RVState (&cv)[K], float term_err, float (&acc)[K],
-                                                   float (&comp)[K], uint32_t& bits, int slot)
+__device__ __forceinline__ void robust_chain_entry(RChain const& e, qv3<int32_t> const (&q)[K],
+                                                   RVState<typename RLanes<K>::V> (&pv)[RLanes<K>::NP],
+                                                   RVState<typename RLanes<K>::V> (&cv)[RLanes<K>::NP], float term_err,
+                                                   typename RLanes<K>::V (&acc)[RLanes<K>::NP],
+                                                   typename RLanes<K>::V (&comp)[RLanes<K>::NP], uint32_t& bits,
+                                                   int slot)
 {
+    using L = RLanes<K>;
+    using V = typename L::V;
     unsigned const lim = 1u << 25, off = 1u << 24;
 #pragma unroll
-    for (int k = 0; k < K; ++k)
+    for (int p = 0; p < L::NP; ++p)
     {
-        int32_t const vx = e.p[0] - q[k].x, vy = e.p[1] - q[k].y, vz = e.p[2] - q[k].z;
-        bool const small = unsigned(vx) + off < lim && unsigned(vy) + off < lim && unsigned(vz) + off < lim;
-        RVState& c = cv[k];
-        c.x = float(vx);
-        c.y = float(vy);
-        c.z = float(vz);
-        float const yz = fmaf(c.y, c.y, c.z * c.z);
-        float const sq = fmaf(c.x, c.x, yz);
-        float const l = sq * rsqrtf(sq);
-        c.n = c.x >= 0.f ? l + c.x : yz;
-        float const d = c.x >= 0.f ? 1.f : l - c.x;
-        c.d = small ? d : __int_as_float(0x7fffffff);
+        RVState<V>& c = cv[p];
+        bool small[L::W];
+#pragma unroll
+        for (int h = 0; h < L::W; ++h)
+        {
+            int const k = p * L::W + h;
+            int32_t const vx = e.p[0] - q[k].x, vy = e.p[1] - q[k].y, vz = e.p[2] - q[k].z;
+            small[h] = unsigned(vx) + off < lim && unsigned(vy) + off < lim && unsigned(vz) + off < lim;
+            ln(c.x, h) = float(vx);
+            ln(c.y, h) = float(vy);
+            ln(c.z, h) = float(vz);
+        }
+        V const yz = lv_fma(c.y, c.y, lv_mul(c.z, c.z));
+        V const sq = lv_fma(c.x, c.x, yz);
+        V rs;
+#pragma unroll
+        for (int h = 0; h < L::W; ++h)
+            ln(rs, h) = rsqrtf(ln(sq, h));
+        V const l = lv_mul(sq, rs);
+        V const lpx = lv_add(l, c.x), lmx = lv_sub(l, c.x);
+#pragma unroll
+        for (int h = 0; h < L::W; ++h)
+        {
+            bool const xpos = ln(c.x, h) >= 0.f;
+            ln(c.n, h) = xpos ? ln(lpx, h) : ln(yz, h);
+            ln(c.d, h) = small[h] ? (xpos ? 1.f : ln(lmx, h)) : __int_as_float(0x7fffffff);
+        }
     }
     if (e.s < 0)
         return; // a chain start: its vertex only
+    V const m1 = lv_set<V>(-1.f);
 #pragma unroll
-    for (int k = 0; k < K; ++k)
+    for (int p = 0; p < L::NP; ++p)
     {
-        RVState const& a = pv[k];
-        RVState const& b = cv[k];
-        float const pn = a.y * b.z, en = fmaf(a.y, b.z, -pn);
-        float const numf = fmaf(a.z, b.y, -pn) - en;
-        float const pz = a.z * b.z, ez = fmaf(a.z, b.z, -pz);
-        float const yzf = fmaf(a.y, b.y, pz) + ez;
-        float const D = a.d * b.d, ab = a.n * b.n, yzs = yzf * D;
-        float const num_s = numf * D, den_s = ab + yzs;
-        float const an = fabsf(num_s), ad = fabsf(den_s);
-        bool const swap = an > ad;
-        float const inv = __fdividef(1.f, fmaxf(swap ? an : ad, 1e-37f));
-        float const an1 = an * inv, ad1 = ad * inv;
+        RVState<V> const& a = pv[p];
+        RVState<V> const& b = cv[p];
+        V const pn = lv_mul(a.y, b.z);
+        V const npn = lv_mul(pn, m1);
+        V const en = lv_fma(a.y, b.z, npn);
+        V const numf = lv_sub(lv_fma(a.z, b.y, npn), en);
+        V const pz = lv_mul(a.z, b.z);
+        V const ez = lv_fma(a.z, b.z, lv_mul(pz, m1));
+        V const yzf = lv_add(lv_fma(a.y, b.y, pz), ez);
+        V const D = lv_mul(a.d, b.d), ab = lv_mul(a.n, b.n), yzs = lv_mul(yzf, D);
+        V const num_s = lv_mul(numf, D), den_s = lv_add(ab, yzs);
+        V an, ad, inv, sab;
+        bool swap[L::W];
+#pragma unroll
+        for (int h = 0; h < L::W; ++h)
+        {
+            float const anh = fabsf(ln(num_s, h)), adh = fabsf(ln(den_s, h));
+            swap[h] = anh > adh;
+            ln(an, h) = anh;
+            ln(ad, h) = adh;
+            ln(inv, h) = __fdividef(1.f, fmaxf(swap[h] ? anh : adh, 1e-37f));
+            ln(sab, h) = __fadd_rn(fabsf(ln(ab, h)), fabsf(ln(yzs, h)));
+        }
+        V const an1 = lv_mul(an, inv), ad1 = lv_mul(ad, inv);
         constexpr float k4u = 4.f * 5.9604645e-8f;
-        float const bound = k4u * fmaf(an1, (fabsf(ab) + fabsf(yzs)) * inv, ad1 * an1);
-        // num == 0 (the reference's exact branches), an out-of-range difference (NaN d) or an ill-conditioned pair
-        bool const need = numf == 0.f || !(bound <= term_err * fmaf(an1, an1, ad1 * ad1));
-        bits |= need ? (1u << (slot * K + k)) : 0u;
-        float const th = atan2_unit(num_s, den_s, swap ? ad1 : an1, swap);
-        two_sum_acc(acc[k], comp[k], need ? 0.f : e.w * th);
+        V const bound = lv_mul(lv_set<V>(k4u), lv_fma(an1, lv_mul(sab, inv), lv_mul(ad1, an1)));
+        V const rhs = lv_mul(lv_set<V>(term_err), lv_fma(an1, an1, lv_mul(ad1, ad1)));
+        V t, x;
+#pragma unroll
+        for (int h = 0; h < L::W; ++h)
+            ln(t, h) = swap[h] ? ln(ad1, h) : ln(an1, h);
+        // atan2(num_s, den_s): atan(t), then the octant
+        V th = atan_unit_lv(t);
+        V const th_sw = lv_sub(lv_set<V>(1.5707963267948966f), th);
+#pragma unroll
+        for (int h = 0; h < L::W; ++h)
+            ln(th, h) = swap[h] ? ln(th_sw, h) : ln(th, h);
+        V const th_neg = lv_sub(lv_set<V>(3.141592653589793f), th);
+        V const w = lv_set<V>(e.w);
+#pragma unroll
+        for (int h = 0; h < L::W; ++h)
+            ln(th, h) = copysignf(ln(den_s, h) < 0.f ? ln(th_neg, h) : ln(th, h), ln(num_s, h));
+        V const term = lv_mul(w, th);
+#pragma unroll
+        for (int h = 0; h < L::W; ++h)
+        {
+            // num == 0 (the reference's exact branches), an out-of-range difference (NaN d) or an ill-conditioned
+            // pair
+            bool const need = ln(numf, h) == 0.f || !(ln(bound, h) <= ln(rhs, h));
+            bits |= need ? (1u << (slot * K + p * L::W + h)) : 0u;
+            ln(x, h) = need ? 0.f : ln(term, h);
+        }
+        two_sum_lv(acc[p], comp[p], x);
     }
 }
 
@@ -712,9 +779,11 @@ __device__ __forceinline__ void robust_chain_entry(RChain const& e, qv3<int32_t>
 // and the batch kernel, so their sums agree bit for bit.
 template <class P, int K>
 __device__ __forceinline__ void robust_chain_step(RChain const* sb, int s, int ne, qv3<int32_t> const (&q)[K],
-                                                  RVState (&st0)[K], RVState (&st1)[K], float term_err,
-                                                  float (&acc)[K], float (&comp)[K], RQueue<K>& fq, int lane,
-                                                  RSeg<typename P::C> const* gseg, double (&half)[K])
+                                                  RVState<typename RLanes<K>::V> (&st0)[RLanes<K>::NP],
+                                                  RVState<typename RLanes<K>::V> (&st1)[RLanes<K>::NP],
+                                                  float term_err, typename RLanes<K>::V (&acc)[RLanes<K>::NP],
+                                                  typename RLanes<K>::V (&comp)[RLanes<K>::NP], RQueue<K>& fq,
+                                                  int lane, RSeg<typename P::C> const* gseg, double (&half)[K])
 {
     uint32_t bits = 0;
     robust_chain_entry<K>(sb[s], q, st1, st0, term_err, acc, comp, bits, 0);
@@ -800,7 +869,7 @@ __global__ void __launch_bounds__(kRobBlock) k_robust_frac(const T* __restrict__
         float acc[1] = {0.f}, comp[1] = {0.f};
         decltype(q) qarr[1] = {q};
         double harr[1] = {0.0};
-        RVState st0[1] = {}, st1[1] = {};
+        RVState<float> st0[1] = {}, st1[1] = {};
         for (int st = 0; st < pipe.n_tiles && n_seg > 0; ++st)
         {
             int const b = it & 1;
