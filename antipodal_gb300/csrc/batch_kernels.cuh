@@ -29,7 +29,7 @@ __device__ __forceinline__ int batch_count(const BMesh& m, const Frame32& f, qv3
     float const w = f.r[6] * ox + f.r[7] * oy + f.r[8] * oz;
     float const qmax = fmaxf(fmaxf(fabsf(ox), fabsf(oy)), fabsf(oz));
     float const tol = (qmax + m.scene_scale) * 3.8146973e-6f + 1e-30f;
-    float const m8 = 8.0f * 1e-6f * (qmax + m.scene_scale);
+    float const m8 = margin_permuted(qmax, m.scene_scale);
     int sum = 0;
     int cand[kRobCand];
     int nc = 0;

@@ -35,6 +35,29 @@ struct Frame32
 // in the ray frame, rounded to float.
 constexpr int kLeafF4 = 3;
 
+// m8 = 8 delta for may_hit and certain_leaf, from the query's largest |coordinate| qmax and the mesh's
+// scene_scale (eps = 2^-24).  delta must bound (1) the error of every float (u, v, w) coordinate and (2) a quarter
+// of the rounding of the float edge functions, 4 eps R with R the largest |query - corner| coordinate difference:
+// then certain_leaf's error model (3 delta (|du| + |dv| + |ru| + |rv|) per edge function, 2 delta per depth, both
+// doubled in the depth test) holds, and may_hit's threshold 8 delta leaves a factor above it.
+// Rotated frame (the mesh intersector's hierarchy for any direction): a query coordinate is rounded to float and
+// rotated by the float frame (rows within eps of the FP64 frame) in at most five rounded operations, so it errs by at
+// most 7 eps sum_i |r_i| |p_i| <= 7 sqrt(3) eps qmax = 7.3e-7 qmax; a leaf corner is projected in FP64 and rounded
+// once, within sqrt(3) eps scene_scale = 1.04e-7 scene_scale; R <= sqrt(3) (qmax + scene_scale), so 4 eps R <=
+// 4.13e-7 (qmax + scene_scale).  delta = 8e-7 qmax + 4.2e-7 scene_scale covers both.
+__device__ __forceinline__ float margin_rotated(float qmax, float scene_scale)
+{
+    return 8.0f * fmaf(8e-7f, qmax, 4.2e-7f * scene_scale);
+}
+// Permutation frame (the robust evaluator's (z, y, -x) for the -x ray): products by 0 and 1 and sums with zeros are
+// exact, so a query coordinate only carries its rounding to float (eps qmax) and a corner its own (eps
+// scene_scale); R <= qmax + scene_scale, so 4 eps R <= 2.4e-7 (qmax + scene_scale).  delta = 3e-7 (qmax +
+// scene_scale) covers both.
+__device__ __forceinline__ float margin_permuted(float qmax, float scene_scale)
+{
+    return 8.0f * 3e-7f * (qmax + scene_scale);
+}
+
 __device__ __forceinline__ bool may_hit(const float4* __restrict__ leaf_uv, int leaf, float u, float v, float m8)
 {
     float4 const a = leaf_uv[kLeafF4 * leaf], b = leaf_uv[kLeafF4 * leaf + 1];
@@ -59,9 +82,10 @@ __device__ __forceinline__ bool may_hit(const float4* __restrict__ leaf_uv, int 
 // is right-handed, so it is the sign of the triangle normal along the ray).  In front or behind: the plane's depth
 // at (u, v) minus the query's, (e1 dw_a + e2 dw_b + e0 dw_c) / E with E = e0 + e1 + e2, against the bound that the
 // edge functions' errors (3 delta (|du| + |dv| + |ru| + |rv|) each, delta = m8 / 8) and the depths' (2 delta each)
-// carry through that quotient, doubled.  delta is 1e-6 of the coordinate scale, far above the rounding of either
-// this float evaluation or the exact test, so a decided leaf gets the exact test's answer; only points within
-// that margin of an edge, a vertex or the plane go to the exact test.
+// carry through that quotient, doubled.  delta bounds the error of the float coordinates and a quarter of the
+// edge functions' rounding (margin_rotated, margin_permuted), and the exact test's own rounding is ~1e-16 of the
+// coordinates, so a decided leaf gets the exact test's answer; only points within that margin of an edge, a vertex
+// or the plane go to the exact test.
 __device__ __forceinline__ int certain_leaf(const float4* __restrict__ leaf_uv, int leaf, float u, float v, float w,
                                             float m8)
 {

@@ -371,7 +371,7 @@ __global__ void __launch_bounds__(kTravBlock) k_traverse(const BvhNode* __restri
             float const w = f.r[6] * ox + f.r[7] * oy + f.r[8] * oz;
             float const qmax = fmaxf(fmaxf(fabsf(ox), fabsf(oy)), fabsf(oz));
             float const tol = (qmax + scene_scale) * 3.8146973e-6f + 1e-30f; // 2^-18 of the coordinate scale
-            float const m8 = 8.0f * 1e-6f * (qmax + scene_scale);            // 8 * delta of may_hit
+            float const m8 = margin_rotated(qmax, scene_scale);
             // Double input: most candidates are decided in float by certain_leaf, whose margins are ~1e9 times the
             // FP64 test's rounding; the rest take NaiveIntersector's exact test.  Float input always takes the exact
             // test: its own rounding is not small enough against the margin for very thin triangles.
@@ -516,7 +516,7 @@ __global__ void __launch_bounds__(kTravBlock) k_cells(const BvhNode* __restrict_
         float const w = f.r[6] * ox + f.r[7] * oy + f.r[8] * oz;
         float const qmax = fmaxf(fmaxf(fabsf(ox), fabsf(oy)), fabsf(oz));
         float const tol = (qmax + scene_scale) * 3.8146973e-6f + 1e-30f; // as in k_traverse
-        float const m8 = 8.0f * 1e-6f * (qmax + scene_scale);
+        float const m8 = margin_rotated(qmax, scene_scale);
         auto const decide = [&](int leaf) -> int
         {
             if constexpr (std::is_same_v<T, double>)

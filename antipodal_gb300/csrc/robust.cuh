@@ -449,7 +449,7 @@ __global__ void __launch_bounds__(kRobBlock) k_robust_count(const BvhNode* __res
             float const w = f.r[6] * ox + f.r[7] * oy + f.r[8] * oz;
             float const qmax = fmaxf(fmaxf(fabsf(ox), fabsf(oy)), fabsf(oz));
             float const tol = (qmax + scene_scale) * 3.8146973e-6f + 1e-30f;
-            float const m8 = 8.0f * 1e-6f * (qmax + scene_scale);
+            float const m8 = margin_permuted(qmax, scene_scale);
             int cand[kRobCand];
             int nc = 0;
             bool const ok = hier_walk(nodes, leaf_uv, u, v, w, tol, m8,
@@ -497,7 +497,7 @@ __global__ void __launch_bounds__(kRobBlock) k_robust_cells(const BvhNode* __res
         float const w = f.r[6] * ox + f.r[7] * oy + f.r[8] * oz;
         float const qmax = fmaxf(fmaxf(fabsf(ox), fabsf(oy)), fabsf(oz));
         float const tol = (qmax + scene_scale) * 3.8146973e-6f + 1e-30f;
-        float const m8 = 8.0f * 1e-6f * (qmax + scene_scale);
+        float const m8 = margin_permuted(qmax, scene_scale);
         int sum = 0;
         int cand[kRobCand];
         int nc = 0;
