@@ -53,12 +53,16 @@ def parse():
     ap.add_argument("--config", choices=["mesh", "cube", "batch", "robust", "param"], default="mesh",
                     help="mesh: the headline single-mesh workload (default); the others are the secondary "
                          "workloads, each printing its own JSON line (see run_secondary)")
-    ap.add_argument("--scale", type=float, default=1.0,
-                    help="secondary workloads: fraction of the full query count (batch: of the grid side)")
+    ap.add_argument("--scale", type=float, default=None,
+                    help="secondary workloads: fraction of the full query count (batch: of the grid side); "
+                         "default 1, except param: 0.04 (40,000 of the 1e6 queries, a few minutes in all)")
     ap.add_argument("--patches", type=int, default=256, help="param workload: bicubic patches (4 curves each)")
     ap.add_argument("--batch-config", default=None,
                     help="batch workload: fixed launch configuration 'block,k,seg_tile,stack' instead of tuning")
-    return ap.parse_args()
+    args = ap.parse_args()
+    if args.scale is None:
+        args.scale = 0.04 if args.config == "param" else 1.0
+    return args
 
 
 def dist_env():
