@@ -469,16 +469,6 @@ __global__ void __launch_bounds__(1024) k_prep_mixed(const double* __restrict__ 
     }
 }
 
-__device__ __forceinline__ void two_sum_acc(float& acc, float& comp, float x)
-{
-    float const s = __fadd_rn(acc, x);
-    float const bp = __fsub_rn(s, acc);
-    float const ap = __fsub_rn(s, bp);
-    float const e = __fadd_rn(__fsub_rn(acc, ap), __fsub_rn(x, bp));
-    acc = s;
-    comp = __fadd_rn(comp, e);
-}
-
 // atan2 for the FP32 terms, our own: reduce to t = min(|y|, |x|) / max(|y|, |x|) in [0, 1], evaluate
 // atan(t) = t * P(t^2) with a degree-8 polynomial P, then unfold the octant.  P's coefficients come from a
 // minimax fit of atan(t) / t on [0, 1] by the Remez exchange algorithm (relative error 1.5e-8 in exact arithmetic,
@@ -496,14 +486,6 @@ __device__ __forceinline__ float atan_unit(float t)
     p = fmaf(p, s, -0.3333307334510578f);
     p = fmaf(p, s, 0.9999999847657755f);
     return t * p;
-}
-// atan2(y, x) given t = min(|x|, |y|) / max(|x|, |y|) and swap = |y| > |x|.
-__device__ __forceinline__ float atan2_unit(float y, float x, float t, bool swap)
-{
-    float a = atan_unit(t);
-    a = swap ? 1.5707963267948966f - a : a;
-    a = x < 0.f ? 3.141592653589793f - a : a;
-    return copysignf(a, y);
 }
 // atan2(y, x) given |x| and |y| already divided by max(|x|, |y|) (so the larger is 1).
 __device__ __forceinline__ float atan2_scaled(float y, float x, float ax1, float ay1)
@@ -581,60 +563,10 @@ __device__ __forceinline__ void fp64_flush(Fp64Queue<K>& q, unsigned c, int lane
     q.head += c;
 }
 
-// Packed FP32 pairs (sm_100 and later): one instruction evaluates the same operation for two queries, each lane
-// rounded as the scalar operation would be.
-__device__ __forceinline__ float2 pk(float x)
-{
-    return make_float2(x, x);
-}
-__device__ __forceinline__ float2 pk_add(float2 a, float2 b)
-{
-    return __fadd2_rn(a, b);
-}
-__device__ __forceinline__ float2 pk_mul(float2 a, float2 b)
-{
-    return __fmul2_rn(a, b);
-}
-__device__ __forceinline__ float2 pk_fma(float2 a, float2 b, float2 c)
-{
-    return __ffma2_rn(a, b, c);
-}
-// a - b, rounded once (b * -1 + a)
-__device__ __forceinline__ float2 pk_sub(float2 a, float2 b)
-{
-    return __ffma2_rn(b, pk(-1.f), a);
-}
-
-// two_sum_acc on each lane of a pair
-__device__ __forceinline__ void two_sum_acc2(float2& acc, float2& comp, float2 x)
-{
-    float2 const s = pk_add(acc, x);
-    float2 const bp = pk_sub(s, acc);
-    float2 const ap = pk_sub(s, bp);
-    float2 const e = pk_add(pk_sub(acc, ap), pk_sub(x, bp));
-    acc = s;
-    comp = pk_add(comp, e);
-}
-
-// atan_unit on each lane of a pair (the same polynomial)
-__device__ __forceinline__ float2 atan_unit2(float2 t)
-{
-    float2 const s = pk_mul(t, t);
-    float2 p = pk(0.0028498897585520423f);
-    p = pk_fma(p, s, pk(-0.01606862951374933f));
-    p = pk_fma(p, s, pk(0.04269152017510156f));
-    p = pk_fma(p, s, pk(-0.07504294615760822f));
-    p = pk_fma(p, s, pk(0.10640934061441572f));
-    p = pk_fma(p, s, pk(-0.1420364447570674f));
-    p = pk_fma(p, s, pk(0.1999261939280182f));
-    p = pk_fma(p, s, pk(-0.3333307334510578f));
-    p = pk_fma(p, s, pk(0.9999999847657755f));
-    return pk_mul(t, p);
-}
-
-// The same operations on a lane vector: one query (float) or a packed pair of queries (float2).  Each lane is
-// rounded as the scalar operation would be, so code written over a lane vector gives bit-identical lanes for one
-// query per thread and for two.
+// The same operations on a lane vector: one query (float) or a packed pair of queries (float2, the paired add /
+// multiply / FMA instructions of sm_100 and later, one instruction for both).  Each lane is rounded as the scalar
+// operation would be, so code written over a lane vector gives bit-identical lanes for one query per thread and
+// for two.
 __device__ __forceinline__ float lv_add(float a, float b)
 {
     return __fadd_rn(a, b);
@@ -690,6 +622,8 @@ __device__ __forceinline__ float ln(float2 const& v, int h)
 {
     return h ? v.y : v.x;
 }
+// Compensated accumulation: acc + x by TwoSum (Knuth), its exact rounding error added to comp.  The pair
+// (acc, comp) carries the sum to well below float's rounding, independently of the order of the terms.
 template <class V>
 __device__ __forceinline__ void two_sum_lv(V& acc, V& comp, V x)
 {
@@ -830,8 +764,8 @@ __global__ void __launch_bounds__(256, mixed_min_blocks<K>())
 #pragma unroll
         for (int p = 0; p < KP; ++p)
         {
-            acc[p] = pk(0.f);
-            comp[p] = pk(0.f);
+            acc[p] = lv_set<float2>(0.f);
+            comp[p] = lv_set<float2>(0.f);
             st0[p] = VState2{};
             st1[p] = VState2{};
         }
@@ -847,21 +781,21 @@ __global__ void __launch_bounds__(256, mixed_min_blocks<K>())
         {
             float4 const A = ent.a, B = ent.b, C = ent.c;
             int const sidx = __float_as_int(C.w);
-            float2 const ax = pk(A.x), ay = pk(A.y), az = pk(A.z), cx = pk(C.x), cy = pk(C.y), cz = pk(C.z);
+            float2 const ax = lv_set<float2>(A.x), ay = lv_set<float2>(A.y), az = lv_set<float2>(A.z), cx = lv_set<float2>(C.x), cy = lv_set<float2>(C.y), cz = lv_set<float2>(C.z);
 #pragma unroll
             for (int p = 0; p < KP; ++p)
             {
                 VState2& c = cv[p];
-                c.x = pk_add(pk_add(ax, nqhx[p]), pk_add(cx, nqlx[p]));
-                c.y = pk_add(pk_add(ay, nqhy[p]), pk_add(cy, nqly[p]));
-                c.z = pk_add(pk_add(az, nqhz[p]), pk_add(cz, nqlz[p]));
-                float2 const r = pk_fma(c.x, c.x, pk_mul(c.y, c.y));
-                float2 const q = pk_fma(c.z, c.z, r);
-                float2 const l = pk_mul(q, make_float2(rsqrtf(q.x), rsqrtf(q.y)));
+                c.x = lv_add(lv_add(ax, nqhx[p]), lv_add(cx, nqlx[p]));
+                c.y = lv_add(lv_add(ay, nqhy[p]), lv_add(cy, nqly[p]));
+                c.z = lv_add(lv_add(az, nqhz[p]), lv_add(cz, nqlz[p]));
+                float2 const r = lv_fma(c.x, c.x, lv_mul(c.y, c.y));
+                float2 const q = lv_fma(c.z, c.z, r);
+                float2 const l = lv_mul(q, make_float2(rsqrtf(q.x), rsqrtf(q.y)));
                 // l + z = n / d with (n, d) = (l + z, 1) for z >= 0 and (x^2 + y^2, l - z) for z < 0, free of
                 // cancellation.  d > 0, or NaN for a near vertex (|v|^2 < near2): the NaN makes the error bound of
                 // both segments at this vertex NaN, which sends them to FP64
-                float2 const lpz = pk_add(l, c.z), lmz = pk_sub(l, c.z);
+                float2 const lpz = lv_add(l, c.z), lmz = lv_sub(l, c.z);
                 float const nan = __int_as_float(0x7fffffff);
                 c.n = make_float2(c.z.x >= 0.f ? lpz.x : r.x, c.z.y >= 0.f ? lpz.y : r.y);
                 c.d = make_float2(q.x < B.w ? nan : (c.z.x >= 0.f ? 1.f : lmz.x),
@@ -869,53 +803,53 @@ __global__ void __launch_bounds__(256, mixed_min_blocks<K>())
             }
             if (may_start && sidx < 0)
                 return;
-            float2 const by = pk(B.y), nbx = pk(-B.x), w = pk(A.w);
+            float2 const by = lv_set<float2>(B.y), nbx = lv_set<float2>(-B.x), w = lv_set<float2>(A.w);
 #pragma unroll
             for (int p = 0; p < KP; ++p)
             {
                 VState2 const& v0 = pv[p];
                 VState2 const& v1 = cv[p];
                 // num from the segment vector B (accurate on its own, no cancellation for a far segment)
-                float2 const ta = pk_mul(v0.x, by), tbn = pk_mul(v0.y, nbx); // v0.x * B.y and -(v0.y * B.x)
-                float2 const num = pk_add(ta, tbn);
+                float2 const ta = lv_mul(v0.x, by), tbn = lv_mul(v0.y, nbx); // v0.x * B.y and -(v0.y * B.x)
+                float2 const num = lv_add(ta, tbn);
                 // scaling num and den by the positive D = d0 * d1 leaves the angle unchanged and removes both
                 // divisions: den * D = n0 * n1 + (v0.x*v1.x + v0.y*v1.y) * D
-                float2 const D = pk_mul(v0.d, v1.d), nn = pk_mul(v0.n, v1.n);
-                float2 const pxy = pk_mul(v0.x, v1.x), pyy = pk_mul(v0.y, v1.y);
-                float2 const num_s = pk_mul(num, D);
-                float2 const den_s = pk_fma(pk_add(pxy, pyy), D, nn);
+                float2 const D = lv_mul(v0.d, v1.d), nn = lv_mul(v0.n, v1.n);
+                float2 const pxy = lv_mul(v0.x, v1.x), pyy = lv_mul(v0.y, v1.y);
+                float2 const num_s = lv_mul(num, D);
+                float2 const den_s = lv_fma(lv_add(pxy, pyy), D, nn);
                 // first-order rounding bounds: num errs by about eps * sn and den by about eps * sd, so the angle
                 // errs by at most eps * (sn * |den| + sd * |num|) / (num^2 + den^2) <= eps * (sn * ad1 + sd * an1) / M
                 // with M = max(|num|, |den|) and an1, ad1 the two divided by M: one of them is 1, the other is the
                 // ratio t that atan2 takes as well
                 float2 const sn =
-                    pk_mul(make_float2(fabsf(ta.x) + fabsf(tbn.x), fabsf(ta.y) + fabsf(tbn.y)), D);
+                    lv_mul(make_float2(fabsf(ta.x) + fabsf(tbn.x), fabsf(ta.y) + fabsf(tbn.y)), D);
                 float2 const sd =
-                    pk_fma(make_float2(fabsf(pxy.x) + fabsf(pyy.x), fabsf(pxy.y) + fabsf(pyy.y)), D, nn);
+                    lv_fma(make_float2(fabsf(pxy.x) + fabsf(pyy.x), fabsf(pxy.y) + fabsf(pyy.y)), D, nn);
                 float2 const an = make_float2(fabsf(num_s.x), fabsf(num_s.y));
                 float2 const ad = make_float2(fabsf(den_s.x), fabsf(den_s.y));
                 bool const sw0 = an.x > ad.x, sw1 = an.y > ad.y;
                 float2 const inv = make_float2(__fdividef(1.f, fmaxf(sw0 ? an.x : ad.x, 1e-37f)),
                                                __fdividef(1.f, fmaxf(sw1 ? an.y : ad.y, 1e-37f)));
-                float2 const t = pk_mul(make_float2(fminf(an.x, ad.x), fminf(an.y, ad.y)), inv);
-                float2 const bound = pk_mul(pk_fma(make_float2(sw0 ? sn.x : sd.x, sw1 ? sn.y : sd.y), t,
+                float2 const t = lv_mul(make_float2(fminf(an.x, ad.x), fminf(an.y, ad.y)), inv);
+                float2 const bound = lv_mul(lv_fma(make_float2(sw0 ? sn.x : sd.x, sw1 ? sn.y : sd.y), t,
                                                    make_float2(sw0 ? sd.x : sn.x, sw1 ? sd.y : sn.y)),
                                             inv); // in units of kEpsBound
                 // a NaN or infinity anywhere (a near vertex, |v| = 0, overflow) makes the bound NaN, which the negated
                 // comparison sends to FP64; so does a branch (den <= 0) decided within the rounding of num
-                float2 const margin = pk_fma(pk(-kEpsBound), sn, an);
+                float2 const margin = lv_fma(lv_set<float2>(-kEpsBound), sn, an);
                 bool const need0 = !(bound.x <= te_units) || fmaxf(den_s.x, margin.x) <= 0.f;
                 bool const need1 = !(bound.y <= te_units) || fmaxf(den_s.y, margin.y) <= 0.f;
                 nb |= (need0 ? (1u << (slot * K + 2 * p)) : 0u) | (need1 ? (1u << (slot * K + 2 * p + 1)) : 0u);
                 // atan2(num_s, den_s): atan(t), then the octant
-                float2 a = atan_unit2(t);
-                float2 const a_sw = pk_sub(pk(1.5707963267948966f), a);
+                float2 a = atan_unit_lv(t);
+                float2 const a_sw = lv_sub(lv_set<float2>(1.5707963267948966f), a);
                 a = make_float2(sw0 ? a_sw.x : a.x, sw1 ? a_sw.y : a.y);
-                float2 const a_neg = pk_sub(pk(3.141592653589793f), a);
+                float2 const a_neg = lv_sub(lv_set<float2>(3.141592653589793f), a);
                 a = make_float2(copysignf(den_s.x < 0.f ? a_neg.x : a.x, num_s.x),
                                 copysignf(den_s.y < 0.f ? a_neg.y : a.y, num_s.y));
-                float2 const term = pk_mul(w, a);
-                two_sum_acc2(acc[p], comp[p], make_float2(need0 ? 0.f : term.x, need1 ? 0.f : term.y));
+                float2 const term = lv_mul(w, a);
+                two_sum_lv(acc[p], comp[p], make_float2(need0 ? 0.f : term.x, need1 ? 0.f : term.y));
             }
         };
         // the marked pairs of `count` entries from sb[s0] into the queue (the caller then drains full batches: at
