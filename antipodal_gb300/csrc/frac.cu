@@ -86,7 +86,8 @@ struct FracPlan
 
 // n_queries: the queries the plan will serve.  Below ctx.mixed_min_pairs (query, segment) pairs the mixed mode runs
 // the exact kernels: its one-block boundary preparation would cost more than the FP64 pairs it saves (a 4-segment
-// boundary with 1e5 queries: 0.21 ms mixed, 0.17 ms exact), and the exact form is the more accurate one.
+// boundary with 1e5 queries: 0.21 ms mixed, 0.17 ms exact), and the exact form is the more accurate one.  So does
+// a boundary of 2^24 segments or more, beyond the mixed kernel's FP64 queue entries (24-bit segment indices).
 // force_mixed: the mixed form whatever the context's fractional mode and the size (double only).
 template <class T>
 int fractional_prepare(Context& ctx, const T* x0_host, const T* d_seg_raw, int64_t n_seg, int64_t n_queries,
@@ -103,7 +104,8 @@ int fractional_prepare(Context& ctx, const T* x0_host, const T* d_seg_raw, int64
     if (n_seg == 0)
         return AGWN_OK;
     AGWN_CHECK_ARG(n_seg < (int64_t(1) << 31), "at most 2^31 - 1 boundary segments");
-    p.mixed = (force_mixed || (ctx.frac_mode == AGWN_FRAC_MIXED && double(n_queries) * double(n_seg) >= ctx.mixed_min_pairs)) &&
+    p.mixed = (force_mixed || (ctx.frac_mode == AGWN_FRAC_MIXED && n_seg < (int64_t(1) << 24) &&
+                               double(n_queries) * double(n_seg) >= ctx.mixed_min_pairs)) &&
               sizeof(T) == 8;
     if (!p.mixed)
     {

@@ -63,12 +63,15 @@ int agwn_context_synchronize(agwn_context* ctx);
 
 enum agwn_option
 {
-    /* Fractional-term precision for double inputs: AGWN_FRAC_EXACT (default) or AGWN_FRAC_MIXED. */
+    /* Fractional-term precision for double inputs: AGWN_FRAC_EXACT (default) or AGWN_FRAC_MIXED.  The mixed mode
+       runs the exact kernels for calls below AGWN_OPT_MIXED_MIN_PAIRS and for boundaries of 2^24 segments or
+       more. */
     AGWN_OPT_FRAC_MODE = 0,
     /* Mixed mode: a (query, segment) pair whose nearer endpoint is closer than tau * segment length is
        evaluated in FP64 with the reference arithmetic.  Default 4. */
     AGWN_OPT_MIXED_TAU = 1,
-    /* Queries owned by each thread in the fractional kernels (1, 2, 4 or 8).  Default 2. */
+    /* Queries owned by each thread in the fractional kernels (1, 2, 4 or 8; the mixed kernel packs them in pairs
+       and runs 1 as 2).  Default 2. */
     AGWN_OPT_QUERIES_PER_THREAD = 2,
     /* Threads per block of the fractional kernels (64..256, a multiple of 32), or 0 (default): 128, and 256 for the
        mixed kernel when the boundary spans more than one segment tile (more queries share each staged tile). */
