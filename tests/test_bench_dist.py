@@ -61,3 +61,14 @@ def test_reference_arm_runs_on_rank_zero_only():
     r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--gpus", "2"],
                        capture_output=True, text=True, env=env, timeout=120)
     assert r.returncode == 0 and r.stdout.strip() == ""
+
+
+def test_workload_scale_defaults(monkeypatch):
+    # the parametric workload defaults to its 4% query sample (its FP64 reference forms at full scale take about
+    # half an hour); the others to their full size; an explicit --scale wins
+    sys.path.insert(0, ROOT)
+    import bench
+    for argv, want in ((["bench.py"], 1.0), (["bench.py", "--config", "param"], 0.04),
+                       (["bench.py", "--config", "robust"], 1.0), (["bench.py", "--config", "param", "--scale", "1"], 1.0)):
+        monkeypatch.setattr(sys, "argv", argv)
+        assert bench.parse().scale == want, argv
