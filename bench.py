@@ -57,6 +57,9 @@ def parse():
                     help="secondary workloads: fraction of the full query count (batch: of the grid side); "
                          "default 1, except param: 0.04 (40,000 of the 1e6 queries, a few minutes in all)")
     ap.add_argument("--patches", type=int, default=256, help="param workload: bicubic patches (4 curves each)")
+    ap.add_argument("--integer-cells", type=int, choices=[0, 1], default=1,
+                    help="mesh workload: 1 looks the integer term's candidates up in the cell grid (default), 0 walks "
+                         "the hierarchy (k_traverse); counts are the same")
     ap.add_argument("--batch-config", default=None,
                     help="batch workload: fixed launch configuration 'block,k,seg_tile,stack' instead of tuning")
     args = ap.parse_args()
@@ -214,6 +217,7 @@ def run_ours(args):
     Q, S, F = len(q), len(bnd), len(idx) // 3
 
     disp = ag.CudaDispatcher(device=local, stream=stream, precision="mixed")
+    disp.set_option(ag._lib.OPT_INTEGER_CELLS, args.integer_cells)
     t0 = time.perf_counter()
     isect = ag.CudaIntersector(disp, verts, idx)
     disp.synchronize()
