@@ -12,11 +12,31 @@ worst-case bounds: on these cases they still decide correctly at 1/100 of their 
 the rounding itself) the same cases give wrong decisions, which shows that the cases reach the rounding.
 """
 
+import os
+import re
 from fractions import Fraction
 
 import numpy as np
 
 F32 = np.float32
+HIER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "antipodal_gb300", "csrc",
+                    "hier.cuh")
+
+
+def device_margin_constants():
+    """The constants of margin_rotated and margin_permuted as hier.cuh writes them, so this test checks the margins
+    the kernels use: (q, s) with delta = q qmax + s scene_scale (rotated) and d with delta = d (qmax + scene_scale)
+    (permuted), each multiplied by 8 into m8."""
+    src = open(HIER).read()
+    rot = re.search(r"margin_rotated\(float qmax, float scene_scale\)\s*\{\s*return 8\.0f \* fmaf\(([0-9.e+-]+)f, qmax, "
+                    r"([0-9.e+-]+)f \* scene_scale\);", src)
+    per = re.search(r"margin_permuted\(float qmax, float scene_scale\)\s*\{\s*return 8\.0f \* ([0-9.e+-]+)f \* "
+                    r"\(qmax \+ scene_scale\);", src)
+    assert rot and per, "margin functions not found in hier.cuh"
+    return (float(rot.group(1)), float(rot.group(2))), float(per.group(1))
+
+
+(ROT_Q, ROT_S), PERM_D = device_margin_constants()
 
 
 def ray_frame(d):
@@ -52,11 +72,11 @@ def project_corners(rd, tri):
 
 
 def margin_rotated(qmax, scene):
-    return F32(8.0) * (F32(8e-7) * qmax + F32(4.2e-7) * scene)
+    return F32(8.0) * (F32(ROT_Q) * qmax + F32(ROT_S) * scene)
 
 
 def margin_permuted(qmax, scene):
-    return F32(8.0) * F32(3e-7) * (qmax + scene)
+    return F32(8.0) * F32(PERM_D) * (qmax + scene)
 
 
 def may_hit(pu, pv, u, v, m8):
@@ -205,6 +225,16 @@ def run(permuted, margin_scale=1.0, n=6000, seed=0):
             if int(dec[j]) != exact_crossing(p[i], d[i], tri[i, 0], tri[i, 1], tri[i, 2]):
                 wrong += 1
     return decided, wrong
+
+
+def test_margins_cover_their_derivation():
+    # the lower bounds the margins are derived from (hier.cuh): rotated frame 7 sqrt(3) eps of qmax for the query
+    # and 4 eps sqrt(3) of (qmax + scene_scale) for the edge functions' rounding; permuted frame 4 eps of (qmax +
+    # scene_scale)
+    eps = 2.0 ** -24
+    assert ROT_Q >= 7 * np.sqrt(3) * eps and ROT_Q >= 4 * np.sqrt(3) * eps
+    assert ROT_S >= 4 * np.sqrt(3) * eps and ROT_S >= np.sqrt(3) * eps
+    assert PERM_D >= 4 * eps
 
 
 def test_permuted_frame_matches_the_exact_order():
