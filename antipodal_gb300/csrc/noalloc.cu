@@ -9,7 +9,7 @@
 //
 // agwn_mesh_batch_fractional_mixed_noalloc_f64 runs the same two kernels as agwn_mesh_batch_fractional_f64 in
 // the mixed mode, but its scratch -- the prepared boundary, the frame and the error flags -- lives in one
-// file-scope static __device__ array of fixed size (kNoAllocMaxSegments segments, about 1.3 MB), created when
+// file-scope static __device__ array of fixed size (kNoAllocMaxSegments segments, 1,409,120 bytes), created when
 // the library is loaded and held by every GPU that loads it until the process exits.  The caller passes the
 // inputs and the output in memory it already owns.  Nothing here calls cudaMalloc, cudaFree or any other
 // allocating routine.
@@ -38,19 +38,35 @@ struct NoAllocScratch
     int flags[FLAG_COUNT];
     long long counters[4];
 };
+// The size the header states; a change of the layout must update it there as well.
+constexpr size_t kNoAllocScratchBytes = 1409120;
+static_assert(sizeof(NoAllocScratch) == kNoAllocScratchBytes, "update the scratch size stated in antipodal_gb300.h");
 
 // The scratch array.  Host code must not pass this symbol to a kernel: on the host it names a stand-in object,
 // not device memory.  Its device address comes from cudaGetSymbolAddress below.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[sizeof(NoAllocScratch)];
 
+bool on_device(const void* p, int device)
+{
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess)
+    {
+        cudaGetLastError();
+        return false;
+    }
+    return (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) && a.device == device;
+}
+
 std::mutex g_noalloc_mutex;
 NoAllocScratch* g_noalloc_ptr[kMaxDevices] = {};
 
-// Device address of the scratch array on the current device, looked up once per device with that device current.
+// Device address of the scratch array on the current device, looked up with that device current on the first call
+// there.  A cached address that no longer lies in this device's memory (the library's module was loaded again,
+// e.g. after cudaDeviceReset) is looked up again.
 int noalloc_scratch(int device, NoAllocScratch** out)
 {
     std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-    if (!g_noalloc_ptr[device])
+    if (!g_noalloc_ptr[device] || !on_device(g_noalloc_ptr[device], device))
     {
         void* p = nullptr;
         cudaError_t const e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
@@ -64,17 +80,6 @@ int noalloc_scratch(int device, NoAllocScratch** out)
     }
     *out = g_noalloc_ptr[device];
     return AGWN_OK;
-}
-
-bool on_device(const void* p, int device)
-{
-    cudaPointerAttributes a{};
-    if (cudaPointerGetAttributes(&a, p) != cudaSuccess)
-    {
-        cudaGetLastError();
-        return false;
-    }
-    return (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) && a.device == device;
 }
 } // namespace
 } // namespace agwn

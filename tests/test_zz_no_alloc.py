@@ -3,9 +3,12 @@
 Callers that own all of the GPU's memory themselves (their own pool allocator with a fixed budget, or a plugin
 inside a framework whose caching allocator must not be bypassed) cannot let a library call cudaMalloc.
 agwn_mesh_batch_fractional_mixed_noalloc_f64 serves them from one fixed static device array instead of a context.
-This test calls it through the C ABI, twice in a row on different inputs (the second call must not see the first
+This test calls it through the C ABI several times in a row on different inputs (no call may see the previous
 call's leftovers in the shared array), and compares each result with agwn_mesh_batch_fractional_f64 in the mixed
-mode on the same device inputs.  The file is named so pytest collects it last.
+mode on the same device inputs.  The boundaries cover both of its tile paths: one 512-entry tile (the icosphere's
+and the cube's boundaries), several double-buffered tiles over chained loops (1,100 segments), and the unchained
+stream of one start entry per segment above 4,096 segments (6,000, and the 8,192-segment maximum).  The file is
+named so pytest collects it last.
 """
 
 import ctypes as C
@@ -28,14 +31,35 @@ def _entry(lib):
     return f
 
 
+def _loops(seed, n_loops, per_loop):
+    """Closed noisy loops of ``per_loop`` segments each, as (n, 7) [pos0, pos1, weight] rows."""
+    rng = np.random.default_rng(seed)
+    rows = []
+    t = np.linspace(0.0, 2.0 * np.pi, per_loop, endpoint=False)
+    for _ in range(n_loops):
+        r = rng.uniform(0.2, 0.6)
+        pts = np.stack([r * np.cos(t), r * np.sin(t), 0.05 * np.sin(3.0 * t)], 1) @ synth.random_rotation(rng).T
+        pts = pts + rng.normal(scale=0.4, size=3) + rng.normal(scale=1e-3, size=pts.shape)
+        w = np.full((per_loop, 1), float(rng.integers(1, 3)))
+        rows.append(np.hstack([pts, np.roll(pts, -1, axis=0), w]))
+    return np.ascontiguousarray(np.vstack(rows))
+
+
 def _inputs():
     v, idx, bnd, _, x0 = synth.open_icosphere(seed=5, level=5, grid=0)
     q1 = synth.grid_queries(v.min(0), v.max(0), 40, 1.2)
     _, _, bnd2, q2, x02 = synth.rotated_open_cube(seed=9, n_queries=30_000)
-    return [(q1, bnd, x0), (q2, bnd2, x02)]
+    cases = [(q1, bnd, x0), (q2, bnd2, x02)]
+    for seed, n_loops, per_loop in ((11, 5, 220), (12, 20, 300), (13, 32, 256)):
+        b = _loops(seed, n_loops, per_loop)
+        ends = b[:, :6].reshape(-1, 3)
+        q = synth.grid_queries(ends.min(0), ends.max(0), 24, 1.3)
+        cases.append((q, b, synth.random_unit(np.random.default_rng(seed))))
+    assert [len(c[1]) for c in cases[2:]] == [1100, 6000, MAX_SEGMENTS]
+    return cases
 
 
-def test_noalloc_matches_regular_entry_point_on_two_calls(gwn):
+def test_noalloc_matches_regular_entry_point_on_calls_in_a_row(gwn):
     torch = pytest.importorskip("torch")
     dev = torch.device("cuda:0")
     f = _entry(gwn.library())
