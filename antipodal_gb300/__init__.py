@@ -429,15 +429,24 @@ def eval_gwnr_mesh_batch(dispatcher: CudaDispatcher, intersector: CudaIntersecto
 
 
 def eval_gwnr_mesh_batch_integer_bruteforce(dispatcher: CudaDispatcher, vertices, indices, positions, out_counts,
-                                            x0):
-    """Every query against every triangle (no hierarchy); double precision only."""
+                                            x0, out_ties=None):
+    """Every query against every triangle (no hierarchy); double precision only.  With ``out_ties`` (int32, one per
+    query) also the number of counted hits that lie exactly on a triangle's edge or vertex, or at the query: the
+    queries whose NaiveIntersector counts include its double count at shared edges."""
     p = _View(positions, np.float64, 3, "positions")
     o = _View(out_counts, np.int32, None, "out_counts", writable=True)
     v = _View(vertices, np.float64, 3, "vertices")
     i = _View(indices, np.int32, None, "indices")
     _, xp = x = _vec3(x0, np.float64)
-    _check(library().agwn_mesh_batch_integer_bruteforce_f64(dispatcher.handle, v.ptr, v.n, i.ptr, i.n, p.ptr, p.n,
-                                                            o.ptr, xp), "bruteforce")
+    if out_ties is None:
+        _check(library().agwn_mesh_batch_integer_bruteforce_f64(dispatcher.handle, v.ptr, v.n, i.ptr, i.n, p.ptr,
+                                                                p.n, o.ptr, xp), "bruteforce")
+    else:
+        t = _View(out_ties, np.int32, None, "out_ties", writable=True)
+        if t.n != p.n:
+            raise ValueError("out_ties needs one entry per query")
+        _check(library().agwn_mesh_batch_integer_ties_f64(dispatcher.handle, v.ptr, v.n, i.ptr, i.n, p.ptr, p.n,
+                                                          o.ptr, t.ptr, xp), "bruteforce with ties")
     del x
 
 

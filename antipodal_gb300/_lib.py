@@ -55,6 +55,7 @@ SIGNATURES = {
     "agwn_mesh_batch_f64": (_I, [_P, _P, _P, _I64, _P, _P, _P, _I64]),
     "agwn_mesh_batch_f32": (_I, [_P, _P, _P, _I64, _P, _P, _P, _I64]),
     "agwn_mesh_batch_integer_bruteforce_f64": (_I, [_P, _P, _I64, _P, _I64, _P, _I64, _P, _P]),
+    "agwn_mesh_batch_integer_ties_f64": (_I, [_P, _P, _I64, _P, _I64, _P, _I64, _P, _P, _P]),
     "agwn_robust_create_f64": (_I, [_P, _I, _P, _I64, _P, _I64, _P, _I64, _PP]),
     "agwn_robust_create_f32": (_I, [_P, _I, _P, _I64, _P, _I64, _P, _I64, _PP]),
     "agwn_robust_destroy": (_I, [_P]),
@@ -64,6 +65,8 @@ SIGNATURES = {
     "agwn_probe_fp32_peak": (_I, [_P, C.POINTER(_D)]),
     "agwn_probe_atan2": (_I, [_P, _P, _P, _I64, _P, _P]),
     "agwn_probe_fp64_peak": (_I, [_P, _P]),
+    "agwn_robust_predicates": (_I, [_P, _I, _P, _P, _P, _P, _I64, _P, _P, _P, _P]),
+    "agwn_probe_i128_mul_sub": (_I, [_P, _P, _P, _P, _P, _I64, _P, _P, _P]),
     "agwn_param_batch_fractional_bezier3_f64": (_I, [_P, _P, _I64, _P, _P, _P, _I64, _I, _I, _D, _P, _P, _P]),
     "agwn_robust_eval_grid_f64": (_I, [_P, _P, _P, _P, _I64, _I64, _I64, _P, _P, _P]),
     "agwn_robust_eval_grid_f32": (_I, [_P, _P, _P, _P, _I64, _I64, _I64, _P, _P, _P]),

@@ -302,7 +302,7 @@ __global__ void k_depth(int n, const int* __restrict__ parent_node, const int* _
 // ---- traversal ----------------------------------------------------------------------------------------------
 // Moller-Trumbore sign with NaiveIntersector's arithmetic and early rejections, in unfused precision S.
 template <class S>
-__device__ __forceinline__ int mt_sign(ev3<S> p, ev3<S> dir, ev3<S> a, ev3<S> b, ev3<S> c)
+__device__ __forceinline__ int mt_sign(ev3<S> p, ev3<S> dir, ev3<S> a, ev3<S> b, ev3<S> c, bool* tie = nullptr)
 {
     ev3<S> const e1 = b - a;
     ev3<S> const e2 = c - a;
@@ -322,6 +322,10 @@ __device__ __forceinline__ int mt_sign(ev3<S> p, ev3<S> dir, ev3<S> a, ev3<S> b,
     S const t = inv * edot(e2, q);
     if (t.v < 0)
         return 0;
+    // a counted hit exactly on the triangle's boundary (an edge or a vertex: the neighbour sharing it counts the
+    // same crossing again) or at the query itself
+    if (tie)
+        *tie = u.v == 0 || v.v == 0 || (u + v).v == 1 || t.v == 0;
     ev3<S> const ng = ecross(e1, e2);
     return edot(ng, dir).v > 0 ? 1 : -1;
 }
@@ -553,23 +557,34 @@ __global__ void __launch_bounds__(kTravBlock) k_cells(const BvhNode* __restrict_
 template <class T>
 __global__ void __launch_bounds__(128) k_bruteforce(const T* __restrict__ verts, const int32_t* __restrict__ idx,
                                                     int64_t n_tri, const T* __restrict__ pos, int64_t n,
-                                                    int32_t* __restrict__ counts, T dx, T dy, T dz)
+                                                    int32_t* __restrict__ counts, T dx, T dy, T dz,
+                                                    int32_t* __restrict__ ties)
 {
     using S = typename exact_of<T>::type;
     ev3<S> const dir{S(dx), S(dy), S(dz)};
     for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
     {
         ev3<S> const p{S(pos[3 * i]), S(pos[3 * i + 1]), S(pos[3 * i + 2])};
-        int sum = 0;
+        int sum = 0, n_ties = 0;
         for (int64_t t = 0; t < n_tri; ++t)
         {
             T const* a = verts + 3 * int64_t(idx[3 * t]);
             T const* b = verts + 3 * int64_t(idx[3 * t + 1]);
             T const* c = verts + 3 * int64_t(idx[3 * t + 2]);
-            sum += mt_sign(p, dir, ev3<S>{S(a[0]), S(a[1]), S(a[2])}, ev3<S>{S(b[0]), S(b[1]), S(b[2])},
-                           ev3<S>{S(c[0]), S(c[1]), S(c[2])});
+            ev3<S> const va{S(a[0]), S(a[1]), S(a[2])}, vb{S(b[0]), S(b[1]), S(b[2])}, vc{S(c[0]), S(c[1]), S(c[2])};
+            if (ties)
+            {
+                bool tie = false;
+                int const h = mt_sign(p, dir, va, vb, vc, &tie);
+                sum += h;
+                n_ties += (h != 0 && tie) ? 1 : 0;
+            }
+            else
+                sum += mt_sign(p, dir, va, vb, vc);
         }
         counts[i] = sum;
+        if (ties)
+            ties[i] = n_ties;
     }
 }
 
@@ -1028,9 +1043,9 @@ int agwn_mesh_batch_integer_f32(agwn_context* ctx, const agwn_bvh* bvh, const fl
 {
     return batch_integer<float>(ctx, bvh, positions, n, out_counts, dir);
 }
-int agwn_mesh_batch_integer_bruteforce_f64(agwn_context* ctx, const double* vertices, int64_t n_vertices,
-                                           const int32_t* indices, int64_t n_indices, const double* positions,
-                                           int64_t n, int32_t* out_counts, const double* dir)
+static int bruteforce_f64(agwn_context* ctx, const double* vertices, int64_t n_vertices, const int32_t* indices,
+                          int64_t n_indices, const double* positions, int64_t n, int32_t* out_counts, const double* dir,
+                          int32_t* out_ties)
 {
     AGWN_CHECK_ARG(ctx && dir, "null context/dir");
     AGWN_CHECK_ARG(n >= 0 && n_vertices >= 0 && n_indices >= 0 && n_indices % 3 == 0, "bad sizes");
@@ -1040,12 +1055,14 @@ int agwn_mesh_batch_integer_bruteforce_f64(agwn_context* ctx, const double* vert
     if (n == 0)
         return AGWN_OK;
     const void *dv = nullptr, *di = nullptr, *dpos = nullptr;
-    void* dout = nullptr;
-    bool host_out = false;
+    void *dout = nullptr, *dties = nullptr;
+    bool host_out = false, host_ties = false;
     AGWN_TRY(stage_in(*ctx, vertices, sizeof(double) * 3 * n_vertices, S_MISC0, &dv));
     AGWN_TRY(stage_in(*ctx, indices, sizeof(int32_t) * n_indices, S_MISC1, &di));
     AGWN_TRY(stage_in(*ctx, positions, sizeof(double) * 3 * n, S_QUERIES, &dpos));
     AGWN_TRY(stage_out(*ctx, out_counts, sizeof(int32_t) * n, S_COUNTS, &dout, &host_out));
+    if (out_ties)
+        AGWN_TRY(stage_out(*ctx, out_ties, sizeof(int32_t) * n, S_OUT, &dties, &host_ties));
     // indices are trusted here as in NaiveIntersector; validate them on the host when they live there
     if (!is_device_pointer(indices))
         for (int64_t i = 0; i < n_indices; ++i)
@@ -1054,10 +1071,28 @@ int agwn_mesh_batch_integer_bruteforce_f64(agwn_context* ctx, const double* vert
     AGWN_TRY(ctx->launch_begin(AGWN_K_INTEGER));
     k_bruteforce<double><<<grid, 128, 0, ctx->stream>>>(static_cast<const double*>(dv), static_cast<const int32_t*>(di),
                                                         n_indices / 3, static_cast<const double*>(dpos), n,
-                                                        static_cast<int32_t*>(dout), dir[0], dir[1], dir[2]);
+                                                        static_cast<int32_t*>(dout), dir[0], dir[1], dir[2],
+                                                        static_cast<int32_t*>(dties));
     AGWN_TRY(ctx->launch_end(AGWN_K_INTEGER));
     if (host_out)
         AGWN_TRY_CUDA(cudaMemcpyAsync(out_counts, dout, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    if (host_ties)
+        AGWN_TRY_CUDA(cudaMemcpyAsync(out_ties, dties, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, ctx->stream));
     return ctx->check_flags();
+}
+
+int agwn_mesh_batch_integer_bruteforce_f64(agwn_context* ctx, const double* vertices, int64_t n_vertices,
+                                           const int32_t* indices, int64_t n_indices, const double* positions,
+                                           int64_t n, int32_t* out_counts, const double* dir)
+{
+    return bruteforce_f64(ctx, vertices, n_vertices, indices, n_indices, positions, n, out_counts, dir, nullptr);
+}
+
+int agwn_mesh_batch_integer_ties_f64(agwn_context* ctx, const double* vertices, int64_t n_vertices,
+                                     const int32_t* indices, int64_t n_indices, const double* positions, int64_t n,
+                                     int32_t* out_counts, int32_t* out_ties, const double* dir)
+{
+    AGWN_CHECK_ARG(n == 0 || out_ties, "null out_ties");
+    return bruteforce_f64(ctx, vertices, n_vertices, indices, n_indices, positions, n, out_counts, dir, out_ties);
 }
 } // extern "C"

@@ -226,24 +226,39 @@ __device__ __forceinline__ double dot_yz(qv3<typename P::C> a, qv3<typename P::C
         return __dadd_rn(__dmul_rn(a.y, b.y), __dmul_rn(a.z, b.z));
 }
 
+// The query's projection into the predicate triangle (a, b, c) in (y, z): the common nonzero sign of its three
+// edges (0 when it is outside or the edges disagree) and the unnormalised barycentric weights, each the edge
+// determinant opposite its vertex.  robust_predicates.hh:390-402.
+struct TriProj
+{
+    int sign;
+    double w0, w1, w2;
+};
+template <class P>
+__device__ __forceinline__ TriProj project_into_tri(qv3<typename P::C> q, qv3<typename P::C> a,
+                                                    qv3<typename P::C> b, qv3<typename P::C> c)
+{
+    int const e01 = edge_sign<P>(q, a, b);
+    int const e12 = edge_sign<P>(q, b, c);
+    int const e20 = edge_sign<P>(q, c, a);
+    if (e01 == 0 || e01 != e12 || e01 != e20)
+        return TriProj{0, 0.0, 0.0, 0.0};
+    return TriProj{e01, P::dbl(edge_det<P>(q, b, c)), P::dbl(edge_det<P>(q, c, a)), P::dbl(edge_det<P>(q, a, b))};
+}
+
 // Signed -x crossing of the predicate triangle (t0, t1, t2) for the query qi: robust_occluded_fn
-// (gwn_mesh_robust.hh:122-145) with project_into_tri (robust_predicates.hh:390-402).
+// (gwn_mesh_robust.hh:122-145) with project_into_tri.
 template <class P>
 __device__ __forceinline__ int robust_crossing(qv3<typename P::C> q, const typename P::C* t)
 {
     using C = typename P::C;
     qv3<C> const a{t[0], t[1], t[2]}, b{t[3], t[4], t[5]}, c{t[6], t[7], t[8]};
-    int const e01 = edge_sign<P>(q, a, b);
-    int const e12 = edge_sign<P>(q, b, c);
-    int const e20 = edge_sign<P>(q, c, a);
-    if (e01 == 0 || e01 != e12 || e01 != e20)
+    TriProj const h = project_into_tri<P>(q, a, b, c);
+    if (h.sign == 0)
         return 0;
-    double const w0 = P::dbl(edge_det<P>(q, b, c));
-    double const w1 = P::dbl(edge_det<P>(q, c, a));
-    double const w2 = P::dbl(edge_det<P>(q, a, b));
-    rd const hx = (rd(w0) * rd(P::cdbl(a.x)) + rd(w1) * rd(P::cdbl(b.x)) + rd(w2) * rd(P::cdbl(c.x))) /
-                  (rd(w0) + rd(w1) + rd(w2));
-    return P::cdbl(q.x) >= hx.v ? -e01 : 0;
+    rd const hx = (rd(h.w0) * rd(P::cdbl(a.x)) + rd(h.w1) * rd(P::cdbl(b.x)) + rd(h.w2) * rd(P::cdbl(c.x))) /
+                  (rd(h.w0) + rd(h.w1) + rd(h.w2));
+    return P::cdbl(q.x) >= hx.v ? -h.sign : 0;
 }
 
 struct Quant

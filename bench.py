@@ -53,19 +53,25 @@ def parse():
     ap.add_argument("--config", choices=["mesh", "cube", "batch", "robust", "param"], default="mesh",
                     help="mesh: the headline single-mesh workload (default); the others are the secondary "
                          "workloads, each printing its own JSON line (see run_secondary)")
-    ap.add_argument("--scale", type=float, default=None,
-                    help="secondary workloads: fraction of the full query count (batch: of the grid side); "
-                         "default 1, except param: 0.04 (40,000 of the 1e6 queries, a few minutes in all)")
+    ap.add_argument("--scale", type=float, default=1.0,
+                    help="secondary workloads: fraction of the full query count (batch: of the grid side)")
+    ap.add_argument("--plain-scale", type=float, default=0.04,
+                    help="param workload: the seeded sample of the queries (fraction) on which the plain FP64 "
+                         "integrator and the ablations are timed (default 0.04: the plain form on all 1e6 queries "
+                         "takes about 100 s per step)")
+    ap.add_argument("--labels", type=float, default=1e7,
+                    help="param workload: plain-integrator depth labels the proposal network is trained on")
+    ap.add_argument("--train-steps", type=int, default=4000, help="param workload: training steps (batch 8192)")
     ap.add_argument("--patches", type=int, default=256, help="param workload: bicubic patches (4 curves each)")
     ap.add_argument("--integer-cells", type=int, choices=[0, 1], default=1,
                     help="mesh workload: 1 looks the integer term's candidates up in the cell grid (default), 0 walks "
                          "the hierarchy (k_traverse); counts are the same")
     ap.add_argument("--batch-config", default=None,
                     help="batch workload: fixed launch configuration 'block,k,seg_tile,stack' instead of tuning")
-    args = ap.parse_args()
-    if args.scale is None:
-        args.scale = 0.04 if args.config == "param" else 1.0
-    return args
+    ap.add_argument("--full-integer-check", type=int, choices=[0, 1], default=1,
+                    help="mesh workload: 1 (default) compares the integer term of every query with the scan of every "
+                         "triangle (NaiveIntersector's rule, no hierarchy) and counts the ties; untimed")
+    return ap.parse_args()
 
 
 def dist_env():
@@ -84,6 +90,15 @@ def reduce_max(x: float, device) -> float:
     t = torch.tensor([float(x)], dtype=torch.float64, device=device)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def p99(t) -> float:
+    """The 99th percentile of all values of a tensor or array (the ceil(0.99 n)-th smallest)."""
+    import torch
+    t = (t if isinstance(t, torch.Tensor) else torch.from_numpy(np.asarray(t))).flatten().double()
+    if t.numel() == 0:
+        return 0.0
+    return float(torch.kthvalue(t, max(1, int(np.ceil(0.99 * t.numel())))).values.item())
 
 
 def workload(grid):
@@ -270,10 +285,27 @@ def run_ours(args):
     frac_ms = st["kernel_ms"]["fractional"] / max(1, st["launches"]["fractional"])
     int_ms = st["kernel_ms"]["integer"] / max(1, st["launches"]["integer"])
 
+    # the integer term of every query against the every-triangle scan, which also reports ties (hits exactly on an
+    # edge or vertex, where NaiveIntersector counts a crossing once per triangle); untimed
+    full_check = None
+    if args.full_integer_check:
+        cnt_cells = torch.empty(Q, dtype=torch.int32, device=dev)
+        cnt_scan = torch.empty(Q, dtype=torch.int32, device=dev)
+        ties = torch.empty(Q, dtype=torch.int32, device=dev)
+        ag.eval_gwnr_mesh_batch_integer(disp, isect, q_dev, cnt_cells, x0)
+        v_dev, i_dev = torch.from_numpy(verts).to(dev), torch.from_numpy(idx).to(dev)
+        t0 = time.perf_counter()
+        ag.eval_gwnr_mesh_batch_integer_bruteforce(disp, v_dev, i_dev, q_dev, cnt_scan, x0, out_ties=ties)
+        disp.synchronize()
+        full_check = {"integer_mismatches_full": int((cnt_cells != cnt_scan).sum().item()),
+                      "queries_checked": Q, "ties_counted": int((ties > 0).sum().item()),
+                      "tie_hits": int(ties.sum().item()), "scan_seconds": time.perf_counter() - t0}
+        del cnt_cells, cnt_scan, ties
+
     # accuracy: chosen vs plain over every query
     diff = (out - out_plain).abs()
     max_err = float(diff.max().item())
-    p99_err = float(torch.quantile(diff[torch.randperm(Q, device=dev)[:1_000_000]].float(), 0.99).item())
+    p99_err = p99(diff)
     n_over = int((diff > 1e-7).sum().item())
 
     # end to end from pinned host buffers (H2D of the queries and D2H of the result inside every step)
@@ -320,6 +352,8 @@ def run_ours(args):
             "sample_size": len(pick),
             "fp64_pair_fraction": st["fp64_pairs"] / max(1, st["pairs"]),
         }
+        if full_check is not None:
+            accuracy.update(full_check)
         cpu = None
         if ws == 1 and not args.no_cpu:
             rate, m, threads = cpu_rate(oracle, q, x0, verts, idx, bnd, args.cpu_seconds, np.random.default_rng(3))
@@ -422,7 +456,11 @@ def run_cube(args, ag, torch, stream, disp, timed):
             "plain": {"value": Q / (ms_plain * 1e-3), "ms_per_step": ms_plain},
             "chosen_over_plain": ms_plain / ms,
             "accuracy": {"max_abs_err_plain_vs_cpu_oracle": float(np.abs(plain.cpu().numpy() - ref).max()),
-                         "max_abs_err_chosen_vs_cpu_oracle": float(np.abs(out.cpu().numpy() - ref).max())},
+                         "p99_abs_err_plain_vs_cpu_oracle": p99(np.abs(plain.cpu().numpy() - ref)),
+                         "max_abs_err_chosen_vs_cpu_oracle": float(np.abs(out.cpu().numpy() - ref).max()),
+                         "p99_abs_err_chosen_vs_cpu_oracle": p99(np.abs(out.cpu().numpy() - ref)),
+                         "queries_over_1e-7": int(np.sum(np.abs(out.cpu().numpy() - ref) > 1e-7)),
+                         "queries": Q},
             "cpu_baseline": {"value": rate, "unit": "queries/s", "cores": os.cpu_count(), "kind": "port",
                              "sample": f"first {m} queries, full GWN"}}
 
@@ -490,7 +528,7 @@ def run_batch(args, ag, torch, stream, disp, timed):
     max_diff = float(diff.max().item())
     n_same = int((diff == 0).sum().item())
     # the fractional term in double precision (RobustMeshGwn<double, int64_grid>) on the first meshes: mixed vs FP64
-    frac_err = 0.0
+    frac_err, frac_diffs = 0.0, []
     for v, i, b, q in wl[:6]:
         r64 = ag.CudaRobustMeshGwn(disp, v.astype(np.float64), i, b.astype(np.float64), precision="int64_grid")
         q64 = q.astype(np.float64)
@@ -501,6 +539,7 @@ def run_batch(args, ag, torch, stream, disp, timed):
             r64.evaluate(q64, o_, c_, f_)
             fr[mode] = f_
         frac_err = max(frac_err, float(np.abs(fr["exact"] - fr["mixed"]).max()))
+        frac_diffs.append(np.abs(fr["exact"] - fr["mixed"]))
         r64.close()
     disp.set_robust_precision("exact")
     # the CPU oracle (the reference's RobustMeshGwn rule) on a few queries of the first meshes, against plain
@@ -529,8 +568,11 @@ def run_batch(args, ag, torch, stream, disp, timed):
                               "bit_identical_to_per_mesh": bool(exact_batch_same)},
             "chosen_over_plain": ms_loop / ms,
             "fp64_pair_fraction": fp64_frac,
-            "accuracy": {"max_abs_diff_chosen_vs_plain": max_diff,
+            "accuracy": {"max_abs_diff_chosen_vs_plain": max_diff, "p99_abs_diff_chosen_vs_plain": p99(diff),
+                         "values_over_1e-7": int((diff > 1e-7).sum().item()),
                          "max_abs_err_fractional_term_f64_first6_meshes": frac_err,
+                         "p99_abs_err_fractional_term_f64_first6_meshes": p99(np.concatenate(frac_diffs)),
+                         "fractional_terms_over_1e-7_first6_meshes": int(sum((d > 1e-7).sum() for d in frac_diffs)),
                          "identical_values": n_same, "values": int(diff.numel()),
                          "sample_plain_max_abs_err_vs_cpu_oracle": worst, "sample_plain_values_not_identical": n_diff,
                          "sample_size": 8 * 200},
@@ -587,8 +629,7 @@ def run_robust(args, ag, torch, stream, disp, timed):
     chosen = {"value": Q / (ms * 1e-3), "ms_per_step": ms,
               "form": "exact_float counts + mixed fractional term (FP32 pairs, FP64 by the evaluator's rule)",
               "max_abs_err_vs_exact_float_fp64": float(d.max().item()),
-              "p99_abs_err_vs_exact_float_fp64": float(torch.quantile(d[torch.randperm(Q, device=d.device)[:1_000_000]],
-                                                                     0.99).item()),
+              "p99_abs_err_vs_exact_float_fp64": p99(d),
               "queries_over_1e-7": int((d > 1e-7).sum().item()),
               "counts_identical_to_exact": bool(torch.equal(cnt, exact["cnt"])),
               "sample_max_abs_err_vs_cpu_oracle": float(np.abs(out.cpu().numpy()[pick] - exact["gw"]).max()),
@@ -610,68 +651,89 @@ def run_robust(args, ag, torch, stream, disp, timed):
 
 
 def run_param(args, ag, torch, stream, disp, timed):
-    """256 bicubic patches (1,024 boundary cubics), float64 queries (30% within 1e-3 of a curve), GK15 at
-    tol 1e-10: the plain adaptive integrator against the learned start-depth proposal (trained here)."""
+    """256 bicubic patches (1,024 boundary cubics), 1e6 float64 queries (30% within 1e-3 of a curve), GK15 at
+    tol 1e-10: the chosen form (learned start depths from a network trained here on 1e7 labels of the plain
+    integrator, double-float panels) on every query, against the plain adaptive FP64 integrator timed on a seeded
+    sample of the same queries (``--plain-scale``; the full plain form takes about 100 s per step) and reported both
+    as measured and extrapolated per query."""
     from antipodal_gb300 import synth
     n_q = max(64, int(1_000_000 * args.scale))
     curves, q, x0 = synth.bezier_patches(seed=0, n_patches=args.patches, n_queries=n_q)
     cfg = ag.IntegrateConfig(0, 10, 1e-10)
+    Q, Cn = len(q), len(curves)
+    # the network: trained on labels of the plain integrator (the shallowest accepted depth per pair) on other
+    # seeded queries and patches, args.labels of them
     net = ag.LearnedGK15Proposal(disp, seed=3, n_classes=11, alpha=0.02)
-    tc, tq, tx = synth.bezier_patches(seed=101, n_patches=256, n_queries=2000)
+    n_train_q = max(16, int(round(args.labels / (256 * 4))))
+    tc, tq, tx = synth.bezier_patches(seed=101, n_patches=256, n_queries=n_train_q)
     t0 = time.perf_counter()
     tqd, tcd = torch.from_numpy(tq).cuda(), torch.from_numpy(tc).cuda()
     lab = net.labels(tqd, tx, tcd, cfg)
     feat = net.features(tqd, tx, tcd, cfg.tol)
-    hist = net.train(feat, lab, steps=4000, batch=8192, lr=2e-3, seed=1)
+    hist = net.train(feat, lab, steps=args.train_steps, batch=8192, lr=2e-3, seed=1)
     torch.cuda.synchronize()
     train_s = time.perf_counter() - t0
-    Q, Cn = len(q), len(curves)
+    n_labels = int(lab.numel())
+    del tqd, tcd, lab, feat
     qd, cd = torch.from_numpy(q).cuda(), torch.from_numpy(curves).cuda()
-    plain = torch.empty(Q, dtype=torch.float64, device="cuda")
-    out = torch.empty_like(plain)
-    nodes_p = torch.empty(Q, dtype=torch.int32, device="cuda")
-    nodes_l = torch.empty_like(nodes_p)
-    ag.eval_gwnr_parametric_batch_fractional(disp, qd, plain, x0, cd, cfg, nodes_per_query=nodes_p)
-    ms_plain = timed(args.steps, lambda: ag.eval_gwnr_parametric_batch_fractional(disp, qd, plain, x0, cd, cfg))
-    # learned start depths with the plain FP64 arithmetic (the ablation of the network alone)
-    ag.eval_gwnr_parametric_batch_fractional(disp, qd, out, x0, cd, cfg, integrator=net, nodes_per_query=nodes_l)
-    ms_learned = timed(args.steps, lambda: ag.eval_gwnr_parametric_batch_fractional(disp, qd, out, x0, cd, cfg,
-                                                                                    integrator=net))
-    err_learned = float((out - plain).abs().max().item())
-    # chosen: learned start depths + double-float panels on the FP32 pipe
+    # chosen: learned start depths + double-float panels, every query
     disp.set_param_precision("mixed")
-    nodes_c = torch.empty_like(nodes_p)
+    out = torch.empty(Q, dtype=torch.float64, device="cuda")
+    nodes_c = torch.empty(Q, dtype=torch.int32, device="cuda")
     ag.eval_gwnr_parametric_batch_fractional(disp, qd, out, x0, cd, cfg, integrator=net, nodes_per_query=nodes_c)
     ms = timed(args.steps, lambda: ag.eval_gwnr_parametric_batch_fractional(disp, qd, out, x0, cd, cfg,
                                                                             integrator=net))
-    err = float((out - plain).abs().max().item())
-    out_df = torch.empty_like(plain)
-    ag.eval_gwnr_parametric_batch_fractional(disp, qd, out_df, x0, cd, cfg)
-    ms_df = timed(args.steps, lambda: ag.eval_gwnr_parametric_batch_fractional(disp, qd, out_df, x0, cd, cfg))
-    err_df = float((out_df - plain).abs().max().item())
+    # the sample: the first Qs queries (the generator shuffles them, so they are a seeded random sample)
+    Qs = max(32, min(Q, int(round(args.plain_scale * Q))))
+    qs = qd[:Qs].contiguous()
+    out_df = torch.empty(Qs, dtype=torch.float64, device="cuda")
+    ag.eval_gwnr_parametric_batch_fractional(disp, qs, out_df, x0, cd, cfg)
+    ms_df = timed(args.steps, lambda: ag.eval_gwnr_parametric_batch_fractional(disp, qs, out_df, x0, cd, cfg))
     disp.set_param_precision("exact")
+    plain = torch.empty(Qs, dtype=torch.float64, device="cuda")
+    nodes_p = torch.empty(Qs, dtype=torch.int32, device="cuda")
+    ag.eval_gwnr_parametric_batch_fractional(disp, qs, plain, x0, cd, cfg, nodes_per_query=nodes_p)
+    ms_plain = timed(args.steps, lambda: ag.eval_gwnr_parametric_batch_fractional(disp, qs, plain, x0, cd, cfg))
+    # learned start depths with the plain FP64 arithmetic (the ablation of the network alone)
+    out_l = torch.empty(Qs, dtype=torch.float64, device="cuda")
+    nodes_l = torch.empty_like(nodes_p)
+    ag.eval_gwnr_parametric_batch_fractional(disp, qs, out_l, x0, cd, cfg, integrator=net, nodes_per_query=nodes_l)
+    ms_learned = timed(args.steps, lambda: ag.eval_gwnr_parametric_batch_fractional(disp, qs, out_l, x0, cd, cfg,
+                                                                                    integrator=net))
+    d = (out[:Qs] - plain).abs()
+    err, err_p99, n_over = float(d.max().item()), p99(d), int((d > 1e-7).sum().item())
+    err_learned = float((out_l - plain).abs().max().item())
+    err_df = float((out_df - plain).abs().max().item())
     panels_p, panels_l = int(nodes_p.sum().item()), int(nodes_l.sum().item())
     fp64 = disp.probe_fp64_peak()
     achieved = panels_p * 15 * 150 / (ms_plain * 1e-3) / 1e12
     o = _oracle()
-    pick = np.random.default_rng(4).choice(Q, size=32, replace=False)
+    pick = np.random.default_rng(4).choice(Qs, size=32, replace=False)
     ref = o.param_frac_bezier3(q[pick], x0, curves, 0, 10, 1e-10)
     rate, m = _cpu_sample_rate(lambda m: o.param_frac_bezier3(q[:m], x0, curves, 0, 10, 1e-10), Q, args.cpu_seconds)
     net.close()
+    plain_rate = Qs / (ms_plain * 1e-3)
     return {"metric": METRIC, "value": Q / (ms * 1e-3), "unit": "queries/s", "ms_per_step": ms,
             "config": {"workload": f"{args.patches} bicubic Bezier patches ({Cn} boundary cubics), {Q} float64 queries "
                                    "(30% within 1e-3 of a curve), adaptive GK15 tol 1e-10, max depth 10",
-                       "queries": Q, "pairs": Q * Cn},
-            "plain": {"value": Q / (ms_plain * 1e-3), "ms_per_step": ms_plain, "panels_per_pair": panels_p / (Q * Cn)},
-            "learned_fp64": {"value": Q / (ms_learned * 1e-3), "ms_per_step": ms_learned,
-                             "panels_per_pair": panels_l / (Q * Cn), "train_seconds": train_s,
-                             "train_loss_first_last": [float(hist[:20].mean()), float(hist[-100:].mean())],
-                             "labels": int(lab.numel()), "max_abs_err_vs_plain": err_learned},
-            "double_float_only": {"value": Q / (ms_df * 1e-3), "ms_per_step": ms_df, "max_abs_err_vs_plain": err_df},
-            "chosen": {"form": "learned start depths + double-float panels",
+                       "queries": Q, "pairs": Q * Cn, "sample_queries": Qs},
+            "chosen": {"form": "learned start depths + double-float panels", "queries": Q,
                        "panels_per_pair": int(nodes_c.sum().item()) / (Q * Cn)},
-            "chosen_over_plain": ms_plain / ms,
-            "accuracy": {"max_abs_err_chosen_vs_plain": err,
+            "plain": {"value": plain_rate, "ms_per_step_sample": ms_plain,
+                      "ms_per_step_extrapolated_full": ms_plain * Q / Qs,
+                      "panels_per_pair": panels_p / (Qs * Cn),
+                      "note": f"timed on the seeded {Qs}-query sample; queries/s is per query, so it extrapolates "
+                              "linearly to the full set"},
+            "learned_fp64": {"value": Qs / (ms_learned * 1e-3), "ms_per_step_sample": ms_learned,
+                             "panels_per_pair": panels_l / (Qs * Cn), "train_seconds": train_s,
+                             "train_steps": args.train_steps,
+                             "train_loss_first_last": [float(hist[:20].mean()), float(hist[-100:].mean())],
+                             "labels": n_labels, "max_abs_err_vs_plain": err_learned},
+            "double_float_only": {"value": Qs / (ms_df * 1e-3), "ms_per_step_sample": ms_df,
+                                  "max_abs_err_vs_plain": err_df},
+            "chosen_over_plain": (Q / (ms * 1e-3)) / plain_rate,
+            "accuracy": {"max_abs_err_chosen_vs_plain": err, "p99_abs_err_chosen_vs_plain": err_p99,
+                         "queries_over_1e-7": n_over, "queries_compared": Qs,
                          "sample_plain_bit_identical_to_cpu_oracle": bool(np.array_equal(plain.cpu().numpy()[pick], ref))},
             "roofline": {"bound": "fp64", "achieved": achieved, "peak": fp64, "unit": "TFLOP/s",
                          "frac": achieved / fp64,

@@ -184,6 +184,13 @@ int agwn_mesh_batch_f32(agwn_context* ctx, const agwn_bvh* bvh, const float* pos
 int agwn_mesh_batch_integer_bruteforce_f64(agwn_context* ctx, const double* vertices, int64_t n_vertices,
                                            const int32_t* indices, int64_t n_indices, const double* positions,
                                            int64_t n, int32_t* out_counts, const double* dir);
+/* The same scan, also reporting ties: out_ties[i] = how many of the hits counted for query i lie exactly on a
+ * triangle's edge or vertex (u = 0, v = 0 or u + v = 1 in Moller-Trumbore's arithmetic) or at the query itself
+ * (t = 0).  NaiveIntersector (intersector.hh:55-100) counts a crossing through a shared edge once per triangle, so
+ * these are the queries whose counts carry its double count (test/test_intersector.cc:85-89). */
+int agwn_mesh_batch_integer_ties_f64(agwn_context* ctx, const double* vertices, int64_t n_vertices,
+                                     const int32_t* indices, int64_t n_indices, const double* positions, int64_t n,
+                                     int32_t* out_counts, int32_t* out_ties, const double* dir);
 
 /* ---- robust mesh GWN ---------------------------------------------------------------------------------------
  * Replaces RobustMeshGwn<T, Precision> (src/antipodal/gwn_mesh_robust.hh:170-424) and eval_gwnr_mesh_batch_robust
@@ -344,16 +351,32 @@ int agwn_param_batch_fractional_learned_bezier3_f64(agwn_context* ctx, const agw
                                                     double tol, float alpha, uint32_t* pair_stats,
                                                     int32_t* nodes_per_query);
 
+/* The robust evaluator's exact predicates (robust_predicates.hh:273-402: edge_sign :315-331, atan2_num :340-356,
+ * project_into_tri :391-402), evaluated on the device for caller-given coordinates so that they can be checked
+ * against the reference's own predicate vectors.  Row i takes the triples q[i], q0[i], q1[i], q2[i] (int32 under
+ * AGWN_ROBUST_INT64_GRID, int64 under AGWN_ROBUST_INT128_GRID, double under AGWN_ROBUST_EXACT_FLOAT) and writes
+ * edge_sign(q, q0, q1), atan2_num(q, q0, q1) rounded to double, project_into_tri(q, q0, q1, q2).sign and, when
+ * weights is not NULL, its weights w0, w1, w2 (3 doubles per row).  These are the functions the robust kernels
+ * call.  Arrays may be host or device memory. */
+int agwn_robust_predicates(agwn_context* ctx, int policy, const void* q, const void* q0, const void* q1,
+                           const void* q2, int64_t n, int32_t* edge_sign, double* num, int32_t* inside,
+                           double* weights);
+/* a[i]*b[i] - c[i]*d[i] in the predicates' 128-bit integer arithmetic (robust_predicates.hh:60-143, int128::mul
+ * and its subtraction and double conversion): the low and high words and the double.  No other use. */
+int agwn_probe_i128_mul_sub(agwn_context* ctx, const int64_t* a, const int64_t* b, const int64_t* c,
+                            const int64_t* d, int64_t n, uint64_t* lo, int64_t* hi, double* dbl);
+
 /* ---- mixed-precision fractional term without allocation --------------------------------------------------
  * No counterpart in the reference.  For callers that cannot allocate device memory -- a program whose own pool
  * allocator owns the GPU's memory budget, or a plugin inside a framework whose allocator must not be bypassed --
  * this runs the mixed form of agwn_mesh_batch_fractional_f64 (default tau and term-error bound, no integer term)
- * with no context and no allocation.  Its scratch is one static device array sized for at most 8192 boundary
- * segments (about 0.9 MB, held on every GPU that loads the library until the process exits); more segments are
+ * with no context and no allocation.  Its scratch is one static device array of 1,409,120 bytes, sized for at most
+ * 8192 boundary segments and held on every GPU that loads the library until the process exits; more segments are
  * rejected with AGWN_ERR_INVALID.  positions, out and boundary must be device memory of the current device;
  * x0 is 3 host doubles.  stream may be NULL (the default stream).  The first call on a device looks up the
- * scratch array's device address, so make that call before any stream capture.  The call returns when the
- * kernels have finished.  All calls share the one scratch array: calls that overlap on the GPU (from several
+ * scratch array's device address, so make that first call before any stream capture.  Every call is synchronous:
+ * it waits for its kernels on `stream` and reads the device's error flags back before it returns.  All calls
+ * share the one scratch array, which keeps the last call's contents: calls that overlap on the GPU (from several
  * host threads or streams) race and must be serialised by the caller. */
 int agwn_mesh_batch_fractional_mixed_noalloc_f64(void* stream, const double* positions, int64_t n, double* out,
                                                  const double* x0, const double* boundary, int64_t n_segments);

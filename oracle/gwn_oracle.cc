@@ -850,6 +850,36 @@ int orc_predicates(int policy, void const* q, void const* q0, void const* q1, vo
     return 0;
 }
 
+// project_into_tri(q, q0, q1, q2) weights w0, w1, w2 per row (robust_predicates.hh:391-402).
+int orc_predicate_weights(int policy, void const* q, void const* q0, void const* q1, void const* q2, int64_t n,
+                          double* out_weights)
+{
+    auto run = [&](auto tag)
+    {
+        using C = decltype(tag);
+        C const* a = static_cast<C const*>(q);
+        C const* b = static_cast<C const*>(q0);
+        C const* c = static_cast<C const*>(q1);
+        C const* d = static_cast<C const*>(q2);
+        for (int64_t i = 0; i < n; ++i)
+        {
+            tri_proj const h = project_into_tri(ld3i(a, i), ld3i(b, i), ld3i(c, i), ld3i(d, i));
+            out_weights[3 * i] = h.w0;
+            out_weights[3 * i + 1] = h.w1;
+            out_weights[3 * i + 2] = h.w2;
+        }
+    };
+    if (policy == 0)
+        run(int32_t{});
+    else if (policy == 1)
+        run(int64_t{});
+    else if (policy == 2)
+        run(double{});
+    else
+        return 1;
+    return 0;
+}
+
 // Parametric fractional GWN over cubic Bezier boundary curves (12 doubles per curve: 4 control points).
 // Follows eval_gwnr_parametric_single_fractional / _batch_fractional, src/antipodal/gwn_parametric.hh:130-186,
 // with IntegratorGK15.  Optional per-(query, curve) outputs, row-major [n][n_curves]: accepted leaves and the

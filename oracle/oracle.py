@@ -20,6 +20,15 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "liboracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libref_gwn.so")
+# Where the reference's src/ directory is read from: $ANTIPODAL_REFERENCE_SRC, else the development container's
+# mount of the reference.  The GPU machines have neither; every user of it falls back when it is absent.
+DEFAULT_REFERENCE_SRC = "/root/reference/src"
+
+
+def reference_src() -> str | None:
+    """The reference's src/ directory if it exists here, else None."""
+    p = os.environ.get("ANTIPODAL_REFERENCE_SRC", DEFAULT_REFERENCE_SRC)
+    return p if p and os.path.isdir(p) else None
 
 _P = C.c_void_p
 _I64 = C.c_int64
@@ -73,6 +82,7 @@ class Oracle:
                 setattr(self, f"_base_{suf}", self._fn(f"gwn_baseline_{suf}", None, _P, _I64, _P, _P, _I64, _P, _I64, _I))
         self._robust = self._fn("robust_eval", _I, _I, _I, _P, _I64, _P, _I64, _P, _I64, _P, _I64, _P, _P, _P, _I)
         self._pred = self._fn("predicates", _I, _I, _P, _P, _P, _P, _I64, _P, _P, _P)
+        self._pred_w = self._fn("predicate_weights", _I, _I, _P, _P, _P, _P, _I64, _P)
         self._param = self._fn("param_frac_bezier3_f64", None, _P, _I64, _P, _P, _P, _I64, _I, _I, _D, _P, _P, _I)
         self._gk15 = self._fn("gk15_known", _D, _I, _D, _D, _I, _I, _D, C.POINTER(_D), C.POINTER(_I))
         if not self.reference:
@@ -159,6 +169,15 @@ class Oracle:
         if self._pred(policy, _ptr(q), _ptr(q0), _ptr(q1), _ptr(q2), n, _ptr(es), _ptr(num), _ptr(ins)) != 0:
             raise ValueError("bad policy")
         return es, num, ins
+
+    def predicate_weights(self, policy, q, q0, q1, q2):
+        """project_into_tri's weights (n, 3): (w0, w1, w2), zero where the query is outside."""
+        dt = {0: np.int32, 1: np.int64, 2: np.float64}[policy]
+        q, q0, q1, q2 = (_c(a, dt).reshape(-1, 3) for a in (q, q0, q1, q2))
+        w = np.empty((len(q), 3), np.float64)
+        if self._pred_w(policy, _ptr(q), _ptr(q0), _ptr(q1), _ptr(q2), len(q), _ptr(w)) != 0:
+            raise ValueError("bad policy")
+        return w
 
     # -- parametric path ---------------------------------------------------------------------------------------
     def param_frac_bezier3(self, pos, x0, ctrl, min_depth=0, max_depth=10, tol=1e-6, threads=0, stats=False):

@@ -197,6 +197,36 @@ int ref_predicates(int policy, void const* q, void const* q0, void const* q1, vo
     return 0;
 }
 
+// project_into_tri(q, q0, q1, q2) weights w0, w1, w2 per row (robust_predicates.hh:391-402).
+int ref_predicate_weights(int policy, void const* q, void const* q0, void const* q1, void const* q2, int64_t n,
+                          double* out_weights)
+{
+    auto run = [&](auto tag)
+    {
+        using C = decltype(tag);
+        auto const* a = static_cast<vec3<C> const*>(q);
+        auto const* b = static_cast<vec3<C> const*>(q0);
+        auto const* c = static_cast<vec3<C> const*>(q1);
+        auto const* d = static_cast<vec3<C> const*>(q2);
+        for (int64_t i = 0; i < n; ++i)
+        {
+            auto const h = robust::project_into_tri(a[i], b[i], c[i], d[i]);
+            out_weights[3 * i] = h.w0;
+            out_weights[3 * i + 1] = h.w1;
+            out_weights[3 * i + 2] = h.w2;
+        }
+    };
+    if (policy == 0)
+        run(std::int32_t{});
+    else if (policy == 1)
+        run(std::int64_t{});
+    else if (policy == 2)
+        run(double{});
+    else
+        return 1;
+    return 0;
+}
+
 void ref_param_frac_bezier3_f64(double const* pos, int64_t n, double* out, double const* x0, double const* ctrl,
                                 int64_t n_curves, int min_depth, int max_depth, double tol, int32_t*, int32_t*,
                                 int threads)

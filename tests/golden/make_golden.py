@@ -22,7 +22,7 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
 from antipodal_gb300 import synth  # noqa: E402
-from oracle.oracle import Oracle, build  # noqa: E402
+from oracle.oracle import Oracle, build, reference_src  # noqa: E402
 
 POLICIES = ["int64_grid", "int128_grid", "exact_float"]
 
@@ -64,7 +64,10 @@ def robust_cases():
 
 
 def main():
-    build(reference_src="/root/reference/src")
+    src = reference_src()
+    if src is None:
+        raise SystemExit("the reference sources are needed: set ANTIPODAL_REFERENCE_SRC to the reference's src/")
+    build(reference_src=src)
     ref = Oracle(reference=True)
     out = {}
 
@@ -134,6 +137,14 @@ def main():
     out["pred_f64_in"], out["pred_f64_sign"], out["pred_f64_num"], out["pred_f64_inside"] = pts, es, num, ins
     es, num, ins = ref.predicates(0, *q32)
     out["pred_i32_sign"], out["pred_i32_num"], out["pred_i32_inside"] = es, num, ins
+    # the 50-bit integer vectors as exact doubles (times 2^-20) under exact_float: random triangles, about 8% of
+    # the queries inside, so the weights are exercised as well
+    pts = q64.astype(np.float64) * 2.0 ** -20
+    es, num, ins = ref.predicates(2, *pts)
+    out["pred_f64tri_in"], out["pred_f64tri_sign"], out["pred_f64tri_num"], out["pred_f64tri_inside"] = pts, es, num, ins
+    # project_into_tri's weights on the same vectors
+    for pol, tag in ((0, "i32"), (1, "i64"), (2, "f64"), (2, "f64tri")):
+        out[f"pred_{tag}_weights"] = ref.predicate_weights(pol, *out[f"pred_{tag}_in"])
 
     # GK15 closed forms (test/math/test_integrate_gk15.cc:18-72)
     gk = [(0, 0.0, np.pi, 0, 10, 1e-10), (1, 0.0, 1.0, 0, 10, 1e-10), (2, 0.0, 1.0, 0, 10, 1e-12),

@@ -11,9 +11,11 @@ import subprocess
 import numpy as np
 import pytest
 
+from oracle.oracle import reference_src
+
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 HEADER = os.path.join(ROOT, "include", "antipodal_gb300.h")
-REF_SRC = "/root/reference/src"
+REF_SRC = reference_src() or ""
 
 
 def declared_functions():

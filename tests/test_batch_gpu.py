@@ -99,3 +99,47 @@ def test_batch_errors(gwn, disp):
     with pytest.raises(gwn.GwnError):
         b.set_config(512, 1, 256, 64)
     b.close()
+
+
+@pytest.mark.parametrize("dt,policy,mode", [(np.float32, "int64_grid", "exact"), (np.float32, "int64_grid", "mixed"),
+                                            (np.float64, "int64_grid", "mixed"), (np.float64, "int128_grid", "exact"),
+                                            (np.float64, "exact_float", "exact")])
+def test_batch_matches_oracle(gwn, disp, oracle, dt, policy, mode):
+    """The batch against the CPU oracle (the reference's RobustMeshGwn rule) on a seeded sample of every mesh's
+    queries: counts bit for bit; values within the exact tolerance (1e-12 double, 1e-6 float, as the golden tests),
+    or in mixed mode within 1e-7 of FP64 (float outputs: plus two ulps of the value's rounding)."""
+    torch = pytest.importorskip("torch")
+    tdt = torch.float32 if dt == np.float32 else torch.float64
+    meshes = build_meshes(dt, seed=3)
+    robust = [gwn.CudaRobustMeshGwn(disp, v, i, b, precision=policy) for v, i, b, _ in meshes]
+    pos = [torch.from_numpy(q).cuda() for *_, q in meshes]
+    outs = [torch.full((len(q),), float("nan"), dtype=tdt, device="cuda") for *_, q in meshes]
+    cnts = [torch.full((len(q),), -7, dtype=torch.int32, device="cuda") for *_, q in meshes]
+    disp.set_robust_precision(mode)
+    try:
+        batch = gwn.CudaRobustBatch(disp, robust, pos, outs, cnts)
+        batch.tune(repeats=1)
+        batch.run(graph=True)
+        torch.cuda.synchronize()
+    finally:
+        disp.set_robust_precision("exact")
+    rng = np.random.default_rng(41)
+    ulps = 0.0 if dt == np.float64 or mode == "exact" else 2 * 2.0 ** -23
+    tol = (1e-12 if dt == np.float64 else 1e-6) if mode == "exact" else 1e-7
+    checked = 0
+    for k, (v, i, b, q) in enumerate(meshes):
+        if len(q) == 0:
+            continue
+        pick = np.sort(rng.choice(len(q), size=min(len(q), 400), replace=False))
+        gw, rc, rf = oracle.robust_eval(policy, v, i, b, q[pick])
+        got_c = cnts[k].cpu().numpy()[pick]
+        got = outs[k].cpu().numpy()[pick].astype(np.float64)
+        assert np.array_equal(got_c, rc), (k, int(np.sum(got_c != rc)))
+        ref = gw.astype(np.float64)
+        err = np.abs(got - ref) - ulps * np.maximum(1, np.abs(ref))
+        assert float(err.max()) <= tol, (k, float(err.max()))
+        checked += len(pick)
+    assert checked > 2000
+    batch.close()
+    for r in robust:
+        r.close()

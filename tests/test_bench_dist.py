@@ -64,11 +64,15 @@ def test_reference_arm_runs_on_rank_zero_only():
 
 
 def test_workload_scale_defaults(monkeypatch):
-    # the parametric workload defaults to its 4% query sample (its FP64 reference forms at full scale take about
-    # half an hour); the others to their full size; an explicit --scale wins
+    # every workload runs its chosen form at full size; the parametric workload times its plain FP64 integrator and
+    # ablations on a 4% seeded sample of the queries (the plain form on all 1e6 takes about 100 s per step) and
+    # trains its network on 1e7 labels; explicit flags win
     sys.path.insert(0, ROOT)
     import bench
-    for argv, want in ((["bench.py"], 1.0), (["bench.py", "--config", "param"], 0.04),
-                       (["bench.py", "--config", "robust"], 1.0), (["bench.py", "--config", "param", "--scale", "1"], 1.0)):
+    for argv, scale, plain, labels in ((["bench.py"], 1.0, 0.04, 1e7), (["bench.py", "--config", "param"], 1.0, 0.04, 1e7),
+                                       (["bench.py", "--config", "robust"], 1.0, 0.04, 1e7),
+                                       (["bench.py", "--config", "param", "--scale", "0.1", "--plain-scale", "0.5",
+                                         "--labels", "2e6"], 0.1, 0.5, 2e6)):
         monkeypatch.setattr(sys, "argv", argv)
-        assert bench.parse().scale == want, argv
+        a = bench.parse()
+        assert (a.scale, a.plain_scale, a.labels) == (scale, plain, labels), argv

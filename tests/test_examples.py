@@ -11,8 +11,10 @@ import zlib
 import numpy as np
 import pytest
 
+from oracle.oracle import reference_src
+
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF_SRC = "/root/reference/src"
+REF_SRC = reference_src() or ""
 LIBDIR = os.path.join(ROOT, "antipodal_gb300")
 
 

@@ -10,10 +10,11 @@ import numpy as np
 import pytest
 
 from antipodal_gb300 import synth
+from oracle.oracle import reference_src
 
 pytestmark = pytest.mark.gpu
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF_SRC = "/root/reference/src"
+REF_SRC = reference_src() or ""
 
 
 def test_frontend_program_matches_oracle(gwn, oracle, tmp_path):

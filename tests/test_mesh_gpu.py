@@ -57,6 +57,38 @@ def test_intersector_cube_counts(gwn, disp, dtype):
         assert c.tolist() == [1, 1, 0, 0]
 
 
+def test_ties_on_axis_aligned_cube_rays(gwn, disp, oracle):
+    """test/test_intersector.cc:85-89: NaiveIntersector is plain Moller-Trumbore and counts a ray through an edge or
+    vertex once per triangle that shares it.  Axis-aligned rays from the closed cube's centre cross each face on the
+    diagonal shared by its two triangles, so they count 2 where a generic direction counts 1.  The device counts
+    (cell grid and hierarchy walk) reproduce the oracle's counts, double counts included, and the tie-reporting
+    scan flags exactly the rays whose hits lie on an edge or vertex."""
+    from antipodal_gb300 import _lib
+    verts, idx = synth.CUBE_VERTS, synth.CUBE_IDX_CLOSED
+    q = np.array([[0, 0, 0], [0.1, -0.2, 0.3], [0.0, 0.25, 0.0], [2, 0, 0], [-2, 0, 0]], np.float64)
+    isect = gwn.CudaIntersector(disp, verts, idx)
+    try:
+        for d in ([1, 0, 0], [-1, 0, 0], [0, 1, 0], [0, 0, -1], [0.31, 0.57, 0.76]):
+            d = np.array(d, np.float64)
+            ref = oracle.int_naive(q, d, verts, idx)
+            for cells in (1, 0):
+                disp.set_option(_lib.OPT_INTEGER_CELLS, cells)
+                c = np.empty(len(q), np.int32)
+                gwn.eval_gwnr_mesh_batch_integer(disp, isect, q, c, d)
+                assert np.array_equal(c, ref), (d, cells, c, ref)
+            bf, ties = np.empty(len(q), np.int32), np.empty(len(q), np.int32)
+            gwn.eval_gwnr_mesh_batch_integer_bruteforce(disp, verts, idx, q, bf, d, out_ties=ties)
+            assert np.array_equal(bf, ref)
+            axis = np.count_nonzero(d) == 1
+            if axis:
+                assert ref[0] == 2 and ties[0] == 2  # both triangles of the exit face, on their shared diagonal
+            else:
+                assert ref[0] == 1 and not ties.any()
+    finally:
+        disp.set_option(_lib.OPT_INTEGER_CELLS, 1)
+        isect.close()
+
+
 def test_rotated_open_cube_full_size(gwn, disp, oracle):
     verts, idx, bnd, q, x0 = synth.rotated_open_cube(seed=0, n_queries=100_000)
     ref = oracle.full_naive(q, x0, verts, idx, bnd)

@@ -77,12 +77,13 @@ def test_robust_golden(oracle, golden):
                 np.testing.assert_allclose(g, golden[f"robust_{name}_{tag}_{pol}_gwn"], rtol=0, atol=tol)
 
 
-@pytest.mark.parametrize("policy,tag", [(0, "i32"), (1, "i64"), (2, "f64")])
+@pytest.mark.parametrize("policy,tag", [(0, "i32"), (1, "i64"), (2, "f64"), (2, "f64tri")])
 def test_predicates_golden(oracle, golden, policy, tag):
     es, num, ins = oracle.predicates(policy, *golden[f"pred_{tag}_in"])
     assert np.array_equal(es, golden[f"pred_{tag}_sign"])
     assert np.array_equal(num, golden[f"pred_{tag}_num"])
     assert np.array_equal(ins, golden[f"pred_{tag}_inside"])
+    assert np.array_equal(oracle.predicate_weights(policy, *golden[f"pred_{tag}_in"]), golden[f"pred_{tag}_weights"])
 
 
 def test_gk15_golden(oracle, golden):
