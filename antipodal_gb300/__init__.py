@@ -171,7 +171,9 @@ class CudaDispatcher:
         _check(library().agwn_context_get_stats(self.handle, C.byref(s), int(reset)), "agwn_context_get_stats")
         names = ["fractional", "integer", "robust", "parametric", "other"]
         return {"kernel_ms": dict(zip(names, list(s.kernel_ms))), "launches": dict(zip(names, list(s.launches))),
-                "fp64_pairs": s.fp64_pairs, "pairs": s.pairs}
+                "fp64_pairs": s.fp64_pairs, "pairs": s.pairs,
+                "integer": {"queries": s.int_queries, "cell_entries": s.int_cell_entries, "leaves": s.int_leaves,
+                            "exact_tests": s.int_exact_tests}}
 
     def probe_fp32_peak(self) -> float:
         """Measured FP32 FMA throughput of this GPU, TFLOP/s."""

@@ -43,6 +43,8 @@ void clear_message();
     } while (0)
 
 // Device-side error flags, one word each, set with atomicOr by kernels and read by the host at synchronisation.
+constexpr int kCounters = 8; // device statistics counters of a context
+
 enum flag_slot
 {
     FLAG_STACK = 0,   // traversal stack exhausted
@@ -133,7 +135,8 @@ struct Context
     bool own_stream = false;
     int* d_flags = nullptr;        // FLAG_COUNT ints
     int* h_flags = nullptr;        // pinned mirror
-    long long* d_counters = nullptr; // [0] fp64 pairs, [1] pairs
+    long long* d_counters = nullptr; // kCounters: [0] fp64 pairs, [1] pairs, [2] parametric skips, [4..7] integer
+                                     // term: queries, cell-list entries, candidate leaves, exact tests
     DevBuf scratch[S_COUNT];
     int sm_count = 0;
     RayCache ray_cache;

@@ -256,9 +256,9 @@ int agwn_context_create(int device, void* stream, agwn_context** out)
             break;
         if ((e = cudaMemset(ctx->d_flags, 0, sizeof(int) * FLAG_COUNT)) != cudaSuccess)
             break;
-        if ((e = cudaMalloc(&ctx->d_counters, sizeof(long long) * 4)) != cudaSuccess)
+        if ((e = cudaMalloc(&ctx->d_counters, sizeof(long long) * kCounters)) != cudaSuccess)
             break;
-        if ((e = cudaMemset(ctx->d_counters, 0, sizeof(long long) * 4)) != cudaSuccess)
+        if ((e = cudaMemset(ctx->d_counters, 0, sizeof(long long) * kCounters)) != cudaSuccess)
             break;
         if ((e = cudaMallocHost(&ctx->h_flags, sizeof(int) * FLAG_COUNT)) != cudaSuccess)
             break;
@@ -432,7 +432,7 @@ int agwn_context_get_stats(agwn_context* ctx, agwn_stats* out, int reset)
     AGWN_CHECK_ARG(ctx && out, "agwn_context_get_stats: null argument");
     AGWN_TRY_CUDA(cudaSetDevice(ctx->device));
     AGWN_TRY(ctx->drain_timing());
-    long long counters[4] = {};
+    long long counters[kCounters] = {};
     AGWN_TRY_CUDA(cudaMemcpyAsync(counters, ctx->d_counters, sizeof(counters), cudaMemcpyDeviceToHost, ctx->stream));
     AGWN_TRY_CUDA(cudaStreamSynchronize(ctx->stream));
     for (int k = 0; k < AGWN_K_COUNT; ++k)
@@ -442,6 +442,10 @@ int agwn_context_get_stats(agwn_context* ctx, agwn_stats* out, int reset)
     }
     out->fp64_pairs = counters[0];
     out->pairs = counters[1];
+    out->int_queries = counters[4];
+    out->int_cell_entries = counters[5];
+    out->int_leaves = counters[6];
+    out->int_exact_tests = counters[7];
     if (reset)
     {
         for (int k = 0; k < AGWN_K_COUNT; ++k)

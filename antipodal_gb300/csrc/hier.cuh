@@ -202,13 +202,13 @@ __device__ __forceinline__ int cell_of(float x, float lo, float inv, int g)
 
 // The leaves listed in the cell of a query's (u, v) point that the walk's leaf conditions admit (the top of the
 // leaf above the query's depth, may_hit), passed to emit; a query outside the grid's extent has none.  The caller
-// takes the hierarchy walk instead when the query's tolerance exceeds g.tol_max.
+// takes the hierarchy walk instead when the query's tolerance exceeds g.tol_max.  Returns the list entries read.
 template <class Emit>
-__device__ __forceinline__ void cell_candidates(CellView const& g, const float4* __restrict__ leaf_uv, float u, float v,
-                                                float w, float tol, float m8, Emit&& emit)
+__device__ __forceinline__ unsigned cell_candidates(CellView const& g, const float4* __restrict__ leaf_uv, float u,
+                                                    float v, float w, float tol, float m8, Emit&& emit)
 {
     if (!(u >= g.umin && u <= g.umax && v >= g.vmin && v <= g.vmax))
-        return;
+        return 0;
     int64_t const c = int64_t(cell_of(v, g.vmin, g.inv_v, g.gv)) * g.gu + cell_of(u, g.umin, g.inv_u, g.gu);
     unsigned const b = g.offsets[c], e = g.offsets[c + 1];
     float const wq = w - tol;
@@ -219,6 +219,98 @@ __device__ __forceinline__ void cell_candidates(CellView const& g, const float4*
         float const wc = leaf_uv[kLeafF4 * leaf + 2].x;
         if (fmaxf(fmaxf(lb.z, lb.w), wc) >= wq && may_hit(leaf_uv, leaf, u, v, m8))
             emit(leaf);
+    }
+    return e - b;
+}
+
+// ---- exact tests of undecided leaves, a warp's worth at a time -----------------------------------------------
+// The float decision (certain_leaf) leaves a few candidates per warp undecided, at different points of each lane's
+// candidate loop, so testing them in place runs each exact test with one or two lanes active.  Instead a query
+// keeps up to kUndecided of them; after its candidates, the warp appends every lane's to a queue in shared memory,
+// and whenever 32 are queued each lane takes one and runs the exact test (for its owner's query, reloaded by
+// index), adding the result to the owner's count.  The query's own float-decided sum is stored first, so the
+// additions are atomic adds to it.
+constexpr int kUndecided = 4;  // undecided leaves a query holds; any beyond are tested in place (rare)
+constexpr unsigned kLeafQCap = 64; // > 31 left over + 32 appended per round
+
+struct LeafQueue
+{
+    int* leaf;         // kLeafQCap entries of this warp
+    long long* query;  // their queries' indices
+    unsigned head = 0, tail = 0; // warp-uniform
+};
+
+// Runs the exact test exact(query, leaf) -> -1, 0 or 1 on the c (<= 32) oldest entries, one per lane.
+template <class Exact>
+__device__ __forceinline__ void leafq_flush(LeafQueue& lq, unsigned c, int lane, int32_t* __restrict__ counts,
+                                            Exact&& exact)
+{
+    __syncwarp(); // the entries, and the owners' counts, are visible to the warp
+    if (unsigned(lane) < c)
+    {
+        unsigned const s = (lq.head + unsigned(lane)) & (kLeafQCap - 1);
+        long long const qi = lq.query[s];
+        int const r = exact(qi, lq.leaf[s]);
+        if (r)
+            atomicAdd(counts + qi, r);
+    }
+    lq.head += c;
+    __syncwarp(); // the slots are free again
+}
+
+// Appends each lane's nu undecided leaves und[0..nu) of query qi (every lane of the warp calls it, after storing
+// its query's count) and tests full batches of 32.
+template <class Exact>
+__device__ __forceinline__ void leafq_push(LeafQueue& lq, int const (&und)[kUndecided], int nu, long long qi, int lane,
+                                           int32_t* __restrict__ counts, Exact&& exact)
+{
+    unsigned const lt = (1u << lane) - 1u;
+    int const most = __reduce_max_sync(0xffffffffu, nu);
+#pragma unroll
+    for (int j = 0; j < kUndecided; ++j)
+    {
+        if (j >= most)
+            break;
+        bool const has = j < nu;
+        unsigned const m = __ballot_sync(0xffffffffu, has);
+        if (has)
+        {
+            unsigned const s = (lq.tail + unsigned(__popc(m & lt))) & (kLeafQCap - 1);
+            lq.leaf[s] = und[j];
+            lq.query[s] = qi;
+        }
+        lq.tail += unsigned(__popc(m));
+        if (lq.tail - lq.head >= 32)
+            leafq_flush(lq, 32, lane, counts, exact);
+    }
+}
+
+// Tests what is left in the queue (at the end of the kernel).
+template <class Exact>
+__device__ __forceinline__ void leafq_drain(LeafQueue& lq, int lane, int32_t* __restrict__ counts, Exact&& exact)
+{
+    while (lq.tail != lq.head)
+        leafq_flush(lq, min(32u, lq.tail - lq.head), lane, counts, exact);
+}
+
+// Integer-term statistics (AGWN_OPT_TIMING): one warp's sums added to counters[4..7] = queries, cell-list entries
+// read, candidate leaves decided, exact tests.
+__device__ __forceinline__ void integer_stats(long long* counters, long long queries, long long entries,
+                                              long long leaves, long long exact_tests)
+{
+    long long v[4] = {queries, entries, leaves, exact_tests};
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+    {
+        for (int o = 16; o > 0; o >>= 1)
+            v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+    }
+    if ((threadIdx.x & 31) == 0)
+    {
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            if (v[k])
+                atomicAdd(reinterpret_cast<unsigned long long*>(counters + 4 + k), static_cast<unsigned long long>(v[k]));
     }
 }
 

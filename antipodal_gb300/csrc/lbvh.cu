@@ -502,89 +502,208 @@ __global__ void k_cell_bin(const float4* __restrict__ leaf_uv, int64_t n, float 
     }
 }
 
+// Double input: most candidates are decided in float by certain_leaf; the undecided ones take NaiveIntersector's
+// exact test a warp's worth at a time (leafq_push).  Float input takes the exact test on every candidate, in place
+// (its own test is float arithmetic, and its rounding is not small against the margin for very thin triangles).
+// The loop over queries is warp-uniform: a lane past the end has no candidates.  stats: counters, or null.
 template <class T>
-__global__ void __launch_bounds__(kTravBlock) k_cells(const BvhNode* __restrict__ nodes, const T* __restrict__ tri,
+__global__ void __launch_bounds__(kTravBlock, 8) k_cells(const BvhNode* __restrict__ nodes, const T* __restrict__ tri,
                                                       const float4* __restrict__ leaf_uv, float scene_scale,
                                                       Frame32 f, CellView g, const T* __restrict__ pos, int64_t n,
-                                                      int32_t* __restrict__ counts, T dx, T dy, T dz, int* flags)
+                                                      int32_t* __restrict__ counts, T dx, T dy, T dz, int* flags,
+                                                      long long* stats)
 {
     using S = typename exact_of<T>::type;
+    constexpr bool kQueue = std::is_same_v<T, double>;
+    __shared__ int s_leaf[kTravBlock / 32][kLeafQCap];
+    __shared__ long long s_query[kTravBlock / 32][kLeafQCap];
     ev3<S> const dir{S(dx), S(dy), S(dz)};
-    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+    int const lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    LeafQueue lq;
+    lq.leaf = s_leaf[warp];
+    lq.query = s_query[warp];
+    auto const exact = [&](long long qi, int leaf) -> int
     {
-        T const px = pos[3 * i], py = pos[3 * i + 1], pz = pos[3 * i + 2];
-        ev3<S> const p{S(px), S(py), S(pz)};
-        float const ox = float(px), oy = float(py), oz = float(pz);
-        float const u = f.r[0] * ox + f.r[1] * oy + f.r[2] * oz;
-        float const v = f.r[3] * ox + f.r[4] * oy + f.r[5] * oz;
-        float const w = f.r[6] * ox + f.r[7] * oy + f.r[8] * oz;
-        float const qmax = fmaxf(fmaxf(fabsf(ox), fabsf(oy)), fabsf(oz));
-        float const tol = (qmax + scene_scale) * 3.8146973e-6f + 1e-30f; // as in k_traverse
-        float const m8 = margin_rotated(qmax, scene_scale);
-        auto const decide = [&](int leaf) -> int
+        ev3<S> const p{S(pos[3 * qi]), S(pos[3 * qi + 1]), S(pos[3 * qi + 2])};
+        return leaf_test<T>(tri, leaf, p, dir);
+    };
+    long long n_q = 0, n_entries = 0, n_leaves = 0, n_exact = 0;
+    int64_t const stride = int64_t(gridDim.x) * blockDim.x;
+    for (int64_t base = blockIdx.x * int64_t(blockDim.x) + (threadIdx.x & ~31); base < n; base += stride)
+    {
+        int64_t const i = base + lane;
+        int und[kUndecided];
+        int nu = 0;
+        if (i < n)
         {
-            if constexpr (std::is_same_v<T, double>)
+            T const px = pos[3 * i], py = pos[3 * i + 1], pz = pos[3 * i + 2];
+            float const ox = float(px), oy = float(py), oz = float(pz);
+            float const u = f.r[0] * ox + f.r[1] * oy + f.r[2] * oz;
+            float const v = f.r[3] * ox + f.r[4] * oy + f.r[5] * oz;
+            float const w = f.r[6] * ox + f.r[7] * oy + f.r[8] * oz;
+            float const qmax = fmaxf(fmaxf(fabsf(ox), fabsf(oy)), fabsf(oz));
+            float const tol = (qmax + scene_scale) * 3.8146973e-6f + 1e-30f; // as in k_traverse
+            float const m8 = margin_rotated(qmax, scene_scale);
+            int sum = 0;
+            auto const consider = [&](int leaf)
             {
-                int const c = certain_leaf(leaf_uv, leaf, u, v, w, m8);
-                if (c != 2)
-                    return c;
-            }
-            return leaf_test<T>(tri, leaf, p, dir);
-        };
-        int sum = 0;
-        int cand[kCand];
-        int nc = 0;
-        auto const consider = [&](int leaf)
-        {
-            if (nc == kCand)
-            {
-                for (int j = 0; j < kCand; ++j)
-                    sum += decide(cand[j]);
-                nc = 0;
-            }
-            cand[nc++] = leaf;
-        };
-        if (tol <= g.tol_max)
-            cell_candidates(g, leaf_uv, u, v, w, tol, m8, consider);
-        else if (!hier_walk(nodes, leaf_uv, u, v, w, tol, m8, consider))
-            atomicOr(flags + FLAG_STACK, 1);
-        for (int j = 0; j < nc; ++j)
-            sum += decide(cand[j]);
-        counts[i] = sum;
+                ++n_leaves;
+                if constexpr (kQueue)
+                {
+                    int const c = certain_leaf(leaf_uv, leaf, u, v, w, m8);
+                    if (c != 2)
+                    {
+                        sum += c;
+                        return;
+                    }
+                    ++n_exact;
+                    if (nu < kUndecided)
+                    {
+                        und[nu++] = leaf;
+                        return;
+                    }
+                }
+                else
+                    ++n_exact;
+                sum += leaf_test<T>(tri, leaf, ev3<S>{S(px), S(py), S(pz)}, dir);
+            };
+            if (tol <= g.tol_max)
+                n_entries += cell_candidates(g, leaf_uv, u, v, w, tol, m8, consider);
+            else if (!hier_walk(nodes, leaf_uv, u, v, w, tol, m8, consider))
+                atomicOr(flags + FLAG_STACK, 1);
+            counts[i] = sum;
+            ++n_q;
+        }
+        if constexpr (kQueue)
+            leafq_push(lq, und, nu, i, lane, counts, exact);
     }
+    if constexpr (kQueue)
+        leafq_drain(lq, lane, counts, exact);
+    if (stats)
+        integer_stats(stats, n_q, n_entries, n_leaves, n_exact);
 }
 
-template <class T>
-__global__ void __launch_bounds__(128) k_bruteforce(const T* __restrict__ verts, const int32_t* __restrict__ idx,
-                                                    int64_t n_tri, const T* __restrict__ pos, int64_t n,
-                                                    int32_t* __restrict__ counts, T dx, T dy, T dz,
-                                                    int32_t* __restrict__ ties)
+// ---- every triangle against every query (NaiveIntersector's loop), with a bounding-box cull ------------------
+// The scan tests each (query, triangle) pair with NaiveIntersector's own Moller-Trumbore arithmetic, skipping
+// only pairs that test cannot count: in a frame whose third axis is the ray direction, the ray of a query is the
+// point (u, v) of the query, and a counted hit lies within the triangle's (u, v) box up to the test's FP64
+// rounding (~1e-15 of the coordinates).  Boxes are rounded outward to float and the query's point is widened by
+// 2^-20 of (query + scene) coordinate scale, far above both roundings.  A triangle or query with a NaN or an
+// infinity is never skipped.  So the counts, and the ties, are the full scan's; no hierarchy is involved.
+constexpr int kScanBlock = 128;
+constexpr int kScanK = 4;        // queries per thread
+constexpr int kScanTile = 2048;  // boxes per shared-memory tile (32 KB)
+
+// Box (umin, vmin, umax, vmax) of every triangle in the frame f, and the largest |vertex coordinate| as float bits
+// (scale_bits, atomicMax; the coordinates' absolute values order like their bits).
+__global__ void k_scan_boxes(const double* __restrict__ verts, const int32_t* __restrict__ idx, int64_t n_tri, Frame64 f,
+                             float4* __restrict__ boxes, unsigned* __restrict__ scale_bits)
 {
-    using S = typename exact_of<T>::type;
-    ev3<S> const dir{S(dx), S(dy), S(dz)};
-    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+    float amax = 0.f;
+    for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; t < n_tri; t += int64_t(gridDim.x) * blockDim.x)
     {
-        ev3<S> const p{S(pos[3 * i]), S(pos[3 * i + 1]), S(pos[3 * i + 2])};
-        int sum = 0, n_ties = 0;
-        for (int64_t t = 0; t < n_tri; ++t)
+        double lo[2] = {INFINITY, INFINITY}, hi[2] = {-INFINITY, -INFINITY};
+        bool finite = true;
+        for (int c = 0; c < 3; ++c)
         {
-            T const* a = verts + 3 * int64_t(idx[3 * t]);
-            T const* b = verts + 3 * int64_t(idx[3 * t + 1]);
-            T const* c = verts + 3 * int64_t(idx[3 * t + 2]);
-            ev3<S> const va{S(a[0]), S(a[1]), S(a[2])}, vb{S(b[0]), S(b[1]), S(b[2])}, vc{S(c[0]), S(c[1]), S(c[2])};
-            if (ties)
+            const double* x = verts + 3 * int64_t(idx[3 * t + c]);
+            finite &= isfinite(x[0]) && isfinite(x[1]) && isfinite(x[2]);
+            amax = fmaxf(amax, float(fmax(fmax(fabs(x[0]), fabs(x[1])), fabs(x[2]))));
+            for (int r = 0; r < 2; ++r)
             {
-                bool tie = false;
-                int const h = mt_sign(p, dir, va, vb, vc, &tie);
-                sum += h;
-                n_ties += (h != 0 && tie) ? 1 : 0;
+                double const u = f.r[3 * r] * x[0] + f.r[3 * r + 1] * x[1] + f.r[3 * r + 2] * x[2];
+                lo[r] = fmin(lo[r], u);
+                hi[r] = fmax(hi[r], u);
             }
-            else
-                sum += mt_sign(p, dir, va, vb, vc);
         }
-        counts[i] = sum;
-        if (ties)
-            ties[i] = n_ties;
+        boxes[t] = finite ? make_float4(__double2float_rd(lo[0]), __double2float_rd(lo[1]), __double2float_ru(hi[0]),
+                                        __double2float_ru(hi[1]))
+                          : make_float4(-INFINITY, -INFINITY, INFINITY, INFINITY);
+    }
+    amax = isfinite(amax) ? amax : 0.f;
+    for (int o = 16; o > 0; o >>= 1)
+        amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, o));
+    if ((threadIdx.x & 31) == 0)
+        atomicMax(scale_bits, __float_as_uint(amax));
+}
+
+__global__ void __launch_bounds__(kScanBlock) k_scan(const double* __restrict__ verts, const int32_t* __restrict__ idx,
+                                                     const float4* __restrict__ boxes, int64_t n_tri,
+                                                     const unsigned* __restrict__ scale_bits, Frame64 f,
+                                                     const double* __restrict__ pos, int64_t n,
+                                                     int32_t* __restrict__ counts, int32_t* __restrict__ ties,
+                                                     double dx, double dy, double dz)
+{
+    __shared__ float4 sbox[kScanTile];
+    ev3<rd> const dir{rd(dx), rd(dy), rd(dz)};
+    float const scene = __uint_as_float(*scale_bits);
+    int64_t const per_block = int64_t(kScanBlock) * kScanK;
+    for (int64_t base = blockIdx.x * per_block; base < n; base += int64_t(gridDim.x) * per_block)
+    {
+        float ulo[kScanK], uhi[kScanK], vlo[kScanK], vhi[kScanK];
+        int sum[kScanK], tie[kScanK];
+#pragma unroll
+        for (int k = 0; k < kScanK; ++k)
+        {
+            int64_t const i = base + threadIdx.x + int64_t(k) * kScanBlock;
+            sum[k] = 0;
+            tie[k] = 0;
+            if (i >= n)
+            {
+                ulo[k] = uhi[k] = vlo[k] = vhi[k] = __int_as_float(0x7fffffff); // NaN: every comparison fails
+                continue;
+            }
+            double const x = pos[3 * i], y = pos[3 * i + 1], z = pos[3 * i + 2];
+            double const u = f.r[0] * x + f.r[1] * y + f.r[2] * z, v = f.r[3] * x + f.r[4] * y + f.r[5] * z;
+            float const m = 9.5367432e-7f * (float(fmax(fmax(fabs(x), fabs(y)), fabs(z))) + scene); // 2^-20
+            bool const ok = fabs(u) < 1e30 && fabs(v) < 1e30 && isfinite(m); // else (NaN, huge) test everything
+            ulo[k] = ok ? float(u) - m : -INFINITY;
+            uhi[k] = ok ? float(u) + m : INFINITY;
+            vlo[k] = ok ? float(v) - m : -INFINITY;
+            vhi[k] = ok ? float(v) + m : INFINITY;
+        }
+        for (int64_t t0 = 0; t0 < n_tri; t0 += kScanTile)
+        {
+            int const cnt = int(n_tri - t0 < kScanTile ? n_tri - t0 : int64_t(kScanTile));
+            __syncthreads();
+            for (int j = threadIdx.x; j < cnt; j += kScanBlock)
+                sbox[j] = boxes[t0 + j];
+            __syncthreads();
+            for (int j = 0; j < cnt; ++j)
+            {
+                float4 const b = sbox[j];
+#pragma unroll
+                for (int k = 0; k < kScanK; ++k)
+                {
+                    if (b.x <= uhi[k] && b.z >= ulo[k] && b.y <= vhi[k] && b.w >= vlo[k])
+                    {
+                        int64_t const i = base + threadIdx.x + int64_t(k) * kScanBlock;
+                        int64_t const t = t0 + j;
+                        const double* a = verts + 3 * int64_t(idx[3 * t]);
+                        const double* bb = verts + 3 * int64_t(idx[3 * t + 1]);
+                        const double* c = verts + 3 * int64_t(idx[3 * t + 2]);
+                        bool tt = false;
+                        int const h = mt_sign(ev3<rd>{rd(pos[3 * i]), rd(pos[3 * i + 1]), rd(pos[3 * i + 2])}, dir,
+                                              ev3<rd>{rd(a[0]), rd(a[1]), rd(a[2])},
+                                              ev3<rd>{rd(bb[0]), rd(bb[1]), rd(bb[2])},
+                                              ev3<rd>{rd(c[0]), rd(c[1]), rd(c[2])}, &tt);
+                        sum[k] += h;
+                        tie[k] += (h != 0 && tt) ? 1 : 0;
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < kScanK; ++k)
+        {
+            int64_t const i = base + threadIdx.x + int64_t(k) * kScanBlock;
+            if (i < n)
+            {
+                counts[i] = sum[k];
+                if (ties)
+                    ties[i] = tie[k];
+            }
+        }
     }
 }
 
@@ -932,7 +1051,8 @@ int integer_run(Context& ctx, const Bvh& bvh, const T* d_pos, int64_t n, int32_t
                                                   static_cast<const T*>(ctx.ray_cache.h.tri.ptr),
                                                   static_cast<const float4*>(ctx.ray_cache.h.leaf_uv.ptr),
                                                   float(bvh.scene_scale), f, v, d_pos, n, d_counts, dir_host[0],
-                                                  dir_host[1], dir_host[2], ctx.d_flags);
+                                                  dir_host[1], dir_host[2], ctx.d_flags,
+                                                  ctx.timing ? ctx.d_counters : nullptr);
         return ctx.launch_end(AGWN_K_INTEGER);
     }
     AGWN_TRY(ctx.launch_begin(AGWN_K_INTEGER));
@@ -1067,13 +1187,35 @@ static int bruteforce_f64(agwn_context* ctx, const double* vertices, int64_t n_v
     if (!is_device_pointer(indices))
         for (int64_t i = 0; i < n_indices; ++i)
             AGWN_CHECK_ARG(indices[i] >= 0 && indices[i] < n_vertices, "triangle index out of range");
-    int const grid = int(std::min<int64_t>(div_up(n, 128), int64_t(ctx->sm_count) * 16));
-    AGWN_TRY(ctx->launch_begin(AGWN_K_INTEGER));
-    k_bruteforce<double><<<grid, 128, 0, ctx->stream>>>(static_cast<const double*>(dv), static_cast<const int32_t*>(di),
-                                                        n_indices / 3, static_cast<const double*>(dpos), n,
-                                                        static_cast<int32_t*>(dout), dir[0], dir[1], dir[2],
-                                                        static_cast<int32_t*>(dties));
-    AGWN_TRY(ctx->launch_end(AGWN_K_INTEGER));
+    int64_t const n_tri = n_indices / 3;
+    if (n_tri == 0)
+    {
+        AGWN_TRY_CUDA(cudaMemsetAsync(dout, 0, sizeof(int32_t) * n, ctx->stream));
+        if (dties)
+            AGWN_TRY_CUDA(cudaMemsetAsync(dties, 0, sizeof(int32_t) * n, ctx->stream));
+    }
+    else
+    {
+        double const dn = dir[0] * dir[0] + dir[1] * dir[1] + dir[2] * dir[2];
+        AGWN_CHECK_ARG(dn > 0 && std::isfinite(dn), "ray direction must be finite and nonzero");
+        void* boxes = nullptr;
+        AGWN_TRY(ctx->scratch_reserve(S_MISC2, sizeof(float4) * n_tri + 256, &boxes));
+        unsigned* const scale_bits = reinterpret_cast<unsigned*>(static_cast<char*>(boxes) + sizeof(float4) * n_tri);
+        AGWN_TRY_CUDA(cudaMemsetAsync(scale_bits, 0, sizeof(unsigned), ctx->stream));
+        Frame64 const f = ray_frame(dir);
+        AGWN_TRY(ctx->launch_begin(AGWN_K_OTHER));
+        k_scan_boxes<<<int(std::min<int64_t>(div_up(n_tri, 256), 4 * int64_t(ctx->sm_count))), 256, 0, ctx->stream>>>(
+            static_cast<const double*>(dv), static_cast<const int32_t*>(di), n_tri, f, static_cast<float4*>(boxes),
+            scale_bits);
+        AGWN_TRY(ctx->launch_end(AGWN_K_OTHER));
+        int const grid = int(std::min<int64_t>(div_up(n, int64_t(kScanBlock) * kScanK), int64_t(ctx->sm_count) * 8));
+        AGWN_TRY(ctx->launch_begin(AGWN_K_INTEGER));
+        k_scan<<<grid, kScanBlock, 0, ctx->stream>>>(static_cast<const double*>(dv), static_cast<const int32_t*>(di),
+                                                     static_cast<const float4*>(boxes), n_tri, scale_bits, f,
+                                                     static_cast<const double*>(dpos), n, static_cast<int32_t*>(dout),
+                                                     static_cast<int32_t*>(dties), dir[0], dir[1], dir[2]);
+        AGWN_TRY(ctx->launch_end(AGWN_K_INTEGER));
+    }
     if (host_out)
         AGWN_TRY_CUDA(cudaMemcpyAsync(out_counts, dout, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, ctx->stream));
     if (host_ties)

@@ -220,7 +220,7 @@ int robust_run(Context& ctx, const Robust& r, const T* d_pos, int64_t n, T* d_ou
             k_robust_cells<T, P><<<grid, kRobBlock, 0, st>>>(
                 static_cast<const BvhNode*>(r.hier.nodes.ptr), static_cast<const C*>(r.tri),
                 static_cast<const float4*>(r.hier.leaf_uv.ptr), float(r.hier.scale), f, cell_view(r.cells), qz, d_pos,
-                n, d_counts, ctx.d_flags);
+                n, d_counts, ctx.d_flags, ctx.timing ? ctx.d_counters : nullptr);
             AGWN_TRY(ctx.launch_end(AGWN_K_ROBUST));
         }
         else

@@ -494,51 +494,74 @@ __global__ void __launch_bounds__(kRobBlock) k_robust_count(const BvhNode* __res
 // where it decides (all three edges, and the depth, beyond margins ~1e8 times the rounding of either
 // computation) its value is robust_crossing's, -e01 or 0.  The other leaves -- within the margin of an edge, a
 // vertex or the plane -- take robust_crossing itself.  The counts are the exact predicate's.
+// The undecided leaves take robust_crossing a warp's worth at a time (leafq_push, hier.cuh); the loop over
+// queries is warp-uniform.  stats: counters, or null.
 template <class T, class P>
 __global__ void __launch_bounds__(kRobBlock) k_robust_cells(const BvhNode* __restrict__ nodes,
                                                             const typename P::C* __restrict__ tri,
                                                             const float4* __restrict__ leaf_uv, float scene_scale,
                                                             Frame32 f, CellView g, Quant qz,
                                                             const T* __restrict__ pos, int64_t n,
-                                                            int32_t* __restrict__ counts, int* flags)
+                                                            int32_t* __restrict__ counts, int* flags,
+                                                            long long* stats)
 {
     using C = typename P::C;
-    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+    __shared__ int s_leaf[kRobBlock / 32][kLeafQCap];
+    __shared__ long long s_query[kRobBlock / 32][kLeafQCap];
+    int const lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    LeafQueue lq;
+    lq.leaf = s_leaf[warp];
+    lq.query = s_query[warp];
+    auto const exact = [&](long long qi, int leaf) -> int
     {
-        qv3<C> const q = quantize<P>(double(pos[3 * i]), double(pos[3 * i + 1]), double(pos[3 * i + 2]), qz);
-        float const ox = float(P::cdbl(q.x)), oy = float(P::cdbl(q.y)), oz = float(P::cdbl(q.z));
-        float const u = f.r[0] * ox + f.r[1] * oy + f.r[2] * oz;
-        float const v = f.r[3] * ox + f.r[4] * oy + f.r[5] * oz;
-        float const w = f.r[6] * ox + f.r[7] * oy + f.r[8] * oz;
-        float const qmax = fmaxf(fmaxf(fabsf(ox), fabsf(oy)), fabsf(oz));
-        float const tol = (qmax + scene_scale) * 3.8146973e-6f + 1e-30f;
-        float const m8 = margin_permuted(qmax, scene_scale);
-        int sum = 0;
-        int cand[kRobCand];
-        int nc = 0;
-        auto const decide = [&](int leaf) -> int
+        qv3<C> const q = quantize<P>(double(pos[3 * qi]), double(pos[3 * qi + 1]), double(pos[3 * qi + 2]), qz);
+        return robust_crossing<P>(q, tri + 9 * int64_t(leaf));
+    };
+    long long n_q = 0, n_entries = 0, n_leaves = 0, n_exact = 0;
+    int64_t const stride = int64_t(gridDim.x) * blockDim.x;
+    for (int64_t base = blockIdx.x * int64_t(blockDim.x) + (threadIdx.x & ~31); base < n; base += stride)
+    {
+        int64_t const i = base + lane;
+        int und[kUndecided];
+        int nu = 0;
+        if (i < n)
         {
-            int const c = certain_leaf(leaf_uv, leaf, u, v, w, m8);
-            return c != 2 ? c : robust_crossing<P>(q, tri + 9 * int64_t(leaf));
-        };
-        auto const consider = [&](int leaf)
-        {
-            if (nc == kRobCand)
+            qv3<C> const q = quantize<P>(double(pos[3 * i]), double(pos[3 * i + 1]), double(pos[3 * i + 2]), qz);
+            float const ox = float(P::cdbl(q.x)), oy = float(P::cdbl(q.y)), oz = float(P::cdbl(q.z));
+            float const u = f.r[0] * ox + f.r[1] * oy + f.r[2] * oz;
+            float const v = f.r[3] * ox + f.r[4] * oy + f.r[5] * oz;
+            float const w = f.r[6] * ox + f.r[7] * oy + f.r[8] * oz;
+            float const qmax = fmaxf(fmaxf(fabsf(ox), fabsf(oy)), fabsf(oz));
+            float const tol = (qmax + scene_scale) * 3.8146973e-6f + 1e-30f;
+            float const m8 = margin_permuted(qmax, scene_scale);
+            int sum = 0;
+            auto const consider = [&](int leaf)
             {
-                for (int j = 0; j < kRobCand; ++j)
-                    sum += decide(cand[j]);
-                nc = 0;
-            }
-            cand[nc++] = leaf;
-        };
-        if (tol <= g.tol_max)
-            cell_candidates(g, leaf_uv, u, v, w, tol, m8, consider);
-        else if (!hier_walk(nodes, leaf_uv, u, v, w, tol, m8, consider))
-            atomicOr(flags + FLAG_STACK, 1);
-        for (int j = 0; j < nc; ++j)
-            sum += decide(cand[j]);
-        counts[i] = sum;
+                ++n_leaves;
+                int const c = certain_leaf(leaf_uv, leaf, u, v, w, m8);
+                if (c != 2)
+                {
+                    sum += c;
+                    return;
+                }
+                ++n_exact;
+                if (nu < kUndecided)
+                    und[nu++] = leaf;
+                else
+                    sum += robust_crossing<P>(q, tri + 9 * int64_t(leaf));
+            };
+            if (tol <= g.tol_max)
+                n_entries += cell_candidates(g, leaf_uv, u, v, w, tol, m8, consider);
+            else if (!hier_walk(nodes, leaf_uv, u, v, w, tol, m8, consider))
+                atomicOr(flags + FLAG_STACK, 1);
+            counts[i] = sum;
+            ++n_q;
+        }
+        leafq_push(lq, und, nu, i, lane, counts, exact);
     }
+    leafq_drain(lq, lane, counts, exact);
+    if (stats)
+        integer_stats(stats, n_q, n_entries, n_leaves, n_exact);
 }
 
 template <class P>

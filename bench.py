@@ -201,9 +201,9 @@ def run_reference(args):
 
 
 # ---- GPU side -------------------------------------------------------------------------------------------------
-def read_traffic():
-    """DRAM bytes per launch of the mixed fractional kernel from the committed ncu summary, if present."""
-    p = os.path.join(ROOT, "profiles", "frac_mixed_icosphere.md")
+def read_traffic(name="frac_mixed_icosphere.md"):
+    """DRAM bytes per full launch of a kernel from its committed ncu summary, if present."""
+    p = os.path.join(ROOT, "profiles", name)
     if not os.path.exists(p):
         return None
     for line in open(p):
@@ -213,6 +213,22 @@ def read_traffic():
             except ValueError:
                 return None
     return None
+
+
+# Algorithmic bytes of the cell-grid integer term: per query its coordinates (24 B) and count (4 B) and its cell's
+# two CSR offsets (8 B); per cell-list entry the leaf index (4 B) and the leaf's float corners (48 B); per exact test
+# the triangle's nine doubles (72 B).
+INT_BYTES_PER_QUERY, INT_BYTES_PER_ENTRY, INT_BYTES_PER_EXACT = 36, 52, 72
+HBM_FALLBACK_GBS = 6800.0
+
+
+def hbm_peak():
+    """(GB/s, source) from MEASURED_PEAKS.json, else the machine's fallback figure."""
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        return float(json.load(open(p))["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return HBM_FALLBACK_GBS, "fallback"
 
 
 def run_ours(args):
@@ -283,7 +299,13 @@ def run_ours(args):
     value = ws * Q / (step_ms * 1e-3)
     launches = int(sum(st["launches"].values()))
     frac_ms = st["kernel_ms"]["fractional"] / max(1, st["launches"]["fractional"])
-    int_ms = st["kernel_ms"]["integer"] / max(1, st["launches"]["integer"])
+    n_int = max(1, st["launches"]["integer"])
+    int_ms = st["kernel_ms"]["integer"] / n_int
+    ic = st["integer"]
+    int_bytes = (ic["queries"] * INT_BYTES_PER_QUERY + ic["cell_entries"] * INT_BYTES_PER_ENTRY +
+                 ic["exact_tests"] * INT_BYTES_PER_EXACT) / n_int
+    hbm, hbm_src = hbm_peak()
+    int_gbs = int_bytes / (int_ms * 1e-3) / 1e9
 
     # the integer term of every query against the every-triangle scan, which also reports ties (hits exactly on an
     # edge or vertex, where NaiveIntersector counts a crossing once per triangle); untimed
@@ -375,7 +397,17 @@ def run_ours(args):
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                          "frac": achieved / peak, "traffic": traffic,
                          "note": f"fractional mixed kernel, {FLOPS_PER_PAIR} algorithmic flop per (query, segment) "
-                                 "pair; peak = FP32 FMA rate measured on this GPU in this run"},
+                                 "pair; peak = FP32 FMA rate measured on this GPU in this run",
+                         "integer": {"bound": "hbm", "achieved": int_gbs, "peak": hbm, "unit": "GB/s",
+                                     "frac": int_gbs / hbm, "traffic": read_traffic("cells_icosphere.md"),
+                                     "bytes_per_launch": int_bytes, "ms_per_launch": int_ms,
+                                     "per_query": {"cell_entries": ic["cell_entries"] / max(1, ic["queries"]),
+                                                   "leaves": ic["leaves"] / max(1, ic["queries"]),
+                                                   "exact_tests": ic["exact_tests"] / max(1, ic["queries"])},
+                                     "note": f"cell-grid integer kernel; algorithmic bytes = {INT_BYTES_PER_QUERY} B "
+                                             f"per query + {INT_BYTES_PER_ENTRY} B per cell-list entry + "
+                                             f"{INT_BYTES_PER_EXACT} B per exact test, from the kernel's own counters; "
+                                             f"peak = HBM copy bandwidth ({hbm_src})"}},
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "queries/s", "h2d_bytes_per_step": int(q.nbytes),
                     "d2h_bytes_per_step": int(Q * 8), "matches_device_result": e2e_match},

@@ -31,7 +31,7 @@
 extern "C" {
 #endif
 
-#define AGWN_ABI_VERSION 1
+#define AGWN_ABI_VERSION 2
 
 /* ---- status ---------------------------------------------------------------------------------------------- */
 enum agwn_status
@@ -138,6 +138,11 @@ typedef struct agwn_stats
     int64_t launches[AGWN_K_COUNT];   /* launches of the library's kernels, by class (always counted)        */
     int64_t fp64_pairs;               /* mixed mode: (query, segment) pairs evaluated in FP64 (when timing)  */
     int64_t pairs;                    /* mixed mode: all (query, segment) pairs evaluated (when timing)      */
+    /* integer term through the cell grid (mesh counts and robust counts), when timing: */
+    int64_t int_queries;              /* queries                                                              */
+    int64_t int_cell_entries;         /* cell-list entries read (each a leaf index and the leaf's corners)     */
+    int64_t int_leaves;               /* candidate leaves decided (in float, or by the exact test)             */
+    int64_t int_exact_tests;          /* leaves the float decision left to the exact test                      */
 } agwn_stats;
 /* Reads (synchronising the stream first) and optionally resets the accumulated statistics. */
 int agwn_context_get_stats(agwn_context* ctx, agwn_stats* out, int reset);

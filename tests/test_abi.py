@@ -44,7 +44,7 @@ def test_every_declared_function_is_exported(lib):
 
 
 def test_status_strings_and_version(lib):
-    assert lib.agwn_abi_version() == 1
+    assert lib.agwn_abi_version() == 2
     assert lib.agwn_status_string(0) == b"ok"
     assert lib.agwn_status_string(7) == b"no CUDA device"
 
