@@ -26,6 +26,7 @@ __all__ = [
     "GwnError", "CudaDispatcher", "CudaIntersector", "CudaRobustMeshGwn", "eval_gwnr_mesh_batch_fractional",
     "eval_gwnr_mesh_batch_integer", "eval_gwnr_mesh_batch", "eval_gwnr_mesh_batch_robust", "build_boundary_segments",
     "IntegrateConfig", "IntegratorGK15", "eval_gwnr_parametric_batch_fractional", "unpack_pair_stats",
+    "CudaBezierPatchIntersector", "eval_gwnr_parametric_batch_integer", "eval_gwnr_parametric_batch",
     "LearnedGK15Proposal", "CudaRobustBatch", "library",
 ]
 
@@ -122,7 +123,7 @@ class CudaDispatcher:
     """
 
     def __init__(self, device: int = 0, stream=None, precision: str = "exact", tau: float = 4.0,
-                 term_err: float = 3e-8, queries_per_thread: int = 2, block: int = 0, seg_tile: int = 512,
+                 term_err: float = 6e-8, queries_per_thread: int = 2, block: int = 0, seg_tile: int = 512,
                  timing: bool = False, mixed_min_pairs: float | None = None):
         lib = library()
         handle = None
@@ -637,6 +638,68 @@ def eval_gwnr_parametric_batch_fractional(dispatcher: CudaDispatcher, positions,
         _check(fn(dispatcher.handle, p.ptr, p.n, o.ptr, xp, c.ptr, c.n, cfg.min_depth, cfg.max_depth, cfg.tol,
                   sd.ptr if sd else None, st.ptr if st else None, nd.ptr if nd else None),
                "eval_gwnr_parametric_batch_fractional")
+    del x
+
+
+class CudaBezierPatchIntersector:
+    """The Intersector role for parametric surfaces made of bicubic Bezier patches: the integer term that
+    eval_gwnr_parametric_batch_integer / eval_gwnr_parametric_batch forward to (gwn_parametric.hh:204-284; the
+    reference ships no parametric intersector).  Each crossing of the ray p + lambda x0 (lambda >= 0) counts
+    sign(N . x0) with N = S_u x S_v, the orientation under which boundary curves running counter-clockwise in (u, v)
+    (synth.bezier_patch_boundary) make fractional + integer the winding number.
+
+    patches: (n, 4, 4, 3) or (n, 48) float64 control points P[patch][v index][u index][xyz]; copied to the
+    device."""
+
+    def __init__(self, dispatcher: CudaDispatcher, patches):
+        self._disp = dispatcher
+        c = _View(patches, np.float64, 48, "patches")
+        h = C.c_void_p()
+        _check(library().agwn_patches_create_f64(dispatcher.handle, c.ptr, c.n, C.byref(h)), "agwn_patches_create_f64")
+        self._h = h
+        self.n = c.n
+
+    @property
+    def handle(self):
+        if self._h is None:
+            raise RuntimeError("intersector is closed")
+        return self._h
+
+    def close(self):
+        if getattr(self, "_h", None) is not None:
+            library().agwn_patches_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def eval_gwnr_parametric_batch_integer(dispatcher: CudaDispatcher, intersector: CudaBezierPatchIntersector,
+                                       positions, out_counts, x0):
+    """gwn_parametric.hh:210-226: out_counts[i] = intersector.signed_intersection_count(positions[i], x0)."""
+    p = _View(positions, np.float64, 3, "positions")
+    o = _View(out_counts, np.int32, None, "out_counts", writable=True)
+    if p.n != o.n:
+        raise ValueError("positions and out_counts must have the same size")
+    _, xp = x = _vec3(x0, np.float64)
+    _check(library().agwn_param_batch_integer_bezier3x3_f64(dispatcher.handle, intersector.handle, p.ptr, p.n, o.ptr,
+                                                            xp), "eval_gwnr_parametric_batch_integer")
+    del x
+
+
+def eval_gwnr_parametric_batch(dispatcher: CudaDispatcher, intersector: CudaBezierPatchIntersector, positions,
+                               out_wnrs, x0, curves, cfg: IntegrateConfig | None = None, integrator=None):
+    """gwn_parametric.hh:259-284: out_wnrs[i] = the fractional term over the boundary curves (as
+    eval_gwnr_parametric_batch_fractional, any integrator) + the patches' signed crossing count along x0."""
+    eval_gwnr_parametric_batch_fractional(dispatcher, positions, out_wnrs, x0, curves, cfg, integrator)
+    p = _View(positions, np.float64, 3, "positions")
+    o = _View(out_wnrs, np.float64, None, "out_wnrs", writable=True)
+    _, xp = x = _vec3(x0, np.float64)
+    _check(library().agwn_param_add_integer_bezier3x3_f64(dispatcher.handle, intersector.handle, p.ptr, p.n, o.ptr,
+                                                          xp), "eval_gwnr_parametric_batch")
     del x
 
 

@@ -149,7 +149,7 @@ struct Context
     // options
     int frac_mode = AGWN_FRAC_EXACT;
     double mixed_tau = 4.0;
-    double mixed_term_err = 3e-8;
+    double mixed_term_err = 6e-8;
     int robust_mode = AGWN_ROBUST_EXACT;
     double robust_term_err = 1e-7;
     int param_mode = AGWN_PARAM_EXACT;

@@ -830,8 +830,8 @@ __global__ void __launch_bounds__(256, mixed_min_blocks<K>())
                 float2 const an = make_float2(fabsf(num_s.x), fabsf(num_s.y));
                 float2 const ad = make_float2(fabsf(den_s.x), fabsf(den_s.y));
                 bool const sw0 = an.x > ad.x, sw1 = an.y > ad.y;
-                float2 const inv = make_float2(__fdividef(1.f, fmaxf(sw0 ? an.x : ad.x, 1e-37f)),
-                                               __fdividef(1.f, fmaxf(sw1 ? an.y : ad.y, 1e-37f)));
+                // (num = den = 0 gives an infinite reciprocal, a NaN t and a NaN bound: the pair goes to FP64)
+                float2 const inv = make_float2(__fdividef(1.f, fmaxf(an.x, ad.x)), __fdividef(1.f, fmaxf(an.y, ad.y)));
                 float2 const t = lv_mul(make_float2(fminf(an.x, ad.x), fminf(an.y, ad.y)), inv);
                 float2 const bound = lv_mul(lv_fma(make_float2(sw0 ? sn.x : sd.x, sw1 ? sn.y : sd.y), t,
                                                    make_float2(sw0 ? sd.x : sn.x, sw1 ? sd.y : sn.y)),
@@ -842,14 +842,16 @@ __global__ void __launch_bounds__(256, mixed_min_blocks<K>())
                 bool const need0 = !(bound.x <= te_units) || fmaxf(den_s.x, margin.x) <= 0.f;
                 bool const need1 = !(bound.y <= te_units) || fmaxf(den_s.y, margin.y) <= 0.f;
                 nb |= (need0 ? (1u << (slot * K + 2 * p)) : 0u) | (need1 ? (1u << (slot * K + 2 * p + 1)) : 0u);
-                // atan2(num_s, den_s): atan(t), then the octant
-                float2 a = atan_unit_lv(t);
-                float2 const a_sw = lv_sub(lv_set<float2>(1.5707963267948966f), a);
-                a = make_float2(sw0 ? a_sw.x : a.x, sw1 ? a_sw.y : a.y);
-                float2 const a_neg = lv_sub(lv_set<float2>(3.141592653589793f), a);
-                a = make_float2(copysignf(den_s.x < 0.f ? a_neg.x : a.x, num_s.x),
-                                copysignf(den_s.y < 0.f ? a_neg.y : a.y, num_s.y));
-                float2 const term = lv_mul(w, a);
+                // atan2(num_s, den_s): atan(t) in [0, pi/4], then the octant as |c1 - a| (pi/2 - a when |num| >
+                // |den|, else a) and |c2 - a| (pi - a when den < 0, else a), signed like num
+                float2 const a = atan_unit_lv(t);
+                float2 const c1 = make_float2(sw0 ? 1.5707963267948966f : 0.f, sw1 ? 1.5707963267948966f : 0.f);
+                float2 const a1 = lv_sub(c1, a);
+                float2 const c2 = make_float2(den_s.x < 0.f ? 3.141592653589793f : 0.f,
+                                              den_s.y < 0.f ? 3.141592653589793f : 0.f);
+                float2 const a2 = lv_sub(c2, make_float2(fabsf(a1.x), fabsf(a1.y)));
+                float2 const ang = make_float2(copysignf(fabsf(a2.x), num_s.x), copysignf(fabsf(a2.y), num_s.y));
+                float2 const term = lv_mul(w, ang);
                 two_sum_lv(acc[p], comp[p], make_float2(need0 ? 0.f : term.x, need1 ? 0.f : term.y));
             }
         };

@@ -292,3 +292,33 @@ def bezier_patches(seed: int = 0, n_patches: int = 256, n_queries: int = 1_000_0
     q = q[rng.permutation(len(q))]
     x0 = random_unit(rng)
     return curves, q, x0
+
+
+def bezier_patch_boundary(patches: np.ndarray) -> np.ndarray:
+    """The 4 boundary cubics of each bicubic patch (n, 4, 4, 3) = P[v][u], counter-clockwise in (u, v) so the patch
+    lies on their left, as (4 n, 12) rows of control points."""
+    out = []
+    for g in np.asarray(patches, np.float64).reshape(-1, 4, 4, 3):
+        out += [g[0, :, :], g[:, 3, :], g[3, ::-1, :], g[::-1, 0, :]]
+    return np.stack(out).reshape(-1, 12)
+
+
+def bezier_cube(inflate: float = 0.3) -> np.ndarray:
+    """A closed surface of 6 bicubic patches: the faces of the cube [-1, 1]^3, each a 4 x 4 control grid oriented
+    outward (S_u x S_v along the outward normal), every control point p then scaled by 1 + inflate (sqrt(3)/|p| - 1),
+    which keeps the corners and bulges the faces.  The scaling is a function of the point alone, so neighbouring
+    faces keep sharing their edge curves and the surface stays closed.  Returns (6, 4, 4, 3) = P[face][v][u]."""
+    axes = np.eye(3)
+    faces = [(0, 1, 2), (0, 2, 1), (1, 2, 0), (1, 0, 2), (2, 0, 1), (2, 1, 0)]  # (normal axis, u axis, v axis)
+    s = np.linspace(-1.0, 1.0, 4)
+    out = []
+    for sign in (1.0, -1.0):
+        for n_ax, a_ax, b_ax in faces[::2] if sign > 0 else faces[1::2]:
+            n, a, b = sign * axes[n_ax], axes[a_ax], axes[b_ax]
+            if np.dot(np.cross(a, b), n) < 0:
+                a, b = b, a
+            g = n[None, None, :] + s[None, :, None] * a[None, None, :] + s[:, None, None] * b[None, None, :]
+            out.append(g)
+    P = np.stack(out)
+    r = np.linalg.norm(P, axis=-1, keepdims=True)
+    return P * ((1.0 + inflate * (np.sqrt(3.0) / r - 1.0)))

@@ -357,6 +357,47 @@ struct CubicBezierBoundary
     std::span<std::array<vec3<double>, 4> const> curves;
 };
 
+// The Intersector role for parametric surfaces of bicubic Bezier patches (the reference ships none: its
+// eval_gwnr_parametric_batch_integer / eval_gwnr_parametric_batch, src/antipodal/gwn_parametric.hh:204-284, take
+// any Intersector).  A crossing of the ray p + lambda x0 (lambda >= 0) counts sign(N . x0), N = S_u x S_v, with
+// S(u, v) = sum B_i(v) B_j(u) P[i][j] and each patch given as its 16 control points P[i][j] at index 4 i + j.  The
+// patches are copied to the device.  signed_intersection_count() is the concept member (one GPU round trip per
+// point).
+class CudaBezierPatchIntersector
+{
+public:
+    CudaBezierPatchIntersector(CudaDispatcher& disp, std::span<std::array<vec3<double>, 16> const> patches)
+      : m_disp(&disp)
+    {
+        static_assert(sizeof(std::array<vec3<double>, 16>) == 48 * sizeof(double));
+        check(agwn_patches_create_f64(disp.handle(), reinterpret_cast<double const*>(patches.data()),
+                                      std::int64_t(patches.size()), &m_patches),
+              "agwn_patches_create_f64");
+    }
+    ~CudaBezierPatchIntersector()
+    {
+        if (m_patches)
+            agwn_patches_destroy(m_patches);
+    }
+    CudaBezierPatchIntersector(CudaBezierPatchIntersector const&) = delete;
+    CudaBezierPatchIntersector& operator=(CudaBezierPatchIntersector const&) = delete;
+
+    [[nodiscard]] int signed_intersection_count(vec3<double> p, vec3<double> dir) const
+    {
+        std::int32_t out = 0;
+        double const d[3] = {dir.x, dir.y, dir.z};
+        check(agwn_param_batch_integer_bezier3x3_f64(m_disp->handle(), m_patches, &p.x, 1, &out, d),
+              "signed_intersection_count");
+        return out;
+    }
+
+    [[nodiscard]] agwn_patches* handle() const noexcept { return m_patches; }
+
+private:
+    CudaDispatcher* m_disp;
+    agwn_patches* m_patches = nullptr;
+};
+
 // Learned start depths for the plain GK15 integrator (no reference counterpart): a 12 -> 64 -> 64 -> 16 MLP on
 // the tensor cores, trained on the plain integrator's depths.  Passed as the integrator of the parametric batch
 // function; every evaluated panel is still accepted or refined by the plain error test.
@@ -569,5 +610,50 @@ inline void eval_gwnr_parametric_batch_fractional(cuda::CudaDispatcher& dispatch
                     integrator.n_classes(), cfg.min_depth, cfg.max_depth, cfg.tol, integrator.alpha(), nullptr,
                     nullptr),
                 "eval_gwnr_parametric_batch_fractional");
+}
+// gwn_parametric.hh:210-226 on the GPU with the Bezier-patch intersector.
+inline void eval_gwnr_parametric_batch_integer(cuda::CudaDispatcher& dispatcher,
+                                               cuda::CudaBezierPatchIntersector const& intersector,
+                                               std::span<vec3<double> const> positions, std::span<int> out_counts,
+                                               vec3<double> x0)
+{
+    cuda::detail::same_size(positions.size(), out_counts.size(), "eval_gwnr_parametric_batch_integer");
+    static_assert(sizeof(int) == sizeof(std::int32_t));
+    double const x[3] = {x0.x, x0.y, x0.z};
+    cuda::check(agwn_param_batch_integer_bezier3x3_f64(dispatcher.handle(), intersector.handle(),
+                                                       cuda::detail::raw(positions), std::int64_t(positions.size()),
+                                                       reinterpret_cast<std::int32_t*>(out_counts.data()), x),
+                "eval_gwnr_parametric_batch_integer");
+}
+
+// gwn_parametric.hh:259-284 on the GPU: the fractional term over the cubic Bezier boundary (plain GK15) plus the
+// patches' crossing count, per point.
+inline void eval_gwnr_parametric_batch(cuda::CudaDispatcher& dispatcher,
+                                       cuda::CudaBezierPatchIntersector const& intersector,
+                                       std::span<vec3<double> const> positions, std::span<double> out_wnrs,
+                                       vec3<double> x0, cuda::CubicBezierBoundary const& boundary,
+                                       integrate_config const& cfg = {})
+{
+    eval_gwnr_parametric_batch_fractional(dispatcher, positions, out_wnrs, x0, boundary, cfg);
+    double const x[3] = {x0.x, x0.y, x0.z};
+    cuda::check(agwn_param_add_integer_bezier3x3_f64(dispatcher.handle(), intersector.handle(),
+                                                     cuda::detail::raw(positions), std::int64_t(positions.size()),
+                                                     out_wnrs.data(), x),
+                "eval_gwnr_parametric_batch");
+}
+
+// The same with the learned start-depth proposal as the integrator.
+inline void eval_gwnr_parametric_batch(cuda::CudaDispatcher& dispatcher,
+                                       cuda::CudaBezierPatchIntersector const& intersector,
+                                       std::span<vec3<double> const> positions, std::span<double> out_wnrs,
+                                       vec3<double> x0, cuda::CubicBezierBoundary const& boundary,
+                                       integrate_config const& cfg, cuda::LearnedGK15Proposal const& integrator)
+{
+    eval_gwnr_parametric_batch_fractional(dispatcher, positions, out_wnrs, x0, boundary, cfg, integrator);
+    double const x[3] = {x0.x, x0.y, x0.z};
+    cuda::check(agwn_param_add_integer_bezier3x3_f64(dispatcher.handle(), intersector.handle(),
+                                                     cuda::detail::raw(positions), std::int64_t(positions.size()),
+                                                     out_wnrs.data(), x),
+                "eval_gwnr_parametric_batch");
 }
 } // namespace antipodal

@@ -81,7 +81,7 @@ enum agwn_option
     /* Segments per shared-memory tile of the fractional kernels (32..2048).  Default 512. */
     AGWN_OPT_SEG_TILE = 5,
     /* Mixed mode: a pair whose first-order FP32 error bound exceeds this many radians is evaluated in FP64.
-       Default 3e-8. */
+       Default 6e-8. */
     AGWN_OPT_MIXED_TERM_ERR = 6,
     /* Robust evaluator's fractional term: AGWN_ROBUST_EXACT (default, the reference's FP64 arithmetic) or
        AGWN_ROBUST_MIXED.  int64_grid: FP32 pairs on the exact integer differences under a first-order error
@@ -348,6 +348,26 @@ int agwn_param_panel_log_bezier3_f64(agwn_context* ctx, const double* positions,
 int agwn_param_panel_features_bezier3_f64(agwn_context* ctx, const double* positions, int64_t n, const double* x0,
                                           const double* curves, int64_t n_curves, double tol, const uint32_t* log,
                                           int64_t n_entries, float* features, uint8_t* labels);
+/* ---- parametric integer term: an Intersector over bicubic Bezier patches ---------------------------------------
+ * eval_gwnr_parametric_batch_integer and eval_gwnr_parametric_batch (src/antipodal/gwn_parametric.hh:204-284)
+ * forward the integer term to an Intersector; the reference ships none for parametric surfaces.  This one counts,
+ * for the ray p + lambda x0 (lambda >= 0), every crossing with a patch S(u, v) = sum B_i(v) B_j(u) P[i][j] by
+ * sign(N . x0), N = S_u x S_v: the mesh intersector's rule, and the orientation under which boundary curves that
+ * run counter-clockwise in (u, v) make fractional + integer the winding number.  Roots are found in FP64 by
+ * subdivision with convex-hull culling in the ray's frame and Newton's iteration on 1/32 x 1/32 cells.
+ * control_points: n_patches x 4 x 4 x 3 doubles, P[patch][i = v index][j = u index][xyz] (host or device); the
+ * patches are copied to the device. */
+typedef struct agwn_patches agwn_patches;
+int agwn_patches_create_f64(agwn_context* ctx, const double* control_points, int64_t n_patches, agwn_patches** out);
+int agwn_patches_destroy(agwn_patches* patches);
+/* out_counts[i] = the signed crossing count of query i along x0 (eval_gwnr_parametric_batch_integer). */
+int agwn_param_batch_integer_bezier3x3_f64(agwn_context* ctx, agwn_patches* patches, const double* positions,
+                                           int64_t n, int32_t* out_counts, const double* x0);
+/* out_wnrs[i] += the same count: after agwn_param_batch_fractional_bezier3_f64 into out_wnrs, the full parametric
+ * GWN of eval_gwnr_parametric_batch. */
+int agwn_param_add_integer_bezier3x3_f64(agwn_context* ctx, agwn_patches* patches, const double* positions,
+                                         int64_t n, double* out_wnrs, const double* x0);
+
 /* agwn_param_batch_fractional_bezier3_f64 with start depths proposed by `mlp` in the same call (kept in device
  * scratch): the learned form of eval_gwnr_parametric_batch_fractional. */
 int agwn_param_batch_fractional_learned_bezier3_f64(agwn_context* ctx, const agwn_mlp* mlp, const double* positions,

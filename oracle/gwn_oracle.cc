@@ -1190,3 +1190,211 @@ void orc_mlp_loss_grad(float const* params, float const* feats, uint8_t const* l
     *loss = total * inv_n;
 }
 } // extern "C"
+
+// ---- parametric integer term: bicubic Bezier patches --------------------------------------------------------
+// The Intersector that eval_gwnr_parametric_batch_integer / eval_gwnr_parametric_batch forward to
+// (src/antipodal/gwn_parametric.hh:204-284).  The reference ships none for parametric surfaces (README.md, TODO),
+// so this restates the project's own rule and method (the device's, antipodal_gb300/csrc/patch.cu) in plain FP64:
+// every crossing of the ray p + lambda dir (lambda >= 0) with a patch S(u, v) = sum B_i(v) B_j(u) P[i][j] counts
+// sign((S_u x S_v) . dir).  Roots come from subdivision of the parameter square with convex-hull culling in the ray
+// frame, down to 1/32 x 1/32 cells, then Newton's iteration from each cell's centre; a converged root is counted by
+// the cell that owns it (half-open cells, the square's far edges closed).  Parity of this term is unpinned: no
+// reference implementation exists.
+namespace orc
+{
+// The ray frame: rows e1, e2, e3 = dir / |dir|, right-handed (the helper axis is the unit axis least aligned
+// with dir).
+inline std::array<double, 9> patch_frame(double const* dir)
+{
+    double const nn = std::sqrt(dir[0] * dir[0] + dir[1] * dir[1] + dir[2] * dir[2]);
+    double const z[3] = {dir[0] / nn, dir[1] / nn, dir[2] / nn};
+    int m = 0;
+    for (int k = 1; k < 3; ++k)
+        if (std::fabs(z[k]) < std::fabs(z[m]))
+            m = k;
+    double a[3] = {0, 0, 0};
+    a[m] = 1.0;
+    double x[3] = {a[1] * z[2] - a[2] * z[1], a[2] * z[0] - a[0] * z[2], a[0] * z[1] - a[1] * z[0]};
+    double const xn = std::sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]);
+    for (double& c : x)
+        c /= xn;
+    double const y[3] = {z[1] * x[2] - z[2] * x[1], z[2] * x[0] - z[0] * x[2], z[0] * x[1] - z[1] * x[0]};
+    return {x[0], x[1], x[2], y[0], y[1], y[2], z[0], z[1], z[2]};
+}
+
+// Control values of a cubic over [a, b] by blossoming.
+inline std::array<double, 4> cubic_on(std::array<double, 4> const& c, double a, double b)
+{
+    auto lerp = [](double p, double q, double t) { return p + t * (q - p); };
+    auto blossom = [&](double t1, double t2, double t3)
+    {
+        double const l0 = lerp(c[0], c[1], t1), l1 = lerp(c[1], c[2], t1), l2 = lerp(c[2], c[3], t1);
+        double const m0 = lerp(l0, l1, t2), m1 = lerp(l1, l2, t2);
+        return lerp(m0, m1, t3);
+    };
+    return {blossom(a, a, a), blossom(a, a, b), blossom(a, b, b), blossom(b, b, b)};
+}
+
+struct patch_net
+{
+    double c[16][3]; // [4 iv + iu][x, y across the ray; w along it], relative to the query
+};
+
+inline void patch_eval(patch_net const& n, double u, double v, double (&s)[3], double (&su)[3], double (&sv)[3])
+{
+    auto basis = [](double t, double (&b)[4], double (&db)[4])
+    {
+        double const r = 1.0 - t;
+        b[0] = r * r * r;
+        b[1] = 3.0 * t * r * r;
+        b[2] = 3.0 * t * t * r;
+        b[3] = t * t * t;
+        db[0] = -3.0 * r * r;
+        db[1] = 3.0 * r * r - 6.0 * t * r;
+        db[2] = 6.0 * t * r - 3.0 * t * t;
+        db[3] = 3.0 * t * t;
+    };
+    double bu[4], dbu[4], bv[4], dbv[4];
+    basis(u, bu, dbu);
+    basis(v, bv, dbv);
+    for (int k = 0; k < 3; ++k)
+    {
+        s[k] = su[k] = sv[k] = 0.0;
+        for (int iv = 0; iv < 4; ++iv)
+            for (int iu = 0; iu < 4; ++iu)
+            {
+                double const p = n.c[4 * iv + iu][k];
+                s[k] += bv[iv] * bu[iu] * p;
+                su[k] += bv[iv] * dbu[iu] * p;
+                sv[k] += dbv[iv] * bu[iu] * p;
+            }
+    }
+}
+
+inline int patch_count(patch_net const& n, double margin)
+{
+    constexpr int kLeaf = 5;
+    int sum = 0;
+    struct cell
+    {
+        int level, iu, iv;
+    };
+    std::vector<cell> todo{{0, 0, 0}};
+    while (!todo.empty())
+    {
+        cell const cl = todo.back();
+        todo.pop_back();
+        double const h = std::ldexp(1.0, -cl.level);
+        double const u0 = cl.iu * h, u1 = (cl.iu + 1) * h, v0 = cl.iv * h, v1 = (cl.iv + 1) * h;
+        double lo[3], hi[3];
+        for (int k = 0; k < 3; ++k)
+        {
+            lo[k] = std::numeric_limits<double>::infinity();
+            hi[k] = -lo[k];
+            std::array<double, 4> rows[4];
+            for (int r = 0; r < 4; ++r)
+                rows[r] = cubic_on({n.c[4 * r][k], n.c[4 * r + 1][k], n.c[4 * r + 2][k], n.c[4 * r + 3][k]}, u0, u1);
+            for (int q = 0; q < 4; ++q)
+                for (double x : cubic_on({rows[0][q], rows[1][q], rows[2][q], rows[3][q]}, v0, v1))
+                {
+                    lo[k] = std::min(lo[k], x);
+                    hi[k] = std::max(hi[k], x);
+                }
+        }
+        if (!(lo[0] <= margin && hi[0] >= -margin && lo[1] <= margin && hi[1] >= -margin && hi[2] >= -margin))
+            continue;
+        if (cl.level < kLeaf)
+        {
+            for (int d = 0; d < 4; ++d)
+                todo.push_back({cl.level + 1, 2 * cl.iu + (d & 1), 2 * cl.iv + (d >> 1)});
+            continue;
+        }
+        double u = 0.5 * (u0 + u1), v = 0.5 * (v0 + v1);
+        double s[3], su[3], sv[3];
+        bool converged = false;
+        for (int it = 0; it < 16; ++it)
+        {
+            patch_eval(n, u, v, s, su, sv);
+            double const det = su[0] * sv[1] - sv[0] * su[1];
+            if (!(det != 0.0) || !std::isfinite(det))
+                break;
+            double const du = -(sv[1] * s[0] - sv[0] * s[1]) / det;
+            double const dv = -(su[0] * s[1] - su[1] * s[0]) / det;
+            u += du;
+            v += dv;
+            if (!(std::fabs(u) < 4.0 && std::fabs(v) < 4.0))
+                break;
+            if (std::fabs(du) + std::fabs(dv) <= 1e-15)
+            {
+                converged = true;
+                break;
+            }
+        }
+        if (!converged)
+            continue;
+        patch_eval(n, u, v, s, su, sv);
+        bool const in_u = u >= u0 && (u < u1 || (u1 == 1.0 && u <= 1.0));
+        bool const in_v = v >= v0 && (v < v1 || (v1 == 1.0 && v <= 1.0));
+        if (!in_u || !in_v || !(std::fabs(s[0]) + std::fabs(s[1]) <= margin) || !(s[2] >= 0.0))
+            continue;
+        double const det = su[0] * sv[1] - sv[0] * su[1];
+        sum += det > 0.0 ? 1 : (det < 0.0 ? -1 : 0);
+    }
+    return sum;
+}
+} // namespace orc
+
+extern "C"
+{
+// Signed crossing counts of the rays pos[i] + lambda dir with the bicubic patches ctrl ([n_patches][4][4][3], row
+// index v, column index u).
+void orc_patch_count_bezier3x3_f64(double const* pos, int64_t n, double const* dir, double const* ctrl,
+                                   int64_t n_patches, int32_t* out_counts, int threads)
+{
+    std::array<double, 9> const f = orc::patch_frame(dir);
+    std::vector<double> net(size_t(48) * size_t(n_patches));
+    std::vector<double> box(size_t(6) * size_t(n_patches));
+    for (int64_t k = 0; k < n_patches; ++k)
+    {
+        double b[6] = {INFINITY, -INFINITY, INFINITY, -INFINITY, -INFINITY, 0.0};
+        for (int j = 0; j < 16; ++j)
+            for (int r = 0; r < 3; ++r)
+            {
+                double const* p = ctrl + 48 * k + 3 * j;
+                double const x = f[3 * r] * p[0] + f[3 * r + 1] * p[1] + f[3 * r + 2] * p[2];
+                net[48 * k + 3 * j + r] = x;
+                b[5] = std::max(b[5], std::fabs(x));
+                if (r < 2)
+                {
+                    b[2 * r] = std::min(b[2 * r], x);
+                    b[2 * r + 1] = std::max(b[2 * r + 1], x);
+                }
+                else
+                    b[4] = std::max(b[4], x);
+            }
+        std::copy(b, b + 6, box.begin() + 6 * k);
+    }
+#pragma omp parallel for schedule(dynamic, 16) num_threads(nthreads(threads))
+    for (int64_t i = 0; i < n; ++i)
+    {
+        double q[3];
+        for (int r = 0; r < 3; ++r)
+            q[r] = f[3 * r] * pos[3 * i] + f[3 * r + 1] * pos[3 * i + 1] + f[3 * r + 2] * pos[3 * i + 2];
+        double const qs = std::max(std::max(std::fabs(q[0]), std::fabs(q[1])), std::fabs(q[2]));
+        int sum = 0;
+        for (int64_t k = 0; k < n_patches; ++k)
+        {
+            double const* b = box.data() + 6 * k;
+            double const m = 1e-9 * (qs + b[5]);
+            if (!(b[0] - m <= q[0] && b[1] + m >= q[0] && b[2] - m <= q[1] && b[3] + m >= q[1] && b[4] + m >= q[2]))
+                continue;
+            orc::patch_net pn;
+            for (int j = 0; j < 16; ++j)
+                for (int r = 0; r < 3; ++r)
+                    pn.c[j][r] = net[48 * k + 3 * j + r] - q[r];
+            sum += orc::patch_count(pn, m);
+        }
+        out_counts[i] = sum;
+    }
+}
+} // extern "C"
