@@ -644,7 +644,7 @@ def eval_gwnr_parametric_batch_fractional(dispatcher: CudaDispatcher, positions,
 class CudaBezierPatchIntersector:
     """The Intersector role for parametric surfaces made of bicubic Bezier patches: the integer term that
     eval_gwnr_parametric_batch_integer / eval_gwnr_parametric_batch forward to (gwn_parametric.hh:204-284; the
-    reference ships no parametric intersector).  Each crossing of the ray p + lambda x0 (lambda >= 0) counts
+    reference ships no parametric intersector).  Each crossing of the ray p + lambda x0 (lambda > 0) counts
     sign(N . x0) with N = S_u x S_v, the orientation under which boundary curves running counter-clockwise in (u, v)
     (synth.bezier_patch_boundary) make fractional + integer the winding number.
 
@@ -678,15 +678,25 @@ class CudaBezierPatchIntersector:
 
 
 def eval_gwnr_parametric_batch_integer(dispatcher: CudaDispatcher, intersector: CudaBezierPatchIntersector,
-                                       positions, out_counts, x0):
-    """gwn_parametric.hh:210-226: out_counts[i] = intersector.signed_intersection_count(positions[i], x0)."""
+                                       positions, out_counts, x0, out_degenerate=None):
+    """gwn_parametric.hh:210-226: out_counts[i] = intersector.signed_intersection_count(positions[i], x0).  With
+    ``out_degenerate`` (int32, one per query): how many of the query's decisions were degenerate (the ray on a
+    patch cell's boundary image, or the query on the surface, within 2^-42 of the coordinates' scale)."""
     p = _View(positions, np.float64, 3, "positions")
     o = _View(out_counts, np.int32, None, "out_counts", writable=True)
     if p.n != o.n:
         raise ValueError("positions and out_counts must have the same size")
     _, xp = x = _vec3(x0, np.float64)
-    _check(library().agwn_param_batch_integer_bezier3x3_f64(dispatcher.handle, intersector.handle, p.ptr, p.n, o.ptr,
-                                                            xp), "eval_gwnr_parametric_batch_integer")
+    if out_degenerate is None:
+        _check(library().agwn_param_batch_integer_bezier3x3_f64(dispatcher.handle, intersector.handle, p.ptr, p.n,
+                                                                o.ptr, xp), "eval_gwnr_parametric_batch_integer")
+    else:
+        d = _View(out_degenerate, np.int32, None, "out_degenerate", writable=True)
+        if d.n != p.n:
+            raise ValueError("out_degenerate needs one entry per query")
+        _check(library().agwn_param_batch_integer_degenerate_bezier3x3_f64(dispatcher.handle, intersector.handle,
+                                                                           p.ptr, p.n, o.ptr, d.ptr, xp),
+               "eval_gwnr_parametric_batch_integer")
     del x
 
 

@@ -85,6 +85,7 @@ SIGNATURES = {
     "agwn_patches_create_f64": (_I, [_P, _P, _I64, _PP]),
     "agwn_patches_destroy": (_I, [_P]),
     "agwn_param_batch_integer_bezier3x3_f64": (_I, [_P, _P, _P, _I64, _P, _P]),
+    "agwn_param_batch_integer_degenerate_bezier3x3_f64": (_I, [_P, _P, _P, _I64, _P, _P, _P]),
     "agwn_param_add_integer_bezier3x3_f64": (_I, [_P, _P, _P, _I64, _P, _P]),
     "agwn_param_panel_log_bezier3_f64": (_I, [_P, _P, _I64, _P, _P, _I64, _I, _I, _D, _P, _I64, _P]),
     "agwn_param_panel_features_bezier3_f64": (_I, [_P, _P, _I64, _P, _P, _I64, _D, _P, _I64, _P, _P]),

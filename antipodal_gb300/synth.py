@@ -262,11 +262,12 @@ def two_tori(seed: int = 0, n_tris: int = 1_000_000, n_holes: int = 20, n_querie
 
 
 def bezier_patches(seed: int = 0, n_patches: int = 256, n_queries: int = 1_000_000, near_frac: float = 0.3,
-                   near_dist: float = 1e-3):
+                   near_dist: float = 1e-3, return_patches: bool = False):
     """``n_patches`` bicubic Bezier patches with control points ~N(0,1); each patch contributes its 4 boundary
     cubics, oriented counter-clockwise in (u, v) so the patch lies on their left.  ``near_frac`` of the queries
     lie within ``near_dist`` of a boundary curve, the rest are uniform in the control points' bounding box.
-    Returns (curves (4*n_patches, 12), queries (n,3), x0)."""
+    Returns (curves (4*n_patches, 12), queries (n,3), x0), and with ``return_patches`` also the patches
+    (n_patches, 4, 4, 3) = P[patch][v][u]."""
     rng = np.random.default_rng(seed)
     P = rng.standard_normal((n_patches, 4, 4, 3))
     curves = []
@@ -291,6 +292,8 @@ def bezier_patches(seed: int = 0, n_patches: int = 256, n_queries: int = 1_000_0
     q = np.concatenate([q_far, pts + off])
     q = q[rng.permutation(len(q))]
     x0 = random_unit(rng)
+    if return_patches:
+        return curves, q, x0, P
     return curves, q, x0
 
 

@@ -690,7 +690,7 @@ def run_param(args, ag, torch, stream, disp, timed):
     as measured and extrapolated per query."""
     from antipodal_gb300 import synth
     n_q = max(64, int(1_000_000 * args.scale))
-    curves, q, x0 = synth.bezier_patches(seed=0, n_patches=args.patches, n_queries=n_q)
+    curves, q, x0, patches = synth.bezier_patches(seed=0, n_patches=args.patches, n_queries=n_q, return_patches=True)
     cfg = ag.IntegrateConfig(0, 10, 1e-10)
     Q, Cn = len(q), len(curves)
     # the network: trained on labels of the plain integrator (the shallowest accepted depth per pair) on other
@@ -715,6 +715,14 @@ def run_param(args, ag, torch, stream, disp, timed):
     ag.eval_gwnr_parametric_batch_fractional(disp, qd, out, x0, cd, cfg, integrator=net, nodes_per_query=nodes_c)
     ms = timed(args.steps, lambda: ag.eval_gwnr_parametric_batch_fractional(disp, qd, out, x0, cd, cfg,
                                                                             integrator=net))
+    # the integer term over the patches themselves (the Bezier-patch intersector): the full parametric GWN is the
+    # chosen fractional term plus these counts
+    isect = ag.CudaBezierPatchIntersector(disp, patches)
+    cnt = torch.empty(Q, dtype=torch.int32, device="cuda")
+    ag.eval_gwnr_parametric_batch_integer(disp, isect, qd, cnt, x0)
+    ms_int = timed(args.steps, lambda: ag.eval_gwnr_parametric_batch_integer(disp, isect, qd, cnt, x0))
+    n_cross = int(cnt.abs().sum().item())
+    isect.close()
     # the sample: the first Qs queries (the generator shuffles them, so they are a seeded random sample)
     Qs = max(32, min(Q, int(round(args.plain_scale * Q))))
     qs = qd[:Qs].contiguous()
@@ -751,6 +759,10 @@ def run_param(args, ag, torch, stream, disp, timed):
                        "queries": Q, "pairs": Q * Cn, "sample_queries": Qs},
             "chosen": {"form": "learned start depths + double-float panels", "queries": Q,
                        "panels_per_pair": int(nodes_c.sum().item()) / (Q * Cn)},
+            "integer_term": {"form": "Bezier-patch intersector (winding numbers of cell boundaries), 256 patches",
+                             "ms_per_step": ms_int, "value": Q / (ms_int * 1e-3), "unit": "queries/s",
+                             "abs_counts_per_query": n_cross / Q,
+                             "full_gwn_ms_per_step": ms + ms_int},
             "plain": {"value": plain_rate, "ms_per_step_sample": ms_plain,
                       "ms_per_step_extrapolated_full": ms_plain * Q / Qs,
                       "panels_per_pair": panels_p / (Qs * Cn),

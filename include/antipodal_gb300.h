@@ -353,8 +353,12 @@ int agwn_param_panel_features_bezier3_f64(agwn_context* ctx, const double* posit
  * forward the integer term to an Intersector; the reference ships none for parametric surfaces.  This one counts,
  * for the ray p + lambda x0 (lambda >= 0), every crossing with a patch S(u, v) = sum B_i(v) B_j(u) P[i][j] by
  * sign(N . x0), N = S_u x S_v: the mesh intersector's rule, and the orientation under which boundary curves that
- * run counter-clockwise in (u, v) make fractional + integer the winding number.  Roots are found in FP64 by
- * subdivision with convex-hull culling in the ray's frame and Newton's iteration on 1/32 x 1/32 cells.
+ * run counter-clockwise in (u, v) make fractional + integer the winding number.  The count over a parameter cell
+ * that lies in front of the query is the topological degree of the patch's projection at the ray: the winding
+ * number of the cell boundary's image (4 cubics) about it.  Cells are split while their depth range holds 0 and
+ * their control box holds the ray; every box test keeps a margin above its rounding (float first, FP64 where float
+ * cannot decide), so the count is exact for the exact patch except in the degenerate cases: the ray within 2^-42
+ * of the coordinates' scale of a cell boundary's image, or the query that close to the surface.
  * control_points: n_patches x 4 x 4 x 3 doubles, P[patch][i = v index][j = u index][xyz] (host or device); the
  * patches are copied to the device. */
 typedef struct agwn_patches agwn_patches;
@@ -363,6 +367,11 @@ int agwn_patches_destroy(agwn_patches* patches);
 /* out_counts[i] = the signed crossing count of query i along x0 (eval_gwnr_parametric_batch_integer). */
 int agwn_param_batch_integer_bezier3x3_f64(agwn_context* ctx, agwn_patches* patches, const double* positions,
                                            int64_t n, int32_t* out_counts, const double* x0);
+/* The same counts, and out_degenerate[i] = how many of query i's decisions were degenerate (decided by a fixed
+ * rule: a cell's winding taken as the chords give it, a cell on the surface counted when its mean depth is >= 0). */
+int agwn_param_batch_integer_degenerate_bezier3x3_f64(agwn_context* ctx, agwn_patches* patches,
+                                                      const double* positions, int64_t n, int32_t* out_counts,
+                                                      int32_t* out_degenerate, const double* x0);
 /* out_wnrs[i] += the same count: after agwn_param_batch_fractional_bezier3_f64 into out_wnrs, the full parametric
  * GWN of eval_gwnr_parametric_batch. */
 int agwn_param_add_integer_bezier3x3_f64(agwn_context* ctx, agwn_patches* patches, const double* positions,

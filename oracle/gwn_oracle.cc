@@ -1194,12 +1194,21 @@ void orc_mlp_loss_grad(float const* params, float const* feats, uint8_t const* l
 // ---- parametric integer term: bicubic Bezier patches --------------------------------------------------------
 // The Intersector that eval_gwnr_parametric_batch_integer / eval_gwnr_parametric_batch forward to
 // (src/antipodal/gwn_parametric.hh:204-284).  The reference ships none for parametric surfaces (README.md, TODO),
-// so this restates the project's own rule and method (the device's, antipodal_gb300/csrc/patch.cu) in plain FP64:
-// every crossing of the ray p + lambda dir (lambda >= 0) with a patch S(u, v) = sum B_i(v) B_j(u) P[i][j] counts
-// sign((S_u x S_v) . dir).  Roots come from subdivision of the parameter square with convex-hull culling in the ray
-// frame, down to 1/32 x 1/32 cells, then Newton's iteration from each cell's centre; a converged root is counted by
-// the cell that owns it (half-open cells, the square's far edges closed).  Parity of this term is unpinned: no
-// reference implementation exists.
+// so this restates the project's own rule (the device's, antipodal_gb300/csrc/patch.cu) in plain FP64: every
+// crossing of the ray p + lambda dir (lambda > 0) with a patch S(u, v) = sum B_i(v) B_j(u) P[i][j] counts
+// sign((S_u x S_v) . dir).
+//
+// Method: in a right-handed frame whose third axis is dir, the patch relative to p is a map F(u, v) = (x, y) of the
+// parameter square with a depth w.  The signed crossings inside a parameter cell whose depth is positive
+// throughout are the topological degree of F over the cell at the origin, which is the winding number of the image
+// of the cell's boundary (4 cubics) about the origin.  Cells are split in four while their control net's box holds
+// the origin and their depth range holds 0; a boundary cubic is split in two while its control points' box holds
+// the origin, and a piece whose box does not contributes the crossing of its chord with the positive x axis.  Every
+// box test keeps a margin of 2^-42 of the coordinates' scale, far above the rounding of the blossoms, so each
+// decision holds for the exact map: the count is exact unless the ray passes within that margin of a cell's
+// boundary image or the query lies within it of the surface (the degenerate cases, counted in `degenerate`).
+// This is written as plain recursion; the device walks the same trees without a stack.
+// Parity of this term is unpinned: no reference implementation exists.
 namespace orc
 {
 // The ray frame: rows e1, e2, e3 = dir / |dir|, right-handed (the helper axis is the unit axis least aligned
@@ -1222,7 +1231,9 @@ inline std::array<double, 9> patch_frame(double const* dir)
     return {x[0], x[1], x[2], y[0], y[1], y[2], z[0], z[1], z[2]};
 }
 
-// Control values of a cubic over [a, b] by blossoming.
+// Control values of the cubic with control values c over [a, b], by blossoming: B(a,a,a), B(a,a,b), B(a,b,b),
+// B(b,b,b).  B(t,t,t) is computed by the same steps whichever end t is, so neighbouring pieces share their
+// end points exactly.
 inline std::array<double, 4> cubic_on(std::array<double, 4> const& c, double a, double b)
 {
     auto lerp = [](double p, double q, double t) { return p + t * (q - p); };
@@ -1235,145 +1246,114 @@ inline std::array<double, 4> cubic_on(std::array<double, 4> const& c, double a, 
     return {blossom(a, a, a), blossom(a, a, b), blossom(a, b, b), blossom(b, b, b)};
 }
 
-struct patch_net
+struct patch_job
 {
     double c[16][3]; // [4 iv + iu][x, y across the ray; w along it], relative to the query
+    double margin;
+    int degenerate = 0;
 };
 
-inline void patch_eval(patch_net const& n, double u, double v, double (&s)[3], double (&su)[3], double (&sv)[3])
+// The crossing of the chord a -> b with the positive x axis: +1 upwards with the origin on its left, -1 downwards
+// with the origin on its right (half-open in y, so chords that meet on the axis count once).
+inline int chord_crossing(double ax, double ay, double bx, double by)
 {
-    auto basis = [](double t, double (&b)[4], double (&db)[4])
-    {
-        double const r = 1.0 - t;
-        b[0] = r * r * r;
-        b[1] = 3.0 * t * r * r;
-        b[2] = 3.0 * t * t * r;
-        b[3] = t * t * t;
-        db[0] = -3.0 * r * r;
-        db[1] = 3.0 * r * r - 6.0 * t * r;
-        db[2] = 6.0 * t * r - 3.0 * t * t;
-        db[3] = 3.0 * t * t;
-    };
-    double bu[4], dbu[4], bv[4], dbv[4];
-    basis(u, bu, dbu);
-    basis(v, bv, dbv);
-    for (int k = 0; k < 3; ++k)
-    {
-        s[k] = su[k] = sv[k] = 0.0;
-        for (int iv = 0; iv < 4; ++iv)
-            for (int iu = 0; iu < 4; ++iu)
-            {
-                double const p = n.c[4 * iv + iu][k];
-                s[k] += bv[iv] * bu[iu] * p;
-                su[k] += bv[iv] * dbu[iu] * p;
-                sv[k] += dbv[iv] * bu[iu] * p;
-            }
-    }
+    double const cross = ax * by - ay * bx;
+    if (ay <= 0.0)
+        return (by > 0.0 && cross > 0.0) ? 1 : 0;
+    return (by <= 0.0 && cross < 0.0) ? -1 : 0;
 }
 
-inline int patch_count(patch_net const& n, double margin)
+// Winding number about the origin of the cubic (x, y) over [t0, t1], with its end points given.
+int cubic_winding(patch_job& job, std::array<double, 4> const& x, std::array<double, 4> const& y, double t0,
+                  double t1, int level, double ax, double ay, double bx, double by)
 {
-    constexpr int kLeaf = 5;
-    int sum = 0;
-    struct cell
+    std::array<double, 4> const px = cubic_on(x, t0, t1), py = cubic_on(y, t0, t1);
+    double const m = job.margin;
+    auto [xlo, xhi] = std::minmax({px[0], px[1], px[2], px[3]});
+    auto [ylo, yhi] = std::minmax({py[0], py[1], py[2], py[3]});
+    if (!(xlo > m || xhi < -m || ylo > m || yhi < -m))
     {
-        int level, iu, iv;
-    };
-    std::vector<cell> todo{{0, 0, 0}};
-    while (!todo.empty())
-    {
-        cell const cl = todo.back();
-        todo.pop_back();
-        double const h = std::ldexp(1.0, -cl.level);
-        double const u0 = cl.iu * h, u1 = (cl.iu + 1) * h, v0 = cl.iv * h, v1 = (cl.iv + 1) * h;
-        double lo[3], hi[3];
-        for (int k = 0; k < 3; ++k)
+        if (level < 50 && std::max(xhi - xlo, yhi - ylo) >= 4.0 * m)
         {
-            lo[k] = std::numeric_limits<double>::infinity();
-            hi[k] = -lo[k];
-            std::array<double, 4> rows[4];
-            for (int r = 0; r < 4; ++r)
-                rows[r] = cubic_on({n.c[4 * r][k], n.c[4 * r + 1][k], n.c[4 * r + 2][k], n.c[4 * r + 3][k]}, u0, u1);
-            for (int q = 0; q < 4; ++q)
-                for (double x : cubic_on({rows[0][q], rows[1][q], rows[2][q], rows[3][q]}, v0, v1))
-                {
-                    lo[k] = std::min(lo[k], x);
-                    hi[k] = std::max(hi[k], x);
-                }
+            double const tm = 0.5 * (t0 + t1);
+            std::array<double, 4> const mx = cubic_on(x, tm, tm), my = cubic_on(y, tm, tm);
+            return cubic_winding(job, x, y, t0, tm, level + 1, ax, ay, mx[0], my[0]) +
+                   cubic_winding(job, x, y, tm, t1, level + 1, mx[0], my[0], bx, by);
         }
-        if (!(lo[0] <= margin && hi[0] >= -margin && lo[1] <= margin && hi[1] >= -margin && hi[2] >= -margin))
-            continue;
-        if (cl.level < kLeaf)
-        {
-            for (int d = 0; d < 4; ++d)
-                todo.push_back({cl.level + 1, 2 * cl.iu + (d & 1), 2 * cl.iv + (d >> 1)});
-            continue;
-        }
-        double u = 0.5 * (u0 + u1), v = 0.5 * (v0 + v1);
-        double s[3], su[3], sv[3];
-        bool converged = false;
-        for (int it = 0; it < 16; ++it)
-        {
-            patch_eval(n, u, v, s, su, sv);
-            double const det = su[0] * sv[1] - sv[0] * su[1];
-            if (!(det != 0.0) || !std::isfinite(det))
-                break;
-            double const du = -(sv[1] * s[0] - sv[0] * s[1]) / det;
-            double const dv = -(su[0] * s[1] - su[1] * s[0]) / det;
-            u += du;
-            v += dv;
-            if (!(std::fabs(u) < 4.0 && std::fabs(v) < 4.0))
-                break;
-            if (std::fabs(du) + std::fabs(dv) <= 1e-15)
-            {
-                converged = true;
-                break;
-            }
-        }
-        if (!converged)
-            continue;
-        patch_eval(n, u, v, s, su, sv);
-        bool const in_u = u >= u0 && (u < u1 || (u1 == 1.0 && u <= 1.0));
-        bool const in_v = v >= v0 && (v < v1 || (v1 == 1.0 && v <= 1.0));
-        if (!in_u || !in_v || !(std::fabs(s[0]) + std::fabs(s[1]) <= margin) || !(s[2] >= 0.0))
-            continue;
-        double const det = su[0] * sv[1] - sv[0] * su[1];
-        sum += det > 0.0 ? 1 : (det < 0.0 ? -1 : 0);
+        ++job.degenerate; // the curve passes within the margin of the origin
     }
-    return sum;
+    return chord_crossing(ax, ay, bx, by);
+}
+
+// Winding number about the origin of a cell net's boundary, counter-clockwise in (u, v).
+int net_winding(patch_job& job, double const (&x)[16], double const (&y)[16])
+{
+    static constexpr int kEdge[4][4] = {{0, 1, 2, 3}, {3, 7, 11, 15}, {15, 14, 13, 12}, {12, 8, 4, 0}};
+    int w = 0;
+    for (auto const& e : kEdge)
+    {
+        std::array<double, 4> const ex = {x[e[0]], x[e[1]], x[e[2]], x[e[3]]};
+        std::array<double, 4> const ey = {y[e[0]], y[e[1]], y[e[2]], y[e[3]]};
+        w += cubic_winding(job, ex, ey, 0.0, 1.0, 0, ex[0], ey[0], ex[3], ey[3]);
+    }
+    return w;
+}
+
+// Signed crossings in front of the query within the cell [u0, u0 + h] x [v0, v0 + h].
+int cell_crossings(patch_job& job, double u0, double v0, double h, int level)
+{
+    double net[3][16];
+    for (int k = 0; k < 3; ++k)
+    {
+        std::array<double, 4> rows[4];
+        for (int r = 0; r < 4; ++r)
+            rows[r] = cubic_on({job.c[4 * r][k], job.c[4 * r + 1][k], job.c[4 * r + 2][k], job.c[4 * r + 3][k]}, u0,
+                               u0 + h);
+        for (int q = 0; q < 4; ++q)
+        {
+            std::array<double, 4> const col = cubic_on({rows[0][q], rows[1][q], rows[2][q], rows[3][q]}, v0, v0 + h);
+            for (int r = 0; r < 4; ++r)
+                net[k][4 * r + q] = col[r];
+        }
+    }
+    double const m = job.margin;
+    auto [xlo, xhi] = std::minmax_element(net[0], net[0] + 16);
+    auto [ylo, yhi] = std::minmax_element(net[1], net[1] + 16);
+    auto [wlo, whi] = std::minmax_element(net[2], net[2] + 16);
+    if (*xlo > m || *xhi < -m || *ylo > m || *yhi < -m || *whi < -m)
+        return 0; // the ray misses the cell, or the cell lies behind the query
+    if (*wlo >= m)
+        return net_winding(job, net[0], net[1]); // in front throughout: the degree over the cell
+    if (level < 30 && *whi - *wlo >= 4.0 * m)
+    {
+        double const g = 0.5 * h;
+        return cell_crossings(job, u0, v0, g, level + 1) + cell_crossings(job, u0 + g, v0, g, level + 1) +
+               cell_crossings(job, u0, v0 + g, g, level + 1) + cell_crossings(job, u0 + g, v0 + g, g, level + 1);
+    }
+    ++job.degenerate; // the query lies within the margin of the surface
+    return *wlo + *whi >= 0.0 ? net_winding(job, net[0], net[1]) : 0;
 }
 } // namespace orc
 
 extern "C"
 {
 // Signed crossing counts of the rays pos[i] + lambda dir with the bicubic patches ctrl ([n_patches][4][4][3], row
-// index v, column index u).
+// index v, column index u); degenerate (nullable): per query, the number of unresolved decisions (see above).
 void orc_patch_count_bezier3x3_f64(double const* pos, int64_t n, double const* dir, double const* ctrl,
-                                   int64_t n_patches, int32_t* out_counts, int threads)
+                                   int64_t n_patches, int32_t* out_counts, int32_t* degenerate, int threads)
 {
     std::array<double, 9> const f = orc::patch_frame(dir);
     std::vector<double> net(size_t(48) * size_t(n_patches));
-    std::vector<double> box(size_t(6) * size_t(n_patches));
+    std::vector<double> scale(size_t(n_patches), 0.0);
     for (int64_t k = 0; k < n_patches; ++k)
-    {
-        double b[6] = {INFINITY, -INFINITY, INFINITY, -INFINITY, -INFINITY, 0.0};
         for (int j = 0; j < 16; ++j)
             for (int r = 0; r < 3; ++r)
             {
                 double const* p = ctrl + 48 * k + 3 * j;
                 double const x = f[3 * r] * p[0] + f[3 * r + 1] * p[1] + f[3 * r + 2] * p[2];
                 net[48 * k + 3 * j + r] = x;
-                b[5] = std::max(b[5], std::fabs(x));
-                if (r < 2)
-                {
-                    b[2 * r] = std::min(b[2 * r], x);
-                    b[2 * r + 1] = std::max(b[2 * r + 1], x);
-                }
-                else
-                    b[4] = std::max(b[4], x);
+                scale[k] = std::max(scale[k], std::fabs(x));
             }
-        std::copy(b, b + 6, box.begin() + 6 * k);
-    }
 #pragma omp parallel for schedule(dynamic, 16) num_threads(nthreads(threads))
     for (int64_t i = 0; i < n; ++i)
     {
@@ -1381,20 +1361,20 @@ void orc_patch_count_bezier3x3_f64(double const* pos, int64_t n, double const* d
         for (int r = 0; r < 3; ++r)
             q[r] = f[3 * r] * pos[3 * i] + f[3 * r + 1] * pos[3 * i + 1] + f[3 * r + 2] * pos[3 * i + 2];
         double const qs = std::max(std::max(std::fabs(q[0]), std::fabs(q[1])), std::fabs(q[2]));
-        int sum = 0;
+        int sum = 0, deg = 0;
         for (int64_t k = 0; k < n_patches; ++k)
         {
-            double const* b = box.data() + 6 * k;
-            double const m = 1e-9 * (qs + b[5]);
-            if (!(b[0] - m <= q[0] && b[1] + m >= q[0] && b[2] - m <= q[1] && b[3] + m >= q[1] && b[4] + m >= q[2]))
-                continue;
-            orc::patch_net pn;
+            orc::patch_job job;
             for (int j = 0; j < 16; ++j)
                 for (int r = 0; r < 3; ++r)
-                    pn.c[j][r] = net[48 * k + 3 * j + r] - q[r];
-            sum += orc::patch_count(pn, m);
+                    job.c[j][r] = net[48 * k + 3 * j + r] - q[r];
+            job.margin = std::ldexp(qs + scale[k], -42);
+            sum += orc::cell_crossings(job, 0.0, 0.0, 1.0, 0);
+            deg += job.degenerate;
         }
         out_counts[i] = sum;
+        if (degenerate)
+            degenerate[i] = deg;
     }
 }
 } // extern "C"

@@ -86,7 +86,7 @@ class Oracle:
         self._param = self._fn("param_frac_bezier3_f64", None, _P, _I64, _P, _P, _P, _I64, _I, _I, _D, _P, _P, _I)
         self._gk15 = self._fn("gk15_known", _D, _I, _D, _D, _I, _I, _D, C.POINTER(_D), C.POINTER(_I))
         if not self.reference:
-            self._patch = self._fn("patch_count_bezier3x3_f64", None, _P, _I64, _P, _P, _I64, _P, _I)
+            self._patch = self._fn("patch_count_bezier3x3_f64", None, _P, _I64, _P, _P, _I64, _P, _P, _I)
         if not self.reference:
             self._feat = self._fn("param_features_bezier3", None, _P, _I64, _P, _P, _I64, _D, _P)
             self._mlp_logits = self._fn("mlp_logits", None, _P, _P, _I64, _P)
@@ -182,13 +182,16 @@ class Oracle:
         return w
 
     # -- parametric path ---------------------------------------------------------------------------------------
-    def patch_count_bezier3x3(self, pos, x0, patches, threads=0):
-        """Signed crossing counts of the rays pos + lambda x0 with bicubic Bezier patches (n, 4, 4, 3)."""
+    def patch_count_bezier3x3(self, pos, x0, patches, threads=0, degenerate=False):
+        """Signed crossing counts of the rays pos + lambda x0 with bicubic Bezier patches (n, 4, 4, 3); with
+        ``degenerate`` also, per query, how many decisions fell within the margin (ray on a cell edge's image,
+        query on the surface)."""
         pos, x0 = _c(pos, np.float64).reshape(-1, 3), _c(x0, np.float64)
         ctrl = _c(patches, np.float64).reshape(-1, 48)
         out = np.empty(len(pos), np.int32)
-        self._patch(_ptr(pos), len(pos), _ptr(x0), _ptr(ctrl), len(ctrl), _ptr(out), threads)
-        return out
+        deg = np.empty(len(pos), np.int32)
+        self._patch(_ptr(pos), len(pos), _ptr(x0), _ptr(ctrl), len(ctrl), _ptr(out), _ptr(deg), threads)
+        return (out, deg) if degenerate else out
 
     def param_frac_bezier3(self, pos, x0, ctrl, min_depth=0, max_depth=10, tol=1e-6, threads=0, stats=False):
         pos, x0, ctrl = _c(pos, np.float64), _c(x0, np.float64), _c(ctrl, np.float64).reshape(-1, 12)

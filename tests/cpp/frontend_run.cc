@@ -1,9 +1,10 @@
 // Runs the C++ front end (include/antipodal/cuda/gwn_cuda.hh) the way a reference user would: the +Y-open unit
 // cube of the reference tests, a 12^3 grid of queries, eval_gwnr_mesh_batch{,_fractional,_integer} through
 // CudaDispatcher / CudaIntersector in both precisions, eval_gwnr_mesh_batch_robust through CudaRobustMeshGwn
-// (exact_float), and eval_gwnr_parametric_batch_fractional over the open cube's boundary as straight cubic Bezier
-// curves (tol 1e-6).  Prints one line per query:
-//   x y z full_exact full_mixed frac_exact count robust param_frac
+// (exact_float), eval_gwnr_parametric_batch_fractional over the open cube's boundary as straight cubic Bezier
+// curves (tol 1e-6), and eval_gwnr_parametric_batch{_integer,} with the open cube's five faces as flat bicubic
+// patches (CudaBezierPatchIntersector).  Prints one line per query:
+//   x y z full_exact full_mixed frac_exact count robust param_frac patch_count param_full
 // or "error <status> <message>" when the library throws (e.g. no GPU).
 #include <antipodal/math/common.hh>
 #include <antipodal/cuda/gwn_cuda.hh>
@@ -58,9 +59,29 @@ int main()
         eval_gwnr_parametric_batch_fractional(disp, P, std::span<double>{param}, x0,
                                               cuda::CubicBezierBoundary{std::span<std::array<dvec3, 4> const>{curves}},
                                               cfg);
+        // each face as a flat bicubic patch: P[i][j] = a + (j/3)(b - a) + (i/3)(c - a) for the face's first triangle
+        // (a, b, c), so that S_u x S_v is that triangle's normal
+        std::vector<std::array<dvec3, 16>> patches;
+        for (size_t f = 0; f < idx.size() / 6; ++f)
+        {
+            dvec3 const a = verts[idx[6 * f]], b = verts[idx[6 * f + 1]], c = verts[idx[6 * f + 2]];
+            std::array<dvec3, 16> g{};
+            for (int i = 0; i < 4; ++i)
+                for (int j = 0; j < 4; ++j)
+                    g[4 * i + j] = dvec3{a.x + j * (b.x - a.x) / 3 + i * (c.x - a.x) / 3,
+                                         a.y + j * (b.y - a.y) / 3 + i * (c.y - a.y) / 3,
+                                         a.z + j * (b.z - a.z) / 3 + i * (c.z - a.z) / 3};
+            patches.push_back(g);
+        }
+        cuda::CudaBezierPatchIntersector const pint{disp, std::span<std::array<dvec3, 16> const>{patches}};
+        std::vector<int> pcount(pts.size());
+        std::vector<double> pfull(pts.size());
+        eval_gwnr_parametric_batch_integer(disp, pint, P, std::span<int>{pcount}, x0);
+        eval_gwnr_parametric_batch(disp, pint, P, std::span<double>{pfull}, x0,
+                                   cuda::CubicBezierBoundary{std::span<std::array<dvec3, 4> const>{curves}}, cfg);
         for (size_t q = 0; q < pts.size(); ++q)
-            std::printf("%.17g %.17g %.17g %.17g %.17g %.17g %d %.17g %.17g\n", pts[q].x, pts[q].y, pts[q].z, exact[q],
-                        mixed[q], frac[q], counts[q], robust[q], param[q]);
+            std::printf("%.17g %.17g %.17g %.17g %.17g %.17g %d %.17g %.17g %d %.17g\n", pts[q].x, pts[q].y, pts[q].z,
+                        exact[q], mixed[q], frac[q], counts[q], robust[q], param[q], pcount[q], pfull[q]);
     }
     catch (cuda::Error const& e)
     {

@@ -116,6 +116,12 @@ void run(cuda::CudaDispatcher& d, cuda::CudaIntersector<double> const& i, std::v
     cuda::LearnedGK15Proposal net{d};
     eval_gwnr_parametric_batch_fractional(d, std::span<dvec3 const>{p}, std::span<double>{o}, x0, cb,
                                           integrate_config{}, net);
+    std::vector<std::array<dvec3, 16>> pats;
+    cuda::CudaBezierPatchIntersector const pint{d, std::span<std::array<dvec3, 16> const>{pats}};
+    eval_gwnr_parametric_batch_integer(d, pint, std::span<dvec3 const>{p}, std::span<int>{c}, x0);
+    eval_gwnr_parametric_batch(d, pint, std::span<dvec3 const>{p}, std::span<double>{o}, x0, cb);
+    eval_gwnr_parametric_batch(d, pint, std::span<dvec3 const>{p}, std::span<double>{o}, x0, cb, integrate_config{}, net);
+    (void)pint.signed_intersection_count(x0, x0);
     std::vector<cuda::CudaRobustBatch<double, robust::int128_grid>::Job> jobs{{&rob, p.data(), 0, o.data()}};
     cuda::CudaRobustBatch<double, robust::int128_grid> batch{d, jobs};
     batch.tune();

@@ -43,3 +43,7 @@ def test_frontend_program_matches_oracle(gwn, oracle, tmp_path):
                       for s in bnd])
     par = oracle.param_frac_bezier3(q, x0, lines, 0, 10, 1e-6)
     assert np.max(np.abs(rows[:, 8] - par)) <= 1e-15
+    # the faces as flat patches: the same surface, so the mesh's crossing counts; the full parametric GWN adds them
+    pcount = rows[:, 9].astype(np.int32)
+    assert np.array_equal(pcount, oracle.int_naive(q, x0, verts, idx))
+    assert np.max(np.abs(rows[:, 10] - (par + pcount))) <= 1e-15
