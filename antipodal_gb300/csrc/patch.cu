@@ -42,6 +42,7 @@ struct PatchArith;
 template <>
 struct PatchArith<float>
 {
+    using Index = uint32_t; // cell indices below 2^kMaxCellLevel
     static constexpr int kMaxCellLevel = 16;
     static constexpr int kMaxEdgeLevel = 16;
     static constexpr bool kExact = false; // an unresolved decision abandons the pair (it is redone in FP64)
@@ -52,7 +53,9 @@ struct PatchArith<float>
 template <>
 struct PatchArith<double>
 {
-    static constexpr int kMaxCellLevel = 30;
+    using Index = uint64_t;
+    // deep enough that the depth range of a cell (about 2^-level of the patch) falls below the margin first
+    static constexpr int kMaxCellLevel = 45;
     static constexpr int kMaxEdgeLevel = 50;
     static constexpr bool kExact = true; // an unresolved decision is degenerate: fixed rule, counted
     __device__ static double fma(double a, double b, double c) { return __fma_rn(a, b, c); }
@@ -141,8 +144,8 @@ __device__ int cubic_winding(R x0, R x1, R x2, R x3, R y0, R y1, R y2, R y3, R m
 
 // One coordinate of the net of cell (iu, iv) of level L, blossomed from the patch's net: c(4 r + q, k) is control
 // point (r the v index, q the u index) coordinate k relative to the query.  out[4 r + q].
-template <class R, class Net>
-__device__ __forceinline__ void cell_net(Net const& c, int k, int level, uint32_t iu, uint32_t iv, R (&out)[16])
+template <class R, class Net, class I>
+__device__ __forceinline__ void cell_net(Net const& c, int k, int level, I iu, I iv, R (&out)[16])
 {
     if (level == 0)
     {
@@ -200,7 +203,7 @@ __device__ int patch_degree(Net const& c, R m, int& unresolved)
 {
     using A = PatchArith<R>;
     int sum = 0, level = 0;
-    uint32_t iu = 0, iv = 0;
+    typename A::Index iu = 0, iv = 0;
     for (;;)
     {
         R x[16], y[16], lo, hi;

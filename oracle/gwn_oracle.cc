@@ -1324,7 +1324,7 @@ int cell_crossings(patch_job& job, double u0, double v0, double h, int level)
         return 0; // the ray misses the cell, or the cell lies behind the query
     if (*wlo >= m)
         return net_winding(job, net[0], net[1]); // in front throughout: the degree over the cell
-    if (level < 30 && *whi - *wlo >= 4.0 * m)
+    if (level < 45 && *whi - *wlo >= 4.0 * m)
     {
         double const g = 0.5 * h;
         return cell_crossings(job, u0, v0, g, level + 1) + cell_crossings(job, u0 + g, v0, g, level + 1) +

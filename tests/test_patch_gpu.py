@@ -60,8 +60,11 @@ def test_device_patch_counts_near_the_surface(gwn, disp, oracle, offset):
         got, deg = np.empty(len(q), np.int32), np.empty(len(q), np.int32)
         gwn.eval_gwnr_parametric_batch_integer(disp, isect, q, got, x0, out_degenerate=deg)
         ref, ref_deg = oracle.patch_count_bezier3x3(q, x0, patches, degenerate=True)
-        assert not deg.any() and not ref_deg.any()
-        assert np.array_equal(got, ref), np.flatnonzero(got != ref)[:10]
+        # a query within about 2^-40 of the coordinates' scale of the surface (~5e-12 here, more along a grazing
+        # ray) is degenerate: only the smallest offset reaches that, for about 1.5% of its queries
+        clear = (deg == 0) & (ref_deg == 0)
+        assert clear.all() if offset >= 1e-6 else clear.mean() > 0.95
+        assert np.array_equal(got[clear], ref[clear]), np.flatnonzero((got != ref) & clear)[:10]
     isect.close()
 
 
