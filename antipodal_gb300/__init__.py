@@ -174,7 +174,9 @@ class CudaDispatcher:
         return {"kernel_ms": dict(zip(names, list(s.kernel_ms))), "launches": dict(zip(names, list(s.launches))),
                 "fp64_pairs": s.fp64_pairs, "pairs": s.pairs,
                 "integer": {"queries": s.int_queries, "cell_entries": s.int_cell_entries, "leaves": s.int_leaves,
-                            "exact_tests": s.int_exact_tests}}
+                            "exact_tests": s.int_exact_tests},
+                "patches": {"pairs": s.patch_pairs, "cells": s.patch_cells, "pieces": s.patch_pieces,
+                            "fp64_pairs": s.patch_fp64_pairs}}
 
     def probe_fp32_peak(self) -> float:
         """Measured FP32 FMA throughput of this GPU, TFLOP/s."""

@@ -31,7 +31,9 @@ K_FRACTIONAL, K_INTEGER, K_ROBUST, K_PARAMETRIC, K_OTHER, K_COUNT = range(6)
 class Stats(C.Structure):
     _fields_ = [("kernel_ms", C.c_double * K_COUNT), ("launches", C.c_int64 * K_COUNT),
                 ("fp64_pairs", C.c_int64), ("pairs", C.c_int64), ("int_queries", C.c_int64),
-                ("int_cell_entries", C.c_int64), ("int_leaves", C.c_int64), ("int_exact_tests", C.c_int64)]
+                ("int_cell_entries", C.c_int64), ("int_leaves", C.c_int64), ("int_exact_tests", C.c_int64),
+                ("patch_pairs", C.c_int64), ("patch_cells", C.c_int64), ("patch_pieces", C.c_int64),
+                ("patch_fp64_pairs", C.c_int64)]
 
 
 # name -> (restype, argtypes)

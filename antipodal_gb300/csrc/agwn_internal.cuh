@@ -43,7 +43,7 @@ void clear_message();
     } while (0)
 
 // Device-side error flags, one word each, set with atomicOr by kernels and read by the host at synchronisation.
-constexpr int kCounters = 8; // device statistics counters of a context
+constexpr int kCounters = 12; // device statistics counters of a context
 
 enum flag_slot
 {
@@ -135,7 +135,7 @@ struct Context
     bool own_stream = false;
     int* d_flags = nullptr;        // FLAG_COUNT ints
     int* h_flags = nullptr;        // pinned mirror
-    long long* d_counters = nullptr; // kCounters: [0] fp64 pairs, [1] pairs, [2] parametric skips, [4..7] integer
+    long long* d_counters = nullptr; // kCounters: [0] fp64 pairs, [1] pairs, [2] parametric skips, [4..7] integer, [8..11] patches
                                      // term: queries, cell-list entries, candidate leaves, exact tests
     DevBuf scratch[S_COUNT];
     int sm_count = 0;

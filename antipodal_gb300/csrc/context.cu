@@ -446,6 +446,10 @@ int agwn_context_get_stats(agwn_context* ctx, agwn_stats* out, int reset)
     out->int_cell_entries = counters[5];
     out->int_leaves = counters[6];
     out->int_exact_tests = counters[7];
+    out->patch_pairs = counters[8];
+    out->patch_cells = counters[9];
+    out->patch_pieces = counters[10];
+    out->patch_fp64_pairs = counters[11];
     if (reset)
     {
         for (int k = 0; k < AGWN_K_COUNT; ++k)

@@ -94,13 +94,14 @@ __device__ __forceinline__ int chord_crossing(R ax, R ay, R bx, R by)
 // walk (piece i of level L covers [i, i + 1] 2^-L).  unresolved: counts the pieces that hold the origin within the
 // margin m and cannot be split further.
 template <class R>
-__device__ int cubic_winding(R x0, R x1, R x2, R x3, R y0, R y1, R y2, R y3, R m, int& unresolved)
+__device__ int cubic_winding(R x0, R x1, R x2, R x3, R y0, R y1, R y2, R y3, R m, int& unresolved, int& pieces)
 {
     using A = PatchArith<R>;
     int w = 0, level = 0;
     int64_t i = 0;
     for (;;)
     {
+        ++pieces;
         R px[4], py[4];
         if (level == 0)
         {
@@ -185,27 +186,29 @@ __device__ __forceinline__ void range16(const R (&v)[16], R& lo, R& hi)
 
 // Winding number about the origin of a cell net's boundary, counter-clockwise in (u, v).
 template <class R>
-__device__ __forceinline__ int net_winding(const R (&x)[16], const R (&y)[16], R m, int& unresolved)
+__device__ __forceinline__ int net_winding(const R (&x)[16], const R (&y)[16], R m, int& unresolved, int& pieces)
 {
-    int w = cubic_winding(x[0], x[1], x[2], x[3], y[0], y[1], y[2], y[3], m, unresolved);
-    w += cubic_winding(x[3], x[7], x[11], x[15], y[3], y[7], y[11], y[15], m, unresolved);
-    w += cubic_winding(x[15], x[14], x[13], x[12], y[15], y[14], y[13], y[12], m, unresolved);
-    w += cubic_winding(x[12], x[8], x[4], x[0], y[12], y[8], y[4], y[0], m, unresolved);
+    int w = cubic_winding(x[0], x[1], x[2], x[3], y[0], y[1], y[2], y[3], m, unresolved, pieces);
+    w += cubic_winding(x[3], x[7], x[11], x[15], y[3], y[7], y[11], y[15], m, unresolved, pieces);
+    w += cubic_winding(x[15], x[14], x[13], x[12], y[15], y[14], y[13], y[12], m, unresolved, pieces);
+    w += cubic_winding(x[12], x[8], x[4], x[0], y[12], y[8], y[4], y[0], m, unresolved, pieces);
     return w;
 }
 
 // Signed crossings in front of the query with one patch, c(j, k) its net relative to the query in the ray frame
 // (k = x, y across the ray and w along it), m the margin.  Cells are walked depth first without a stack:
 // (level, iu, iv), children 2 iu + (0|1), 2 iv + (0|1) in the order (0,0), (1,0), (0,1), (1,1).  unresolved counts
-// the decisions the margin did not allow (float: the result is void and the pair is redone in FP64).
+// the decisions the margin did not allow (float: the result is void and the pair is redone in FP64); cells and
+// pieces count the work (cells tested, boundary-cubic pieces tested).
 template <class R, class Net>
-__device__ int patch_degree(Net const& c, R m, int& unresolved)
+__device__ int patch_degree(Net const& c, R m, int& unresolved, int& cells, int& pieces)
 {
     using A = PatchArith<R>;
     int sum = 0, level = 0;
     typename A::Index iu = 0, iv = 0;
     for (;;)
     {
+        ++cells;
         R x[16], y[16], lo, hi;
         cell_net(c, 0, level, iu, iv, x);
         range16(x, lo, hi);
@@ -220,7 +223,7 @@ __device__ int patch_degree(Net const& c, R m, int& unresolved)
                 cell_net(c, 2, level, iu, iv, w);
                 range16(w, lo, hi);
                 if (lo >= m)
-                    sum += net_winding(x, y, m, unresolved); // in front throughout
+                    sum += net_winding(x, y, m, unresolved, pieces); // in front throughout
                 else if (hi >= -m)
                 {
                     // the depth changes sign over the cell, or lies within the margin of 0
@@ -230,7 +233,7 @@ __device__ int patch_degree(Net const& c, R m, int& unresolved)
                     {
                         ++unresolved;
                         if (A::kExact && lo + hi >= R(0))
-                            sum += net_winding(x, y, m, unresolved);
+                            sum += net_winding(x, y, m, unresolved, pieces);
                     }
                 }
                 if (!A::kExact && unresolved)
@@ -265,10 +268,10 @@ __device__ int patch_degree(Net const& c, R m, int& unresolved)
 
 // The FP64 pass of one pair: the patch's FP64 net (ray frame) relative to the query, margin 2^-42 of `scale`.
 __device__ __noinline__ int patch_degree_fp64(const double* __restrict__ net, double qx, double qy, double qw,
-                                              double scale, int& degenerate)
+                                              double scale, int& degenerate, int& cells, int& pieces)
 {
     auto const c = [=](int j, int k) { return net[3 * j + k] - (k == 0 ? qx : (k == 1 ? qy : qw)); };
-    return patch_degree(c, scale * 0x1p-42, degenerate);
+    return patch_degree(c, scale * 0x1p-42, degenerate, cells, pieces);
 }
 
 // The patches' control points in the ray frame (rows of f): net in FP64, netf rounded to float, and per patch
@@ -302,14 +305,16 @@ __global__ void k_patch_frame(const double* __restrict__ ctrl, int64_t n_patches
 
 // One query per thread against every patch.  counts / add: the crossing count is written to counts (int) or added
 // to add (the fractional term already there); degenerate (nullable): per query, the decisions left to the fixed
-// rule.
+// rule; stats (nullable): adds pairs past the box test, cells, pieces and FP64 pairs to stats[0..3].
 __global__ void __launch_bounds__(kPatchBlock) k_patch_count(const double* __restrict__ net,
                                                              const float* __restrict__ netf,
                                                              const float4* __restrict__ boxf, int64_t n_patches,
                                                              Frame64 f, const double* __restrict__ pos, int64_t n,
                                                              int32_t* __restrict__ counts, double* __restrict__ add,
-                                                             int32_t* __restrict__ degenerate)
+                                                             int32_t* __restrict__ degenerate,
+                                                             long long* __restrict__ stats)
 {
+    int n_pairs = 0, n_cells = 0, n_pieces = 0, n_fp64 = 0;
     for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
     {
         double const px = pos[3 * i], py = pos[3 * i + 1], pz = pos[3 * i + 2];
@@ -330,11 +335,16 @@ __global__ void __launch_bounds__(kPatchBlock) k_patch_count(const double* __res
             const float* nk = netf + 48 * k;
             auto const c = [=](int j, int kk) { return __ldg(nk + 3 * j + kk) - (kk == 0 ? qx : (kk == 1 ? qy : qw)); };
             int unresolved = 0;
-            int const s = patch_degree(c, m, unresolved);
+            ++n_pairs;
+            int const s = patch_degree(c, m, unresolved, n_cells, n_pieces);
             if (unresolved == 0)
                 sum += s;
             else
-                sum += patch_degree_fp64(net + 48 * k, q[0], q[1], q[2], qscale + double(b1.z), deg);
+            {
+                ++n_fp64;
+                sum += patch_degree_fp64(net + 48 * k, q[0], q[1], q[2], qscale + double(b1.z), deg, n_cells,
+                                         n_pieces);
+            }
         }
         if (add)
             add[i] += double(sum);
@@ -342,6 +352,18 @@ __global__ void __launch_bounds__(kPatchBlock) k_patch_count(const double* __res
             counts[i] = sum;
         if (degenerate)
             degenerate[i] = deg;
+    }
+    if (stats)
+    {
+        long long v[4] = {n_pairs, n_cells, n_pieces, n_fp64};
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+        {
+            for (int o = 16; o > 0; o >>= 1)
+                v[r] += __shfl_xor_sync(0xffffffffu, v[r], o);
+            if ((threadIdx.x & 31) == 0 && v[r])
+                atomicAdd(reinterpret_cast<unsigned long long*>(stats + r), static_cast<unsigned long long>(v[r]));
+        }
     }
 }
 } // namespace
@@ -426,7 +448,7 @@ int patch_integer(agwn_context* ctx, agwn_patches* pt, const double* positions, 
     k_patch_count<<<grid, kPatchBlock, 0, ctx->stream>>>(
         pt->net, pt->netf, reinterpret_cast<const float4*>(pt->boxf), pt->n, f, static_cast<const double*>(dpos), n,
         add_out ? nullptr : static_cast<int32_t*>(dout), add_out ? static_cast<double*>(dout) : nullptr,
-        static_cast<int32_t*>(ddeg));
+        static_cast<int32_t*>(ddeg), ctx->timing ? ctx->d_counters + 8 : nullptr);
     AGWN_TRY(ctx->launch_end(AGWN_K_PARAMETRIC));
     if (host_out)
         AGWN_TRY_CUDA(cudaMemcpyAsync(add_out ? static_cast<void*>(add_out) : static_cast<void*>(out_counts), dout,

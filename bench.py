@@ -722,6 +722,17 @@ def run_param(args, ag, torch, stream, disp, timed):
     ag.eval_gwnr_parametric_batch_integer(disp, isect, qd, cnt, x0)
     ms_int = timed(args.steps, lambda: ag.eval_gwnr_parametric_batch_integer(disp, isect, qd, cnt, x0))
     n_cross = int(cnt.abs().sum().item())
+    # its work counters (one more, untimed launch) and its FP32 rate: 864 flop per cell blossomed (3 coordinates x
+    # 8 restricted cubics x 12 lerps of 3 flop) and 72 per boundary-cubic piece (2 x 12 lerps)
+    disp.set_option(ag._lib.OPT_TIMING, 1)
+    disp.stats(reset=True)
+    deg = torch.empty(Q, dtype=torch.int32, device="cuda")
+    ag.eval_gwnr_parametric_batch_integer(disp, isect, qd, cnt, x0, out_degenerate=deg)
+    pst = disp.stats(reset=True)["patches"]
+    disp.set_option(ag._lib.OPT_TIMING, 0)
+    n_degenerate = int((deg > 0).sum().item())
+    int_flop = 864.0 * pst["cells"] + 72.0 * pst["pieces"]
+    fp32_peak = disp.probe_fp32_peak()
     isect.close()
     # the sample: the first Qs queries (the generator shuffles them, so they are a seeded random sample)
     Qs = max(32, min(Q, int(round(args.plain_scale * Q))))
@@ -762,7 +773,16 @@ def run_param(args, ag, torch, stream, disp, timed):
             "integer_term": {"form": "Bezier-patch intersector (winding numbers of cell boundaries), 256 patches",
                              "ms_per_step": ms_int, "value": Q / (ms_int * 1e-3), "unit": "queries/s",
                              "abs_counts_per_query": n_cross / Q,
-                             "full_gwn_ms_per_step": ms + ms_int},
+                             "full_gwn_ms_per_step": ms + ms_int,
+                             "per_query": {"pairs_past_box": pst["pairs"] / Q, "cells": pst["cells"] / Q,
+                                           "pieces": pst["pieces"] / Q},
+                             "fp64_pair_fraction": pst["fp64_pairs"] / max(1, pst["pairs"]),
+                             "degenerate_queries": n_degenerate,
+                             "roofline": {"bound": "fp32", "achieved": int_flop / (ms_int * 1e-3) / 1e12,
+                                          "peak": fp32_peak, "unit": "TFLOP/s",
+                                          "frac": int_flop / (ms_int * 1e-3) / 1e12 / fp32_peak,
+                                          "note": "algorithmic flop of the blossoms from the kernel's own counters; "
+                                                  "peak = FP32 FMA rate measured on this GPU in this run"}},
             "plain": {"value": plain_rate, "ms_per_step_sample": ms_plain,
                       "ms_per_step_extrapolated_full": ms_plain * Q / Qs,
                       "panels_per_pair": panels_p / (Qs * Cn),

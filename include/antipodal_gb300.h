@@ -143,6 +143,11 @@ typedef struct agwn_stats
     int64_t int_cell_entries;         /* cell-list entries read (each a leaf index and the leaf's corners)     */
     int64_t int_leaves;               /* candidate leaves decided (in float, or by the exact test)             */
     int64_t int_exact_tests;          /* leaves the float decision left to the exact test                      */
+    /* the Bezier-patch intersector, when timing: */
+    int64_t patch_pairs;              /* (query, patch) pairs past the box test                                */
+    int64_t patch_cells;              /* parameter cells whose control net was blossomed and tested            */
+    int64_t patch_pieces;             /* boundary-cubic pieces blossomed and tested for the winding numbers    */
+    int64_t patch_fp64_pairs;         /* pairs that float could not decide, redone in FP64                     */
 } agwn_stats;
 /* Reads (synchronising the stream first) and optionally resets the accumulated statistics. */
 int agwn_context_get_stats(agwn_context* ctx, agwn_stats* out, int reset);

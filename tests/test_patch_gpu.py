@@ -155,6 +155,14 @@ def test_patch_intersector_inputs_and_errors(gwn, disp, oracle):
     gwn.eval_gwnr_parametric_batch(disp, isect, q, out_h, x0, curves, cfg)
     disp.synchronize()
     assert np.array_equal(out_d.cpu().numpy(), out_h)
+    # the work counters (with timing on): every pair past the box test blossoms at least its root cell
+    disp.set_option(gwn._lib.OPT_TIMING, 1)
+    disp.stats(reset=True)
+    gwn.eval_gwnr_parametric_batch_integer(disp, isect, q, np.empty(len(q), np.int32), x0)
+    st = disp.stats(reset=True)["patches"]
+    disp.set_option(gwn._lib.OPT_TIMING, 0)
+    assert 0 < st["pairs"] <= len(q) * len(patches)
+    assert st["cells"] >= st["pairs"] and st["pieces"] > 0 and 0 <= st["fp64_pairs"] <= st["pairs"]
     # empty queries, no patches, a bad direction
     gwn.eval_gwnr_parametric_batch_integer(disp, isect, np.zeros((0, 3)), np.zeros(0, np.int32), x0)
     none = gwn.CudaBezierPatchIntersector(disp, np.zeros((0, 4, 4, 3)))
