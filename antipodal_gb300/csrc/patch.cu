@@ -34,8 +34,6 @@ namespace agwn
 {
 namespace
 {
-constexpr int kPatchBlock = 128;
-
 template <class R>
 struct PatchArith;
 
@@ -195,73 +193,79 @@ __device__ __forceinline__ int net_winding(const R (&x)[16], const R (&y)[16], R
     return w;
 }
 
-// Signed crossings in front of the query with one patch, c(j, k) its net relative to the query in the ray frame
-// (k = x, y across the ray and w along it), m the margin.  Cells are walked depth first without a stack:
-// (level, iu, iv), children 2 iu + (0|1), 2 iv + (0|1) in the order (0,0), (1,0), (0,1), (1,1).  unresolved counts
-// the decisions the margin did not allow (float: the result is void and the pair is redone in FP64); cells and
-// pieces count the work (cells tested, boundary-cubic pieces tested).
+// One step of the walk over a patch's parameter cells, depth first without a stack: cell (level, iu, iv), children
+// 2 iu + (0|1), 2 iv + (0|1) in the order (0,0), (1,0), (0,1), (1,1).  The step tests the cell (c(j, k): the
+// patch's net relative to the query in the ray frame, k = x, y across the ray and w along it; m the margin), adds
+// its boundary's winding number to sum when it lies in front, and moves to the next cell.  Returns false when the
+// walk is over: every cell done, or (float) a decision the margin did not allow, counted in unresolved (the result
+// is then void and the pair is redone in FP64).  pieces counts the boundary-cubic pieces tested.
+template <class R, class Net, class I>
+__device__ __forceinline__ bool walk_cell(Net const& c, R m, int& level, I& iu, I& iv, int& sum, int& unresolved,
+                                          int& pieces)
+{
+    using A = PatchArith<R>;
+    R x[16], y[16], lo, hi;
+    cell_net(c, 0, level, iu, iv, x);
+    range16(x, lo, hi);
+    if (!(lo > m || hi < -m))
+    {
+        cell_net(c, 1, level, iu, iv, y);
+        range16(y, lo, hi);
+        if (!(lo > m || hi < -m))
+        {
+            R w[16];
+            cell_net(c, 2, level, iu, iv, w);
+            range16(w, lo, hi);
+            if (lo >= m)
+                sum += net_winding(x, y, m, unresolved, pieces); // in front throughout
+            else if (hi >= -m)
+            {
+                // the depth changes sign over the cell, or lies within the margin of 0
+                if (level < A::kMaxCellLevel && hi - lo >= R(4) * m)
+                {
+                    ++level;
+                    iu *= 2;
+                    iv *= 2;
+                    return true;
+                }
+                ++unresolved;
+                if (A::kExact && lo + hi >= R(0))
+                    sum += net_winding(x, y, m, unresolved, pieces);
+            }
+            if (!A::kExact && unresolved)
+                return false;
+        }
+    }
+    while (level > 0 && (iu & 1) && (iv & 1))
+    {
+        iu >>= 1;
+        iv >>= 1;
+        --level;
+    }
+    if (level == 0)
+        return false;
+    if (iu & 1)
+    {
+        iu -= 1;
+        iv += 1;
+    }
+    else
+        iu += 1;
+    return true;
+}
+
+// Signed crossings in front of the query with one patch: the whole walk.  unresolved counts the decisions left to
+// the fixed rule (FP64) or that void the result (float); cells and pieces count the work.
 template <class R, class Net>
 __device__ int patch_degree(Net const& c, R m, int& unresolved, int& cells, int& pieces)
 {
-    using A = PatchArith<R>;
     int sum = 0, level = 0;
-    typename A::Index iu = 0, iv = 0;
-    for (;;)
+    typename PatchArith<R>::Index iu = 0, iv = 0;
+    bool more = true;
+    while (more)
     {
         ++cells;
-        R x[16], y[16], lo, hi;
-        cell_net(c, 0, level, iu, iv, x);
-        range16(x, lo, hi);
-        bool descend = false;
-        if (!(lo > m || hi < -m))
-        {
-            cell_net(c, 1, level, iu, iv, y);
-            range16(y, lo, hi);
-            if (!(lo > m || hi < -m))
-            {
-                R w[16];
-                cell_net(c, 2, level, iu, iv, w);
-                range16(w, lo, hi);
-                if (lo >= m)
-                    sum += net_winding(x, y, m, unresolved, pieces); // in front throughout
-                else if (hi >= -m)
-                {
-                    // the depth changes sign over the cell, or lies within the margin of 0
-                    if (level < A::kMaxCellLevel && hi - lo >= R(4) * m)
-                        descend = true;
-                    else
-                    {
-                        ++unresolved;
-                        if (A::kExact && lo + hi >= R(0))
-                            sum += net_winding(x, y, m, unresolved, pieces);
-                    }
-                }
-                if (!A::kExact && unresolved)
-                    return 0;
-            }
-        }
-        if (descend)
-        {
-            ++level;
-            iu *= 2;
-            iv *= 2;
-            continue;
-        }
-        while (level > 0 && (iu & 1) && (iv & 1))
-        {
-            iu >>= 1;
-            iv >>= 1;
-            --level;
-        }
-        if (level == 0)
-            break;
-        if (iu & 1)
-        {
-            iu -= 1;
-            iv += 1;
-        }
-        else
-            iu += 1;
+        more = walk_cell(c, m, level, iu, iv, sum, unresolved, pieces);
     }
     return sum;
 }
@@ -303,55 +307,202 @@ __global__ void k_patch_frame(const double* __restrict__ ctrl, int64_t n_patches
     }
 }
 
-// One query per thread against every patch.  counts / add: the crossing count is written to counts (int) or added
-// to add (the fractional term already there); degenerate (nullable): per query, the decisions left to the fixed
-// rule; stats (nullable): adds pairs past the box test, cells, pieces and FP64 pairs to stats[0..3].
-__global__ void __launch_bounds__(kPatchBlock) k_patch_count(const double* __restrict__ net,
-                                                             const float* __restrict__ netf,
-                                                             const float4* __restrict__ boxf, int64_t n_patches,
-                                                             Frame64 f, const double* __restrict__ pos, int64_t n,
-                                                             int32_t* __restrict__ counts, double* __restrict__ add,
-                                                             int32_t* __restrict__ degenerate,
-                                                             long long* __restrict__ stats)
+// Pairs are queued per warp: a warp owns 32 queries (one per lane), tests them against the patches of the
+// shared-memory tile one patch at a time, and appends the (query, patch) pairs that pass the box test to its queue;
+// every lane that has no pair takes the next one, and each turn of the loop runs one cell of every lane's walk, so
+// the lanes stay busy however unevenly the work falls on the pairs.  Pairs that float cannot decide go to a second
+// queue and run in FP64 32 at a time.  The tile holds each patch's float net at a stride of 49 floats (lanes on
+// different patches then fall in different banks) and its box.
+constexpr int kPatchWarps = 4;
+constexpr int kPatchQueue = 64;   // ring size: below 32 entries are topped up by at most 32, and drained to below 32
+constexpr int kNetStride = 49;    // floats per patch net in shared memory
+constexpr int kPatchTileMax = 512; // patches per shared-memory tile
+
+struct PatchWarp
 {
-    int n_pairs = 0, n_cells = 0, n_pieces = 0, n_fp64 = 0;
-    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+    double qd[32][3];   // the queries in the ray frame (FP64)
+    float qf[32][3];    // ... in float
+    float qscale[32];   // largest |coordinate| of each
+    int sum[32];
+    int deg[32];
+    uint32_t queue[kPatchQueue];  // (patch in tile << 5) | lane
+    uint32_t fqueue[kPatchQueue]; // the same, for FP64
+};
+
+// The FP64 walk of the queued pairs fq[head .. head + count) (count <= 32, lane j takes entry j).
+__device__ __forceinline__ void patch_fp64_batch(PatchWarp& w, const double* __restrict__ net64, const float* s_box,
+                                                 int64_t tile_base, uint32_t head, uint32_t count, int lane,
+                                                 int& n_cells, int& n_pieces)
+{
+    if (uint32_t(lane) < count)
     {
-        double const px = pos[3 * i], py = pos[3 * i + 1], pz = pos[3 * i + 2];
-        double q[3];
-        for (int r = 0; r < 3; ++r)
-            q[r] = f.r[3 * r] * px + f.r[3 * r + 1] * py + f.r[3 * r + 2] * pz;
-        double const qscale = fmax(fmax(fabs(q[0]), fabs(q[1])), fabs(q[2]));
-        float const qx = float(q[0]), qy = float(q[1]), qw = float(q[2]);
-        int sum = 0, deg = 0;
-        for (int64_t k = 0; k < n_patches; ++k)
+        uint32_t const e = w.fqueue[(head + lane) & (kPatchQueue - 1)];
+        int const src = int(e & 31u), p = int(e >> 5);
+        int deg = 0;
+        int const s = patch_degree_fp64(net64 + 48 * (tile_base + p), w.qd[src][0], w.qd[src][1], w.qd[src][2],
+                                        double(w.qscale[src]) + double(s_box[8 * p + 6]), deg, n_cells, n_pieces);
+        atomicAdd(&w.sum[src], s);
+        if (deg)
+            atomicAdd(&w.deg[src], deg);
+    }
+    __syncwarp();
+}
+
+// counts / add: the crossing count is written to counts (int) or added to add (the fractional term already there);
+// degenerate (nullable): per query, the decisions left to the fixed rule; stats (nullable): adds pairs past the box
+// test, cells, pieces and FP64 pairs to stats[0..3].
+__global__ void __launch_bounds__(32 * kPatchWarps) k_patch_count(
+    const double* __restrict__ net64, const float* __restrict__ netf, const float* __restrict__ boxf,
+    int64_t n_patches, int tile, Frame64 f, const double* __restrict__ pos, int64_t n, int32_t* __restrict__ counts,
+    double* __restrict__ add, int32_t* __restrict__ degenerate, long long* __restrict__ stats)
+{
+    extern __shared__ __align__(16) float s_tile[]; // tile x kNetStride nets, then tile x 8 box values
+    __shared__ PatchWarp s_warp[kPatchWarps];
+    float* const s_net = s_tile;
+    float* const s_box = s_tile + tile * kNetStride; // tile is a multiple of 4: 16-byte aligned
+    int const lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned const lt = (1u << lane) - 1u;
+    PatchWarp& w = s_warp[warp];
+    int const n_ptiles = int((n_patches + tile - 1) / tile);
+    int n_pairs = 0, n_cells = 0, n_pieces = 0, n_fp64 = 0;
+
+    auto load_tile = [&](int pt)
+    {
+        int64_t const base = int64_t(pt) * tile;
+        int const tn = int(n_patches - base < tile ? n_patches - base : int64_t(tile));
+        for (int j = threadIdx.x; j < tn * 48; j += blockDim.x)
+            s_net[(j / 48) * kNetStride + j % 48] = netf[48 * base + j];
+        for (int j = threadIdx.x; j < tn * 8; j += blockDim.x)
+            s_box[j] = boxf[8 * base + j];
+    };
+    if (n_ptiles == 1)
+    {
+        load_tile(0);
+        __syncthreads();
+    }
+
+    int64_t const per_block = 32 * kPatchWarps;
+    for (int64_t bt = blockIdx.x; bt * per_block < n; bt += gridDim.x)
+    {
+        int64_t const i = bt * per_block + 32 * warp + lane;
+        bool const valid = i < n;
+        double q[3] = {0.0, 0.0, 0.0};
+        if (valid)
         {
-            float4 const b0 = boxf[2 * k], b1 = boxf[2 * k + 1];
-            // 2^-16 of the scale: the float values compared below err by less than 2^-18.5 of it
-            float const m = 1.52587890625e-5f * (float(qscale) + b1.z);
-            if (b0.x - qx > m || b0.y - qx < -m || b0.z - qy > m || b0.w - qy < -m || b1.y - qw < -m)
-                continue;
-            // the net relative to the query, read again (from L1) by every cell rather than held in registers
-            const float* nk = netf + 48 * k;
-            auto const c = [=](int j, int kk) { return __ldg(nk + 3 * j + kk) - (kk == 0 ? qx : (kk == 1 ? qy : qw)); };
-            int unresolved = 0;
-            ++n_pairs;
-            int const s = patch_degree(c, m, unresolved, n_cells, n_pieces);
-            if (unresolved == 0)
-                sum += s;
-            else
-            {
-                ++n_fp64;
-                sum += patch_degree_fp64(net + 48 * k, q[0], q[1], q[2], qscale + double(b1.z), deg, n_cells,
-                                         n_pieces);
-            }
+            double const px = pos[3 * i], py = pos[3 * i + 1], pz = pos[3 * i + 2];
+            for (int r = 0; r < 3; ++r)
+                q[r] = f.r[3 * r] * px + f.r[3 * r + 1] * py + f.r[3 * r + 2] * pz;
         }
-        if (add)
-            add[i] += double(sum);
-        else
-            counts[i] = sum;
-        if (degenerate)
-            degenerate[i] = deg;
+        float const my_x = float(q[0]), my_y = float(q[1]), my_w = float(q[2]);
+        float const my_scale = float(fmax(fmax(fabs(q[0]), fabs(q[1])), fabs(q[2])));
+        for (int r = 0; r < 3; ++r)
+            w.qd[lane][r] = q[r];
+        w.qf[lane][0] = my_x;
+        w.qf[lane][1] = my_y;
+        w.qf[lane][2] = my_w;
+        // every value the float walk compares errs by less than 2^-18.5 of the coordinates' scale (the float nets'
+        // and queries' rounding and the blossoms'); the margin is 2^-16 of it
+        w.qscale[lane] = my_scale;
+        w.sum[lane] = 0;
+        w.deg[lane] = 0;
+        __syncwarp();
+
+        for (int pt = 0; pt < n_ptiles; ++pt)
+        {
+            if (n_ptiles > 1)
+            {
+                __syncthreads();
+                load_tile(pt);
+                __syncthreads();
+            }
+            int64_t const tile_base = int64_t(pt) * tile;
+            int const tn = int(n_patches - tile_base < tile ? n_patches - tile_base : int64_t(tile));
+            uint32_t head = 0, tail = 0, fhead = 0, ftail = 0;
+            int kn = 0;
+            // this lane's pair: its queue entry (or -1), its query and margin, and the walk's state
+            int cur = -1;
+            float cx = 0.f, cy = 0.f, cw = 0.f, cm = 0.f;
+            int level = 0, csum = 0, unresolved = 0;
+            uint32_t iu = 0, iv = 0;
+            for (;;)
+            {
+                // top the queue up: the next patches' box tests for the warp's 32 queries
+                while (tail - head < 32 && kn < tn)
+                {
+                    float4 const b0 = *reinterpret_cast<const float4*>(s_box + 8 * kn);
+                    float4 const b1 = *reinterpret_cast<const float4*>(s_box + 8 * kn + 4);
+                    float const m = 1.52587890625e-5f * (my_scale + b1.z);
+                    bool const pass = valid && !(b0.x - my_x > m || b0.y - my_x < -m || b0.z - my_y > m ||
+                                                 b0.w - my_y < -m || b1.y - my_w < -m);
+                    unsigned const bal = __ballot_sync(0xffffffffu, pass);
+                    if (pass)
+                        w.queue[(tail + __popc(bal & lt)) & (kPatchQueue - 1)] = (uint32_t(kn) << 5) | uint32_t(lane);
+                    tail += __popc(bal);
+                    ++kn;
+                }
+                __syncwarp();
+                // lanes without a pair take the next ones
+                bool const idle = cur < 0;
+                unsigned const ib = __ballot_sync(0xffffffffu, idle);
+                uint32_t const rank = __popc(ib & lt);
+                if (idle && head + rank < tail)
+                {
+                    cur = int(w.queue[(head + rank) & (kPatchQueue - 1)]);
+                    int const src = cur & 31, p = cur >> 5;
+                    cx = w.qf[src][0];
+                    cy = w.qf[src][1];
+                    cw = w.qf[src][2];
+                    cm = 1.52587890625e-5f * (w.qscale[src] + s_box[8 * p + 6]);
+                    level = 0;
+                    iu = iv = 0;
+                    csum = 0;
+                    unresolved = 0;
+                    ++n_pairs;
+                }
+                head += min(uint32_t(__popc(ib)), tail - head);
+                if (__ballot_sync(0xffffffffu, cur >= 0) == 0)
+                    break; // queue empty and every patch of the tile tested
+                bool finished = false;
+                if (cur >= 0)
+                {
+                    const float* nk = s_net + (cur >> 5) * kNetStride;
+                    auto const c = [=](int j, int kk)
+                    { return nk[3 * j + kk] - (kk == 0 ? cx : (kk == 1 ? cy : cw)); };
+                    ++n_cells;
+                    finished = !walk_cell(c, cm, level, iu, iv, csum, unresolved, n_pieces);
+                }
+                bool const to_fp64 = finished && unresolved;
+                unsigned const fb = __ballot_sync(0xffffffffu, to_fp64);
+                if (to_fp64)
+                    w.fqueue[(ftail + __popc(fb & lt)) & (kPatchQueue - 1)] = uint32_t(cur);
+                else if (finished)
+                    atomicAdd(&w.sum[cur & 31], csum);
+                ftail += __popc(fb);
+                n_fp64 += to_fp64 ? 1 : 0;
+                if (finished)
+                    cur = -1;
+                __syncwarp();
+                if (ftail - fhead >= 32)
+                {
+                    patch_fp64_batch(w, net64, s_box, tile_base, fhead, 32, lane, n_cells, n_pieces);
+                    fhead += 32;
+                }
+            }
+            if (ftail != fhead)
+                patch_fp64_batch(w, net64, s_box, tile_base, fhead, ftail - fhead, lane, n_cells, n_pieces);
+        }
+        __syncwarp();
+        if (valid)
+        {
+            int const sum = w.sum[lane];
+            if (add)
+                add[i] += double(sum);
+            else
+                counts[i] = sum;
+            if (degenerate)
+                degenerate[i] = w.deg[lane];
+        }
+        __syncwarp();
     }
     if (stats)
     {
@@ -361,7 +512,7 @@ __global__ void __launch_bounds__(kPatchBlock) k_patch_count(const double* __res
         {
             for (int o = 16; o > 0; o >>= 1)
                 v[r] += __shfl_xor_sync(0xffffffffu, v[r], o);
-            if ((threadIdx.x & 31) == 0 && v[r])
+            if (lane == 0 && v[r])
                 atomicAdd(reinterpret_cast<unsigned long long*>(stats + r), static_cast<unsigned long long>(v[r]));
         }
     }
@@ -443,10 +594,19 @@ int patch_integer(agwn_context* ctx, agwn_patches* pt, const double* positions, 
     bool host_deg = false;
     if (out_degenerate)
         AGWN_TRY(stage_out(*ctx, out_degenerate, sizeof(int32_t) * n, S_MISC0, &ddeg, &host_deg));
-    int const grid = std::max(1, int(std::min<int64_t>(div_up(n, kPatchBlock), 16 * int64_t(ctx->sm_count))));
+    // one shared-memory tile of patches (a multiple of 4, so that the boxes after the nets stay 16-byte aligned),
+    // and as many blocks as fit on the SMs at once
+    int const tile = int(std::min<int64_t>(kPatchTileMax, std::max<int64_t>(4, div_up(pt->n, 4) * 4)));
+    size_t const smem = sizeof(float) * size_t(tile) * (kNetStride + 8);
+    int const block = 32 * kPatchWarps;
+    AGWN_TRY_CUDA(cudaFuncSetAttribute(k_patch_count, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+    int per_sm = 0;
+    AGWN_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_patch_count, block, smem));
+    AGWN_CHECK_ARG(per_sm >= 1, "the patch kernel does not fit on an SM (smem %zu)", smem);
+    int const grid = int(std::max<int64_t>(1, std::min<int64_t>(div_up(n, block), int64_t(per_sm) * ctx->sm_count)));
     AGWN_TRY(ctx->launch_begin(AGWN_K_PARAMETRIC));
-    k_patch_count<<<grid, kPatchBlock, 0, ctx->stream>>>(
-        pt->net, pt->netf, reinterpret_cast<const float4*>(pt->boxf), pt->n, f, static_cast<const double*>(dpos), n,
+    k_patch_count<<<grid, block, smem, ctx->stream>>>(
+        pt->net, pt->netf, pt->boxf, pt->n, tile, f, static_cast<const double*>(dpos), n,
         add_out ? nullptr : static_cast<int32_t*>(dout), add_out ? static_cast<double*>(dout) : nullptr,
         static_cast<int32_t*>(ddeg), ctx->timing ? ctx->d_counters + 8 : nullptr);
     AGWN_TRY(ctx->launch_end(AGWN_K_PARAMETRIC));
