@@ -832,10 +832,11 @@ __global__ void __launch_bounds__(256, mixed_min_blocks<K>())
                 bool const sw0 = an.x > ad.x, sw1 = an.y > ad.y;
                 // (num = den = 0 gives an infinite reciprocal, a NaN t and a NaN bound: the pair goes to FP64)
                 float2 const inv = make_float2(__fdividef(1.f, fmaxf(an.x, ad.x)), __fdividef(1.f, fmaxf(an.y, ad.y)));
-                float2 const t = lv_mul(make_float2(fminf(an.x, ad.x), fminf(an.y, ad.y)), inv);
-                float2 const bound = lv_mul(lv_fma(make_float2(sw0 ? sn.x : sd.x, sw1 ? sn.y : sd.y), t,
-                                                   make_float2(sw0 ? sd.x : sn.x, sw1 ? sd.y : sn.y)),
-                                            inv); // in units of kEpsBound
+                // an1, ad1: |num| and |den| over M, t the smaller; the bound (sn * ad1 + sd * an1) / M as packed
+                // products, without per-lane selects
+                float2 const an1 = lv_mul(an, inv), ad1 = lv_mul(ad, inv);
+                float2 const t = make_float2(fminf(an1.x, ad1.x), fminf(an1.y, ad1.y));
+                float2 const bound = lv_mul(lv_fma(sn, ad1, lv_mul(sd, an1)), inv); // in units of kEpsBound
                 // a NaN or infinity anywhere (a near vertex, |v| = 0, overflow) makes the bound NaN, which the negated
                 // comparison sends to FP64; so does a branch (den <= 0) decided within the rounding of num
                 float2 const margin = lv_fma(lv_set<float2>(-kEpsBound), sn, an);
