@@ -19,7 +19,7 @@
 // own net at dyadic parameters, so that rounding does not grow with the depth of a split), hence each decision,
 // and the count, holds for the exact map.  Unlike Newton's iteration the degree needs no root to be isolated: two
 // crossings near a fold of the map (a ray almost tangent to the patch) cancel in it as they should.
-// Each pair runs first in float with a margin of 2^-16 of the coordinates' scale; a decision that float cannot
+// Each pair runs first in float with a margin of 2^-17 of the coordinates' scale; a decision that float cannot
 // make (a boundary image or the surface within that margin of the ray) sends the pair to FP64 with a margin of
 // 2^-42.  What FP64 cannot make either is degenerate (the ray on a cell boundary's image within 2^-42 of the scale,
 // or the query that close to the surface): it is decided by a fixed rule and counted.
@@ -400,8 +400,11 @@ __global__ void __launch_bounds__(32 * kPatchWarps) k_patch_count(
         w.qf[lane][0] = my_x;
         w.qf[lane][1] = my_y;
         w.qf[lane][2] = my_w;
-        // every value the float walk compares errs by less than 2^-18.5 of the coordinates' scale (the float nets'
-        // and queries' rounding and the blossoms'); the margin is 2^-16 of it
+        // Float margin: with S the coordinates' scale and u = 2^-24, a float net value relative to the query errs by
+        // at most 2 u S (the net's and the query's rounding, the difference), each level of lerps adds 3 u S, so a
+        // cell's net errs by 20 u S (6 levels) and a boundary piece's control points by 29 u S (3 more); the
+        // piece, its chord and the straight joins between their ends then keep within 41 u S of the piece's box.
+        // The margin m = 2^-17 S = 128 u S is three times that.
         w.qscale[lane] = my_scale;
         w.sum[lane] = 0;
         w.deg[lane] = 0;
@@ -431,7 +434,7 @@ __global__ void __launch_bounds__(32 * kPatchWarps) k_patch_count(
                 {
                     float4 const b0 = *reinterpret_cast<const float4*>(s_box + 8 * kn);
                     float4 const b1 = *reinterpret_cast<const float4*>(s_box + 8 * kn + 4);
-                    float const m = 1.52587890625e-5f * (my_scale + b1.z);
+                    float const m = 7.62939453125e-6f * (my_scale + b1.z);
                     bool const pass = valid && !(b0.x - my_x > m || b0.y - my_x < -m || b0.z - my_y > m ||
                                                  b0.w - my_y < -m || b1.y - my_w < -m);
                     unsigned const bal = __ballot_sync(0xffffffffu, pass);
@@ -452,7 +455,7 @@ __global__ void __launch_bounds__(32 * kPatchWarps) k_patch_count(
                     cx = w.qf[src][0];
                     cy = w.qf[src][1];
                     cw = w.qf[src][2];
-                    cm = 1.52587890625e-5f * (w.qscale[src] + s_box[8 * p + 6]);
+                    cm = 7.62939453125e-6f * (w.qscale[src] + s_box[8 * p + 6]);
                     level = 0;
                     iu = iv = 0;
                     csum = 0;
