@@ -104,9 +104,10 @@ int Context::drain_timing()
 {
     if (n_pending == 0)
         return AGWN_OK;
-    AGWN_TRY_CUDA(cudaStreamSynchronize(stream));
     for (int i = 0; i < n_pending; ++i)
     {
+        // each launch's own end event: chunked calls record them on more than one stream
+        AGWN_TRY_CUDA(cudaEventSynchronize(ev_end[i]));
         float ms = 0.f;
         AGWN_TRY_CUDA(cudaEventElapsedTime(&ms, ev_begin[i], ev_end[i]));
         kernel_ms[pending_class[i]] += ms;

@@ -284,6 +284,40 @@ int frac_mixed_robust_pf(Context& ctx, const double* d_pos, int64_t n, double* d
                                    RobustFallbackPF{static_cast<const RSeg<double>*>(rseg)});
 }
 
+int frac_mixed_robust_pf_chunked(Context& ctx, const double* d_pos, int64_t n, double* d_out, int32_t* d_counts,
+                                 const double* d_raw, int64_t n_seg, const void* rseg, ChunkCounts count, void* user)
+{
+    if (n == 0)
+        return AGWN_OK;
+    AGWN_TRY(ctx.ensure_pipeline());
+    int64_t chunk = std::max<int64_t>(int64_t(1) << 20, (n + 7) / 8);
+    chunk = (chunk + 1023) / 1024 * 1024;
+    double const x0[3] = {-1.0, 0.0, 0.0};
+    FracPlan<double> plan;
+    AGWN_TRY(fractional_prepare<double>(ctx, x0, d_raw, n_seg, n, &plan, true));
+    cudaEvent_t const ready = ctx.pipe_ev[6];
+    cudaEvent_t const joined = ctx.pipe_ev[7];
+    cudaStream_t const main = ctx.stream;
+    cudaStream_t const cs[2] = {main, ctx.compute2};
+    AGWN_TRY_CUDA(cudaEventRecord(ready, main));
+    AGWN_TRY_CUDA(cudaStreamWaitEvent(cs[1], ready, 0));
+    int rc = AGWN_OK;
+    for (int64_t i = 0; i * chunk < n && rc == AGWN_OK; ++i)
+    {
+        int64_t const q0 = i * chunk, m = std::min(chunk, n - q0);
+        ctx.stream = cs[i & 1];
+        rc = count(user, ctx, d_pos + 3 * q0, m, d_counts + q0);
+        if (rc == AGWN_OK)
+            rc = n_seg == 0 ? fractional_launch<double>(ctx, plan, d_pos + 3 * q0, m, d_out + q0, d_counts + q0)
+                            : fractional_launch_mixed(ctx, plan, d_pos + 3 * q0, m, d_out + q0, d_counts + q0,
+                                                      RobustFallbackPF{static_cast<const RSeg<double>*>(rseg)});
+        ctx.stream = main;
+    }
+    AGWN_TRY_CUDA(cudaEventRecord(joined, cs[1]));
+    AGWN_TRY_CUDA(cudaStreamWaitEvent(main, joined, 0));
+    return rc;
+}
+
 // --------------------------------------------------------------------------------------------------------------
 // C ABI: mesh batch functions
 // --------------------------------------------------------------------------------------------------------------
@@ -368,6 +402,52 @@ int mesh_batch_pipelined(Context& ctx, const agwn_bvh* bvh, const T* positions, 
     return ctx.check_flags();
 }
 
+// Device queries and device results of the full GWN: the batch runs in 8 chunks whose kernels alternate between the
+// context's stream
+// and a second compute stream, as the host-array pipeline's do, so that the next chunk's integer and fractional
+// kernels fill the SMs that the end of the current chunk's fractional kernel leaves idle.  Each chunk reads and
+// writes its own slices (queries, counts, results), so no chunk waits for another; the boundary, the hierarchy and
+// its cell grid are prepared once on the context's stream before either stream starts.
+template <class T>
+int mesh_batch_chunked(Context& ctx, const agwn_bvh* bvh, const T* dpos, int64_t n, T* dout, const T* x0,
+                       const T* dseg, int64_t n_seg)
+{
+    AGWN_TRY(ctx.ensure_pipeline());
+    int64_t chunk = std::max<int64_t>(int64_t(1) << 20, (n + 7) / 8);
+    chunk = (chunk + 1023) / 1024 * 1024;
+    bool const with_int = bvh && bvh->n_tri > 0;
+    int32_t* dcounts = nullptr;
+    if (with_int)
+        AGWN_TRY(ctx.scratch_reserve(S_COUNTS, sizeof(int32_t) * size_t(n), reinterpret_cast<void**>(&dcounts)));
+    cudaEvent_t const ready = ctx.pipe_ev[6];  // the prepared boundary, hierarchy and cell grid
+    cudaEvent_t const joined = ctx.pipe_ev[7]; // the second compute stream's last kernels
+    cudaStream_t const main = ctx.stream;
+    cudaStream_t const cs[2] = {main, ctx.compute2};
+    FracPlan<T> plan;
+    AGWN_TRY(fractional_prepare<T>(ctx, x0, dseg, n_seg, n, &plan));
+    if (with_int)
+        AGWN_TRY(integer_prepare<T>(ctx, *bvh, x0));
+    AGWN_TRY_CUDA(cudaEventRecord(ready, main));
+    AGWN_TRY_CUDA(cudaStreamWaitEvent(cs[1], ready, 0));
+    int64_t const n_chunks = (n + chunk - 1) / chunk;
+    int rc = AGWN_OK;
+    for (int64_t i = 0; i < n_chunks && rc == AGWN_OK; ++i)
+    {
+        int64_t const q0 = i * chunk, m = std::min(chunk, n - q0);
+        int32_t* const cb = with_int ? dcounts + q0 : nullptr;
+        ctx.stream = cs[i & 1]; // the launches below go to this chunk's compute stream
+        if (with_int)
+            rc = integer_run<T>(ctx, *bvh, dpos + 3 * q0, m, cb, x0);
+        if (rc == AGWN_OK)
+            rc = fractional_launch<T>(ctx, plan, dpos + 3 * q0, m, dout + q0, cb);
+        ctx.stream = main;
+    }
+    // the context's stream continues after everything of the second one
+    AGWN_TRY_CUDA(cudaEventRecord(joined, cs[1]));
+    AGWN_TRY_CUDA(cudaStreamWaitEvent(main, joined, 0));
+    return rc;
+}
+
 template <class T>
 int mesh_batch(agwn_context* ctx, const agwn_bvh* bvh, const T* positions, int64_t n, T* out, const T* x0,
                const T* boundary, int64_t n_seg, bool want_frac)
@@ -394,6 +474,15 @@ int mesh_batch(agwn_context* ctx, const agwn_bvh* bvh, const T* positions, int64
         AGWN_TRY(stage_in(*ctx, boundary, sizeof(T) * 7 * n_seg, S_MISC0, &dseg));
         return mesh_batch_pipelined<T>(*ctx, bvh, positions, n, out, x0, static_cast<const T*>(dseg), n_seg,
                                        want_frac);
+    }
+    if (n >= (int64_t(1) << 21) && want_frac && bvh && bvh->n_tri > 0 && is_device_pointer(positions) &&
+        is_device_pointer(out))
+    {
+        AGWN_TRY(stage_in(*ctx, boundary, sizeof(T) * 7 * n_seg, S_MISC0, &dseg));
+        AGWN_TRY(mesh_batch_chunked<T>(*ctx, bvh, positions, n, out, x0, static_cast<const T*>(dseg), n_seg));
+        if (dseg != boundary)
+            return ctx->check_flags(); // a staged host boundary must outlive its copy: finish before returning
+        return AGWN_OK;
     }
     AGWN_TRY(stage_in(*ctx, positions, sizeof(T) * 3 * n, S_QUERIES, &dpos));
     AGWN_TRY(stage_in(*ctx, boundary, sizeof(T) * 7 * n_seg, S_MISC0, &dseg));

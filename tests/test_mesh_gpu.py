@@ -249,8 +249,9 @@ def test_own_atan2_against_cuda_and_fp64(gwn, disp):
 
 
 def test_host_arrays_pipelined_equal_device_arrays(gwn):
-    """Host queries and results of 2^21 or more run through the chunked upload/compute/download pipeline; the values
-    must equal the device-array call's bit for bit, in both precisions of the fractional term."""
+    """Host queries and results of 2^21 or more run through the chunked upload/compute/download pipeline, and device
+    arrays of that size in chunks on two compute streams; the values must equal each other and those of calls on
+    single chunks (below 2^21, one stream) bit for bit, in both precisions of the fractional term."""
     torch = pytest.importorskip("torch")
     verts, idx, bnd, q, x0 = synth.open_icosphere(seed=2, level=4, grid=128)
     assert len(q) >= 1 << 21
@@ -263,6 +264,12 @@ def test_host_arrays_pipelined_equal_device_arrays(gwn):
         od = torch.empty(len(q), dtype=torch.float64, device="cuda")
         gwn.eval_gwnr_mesh_batch(disp, isect, qd, od, x0, torch.from_numpy(bnd).cuda())
         disp.synchronize()
+        # the first two chunks (2^20 queries each here) as calls of their own
+        for a, b in ((0, 1 << 20), (1 << 20, 1 << 21)):
+            part = torch.empty(b - a, dtype=torch.float64, device="cuda")
+            gwn.eval_gwnr_mesh_batch(disp, isect, qd[a:b].contiguous(), part, x0, torch.from_numpy(bnd).cuda())
+            disp.synchronize()
+            assert torch.equal(part, od[a:b]), (prec, a)
         qh = torch.from_numpy(q).pin_memory().numpy()
         oh = torch.empty(len(q), dtype=torch.float64).pin_memory().numpy()
         gwn.eval_gwnr_mesh_batch(disp, isect, qh, oh, x0, bnd)
