@@ -29,6 +29,14 @@ int fractional_run(Context& ctx, const T* d_pos, int64_t n, T* d_out, const int3
 // same order).  out = fractional term + counts (counts may be null).
 int frac_mixed_robust_pf(Context& ctx, const double* d_pos, int64_t n, double* d_out, const int32_t* d_counts,
                          const double* d_raw, int64_t n_seg, const void* rseg);
+// The same with the counts made chunk by chunk: the queries run in 8 chunks whose kernels alternate between the
+// context's stream and a second compute stream (count(user, ctx, chunk queries, m, chunk counts) launches a chunk's
+// counts on ctx.stream, then the chunk's fractional kernel adds them), so that one chunk's counts overlap another's
+// fractional term.  d_counts: n ints of scratch.
+using ChunkCounts = int (*)(void* user, Context& ctx, const double* d_pos, int64_t m, int32_t* d_counts);
+int frac_mixed_robust_pf_chunked(Context& ctx, const double* d_pos, int64_t n, double* d_out, int32_t* d_counts,
+                                 const double* d_raw, int64_t n_seg, const void* rseg, ChunkCounts count,
+                                 void* user);
 
 // Integer term over a BVH for `n` device-resident queries.
 template <class T>
