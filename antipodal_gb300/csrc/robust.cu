@@ -195,6 +195,27 @@ __global__ void k_frac_plus_counts(const double* __restrict__ frac, const int32_
         out[i] = frac[i] + double(counts[i]);
 }
 
+// The exact_float counts of one chunk of queries through the cell grid (frac_mixed_robust_pf_chunked's callback).
+struct RobustCountJob
+{
+    const Robust* r;
+    Quant qz;
+    Frame32 f;
+};
+
+int robust_count_chunk(void* user, Context& ctx, const double* d_pos, int64_t m, int32_t* d_counts)
+{
+    RobustCountJob const& j = *static_cast<const RobustCountJob*>(user);
+    Robust const& r = *j.r;
+    int const grid = int(std::min<int64_t>(div_up(m, kRobBlock), int64_t(ctx.sm_count) * 16));
+    AGWN_TRY(ctx.launch_begin(AGWN_K_ROBUST));
+    k_robust_cells<double, PF><<<grid, kRobBlock, 0, ctx.stream>>>(
+        static_cast<const BvhNode*>(r.hier.nodes.ptr), static_cast<const typename PF::C*>(r.tri),
+        static_cast<const float4*>(r.hier.leaf_uv.ptr), float(r.hier.scale), j.f, cell_view(r.cells), j.qz, d_pos, m,
+        d_counts, ctx.d_flags, ctx.timing ? ctx.d_counters : nullptr);
+    return ctx.launch_end(AGWN_K_ROBUST);
+}
+
 template <class T, class P>
 int robust_run(Context& ctx, const Robust& r, const T* d_pos, int64_t n, T* d_out, int32_t* d_counts, T* d_frac,
                bool counts_ready = false)
@@ -202,6 +223,32 @@ int robust_run(Context& ctx, const Robust& r, const T* d_pos, int64_t n, T* d_ou
     using C = typename P::C;
     Quant qz{{r.center[0], r.center[1], r.center[2]}, r.scale};
     cudaStream_t const st = ctx.stream;
+    if constexpr (std::is_same_v<P, PF> && std::is_same_v<T, double>)
+    {
+        // mixed exact_float over many queries: counts and fractional term in chunks on two streams, so that one
+        // chunk's counts (FP64 predicates) overlap another chunk's fractional term (FP32 pairs)
+        if (!counts_ready && !d_frac && n >= (int64_t(1) << 21) && r.n_tri > 1 && ctx.integer_cells &&
+            ctx.robust_mode == AGWN_ROBUST_MIXED && r.n_seg > 0 && r.n_seg < (int64_t(1) << 24))
+        {
+            if (!r.cells.valid)
+                AGWN_TRY(build_cells(ctx, r.hier, float(r.hier.scale), r.cells));
+            if (r.cells.valid)
+            {
+                double* raw = nullptr;
+                AGWN_TRY(ctx.scratch_reserve(S_MISC2, sizeof(double) * 7 * size_t(r.n_seg),
+                                             reinterpret_cast<void**>(&raw)));
+                AGWN_TRY(ctx.launch_begin(AGWN_K_OTHER));
+                k_rseg_raw<<<int(std::min<int64_t>(div_up(r.n_seg, 256), 4 * ctx.sm_count)), 256, 0, st>>>(
+                    static_cast<const RSeg<double>*>(r.seg), r.n_seg, raw);
+                AGWN_TRY(ctx.launch_end(AGWN_K_OTHER));
+                RobustCountJob job{&r, qz, {}};
+                for (int k = 0; k < 9; ++k)
+                    job.f.r[k] = r.hier.frame[k];
+                return frac_mixed_robust_pf_chunked(ctx, d_pos, n, d_out, d_counts, raw, r.n_seg, r.seg,
+                                                    &robust_count_chunk, &job);
+            }
+        }
+    }
     if (counts_ready)
         ;
     else if (r.n_tri == 0)

@@ -192,6 +192,37 @@ def test_robust_mixed_exact_float_matches_exact(gwn, disp):
             assert d.max() <= 1e-7, (kind, k, d.max())
 
 
+def test_robust_mixed_exact_float_chunked_equals_single_chunks(gwn, disp):
+    """exact_float mixed over 2^21 or more queries runs counts and fractional term in chunks on two compute streams;
+    the values must equal those of calls on single chunks (below 2^21, one stream) bit for bit, and the counts those
+    of the separate-output path."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(41)
+    v, i = synth.noisy_mesh("torus", 8000, 9, rng)
+    b = synth.boundary_segments(v, i)
+    q = synth.grid_queries(v.min(0), v.max(0), 129, 1.2)
+    assert len(q) >= 1 << 21
+    r = gwn.CudaRobustMeshGwn(disp, v, i, b, precision="exact_float")
+    try:
+        disp.set_robust_precision("mixed")
+        qd = torch.from_numpy(q).cuda()
+        out = torch.empty(len(q), dtype=torch.float64, device="cuda")
+        r.evaluate(qd, out)
+        disp.synchronize()
+        for a, e in ((0, 1 << 20), (1 << 20, 1 << 21)):
+            part = torch.empty(e - a, dtype=torch.float64, device="cuda")
+            r.evaluate(qd[a:e].contiguous(), part)
+            disp.synchronize()
+            assert torch.equal(part, out[a:e]), a
+        # the separate outputs (counts and fractional term) take the unchunked path: same values
+        o, c, f = np.empty(len(q)), np.empty(len(q), np.int32), np.empty(len(q))
+        r.evaluate(q, o, c, f)
+        assert np.array_equal(o, out.cpu().numpy())
+    finally:
+        disp.set_robust_precision("exact")
+        r.close()
+
+
 @pytest.mark.parametrize("pol", ["int64_grid", "int128_grid", "exact_float"])
 def test_robust_counts_cells_equal_the_walk(gwn, pol):
     """The robust counts with candidate leaves from the cell grid (default) and from the hierarchy walk (option 0):
