@@ -19,10 +19,12 @@
 // own net at dyadic parameters, so that rounding does not grow with the depth of a split), hence each decision,
 // and the count, holds for the exact map.  Unlike Newton's iteration the degree needs no root to be isolated: two
 // crossings near a fold of the map (a ray almost tangent to the patch) cancel in it as they should.
-// Each pair runs first in float with a margin of 2^-17 of the coordinates' scale; a decision that float cannot
-// make (a boundary image or the surface within that margin of the ray) sends the pair to FP64 with a margin of
-// 2^-42.  What FP64 cannot make either is degenerate (the ray on a cell boundary's image within 2^-42 of the scale,
-// or the query that close to the surface): it is decided by a fixed rule and counted.
+// Each pair runs in float with a margin of 2^-17 of the coordinates' scale; a decision that float cannot make (a
+// boundary image or the surface within that margin of the ray) is taken in FP64, with a margin of 2^-42, for that
+// cell alone: its winding, or the walk of its subtree.  Since every decision holds for the exact patch, the cells'
+// contributions add up to the count whichever arithmetic decided them.  What FP64 cannot decide either is
+// degenerate (the ray on a cell boundary's image within 2^-42 of the scale, or the query that close to the
+// surface): it is decided by a fixed rule and counted.
 
 #include "agwn_internal.cuh"
 #include "hier.cuh"
@@ -193,15 +195,37 @@ __device__ __forceinline__ int net_winding(const R (&x)[16], const R (&y)[16], R
     return w;
 }
 
+// After cell (level, iu, iv) is done: the next cell of the walk over the subtree of level root, or false at its end.
+template <class I>
+__device__ __forceinline__ bool walk_next(int& level, I& iu, I& iv, int root)
+{
+    while (level > root && (iu & 1) && (iv & 1))
+    {
+        iu >>= 1;
+        iv >>= 1;
+        --level;
+    }
+    if (level == root)
+        return false;
+    if (iu & 1)
+    {
+        iu -= 1;
+        iv += 1;
+    }
+    else
+        iu += 1;
+    return true;
+}
+
 // One step of the walk over a patch's parameter cells, depth first without a stack: cell (level, iu, iv), children
-// 2 iu + (0|1), 2 iv + (0|1) in the order (0,0), (1,0), (0,1), (1,1).  The step tests the cell (c(j, k): the
-// patch's net relative to the query in the ray frame, k = x, y across the ray and w along it; m the margin), adds
-// its boundary's winding number to sum when it lies in front, and moves to the next cell.  Returns false when the
-// walk is over: every cell done, or (float) a decision the margin did not allow, counted in unresolved (the result
-// is then void and the pair is redone in FP64).  pieces counts the boundary-cubic pieces tested.
+// 2 iu + (0|1), 2 iv + (0|1) in the order (0,0), (1,0), (0,1), (1,1), the walk covering the subtree of one cell of
+// level root.  The step tests the cell (c(j, k): the patch's net relative to the query in the ray frame, k = x, y
+// across the ray and w along it; m the margin), adds its boundary's winding number to sum when it lies in front,
+// and moves to the next cell.  Returns false when the walk is over: every cell done, or (float) a decision the
+// margin did not allow, counted in unresolved.  pieces counts the boundary-cubic pieces tested.
 template <class R, class Net, class I>
 __device__ __forceinline__ bool walk_cell(Net const& c, R m, int& level, I& iu, I& iv, int& sum, int& unresolved,
-                                          int& pieces)
+                                          int& pieces, int root = 0)
 {
     using A = PatchArith<R>;
     R x[16], y[16], lo, hi;
@@ -236,46 +260,95 @@ __device__ __forceinline__ bool walk_cell(Net const& c, R m, int& level, I& iu, 
                 return false;
         }
     }
-    while (level > 0 && (iu & 1) && (iv & 1))
-    {
-        iu >>= 1;
-        iv >>= 1;
-        --level;
-    }
-    if (level == 0)
-        return false;
-    if (iu & 1)
-    {
-        iu -= 1;
-        iv += 1;
-    }
-    else
-        iu += 1;
-    return true;
+    return walk_next(level, iu, iv, root);
 }
 
 // Signed crossings in front of the query with one patch: the whole walk.  unresolved counts the decisions left to
 // the fixed rule (FP64) or that void the result (float); cells and pieces count the work.
 template <class R, class Net>
-__device__ int patch_degree(Net const& c, R m, int& unresolved, int& cells, int& pieces)
+__device__ int patch_degree(Net const& c, R m, int& unresolved, int& cells, int& pieces, int root = 0,
+                            typename PatchArith<R>::Index root_iu = 0, typename PatchArith<R>::Index root_iv = 0)
 {
-    int sum = 0, level = 0;
-    typename PatchArith<R>::Index iu = 0, iv = 0;
+    int sum = 0, level = root;
+    typename PatchArith<R>::Index iu = root_iu, iv = root_iv;
     bool more = true;
     while (more)
     {
         ++cells;
-        more = walk_cell(c, m, level, iu, iv, sum, unresolved, pieces);
+        more = walk_cell(c, m, level, iu, iv, sum, unresolved, pieces, root);
     }
     return sum;
 }
 
-// The FP64 pass of one pair: the patch's FP64 net (ray frame) relative to the query, margin 2^-42 of `scale`.
-__device__ __noinline__ int patch_degree_fp64(const double* __restrict__ net, double qx, double qy, double qw,
-                                              double scale, int& degenerate, int& cells, int& pieces)
+// The FP64 walk of the subtree of one cell (level, iu, iv) of a pair (a cell whose depth float could not resolve):
+// the patch's FP64 net (ray frame) relative to the query, margin 2^-42 of `scale`.
+__device__ __noinline__ int patch_subtree_fp64(const double* __restrict__ net, double qx, double qy, double qw,
+                                               double scale, int level, uint64_t iu, uint64_t iv, int& degenerate,
+                                               int& cells, int& pieces)
 {
     auto const c = [=](int j, int k) { return net[3 * j + k] - (k == 0 ? qx : (k == 1 ? qy : qw)); };
-    return patch_degree(c, scale * 0x1p-42, degenerate, cells, pieces);
+    return patch_degree(c, scale * 0x1p-42, degenerate, cells, pieces, level, iu, iv);
+}
+
+// The FP64 winding number of one cell's boundary (a cell in front whose float winding the margin did not allow).
+__device__ __noinline__ int patch_winding_fp64(const double* __restrict__ net, double qx, double qy, double qw,
+                                               double scale, int level, uint64_t iu, uint64_t iv, int& degenerate,
+                                               int& pieces)
+{
+    auto const c = [=](int j, int k) { return net[3 * j + k] - (k == 0 ? qx : (k == 1 ? qy : qw)); };
+    double x[16], y[16];
+    cell_net(c, 0, level, iu, iv, x);
+    cell_net(c, 1, level, iu, iv, y);
+    return net_winding(x, y, scale * 0x1p-42, degenerate, pieces);
+}
+
+// The float winding number of one cell's boundary, c its patch's float net relative to the query.
+template <class Net>
+__device__ __noinline__ int patch_winding_f(Net const c, float m, int level, uint32_t iu, uint32_t iv,
+                                            int& unresolved, int& pieces)
+{
+    float x[16], y[16];
+    cell_net(c, 0, level, iu, iv, x);
+    cell_net(c, 1, level, iu, iv, y);
+    return net_winding(x, y, m, unresolved, pieces);
+}
+
+// The float walk's step with the work that varies most from lane to lane taken out, for the queued kernel: a cell
+// in front is left to a winding job (event 1) and a cell whose depth float cannot resolve to an FP64 job over its
+// subtree (event 2), both for the cell (level, iu, iv) as it was on entry; otherwise as walk_cell.
+template <class Net>
+__device__ __forceinline__ bool walk_cell_queued(Net const& c, float m, int& level, uint32_t& iu, uint32_t& iv,
+                                                 int& event)
+{
+    using A = PatchArith<float>;
+    event = 0;
+    float x[16], lo, hi;
+    cell_net(c, 0, level, iu, iv, x);
+    range16(x, lo, hi);
+    if (!(lo > m || hi < -m))
+    {
+        cell_net(c, 1, level, iu, iv, x);
+        range16(x, lo, hi);
+        if (!(lo > m || hi < -m))
+        {
+            cell_net(c, 2, level, iu, iv, x);
+            range16(x, lo, hi);
+            if (lo >= m)
+                event = 1;
+            else if (hi >= -m)
+            {
+                if (level < A::kMaxCellLevel && hi - lo >= 4.f * m)
+                {
+                    ++level;
+                    iu *= 2;
+                    iv *= 2;
+                    return true;
+                }
+                event = 2;
+            }
+        }
+    }
+    return walk_next(level, iu, iv, 0);
 }
 
 // The patches' control points in the ray frame (rows of f): net in FP64, netf rounded to float, and per patch
@@ -307,11 +380,15 @@ __global__ void k_patch_frame(const double* __restrict__ ctrl, int64_t n_patches
     }
 }
 
-// Pairs are queued per warp: a warp owns 32 queries (one per lane), tests them against the patches of the
-// shared-memory tile one patch at a time, and appends the (query, patch) pairs that pass the box test to its queue;
-// every lane that has no pair takes the next one, and each turn of the loop runs one cell of every lane's walk, so
-// the lanes stay busy however unevenly the work falls on the pairs.  Pairs that float cannot decide go to a second
-// queue and run in FP64 32 at a time.  The tile holds each patch's float net at a stride of 49 floats (lanes on
+// Work is queued per warp, so that the lanes stay busy however unevenly it falls.  A warp owns 32 queries (one per
+// lane) and tests them against the patches of the shared-memory tile one patch at a time; the (query, patch) pairs
+// that pass the box test go to a ring of pairs.  Every lane that has no pair takes the next one, and each turn of
+// the loop runs one cell of every lane's float walk.  The two kinds of work whose length varies most leave the walk
+// as jobs of their own, evaluated 32 at a time, one per lane, when 32 have gathered: the winding number of a cell
+// in front (its boundary's control points blossomed again from the patch), and the FP64 walk of the subtree of a
+// cell whose depth float could not resolve.  A winding that float cannot decide is taken in FP64 for that cell.
+// Every decision, float or FP64, holds for the exact patch, so the cells' contributions add up to the count
+// whichever arithmetic decided them.  The tile holds each patch's float net at a stride of 49 floats (lanes on
 // different patches then fall in different banks) and its box.
 constexpr int kPatchWarps = 4;
 constexpr int kPatchQueue = 64;   // ring size: below 32 entries are topped up by at most 32, and drained to below 32
@@ -320,28 +397,62 @@ constexpr int kPatchTileMax = 512; // patches per shared-memory tile
 
 struct PatchWarp
 {
-    double qd[32][3];   // the queries in the ray frame (FP64)
-    float qf[32][3];    // ... in float
-    float qscale[32];   // largest |coordinate| of each
+    double qd[32][3];              // the queries in the ray frame (FP64)
+    float qf[32][3];               // ... in float
+    float qscale[32];              // largest |coordinate| of each
     int sum[32];
     int deg[32];
-    uint32_t queue[kPatchQueue];  // (patch in tile << 5) | lane
-    uint32_t fqueue[kPatchQueue]; // the same, for FP64
+    uint32_t queue[kPatchQueue];   // pairs: (patch in tile << 5) | lane
+    uint32_t jcell[2][kPatchQueue]; // jobs, [0] windings, [1] FP64 subtrees: lane | patch << 5 | level << 14 ...
+    uint32_t juv[2][kPatchQueue];   // ... and iu | iv << 16
 };
 
-// The FP64 walk of the queued pairs fq[head .. head + count) (count <= 32, lane j takes entry j).
-__device__ __forceinline__ void patch_fp64_batch(PatchWarp& w, const double* __restrict__ net64, const float* s_box,
-                                                 int64_t tile_base, uint32_t head, uint32_t count, int lane,
-                                                 int& n_cells, int& n_pieces)
+// Margin of the float walk for query src and patch p.  With S the coordinates' scale and u = 2^-24, a float net value
+// relative to the query errs by at most 2 u S (the net's and the query's rounding, the difference), each level of
+// lerps adds 3 u S, so a cell's net errs by 20 u S (6 levels) and a boundary piece's control points by 29 u S (3
+// more); the piece, its chord and the straight joins between their ends then keep within 41 u S of the piece's box.
+// The margin m = 2^-17 S = 128 u S is three times that.
+__device__ __forceinline__ float patch_margin(PatchWarp const& w, const float* s_box, int src, int p)
+{
+    return 7.62939453125e-6f * (w.qscale[src] + s_box[8 * p + 6]);
+}
+
+// The jobs j[head .. head + count) of kind 0 (windings) or 1 (FP64 subtrees), count <= 32, lane k taking entry k.
+__device__ __forceinline__ void patch_jobs(PatchWarp& w, int kind, const double* __restrict__ net64,
+                                           const float* s_net, const float* s_box, int64_t tile_base, uint32_t head,
+                                           uint32_t count, int lane, int& n_cells, int& n_pieces, int& n_fp64)
 {
     if (uint32_t(lane) < count)
     {
-        uint32_t const e = w.fqueue[(head + lane) & (kPatchQueue - 1)];
-        int const src = int(e & 31u), p = int(e >> 5);
-        int deg = 0;
-        int const s = patch_degree_fp64(net64 + 48 * (tile_base + p), w.qd[src][0], w.qd[src][1], w.qd[src][2],
-                                        double(w.qscale[src]) + double(s_box[8 * p + 6]), deg, n_cells, n_pieces);
-        atomicAdd(&w.sum[src], s);
+        uint32_t const e = w.jcell[kind][(head + lane) & (kPatchQueue - 1)];
+        uint32_t const uv = w.juv[kind][(head + lane) & (kPatchQueue - 1)];
+        int const src = int(e & 31u), p = int((e >> 5) & 511u), level = int(e >> 14);
+        uint32_t const iu = uv & 0xffffu, iv = uv >> 16;
+        double const scale = double(w.qscale[src]) + double(s_box[8 * p + 6]);
+        const double* nk64 = net64 + 48 * (tile_base + p);
+        int s = 0, deg = 0;
+        if (kind == 0)
+        {
+            const float* nk = s_net + p * kNetStride;
+            float const qx = w.qf[src][0], qy = w.qf[src][1], qw = w.qf[src][2];
+            auto const c = [=](int j, int kk) { return nk[3 * j + kk] - (kk == 0 ? qx : (kk == 1 ? qy : qw)); };
+            int unresolved = 0;
+            s = patch_winding_f(c, patch_margin(w, s_box, src, p), level, iu, iv, unresolved, n_pieces);
+            if (unresolved)
+            {
+                ++n_fp64;
+                s = patch_winding_fp64(nk64, w.qd[src][0], w.qd[src][1], w.qd[src][2], scale, level, iu, iv, deg,
+                                       n_pieces);
+            }
+        }
+        else
+        {
+            ++n_fp64;
+            s = patch_subtree_fp64(nk64, w.qd[src][0], w.qd[src][1], w.qd[src][2], scale, level, iu, iv, deg, n_cells,
+                                   n_pieces);
+        }
+        if (s)
+            atomicAdd(&w.sum[src], s);
         if (deg)
             atomicAdd(&w.deg[src], deg);
     }
@@ -350,7 +461,7 @@ __device__ __forceinline__ void patch_fp64_batch(PatchWarp& w, const double* __r
 
 // counts / add: the crossing count is written to counts (int) or added to add (the fractional term already there);
 // degenerate (nullable): per query, the decisions left to the fixed rule; stats (nullable): adds pairs past the box
-// test, cells, pieces and FP64 pairs to stats[0..3].
+// test, cells, pieces and FP64 jobs to stats[0..3].
 __global__ void __launch_bounds__(32 * kPatchWarps) k_patch_count(
     const double* __restrict__ net64, const float* __restrict__ netf, const float* __restrict__ boxf,
     int64_t n_patches, int tile, Frame64 f, const double* __restrict__ pos, int64_t n, int32_t* __restrict__ counts,
@@ -400,11 +511,6 @@ __global__ void __launch_bounds__(32 * kPatchWarps) k_patch_count(
         w.qf[lane][0] = my_x;
         w.qf[lane][1] = my_y;
         w.qf[lane][2] = my_w;
-        // Float margin: with S the coordinates' scale and u = 2^-24, a float net value relative to the query errs by
-        // at most 2 u S (the net's and the query's rounding, the difference), each level of lerps adds 3 u S, so a
-        // cell's net errs by 20 u S (6 levels) and a boundary piece's control points by 29 u S (3 more); the
-        // piece, its chord and the straight joins between their ends then keep within 41 u S of the piece's box.
-        // The margin m = 2^-17 S = 128 u S is three times that.
         w.qscale[lane] = my_scale;
         w.sum[lane] = 0;
         w.deg[lane] = 0;
@@ -420,12 +526,12 @@ __global__ void __launch_bounds__(32 * kPatchWarps) k_patch_count(
             }
             int64_t const tile_base = int64_t(pt) * tile;
             int const tn = int(n_patches - tile_base < tile ? n_patches - tile_base : int64_t(tile));
-            uint32_t head = 0, tail = 0, fhead = 0, ftail = 0;
+            uint32_t head = 0, tail = 0, jhead[2] = {0, 0}, jtail[2] = {0, 0};
             int kn = 0;
             // this lane's pair: its queue entry (or -1), its query and margin, and the walk's state
             int cur = -1;
             float cx = 0.f, cy = 0.f, cw = 0.f, cm = 0.f;
-            int level = 0, csum = 0, unresolved = 0;
+            int level = 0;
             uint32_t iu = 0, iv = 0;
             for (;;)
             {
@@ -455,16 +561,18 @@ __global__ void __launch_bounds__(32 * kPatchWarps) k_patch_count(
                     cx = w.qf[src][0];
                     cy = w.qf[src][1];
                     cw = w.qf[src][2];
-                    cm = 7.62939453125e-6f * (w.qscale[src] + s_box[8 * p + 6]);
+                    cm = patch_margin(w, s_box, src, p);
                     level = 0;
                     iu = iv = 0;
-                    csum = 0;
-                    unresolved = 0;
                     ++n_pairs;
                 }
                 head += min(uint32_t(__popc(ib)), tail - head);
                 if (__ballot_sync(0xffffffffu, cur >= 0) == 0)
                     break; // queue empty and every patch of the tile tested
+                // one cell of every lane's walk
+                int event = 0;
+                int const e_level = level;
+                uint32_t const e_iu = iu, e_iv = iv;
                 bool finished = false;
                 if (cur >= 0)
                 {
@@ -472,27 +580,39 @@ __global__ void __launch_bounds__(32 * kPatchWarps) k_patch_count(
                     auto const c = [=](int j, int kk)
                     { return nk[3 * j + kk] - (kk == 0 ? cx : (kk == 1 ? cy : cw)); };
                     ++n_cells;
-                    finished = !walk_cell(c, cm, level, iu, iv, csum, unresolved, n_pieces);
+                    finished = !walk_cell_queued(c, cm, level, iu, iv, event);
                 }
-                bool const to_fp64 = finished && unresolved;
-                unsigned const fb = __ballot_sync(0xffffffffu, to_fp64);
-                if (to_fp64)
-                    w.fqueue[(ftail + __popc(fb & lt)) & (kPatchQueue - 1)] = uint32_t(cur);
-                else if (finished)
-                    atomicAdd(&w.sum[cur & 31], csum);
-                ftail += __popc(fb);
-                n_fp64 += to_fp64 ? 1 : 0;
+                // the cell's job, if it left one
+#pragma unroll
+                for (int kind = 0; kind < 2; ++kind)
+                {
+                    bool const push = event == kind + 1;
+                    unsigned const pb = __ballot_sync(0xffffffffu, push);
+                    if (push)
+                    {
+                        uint32_t const slot = (jtail[kind] + __popc(pb & lt)) & (kPatchQueue - 1);
+                        w.jcell[kind][slot] = uint32_t(cur & 31) | (uint32_t(cur >> 5) << 5) | (uint32_t(e_level) << 14);
+                        w.juv[kind][slot] = e_iu | (e_iv << 16);
+                    }
+                    jtail[kind] += __popc(pb);
+                }
                 if (finished)
                     cur = -1;
                 __syncwarp();
-                if (ftail - fhead >= 32)
-                {
-                    patch_fp64_batch(w, net64, s_box, tile_base, fhead, 32, lane, n_cells, n_pieces);
-                    fhead += 32;
-                }
+#pragma unroll
+                for (int kind = 0; kind < 2; ++kind)
+                    if (jtail[kind] - jhead[kind] >= 32)
+                    {
+                        patch_jobs(w, kind, net64, s_net, s_box, tile_base, jhead[kind], 32, lane, n_cells, n_pieces,
+                                   n_fp64);
+                        jhead[kind] += 32;
+                    }
             }
-            if (ftail != fhead)
-                patch_fp64_batch(w, net64, s_box, tile_base, fhead, ftail - fhead, lane, n_cells, n_pieces);
+#pragma unroll
+            for (int kind = 0; kind < 2; ++kind)
+                if (jtail[kind] != jhead[kind])
+                    patch_jobs(w, kind, net64, s_net, s_box, tile_base, jhead[kind], jtail[kind] - jhead[kind], lane,
+                               n_cells, n_pieces, n_fp64);
         }
         __syncwarp();
         if (valid)

@@ -802,7 +802,7 @@ def run_param(args, ag, torch, stream, disp, timed):
                              "full_gwn_ms_per_step": ms + ms_int,
                              "per_query": {"pairs_past_box": pst["pairs"] / Q, "cells": pst["cells"] / Q,
                                            "pieces": pst["pieces"] / Q},
-                             "fp64_pair_fraction": pst["fp64_pairs"] / max(1, pst["pairs"]),
+                             "fp64_jobs_per_pair": pst["fp64_pairs"] / max(1, pst["pairs"]),
                              "degenerate_queries": n_degenerate,
                              "roofline": {"bound": "fp32", "achieved": int_flop / (ms_int * 1e-3) / 1e12,
                                           "peak": fp32_peak, "unit": "TFLOP/s",

@@ -147,7 +147,8 @@ typedef struct agwn_stats
     int64_t patch_pairs;              /* (query, patch) pairs past the box test                                */
     int64_t patch_cells;              /* parameter cells whose control net was blossomed and tested            */
     int64_t patch_pieces;             /* boundary-cubic pieces blossomed and tested for the winding numbers    */
-    int64_t patch_fp64_pairs;         /* pairs that float could not decide, redone in FP64                     */
+    int64_t patch_fp64_pairs;         /* decisions float could not make, taken in FP64 (a cell's winding or   
+                                         a cell's subtree)                                                     */
 } agwn_stats;
 /* Reads (synchronising the stream first) and optionally resets the accumulated statistics. */
 int agwn_context_get_stats(agwn_context* ctx, agwn_stats* out, int reset);
@@ -361,9 +362,10 @@ int agwn_param_panel_features_bezier3_f64(agwn_context* ctx, const double* posit
  * run counter-clockwise in (u, v) make fractional + integer the winding number.  The count over a parameter cell
  * that lies in front of the query is the topological degree of the patch's projection at the ray: the winding
  * number of the cell boundary's image (4 cubics) about it.  Cells are split while their depth range holds 0 and
- * their control box holds the ray; every box test keeps a margin above its rounding (float first, FP64 where float
- * cannot decide), so the count is exact for the exact patch except in the degenerate cases: the ray within 2^-42
- * of the coordinates' scale of a cell boundary's image, or the query that close to the surface.
+ * their control box holds the ray; every box test keeps a margin above its rounding (float first, FP64 for the
+ * cells whose decision float cannot make), so the count is exact for the exact patch except in the degenerate
+ * cases: the ray within 2^-42 of the coordinates' scale of a cell boundary's image, or the query that close to the
+ * surface.
  * control_points: n_patches x 4 x 4 x 3 doubles, P[patch][i = v index][j = u index][xyz] (host or device); the
  * patches are copied to the device. */
 typedef struct agwn_patches agwn_patches;
