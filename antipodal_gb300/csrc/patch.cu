@@ -313,41 +313,44 @@ __device__ __noinline__ int patch_winding_f(Net const c, float m, int level, uin
     return net_winding(x, y, m, unresolved, pieces);
 }
 
-// The float walk's step with the work that varies most from lane to lane taken out, for the queued kernel: a cell
-// in front is left to a winding job (event 1) and a cell whose depth float cannot resolve to an FP64 job over its
-// subtree (event 2), both for the cell (level, iu, iv) as it was on entry; otherwise as walk_cell.
+// One coordinate (phase 0: x, 1: y, 2: w) of the float walk's current cell, c(j, 0) giving that coordinate of the
+// patch's net relative to the query.  x and y drop the cell when their box misses the origin (the walk moves to the
+// next cell) and otherwise pass it to the next phase.  w decides: a cell in front is left to a winding job (event 1),
+// a cell whose depth float cannot resolve to an FP64 job over its subtree (event 2), both for the cell as it was on
+// entry, and a cell whose depth changes sign is split.  Every call costs the same, so lanes in different phases stay
+// together.
 template <class Net>
-__device__ __forceinline__ bool walk_cell_queued(Net const& c, float m, int& level, uint32_t& iu, uint32_t& iv,
-                                                 int& event)
+__device__ __forceinline__ bool walk_phase(Net const& c, float m, int& level, uint32_t& iu, uint32_t& iv, int& phase,
+                                           int& event)
 {
     using A = PatchArith<float>;
     event = 0;
     float x[16], lo, hi;
     cell_net(c, 0, level, iu, iv, x);
     range16(x, lo, hi);
-    if (!(lo > m || hi < -m))
+    if (phase < 2)
     {
-        cell_net(c, 1, level, iu, iv, x);
-        range16(x, lo, hi);
         if (!(lo > m || hi < -m))
         {
-            cell_net(c, 2, level, iu, iv, x);
-            range16(x, lo, hi);
-            if (lo >= m)
-                event = 1;
-            else if (hi >= -m)
-            {
-                if (level < A::kMaxCellLevel && hi - lo >= 4.f * m)
-                {
-                    ++level;
-                    iu *= 2;
-                    iv *= 2;
-                    return true;
-                }
-                event = 2;
-            }
+            ++phase;
+            return true;
         }
     }
+    else if (lo >= m)
+        event = 1;
+    else if (hi >= -m)
+    {
+        if (level < A::kMaxCellLevel && hi - lo >= 4.f * m)
+        {
+            ++level;
+            iu *= 2;
+            iv *= 2;
+            phase = 0;
+            return true;
+        }
+        event = 2;
+    }
+    phase = 0;
     return walk_next(level, iu, iv, 0);
 }
 
@@ -383,7 +386,7 @@ __global__ void k_patch_frame(const double* __restrict__ ctrl, int64_t n_patches
 // Work is queued per warp, so that the lanes stay busy however unevenly it falls.  A warp owns 32 queries (one per
 // lane) and tests them against the patches of the shared-memory tile one patch at a time; the (query, patch) pairs
 // that pass the box test go to a ring of pairs.  Every lane that has no pair takes the next one, and each turn of
-// the loop runs one cell of every lane's float walk.  The two kinds of work whose length varies most leave the walk
+// the loop runs one coordinate of the current cell of every lane's float walk (walk_phase).  The two kinds of work whose length varies most leave the walk
 // as jobs of their own, evaluated 32 at a time, one per lane, when 32 have gathered: the winding number of a cell
 // in front (its boundary's control points blossomed again from the patch), and the FP64 walk of the subtree of a
 // cell whose depth float could not resolve.  A winding that float cannot decide is taken in FP64 for that cell.
@@ -531,7 +534,7 @@ __global__ void __launch_bounds__(32 * kPatchWarps) k_patch_count(
             // this lane's pair: its queue entry (or -1), its query and margin, and the walk's state
             int cur = -1;
             float cx = 0.f, cy = 0.f, cw = 0.f, cm = 0.f;
-            int level = 0;
+            int level = 0, phase = 0;
             uint32_t iu = 0, iv = 0;
             for (;;)
             {
@@ -563,6 +566,7 @@ __global__ void __launch_bounds__(32 * kPatchWarps) k_patch_count(
                     cw = w.qf[src][2];
                     cm = patch_margin(w, s_box, src, p);
                     level = 0;
+                    phase = 0;
                     iu = iv = 0;
                     ++n_pairs;
                 }
@@ -576,11 +580,12 @@ __global__ void __launch_bounds__(32 * kPatchWarps) k_patch_count(
                 bool finished = false;
                 if (cur >= 0)
                 {
-                    const float* nk = s_net + (cur >> 5) * kNetStride;
-                    auto const c = [=](int j, int kk)
-                    { return nk[3 * j + kk] - (kk == 0 ? cx : (kk == 1 ? cy : cw)); };
-                    ++n_cells;
-                    finished = !walk_cell_queued(c, cm, level, iu, iv, event);
+                    // this phase's coordinate of the net relative to the query
+                    const float* nk = s_net + (cur >> 5) * kNetStride + phase;
+                    float const qk = phase == 0 ? cx : (phase == 1 ? cy : cw);
+                    auto const c = [=](int j, int) { return nk[3 * j] - qk; };
+                    n_cells += phase == 0;
+                    finished = !walk_phase(c, cm, level, iu, iv, phase, event);
                 }
                 // the cell's job, if it left one
 #pragma unroll
