@@ -61,7 +61,7 @@ def parse():
                          "takes about 100 s per step)")
     ap.add_argument("--labels", type=float, default=1e7,
                     help="param workload: plain-integrator depth labels the proposal network is trained on")
-    ap.add_argument("--train-steps", type=int, default=4000, help="param workload: training steps (batch 8192)")
+    ap.add_argument("--train-steps", type=int, default=32000, help="param workload: training steps (batch 8192)")
     ap.add_argument("--patches", type=int, default=256, help="param workload: bicubic patches (4 curves each)")
     ap.add_argument("--integer-cells", type=int, choices=[0, 1], default=1,
                     help="mesh workload: 1 looks the integer term's candidates up in the cell grid (default), 0 walks "
@@ -721,7 +721,10 @@ def run_param(args, ag, torch, stream, disp, timed):
     Q, Cn = len(q), len(curves)
     # the network: trained on labels of the plain integrator (the shallowest accepted depth per pair) on other
     # seeded queries and patches, args.labels of them
-    net = ag.LearnedGK15Proposal(disp, seed=3, n_classes=11, alpha=0.02)
+    # alpha 0.9: the labels are each pair's shallowest accepted depth, a lower bound on the cheapest start depth (most
+    # of a pair's tree lies deeper), so starting near the upper end of the predicted distribution evaluates the fewest
+    # panels; every evaluated panel is still verified by the plain test
+    net = ag.LearnedGK15Proposal(disp, seed=3, n_classes=11, alpha=0.9)
     n_train_q = max(16, int(round(args.labels / (256 * 4))))
     tc, tq, tx = synth.bezier_patches(seed=101, n_patches=256, n_queries=n_train_q)
     t0 = time.perf_counter()

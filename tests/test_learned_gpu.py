@@ -125,6 +125,17 @@ def test_ablation_proposal_saves_panels_at_equal_accuracy(gwn, trained):
     assert np.array_equal(got[exact_rows], plain[exact_rows])
     # elsewhere both trees are partitions of [0, 1] whose accepted error estimates sum to <= tol per curve
     assert np.abs(got - plain).max() <= 2 * cfg.tol * c / (4 * np.pi)
+    # a larger alpha starts deeper (the labels are the shallowest accepted depth, a lower bound on the cheapest start:
+    # most of a pair's tree lies deeper): fewer panels still, and still within the plain bound
+    deep = gwn.LearnedGK15Proposal(disp, n_classes=11, alpha=0.9, params=net.params)
+    nodes_deep = np.empty(n, np.int32)
+    got_deep = np.empty(n)
+    gwn.eval_gwnr_parametric_batch_fractional(disp, q, got_deep, x0, curves, cfg, integrator=deep,
+                                              nodes_per_query=nodes_deep)
+    print(f"panels saved at alpha 0.9: {1.0 - nodes_deep.sum() / nodes_plain.sum():.3f}")
+    assert nodes_deep.sum() < nodes.sum()
+    assert np.abs(got_deep - plain).max() <= 2 * cfg.tol * c / (4 * np.pi)
+    deep.close()
     # without the network (all start depths 0) the plain integrator is reproduced exactly
     zero = np.zeros((n, c), np.uint8)
     base = np.empty(n)
