@@ -172,7 +172,7 @@ class CudaDispatcher:
         _check(library().agwn_context_get_stats(self.handle, C.byref(s), int(reset)), "agwn_context_get_stats")
         names = ["fractional", "integer", "robust", "parametric", "other"]
         return {"kernel_ms": dict(zip(names, list(s.kernel_ms))), "launches": dict(zip(names, list(s.launches))),
-                "fp64_pairs": s.fp64_pairs, "pairs": s.pairs,
+                "fp64_pairs": s.fp64_pairs, "pairs": s.pairs, "certified_pairs": s.certified_pairs,
                 "integer": {"queries": s.int_queries, "cell_entries": s.int_cell_entries, "leaves": s.int_leaves,
                             "exact_tests": s.int_exact_tests},
                 "patches": {"pairs": s.patch_pairs, "cells": s.patch_cells, "pieces": s.patch_pieces,

@@ -21,7 +21,7 @@ STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA runtime error", 3: "out of de
 
 OPT_FRAC_MODE, OPT_MIXED_TAU, OPT_QUERIES_PER_THREAD, OPT_FRAC_BLOCK, OPT_TIMING, OPT_SEG_TILE, \
     OPT_MIXED_TERM_ERR, OPT_ROBUST_MODE, OPT_ROBUST_TERM_ERR, OPT_PARAM_MODE, OPT_INTEGER_CELLS, \
-    OPT_MIXED_MIN_PAIRS = range(12)
+    OPT_MIXED_MIN_PAIRS, OPT_MIXED_CERTIFY = range(13)
 ROBUST_EXACT, ROBUST_MIXED = 0, 1
 PARAM_EXACT, PARAM_MIXED = 0, 1
 FRAC_EXACT, FRAC_MIXED = 0, 1
@@ -33,7 +33,7 @@ class Stats(C.Structure):
                 ("fp64_pairs", C.c_int64), ("pairs", C.c_int64), ("int_queries", C.c_int64),
                 ("int_cell_entries", C.c_int64), ("int_leaves", C.c_int64), ("int_exact_tests", C.c_int64),
                 ("patch_pairs", C.c_int64), ("patch_cells", C.c_int64), ("patch_pieces", C.c_int64),
-                ("patch_fp64_pairs", C.c_int64)]
+                ("patch_fp64_pairs", C.c_int64), ("certified_pairs", C.c_int64)]
 
 
 # name -> (restype, argtypes)

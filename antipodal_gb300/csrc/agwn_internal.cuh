@@ -135,7 +135,7 @@ struct Context
     bool own_stream = false;
     int* d_flags = nullptr;        // FLAG_COUNT ints
     int* h_flags = nullptr;        // pinned mirror
-    long long* d_counters = nullptr; // kCounters: [0] fp64 pairs, [1] pairs, [2] parametric skips, [4..7] integer, [8..11] patches
+    long long* d_counters = nullptr; // kCounters: [0] fp64 pairs, [1] pairs, [2] parametric skips, [3] certified pairs, [4..7] integer, [8..11] patches
                                      // term: queries, cell-list entries, candidate leaves, exact tests
     DevBuf scratch[S_COUNT];
     int sm_count = 0;
@@ -157,6 +157,7 @@ struct Context
     float panel_beta = 0.02f;
     int integer_cells = 1;
     double mixed_min_pairs = double(1 << 20);
+    bool mixed_certify = true;
     int queries_per_thread = 2;
     int frac_block = 0; // 0: chosen per launch (frac.cu)
     int seg_tile = 512;

@@ -377,6 +377,10 @@ int agwn_context_set_option(agwn_context* ctx, int option, double value)
         AGWN_CHECK_ARG(std::isfinite(value) && value >= 0.0, "mixed minimum pairs must be finite and >= 0");
         ctx->mixed_min_pairs = value;
         return AGWN_OK;
+    case AGWN_OPT_MIXED_CERTIFY:
+        AGWN_CHECK_ARG(value == 0 || value == 1, "mixed certify must be 0 or 1");
+        ctx->mixed_certify = value != 0.0;
+        return AGWN_OK;
     default:
         return fail(AGWN_ERR_INVALID, "unknown option %d", option);
     }
@@ -423,6 +427,9 @@ int agwn_context_get_option(agwn_context* ctx, int option, double* value)
     case AGWN_OPT_MIXED_MIN_PAIRS:
         *value = ctx->mixed_min_pairs;
         return AGWN_OK;
+    case AGWN_OPT_MIXED_CERTIFY:
+        *value = ctx->mixed_certify ? 1.0 : 0.0;
+        return AGWN_OK;
     default:
         return fail(AGWN_ERR_INVALID, "unknown option %d", option);
     }
@@ -451,6 +458,7 @@ int agwn_context_get_stats(agwn_context* ctx, agwn_stats* out, int reset)
     out->patch_cells = counters[9];
     out->patch_pieces = counters[10];
     out->patch_fp64_pairs = counters[11];
+    out->certified_pairs = counters[3];
     if (reset)
     {
         for (int k = 0; k < AGWN_K_COUNT; ++k)

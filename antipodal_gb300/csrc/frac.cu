@@ -214,14 +214,14 @@ int fractional_launch_mixed(Context& ctx, const FracPlan<T>& p, const double* d_
     int const block = ctx.frac_block ? ctx.frac_block : (p.nbuf > 1 || p.tile > 512 ? 256 : 128);
     int64_t const n_qtiles = (n + int64_t(block) * K - 1) / (int64_t(block) * K);
     size_t const smem = size_t(p.nbuf) * p.tile * sizeof(SegM);
-    float const tau = float(ctx.mixed_tau);
     auto launch = [&](auto kern) -> int
     {
         int grid = 0;
         AGWN_TRY(launch_persistent(ctx, kern, block, smem, n_qtiles, &grid));
         AGWN_TRY(ctx.launch_begin(AGWN_K_FRACTIONAL));
         kern<<<grid, block, smem, ctx.stream>>>(d_pos, n, d_out, d_counts, p.x0d[0], p.x0d[1], p.x0d[2], p.rot,
-                                                p.frame, tau, float(ctx.mixed_term_err), p.segm, fb, p.n_seg, p.tile,
+                                                p.frame, int(ctx.mixed_certify), float(ctx.mixed_term_err), p.segm, fb,
+                                                p.n_seg, p.tile,
                                                 ctx.d_flags, ctx.d_counters, ctx.timing);
         return ctx.launch_end(AGWN_K_FRACTIONAL);
     };

@@ -652,6 +652,22 @@ __device__ __forceinline__ V atan_unit_lv(V t)
     return lv_mul(t, p);
 }
 
+// The reciprocal and the reciprocal square root of the mixed kernel as single approximate instructions (inline PTX,
+// flushing subnormal inputs to zero), so that every inlined copy of the pair arithmetic rounds alike.  A flushed
+// input gives an infinite result, which the error bound turns into a NaN that sends the pair to FP64.
+__device__ __forceinline__ float rcp_approx(float x)
+{
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ float rsqrt_approx(float x)
+{
+    float r;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
 // Per-vertex quantities of one boundary vertex relative to two queries (frame coordinates, one lane each):
 // v = vertex - query and the half-angle form (n, d) of l + z, l = |v|; d is NaN at a near vertex.
 struct VState2
@@ -666,16 +682,66 @@ constexpr int mixed_min_blocks()
     return K >= 8 ? 1 : (K >= 4 ? 2 : (K >= 2 ? 3 : 4));
 }
 
+// Certified groups of the entry stream.  Group g of a tile is its entries [g G, g G + G) with the vertex before
+// them.  In the frame (ray along +z) let r be the xy-distance from a query to a segment and L the segment's xy-length.
+// With lambda = L / r, the segment subtends at most the angle lambda across the ray, den > 0, |num| / den <=
+// lambda / cos(lambda), and the first-order bound the kernel computes per pair is at most
+// lambda (1 / cos(lambda) + 1 / cos^2(lambda)) <= 2.02 lambda for lambda <= 0.1.  So r >= kappa L with
+// kappa = max(10, 3 / te_units) keeps every pair's bound below 0.75 of te_units: no pair goes to FP64, and the angle
+// lies in the first octant (|num| < den), where atan2 needs no unfolding.  With r also at least the near distance
+// of each vertex (sqrt of its near2), no vertex state is NaN.  A warp tests this once per group and query tile
+// against circles: each of its query slots' xy-circle and the group's, of centre (cx, cy) and reach = radius +
+// max(kappa L_max, near distance), with a relative and an absolute slack for the float arithmetic of the test.
+// Groups holding a chain start, the first group of a tile (its vertex before lies in the previous tile) and a
+// tile's last, partial group take the full path.  A certified group's terms are bit-identical to the full path's:
+// the same operations minus the selects that the certificate fixes.
+constexpr int kCertG = 16;
+constexpr int kCertMaxGroups = 128; // tiles of up to 2,048 entries
+
+__device__ __forceinline__ float4 cert_group(SegM const* __restrict__ sb, int g, float kappa)
+{
+    int const e0 = g * kCertG;
+    if (e0 == 0)
+        return make_float4(0.f, 0.f, INFINITY, 0.f);
+    float xmin = INFINITY, xmax = -INFINITY, ymin = INFINITY, ymax = -INFINITY, l2 = 0.f, near2 = 0.f, amax = 0.f;
+    bool start = false;
+    for (int e = e0 - 1; e < e0 + kCertG; ++e)
+    {
+        SegM const& s = sb[e];
+        float const x = s.a.x + s.c.x, y = s.a.y + s.c.y;
+        xmin = fminf(xmin, x);
+        xmax = fmaxf(xmax, x);
+        ymin = fminf(ymin, y);
+        ymax = fmaxf(ymax, y);
+        amax = fmaxf(amax, fmaxf(fmaxf(fabsf(s.a.x), fabsf(s.a.y)), fabsf(s.a.z)));
+        near2 = fmaxf(near2, s.b.w);
+        if (e >= e0)
+        {
+            start |= __float_as_int(s.c.w) < 0;
+            l2 = fmaxf(l2, s.b.x * s.b.x + s.b.y * s.b.y);
+        }
+    }
+    float const thr = fmaxf(kappa * sqrtf(l2), sqrtf(near2));
+    // the range guard: vertices within 2^24 and distances of at least 2^-30 keep every product of the certified
+    // path (up to the fourth power of a distance) normal and finite in float
+    if (start || !(amax <= 16777216.f) || !(thr >= 9.3132257e-10f))
+        return make_float4(0.f, 0.f, INFINITY, 0.f);
+    float const cx = 0.5f * (xmin + xmax), cy = 0.5f * (ymin + ymax);
+    float const rad = 0.5f * sqrtf((xmax - xmin) * (xmax - xmin) + (ymax - ymin) * (ymax - ymin));
+    float const reach = rad + thr;
+    float const slack = 1e-5f * (fabsf(cx) + fabsf(cy) + reach);
+    return make_float4(cx, cy, 1.01f * reach + slack, 0.f);
+}
+
 // fb: the FP64 rule for the pairs the FP32 path turns down (MeshFallback, or the robust evaluator's).  K (even)
 // queries per thread, evaluated as K / 2 packed pairs.
 template <int K, class FB>
 __global__ void __launch_bounds__(256, mixed_min_blocks<K>())
     k_frac_mixed(const double* __restrict__ pos, int64_t n, double* __restrict__ out, const int32_t* __restrict__ counts,
-                 double x0x, double x0y, double x0z, Rot rot, const Frame* __restrict__ frame, float tau,
+                 double x0x, double x0y, double x0z, Rot rot, const Frame* __restrict__ frame, int certify,
                  float term_err, const SegM* __restrict__ seg, FB fb, int64_t n_seg, int tile, int* flags,
                  long long* counters, int count_pairs)
 {
-    (void)tau;
     static_assert(K % 2 == 0, "queries per thread come in packed pairs");
     constexpr int KP = K / 2;
     extern __shared__ __align__(128) unsigned char smem[];
@@ -684,6 +750,7 @@ __global__ void __launch_bounds__(256, mixed_min_blocks<K>())
     __shared__ double centre[3];
     __shared__ uint32_t q_entries[8][Fp64Queue<K>::kCap];
     __shared__ double q_results[8][32];
+    __shared__ float4 s_grp[kCertMaxGroups];
 
     // the entry stream (chain starts and segments, k_prep_mixed) is what the tiles walk
     int64_t const n_entries = frame->n_entries;
@@ -722,6 +789,16 @@ __global__ void __launch_bounds__(256, mixed_min_blocks<K>())
     // Rounding bound per FP32 operation chain (4 eps32), and the term error bound in its units.
     constexpr float kEpsBound = 4.0f * 5.9604645e-8f;
     float const te_units = term_err / kEpsBound;
+    // kappa: the certificate's distance in longest segments (infinite with certify 0: no group certified)
+    float const kappa = certify ? fmaxf(10.f, 3.f / te_units) : INFINITY;
+    // the certified groups of the tile in shared memory (every thread calls it; ends with a block barrier)
+    auto groups_of = [&](SegM const* sb, int cnt)
+    {
+        int const ng = min(cnt / kCertG, kCertMaxGroups);
+        for (int g = threadIdx.x; g < ng; g += blockDim.x)
+            s_grp[g] = cert_group(sb, g, kappa);
+        __syncthreads();
+    };
     double const two_pi = 2.0 * kPi<double>;
     ev3<rd> const x1{rd(-x0x), rd(-x0y), rd(-x0z)};
     Fp64Queue<K> fq;
@@ -729,6 +806,7 @@ __global__ void __launch_bounds__(256, mixed_min_blocks<K>())
     fq.res = q_results[warp];
 
     int it = 0;
+    long long n_cert = 0; // entries of certified groups this warp evaluated (warp-uniform)
     for (int j = 0; j < my_qtiles; ++j)
     {
         int64_t const tile_base = (blockIdx.x + int64_t(j) * gridDim.x) * per_tile;
@@ -770,6 +848,29 @@ __global__ void __launch_bounds__(256, mixed_min_blocks<K>())
             st0[p] = VState2{};
             st1[p] = VState2{};
         }
+        // each query slot's xy-circle over the warp's 32 lanes (centre, radius with a slack); a slot with a
+        // coordinate beyond 2^24 (or NaN) gets an infinite radius, so none of the warp's groups is certified
+        float scx[K], scy[K], srad[K];
+#pragma unroll
+        for (int k = 0; k < K; ++k)
+        {
+            float const x = -ln(nqhx[k / 2], k & 1), y = -ln(nqhy[k / 2], k & 1), z = -ln(nqhz[k / 2], k & 1);
+            float x0 = x, x1 = x, y0 = y, y1 = y;
+            bool sane = fmaxf(fmaxf(fabsf(x), fabsf(y)), fabsf(z)) <= 16777216.f;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1)
+            {
+                x0 = fminf(x0, __shfl_xor_sync(0xffffffffu, x0, o));
+                x1 = fmaxf(x1, __shfl_xor_sync(0xffffffffu, x1, o));
+                y0 = fminf(y0, __shfl_xor_sync(0xffffffffu, y0, o));
+                y1 = fmaxf(y1, __shfl_xor_sync(0xffffffffu, y1, o));
+            }
+            sane = __all_sync(0xffffffffu, sane);
+            scx[k] = 0.5f * (x0 + x1);
+            scy[k] = 0.5f * (y0 + y1);
+            float const rad = 0.5f * sqrtf((x1 - x0) * (x1 - x0) + (y1 - y0) * (y1 - y0));
+            srad[k] = sane ? 1.01f * rad + 1e-5f * (fabsf(scx[k]) + fabsf(scy[k]) + rad) : INFINITY;
+        }
         // Pairs that go to FP64 are marked in a bit mask (bit slot * K + k) while two entries are evaluated, and
         // pushed to the warp's queue afterwards behind one warp-uniform branch that is rarely taken.
         uint32_t nb = 0;
@@ -778,10 +879,9 @@ __global__ void __launch_bounds__(256, mixed_min_blocks<K>())
         // the common case) the body has no branches: a term taken to FP64 adds an exact zero to the TwoSum, so the
         // compiler schedules consecutive entries together.  With may_start true a chain start skips the pair term.
         // The arithmetic runs on packed pairs of queries; selects and comparisons per lane.
-        auto step = [&](SegM const& ent, VState2 (&pv)[KP], VState2 (&cv)[KP], bool may_start, int slot)
+        auto vertex = [&](SegM const& ent, VState2 (&cv)[KP])
         {
             float4 const A = ent.a, B = ent.b, C = ent.c;
-            int const sidx = __float_as_int(C.w);
             float2 const ax = lv_set<float2>(A.x), ay = lv_set<float2>(A.y), az = lv_set<float2>(A.z), cx = lv_set<float2>(C.x), cy = lv_set<float2>(C.y), cz = lv_set<float2>(C.z);
 #pragma unroll
             for (int p = 0; p < KP; ++p)
@@ -792,7 +892,7 @@ __global__ void __launch_bounds__(256, mixed_min_blocks<K>())
                 c.z = lv_add(lv_add(az, nqhz[p]), lv_add(cz, nqlz[p]));
                 float2 const r = lv_fma(c.x, c.x, lv_mul(c.y, c.y));
                 float2 const q = lv_fma(c.z, c.z, r);
-                float2 const l = lv_mul(q, make_float2(rsqrtf(q.x), rsqrtf(q.y)));
+                float2 const l = lv_mul(q, make_float2(rsqrt_approx(q.x), rsqrt_approx(q.y)));
                 // l + z = n / d with (n, d) = (l + z, 1) for z >= 0 and (x^2 + y^2, l - z) for z < 0, free of
                 // cancellation.  d > 0, or NaN for a near vertex (|v|^2 < near2): the NaN makes the error bound of
                 // both segments at this vertex NaN, which sends them to FP64
@@ -802,6 +902,34 @@ __global__ void __launch_bounds__(256, mixed_min_blocks<K>())
                 c.d = make_float2(q.x < B.w ? nan : (c.z.x >= 0.f ? 1.f : lmz.x),
                                   q.y < B.w ? nan : (c.z.y >= 0.f ? 1.f : lmz.y));
             }
+        };
+        // a certified pair term: the full path's operations with need = false, |num| <= den and den > 0
+        auto fast = [&](SegM const& ent, VState2 (&pv)[KP], VState2 (&cv)[KP])
+        {
+            vertex(ent, cv);
+            float4 const A = ent.a, B = ent.b;
+            float2 const by = lv_set<float2>(B.y), nbx = lv_set<float2>(-B.x), w = lv_set<float2>(A.w);
+#pragma unroll
+            for (int p = 0; p < KP; ++p)
+            {
+                VState2 const& v0 = pv[p];
+                VState2 const& v1 = cv[p];
+                float2 const num = lv_fma(v0.x, by, lv_mul(v0.y, nbx));
+                float2 const D = lv_mul(v0.d, v1.d), nn = lv_mul(v0.n, v1.n);
+                float2 const num_s = lv_mul(num, D);
+                float2 const den_s = lv_fma(lv_fma(v0.x, v1.x, lv_mul(v0.y, v1.y)), D, nn);
+                float2 const an = make_float2(fabsf(num_s.x), fabsf(num_s.y));
+                float2 const inv = make_float2(rcp_approx(den_s.x), rcp_approx(den_s.y));
+                float2 const a = atan_unit_lv(lv_mul(an, inv));
+                float2 const ang = make_float2(copysignf(a.x, num_s.x), copysignf(a.y, num_s.y));
+                two_sum_lv(acc[p], comp[p], lv_mul(w, ang));
+            }
+        };
+        auto step = [&](SegM const& ent, VState2 (&pv)[KP], VState2 (&cv)[KP], bool may_start, int slot)
+        {
+            vertex(ent, cv);
+            float4 const A = ent.a, B = ent.b, C = ent.c;
+            int const sidx = __float_as_int(C.w);
             if (may_start && sidx < 0)
                 return;
             float2 const by = lv_set<float2>(B.y), nbx = lv_set<float2>(-B.x), w = lv_set<float2>(A.w);
@@ -811,14 +939,16 @@ __global__ void __launch_bounds__(256, mixed_min_blocks<K>())
                 VState2 const& v0 = pv[p];
                 VState2 const& v1 = cv[p];
                 // num from the segment vector B (accurate on its own, no cancellation for a far segment)
-                float2 const ta = lv_mul(v0.x, by), tbn = lv_mul(v0.y, nbx); // v0.x * B.y and -(v0.y * B.x)
-                float2 const num = lv_add(ta, tbn);
+                // num = v0.x * B.y - v0.y * B.x and v0.x * v1.x + v0.y * v1.y as written FMAs (the certified path
+                // computes the same); ta and pxy are the products for the error bound
+                float2 const ta = lv_mul(v0.x, by), tbn = lv_mul(v0.y, nbx);
+                float2 const num = lv_fma(v0.x, by, tbn);
                 // scaling num and den by the positive D = d0 * d1 leaves the angle unchanged and removes both
                 // divisions: den * D = n0 * n1 + (v0.x*v1.x + v0.y*v1.y) * D
                 float2 const D = lv_mul(v0.d, v1.d), nn = lv_mul(v0.n, v1.n);
                 float2 const pxy = lv_mul(v0.x, v1.x), pyy = lv_mul(v0.y, v1.y);
                 float2 const num_s = lv_mul(num, D);
-                float2 const den_s = lv_fma(lv_add(pxy, pyy), D, nn);
+                float2 const den_s = lv_fma(lv_fma(v0.x, v1.x, pyy), D, nn);
                 // first-order rounding bounds: num errs by about eps * sn and den by about eps * sd, so the angle
                 // errs by at most eps * (sn * |den| + sd * |num|) / (num^2 + den^2) <= eps * (sn * ad1 + sd * an1) / M
                 // with M = max(|num|, |den|) and an1, ad1 the two divided by M: one of them is 1, the other is the
@@ -831,7 +961,7 @@ __global__ void __launch_bounds__(256, mixed_min_blocks<K>())
                 float2 const ad = make_float2(fabsf(den_s.x), fabsf(den_s.y));
                 bool const sw0 = an.x > ad.x, sw1 = an.y > ad.y;
                 // (num = den = 0 gives an infinite reciprocal, a NaN t and a NaN bound: the pair goes to FP64)
-                float2 const inv = make_float2(__fdividef(1.f, fmaxf(an.x, ad.x)), __fdividef(1.f, fmaxf(an.y, ad.y)));
+                float2 const inv = make_float2(rcp_approx(fmaxf(an.x, ad.x)), rcp_approx(fmaxf(an.y, ad.y)));
                 // an1, ad1: |num| and |den| over M, t the smaller; the bound (sn * ad1 + sd * an1) / M as packed
                 // products, without per-lane selects
                 float2 const an1 = lv_mul(an, inv), ad1 = lv_mul(ad, inv);
@@ -895,36 +1025,72 @@ __global__ void __launch_bounds__(256, mixed_min_blocks<K>())
             }
             SegM const* sb = pipe.buf[b];
             int const cnt = pipe.tile_count(st);
-            // tiles start at even positions of the stream (the tile is even), so the alternation runs across them;
-            // only the last tile can end on an odd count
-            int s = 0;
-            for (; s + 1 < cnt; s += 2)
+            int const ng = min(cnt / kCertG, kCertMaxGroups);
+            if (!pipe.single || j == 0)
+                groups_of(sb, cnt);
+            // tiles start at even positions of the stream (the tile and the group are even), so the alternation runs
+            // across groups and tiles; only the last tile can end on an odd count
+            uint32_t cmask = 0;
+            for (int s0 = 0; s0 < cnt; s0 += kCertG)
             {
-                if ((__float_as_int(sb[s].c.w) | __float_as_int(sb[s + 1].c.w)) >= 0)
+                int const g = s0 / kCertG;
+                if ((g & 31) == 0)
                 {
-                    step(sb[s], st1, st0, false, 0);
-                    step(sb[s + 1], st0, st1, false, 1);
+                    // lane l tests group g + l against every query slot of the warp
+                    int const gl = g + lane;
+                    bool ok = gl < ng;
+                    if (ok)
+                    {
+                        float4 const c = s_grp[gl];
+#pragma unroll
+                        for (int k = 0; k < K; ++k)
+                        {
+                            float const dx = c.x - scx[k], dy = c.y - scy[k], need = c.z + srad[k];
+                            ok = ok && dx * dx + dy * dy >= need * need;
+                        }
+                    }
+                    cmask = __ballot_sync(0xffffffffu, ok);
                 }
-                else
+                if ((cmask >> (g & 31)) & 1u)
+                {
+                    n_cert += kCertG;
+                    for (int s = s0; s < s0 + kCertG; s += 2)
+                    {
+                        fast(sb[s], st1, st0);
+                        fast(sb[s + 1], st0, st1);
+                    }
+                    continue;
+                }
+                int const e1 = min(s0 + kCertG, cnt);
+                int s = s0;
+                for (; s + 1 < e1; s += 2)
+                {
+                    if ((__float_as_int(sb[s].c.w) | __float_as_int(sb[s + 1].c.w)) >= 0)
+                    {
+                        step(sb[s], st1, st0, false, 0);
+                        step(sb[s + 1], st0, st1, false, 1);
+                    }
+                    else
+                    {
+                        step(sb[s], st1, st0, true, 0);
+                        step(sb[s + 1], st0, st1, true, 1);
+                    }
+                    if (__any_sync(0xffffffffu, nb != 0))
+                    {
+                        push(sb, s, 2);
+                        while (fq.tail - fq.head >= 32)
+                            fp64_flush<K>(fq, 32, lane, warp, tile_base, pos, n, fb, x1, acc64);
+                    }
+                }
+                if (s < e1)
                 {
                     step(sb[s], st1, st0, true, 0);
-                    step(sb[s + 1], st0, st1, true, 1);
-                }
-                if (__any_sync(0xffffffffu, nb != 0))
-                {
-                    push(sb, s, 2);
-                    while (fq.tail - fq.head >= 32)
-                        fp64_flush<K>(fq, 32, lane, warp, tile_base, pos, n, fb, x1, acc64);
-                }
-            }
-            if (s < cnt)
-            {
-                step(sb[s], st1, st0, true, 0);
-                if (__any_sync(0xffffffffu, nb != 0))
-                {
-                    push(sb, s, 1);
-                    while (fq.tail - fq.head >= 32)
-                        fp64_flush<K>(fq, 32, lane, warp, tile_base, pos, n, fb, x1, acc64);
+                    if (__any_sync(0xffffffffu, nb != 0))
+                    {
+                        push(sb, s, 1);
+                        while (fq.tail - fq.head >= 32)
+                            fp64_flush<K>(fq, 32, lane, warp, tile_base, pos, n, fb, x1, acc64);
+                    }
                 }
             }
             if (!pipe.single)
@@ -969,6 +1135,7 @@ __global__ void __launch_bounds__(256, mixed_min_blocks<K>())
             }
         }
         atomicAdd(reinterpret_cast<unsigned long long*>(counters), static_cast<unsigned long long>(fq.tail));
+        atomicAdd(reinterpret_cast<unsigned long long*>(counters + 3), static_cast<unsigned long long>(n_cert * 32 * K));
         atomicAdd(reinterpret_cast<unsigned long long*>(counters + 1), static_cast<unsigned long long>(tot));
     }
 }

@@ -143,7 +143,7 @@ extern "C" int agwn_mesh_batch_fractional_mixed_noalloc_f64(void* stream, const 
     int64_t const n_qtiles = (n + per_tile - 1) / per_tile;
     int const grid = int(std::max<int64_t>(1, std::min<int64_t>(n_qtiles, int64_t(per_sm) * sm_count)));
     kern<<<grid, kNoAllocBlock, smem, st>>>(positions, n, out, nullptr, x0[0], x0[1], x0[2], rot, &scr->frame,
-                                            float(defaults.mixed_tau), float(defaults.mixed_term_err), scr->seg,
+                                            int(defaults.mixed_certify), float(defaults.mixed_term_err), scr->seg,
                                             MeshFallback{scr->seg64}, n_segments, tile, scr->flags, scr->counters, 0);
     AGWN_TRY_CUDA(cudaGetLastError());
     AGWN_TRY_CUDA(cudaStreamSynchronize(st));

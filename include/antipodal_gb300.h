@@ -103,7 +103,11 @@ enum agwn_option
     /* Mixed modes (mesh, and the robust evaluator's exact_float): below this many (query, segment) pairs in one
        call the exact FP64 kernels run instead, which are the faster ones there (the mixed form's boundary
        preparation costs more than the FP64 pairs it saves).  Default 2^20; 0 always runs the mixed form. */
-    AGWN_OPT_MIXED_MIN_PAIRS = 11
+    AGWN_OPT_MIXED_MIN_PAIRS = 11,
+    /* Mixed kernel: 1 (default) evaluates the boundary groups that a warp's queries certify (every pair far enough
+       across the ray for its error bound to pass and its angle to lie in the first octant) without the per-pair
+       bound and octant unfolding; 0 takes the per-pair path everywhere.  The results are the same bit for bit. */
+    AGWN_OPT_MIXED_CERTIFY = 12
 };
 enum agwn_param_mode
 {
@@ -149,6 +153,8 @@ typedef struct agwn_stats
     int64_t patch_pieces;             /* boundary-cubic pieces blossomed and tested for the winding numbers    */
     int64_t patch_fp64_pairs;         /* decisions float could not make, taken in FP64 (a cell's winding or   
                                          a cell's subtree)                                                     */
+    int64_t certified_pairs;          /* mixed mode: pairs in boundary groups the warp certified (when timing;
+                                         counted over whole warps, padding lanes of the last query tile too)    */
 } agwn_stats;
 /* Reads (synchronising the stream first) and optionally resets the accumulated statistics. */
 int agwn_context_get_stats(agwn_context* ctx, agwn_stats* out, int reset);

@@ -344,6 +344,67 @@ def test_mixed_chains_across_tiles(gwn, oracle, n_seg, seg_tile, qpt):
     _check_mixed(gwn, oracle, q, x0, segs, seg_tile=seg_tile, qpt=qpt)
 
 
+def _clustered_queries(rng, n_clusters, lo=-1.6, hi=1.6, spread=0.03):
+    # 32 consecutive queries (one warp slot of the fractional kernels) around each of n_clusters random centres
+    c = rng.uniform(lo, hi, size=(n_clusters, 1, 3))
+    return (c + rng.uniform(-spread, spread, size=(n_clusters, 32, 3))).reshape(-1, 3)
+
+
+@pytest.mark.parametrize("n_seg,seg_tile,qpt", [(212, 512, 2), (600, 512, 2), (600, 128, 4), (300, 64, 8)])
+def test_mixed_certified_groups_equal_the_per_pair_path(gwn, oracle, n_seg, seg_tile, qpt):
+    """Boundary groups of 16 entries that lie far enough across the ray from all of a warp's queries (every pair's
+    error bound below the FP64 threshold, every angle in the first octant) are evaluated without the per-pair bound
+    and octant unfolding.  The operations left are the per-pair path's own, so certification on and off give the
+    same results bit for bit: one tile or several, chain starts inside groups, every queries-per-thread variant."""
+    from antipodal_gb300 import _lib
+    rng = np.random.default_rng(n_seg + seg_tile)
+    x0 = synth.unit_x0()
+    q = _clustered_queries(rng, 1024)
+    segs = np.concatenate([_polyline(rng, n_seg, True), _polyline(rng, 40, False, centre=(0.2, -0.1, 0.3),
+                                                                   radius=0.4)])
+    ref = oracle.frac_batch(q, x0, segs)
+    outs, stats = {}, {}
+    for cert in (1, 0):
+        with gwn.CudaDispatcher(precision="mixed", queries_per_thread=qpt, seg_tile=seg_tile, mixed_min_pairs=0,
+                                timing=True) as d:
+            assert d.get_option(_lib.OPT_MIXED_CERTIFY) == 1.0
+            d.set_option(_lib.OPT_MIXED_CERTIFY, cert)
+            out = np.empty(len(q))
+            gwn.eval_gwnr_mesh_batch_fractional(d, q, out, x0, segs)
+            outs[cert], stats[cert] = out, d.stats()
+    assert np.array_equal(outs[1], outs[0])
+    assert np.abs(outs[1] - ref).max() <= TOL_MIXED, np.abs(outs[1] - ref).max()
+    assert stats[0]["certified_pairs"] == 0
+    # (eight query slots per warp and 64-entry tiles certify the fewest: 8% of the pairs)
+    assert stats[1]["certified_pairs"] >= 0.05 * stats[1]["pairs"], (stats[1]["certified_pairs"], stats[1]["pairs"])
+    assert stats[1]["fp64_pairs"] == stats[0]["fp64_pairs"]
+
+
+def test_mixed_certified_groups_range_guard(gwn, oracle):
+    # far-off queries (2^25 across) and a boundary scaled to 1e-12: no group is certified there (float products of
+    # the certified path would overflow or underflow), and the results still equal the per-pair path's
+    from antipodal_gb300 import _lib
+    rng = np.random.default_rng(5)
+    x0 = synth.unit_x0()
+    segs = _polyline(rng, 200, True)
+    for scale, qscale in ((1.0, 3.4e7), (1e-12, 1e-12)):
+        s = segs.copy()
+        s[:, :6] *= scale
+        q = _clustered_queries(rng, 64) * qscale
+        outs = {}
+        for cert in (1, 0):
+            with gwn.CudaDispatcher(precision="mixed", mixed_min_pairs=0, timing=True) as d:
+                d.set_option(_lib.OPT_MIXED_CERTIFY, cert)
+                out = np.empty(len(q))
+                gwn.eval_gwnr_mesh_batch_fractional(d, q, out, x0, s)
+                outs[cert] = out
+                if cert:
+                    assert d.stats()["certified_pairs"] == 0
+        assert np.array_equal(outs[1], outs[0])
+        assert np.all(np.isfinite(outs[1]))
+        assert np.abs(outs[1] - oracle.frac_batch(q, x0, s)).max() <= TOL_MIXED
+
+
 @pytest.mark.parametrize("n_seg", [4096, 4097])
 def test_mixed_chain_limit(gwn, oracle, n_seg):
     # up to 4096 segments the boundary is chained; above, every segment is a chain of its own

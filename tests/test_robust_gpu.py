@@ -10,7 +10,7 @@ import os
 import numpy as np
 import pytest
 
-from antipodal_gb300 import synth
+from antipodal_gb300 import _lib, synth
 
 pytestmark = pytest.mark.gpu
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "reference_golden.npz")
@@ -183,7 +183,13 @@ def test_robust_mixed_exact_float_matches_exact(gwn, disp):
                 r.evaluate(q, o2)  # without the separate outputs: the other launch path
                 assert np.array_equal(o, o2)
                 outs[mode] = (o, c, f)
+            # the mixed kernel's certified boundary groups (on by default) change no value
+            disp.set_option(_lib.OPT_MIXED_CERTIFY, 0)
+            o3 = np.empty(len(q))
+            r.evaluate(q, o3)
+            assert np.array_equal(o3, outs["mixed"][0])
         finally:
+            disp.set_option(_lib.OPT_MIXED_CERTIFY, 1)
             disp.set_robust_precision("exact")
             r.close()
         assert np.array_equal(outs["exact"][1], outs["mixed"][1])
