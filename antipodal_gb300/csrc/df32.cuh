@@ -1,12 +1,14 @@
 // Double-float arithmetic: a value is hi + lo, two floats with |lo| <= ulp(hi) / 2, about 44 significant bits,
 // computed on the FP32 pipe (64x the FP64 rate of this GPU).  Built from the error-free transformations TwoSum
 // (Knuth), FastTwoSum (Dekker, |a| >= |b|) and TwoProduct by FMA; add is the "sloppy" variant (error relative to
-// |a| + |b|), multiply folds the cross terms into the FMA error term, divide and sqrt take one Newton-style
-// correction of a float estimate.  Every step is written with explicit round-to-nearest intrinsics so the compiler
+// |a| + |b|), multiply folds the cross terms into the FMA error term, divide takes two Newton-style corrections of
+// a float estimate and sqrt one.  Every step is written with explicit round-to-nearest intrinsics so the compiler
 // cannot reassociate or contract them.
 #pragma once
 
 #include <cuda_runtime.h>
+
+#include "approx.cuh"
 
 namespace agwn
 {
@@ -72,18 +74,19 @@ __device__ __forceinline__ df df_scale(df a, float p2)
 }
 __device__ __forceinline__ df operator/(df a, df b)
 {
-    float const q1 = __fdividef(a.hi, b.hi);
+    float const rb = rcp_approx(b.hi); // one reciprocal for the three float quotients
+    float const q1 = __fmul_rn(a.hi, rb);
     df const r = a - b * df_make(q1);
-    float const q2 = __fdividef(r.hi, b.hi);
+    float const q2 = __fmul_rn(r.hi, rb);
     df const q = fast_two_sum(q1, q2);
     df const r2 = a - b * q; // a second correction brings the quotient to double-float accuracy
-    return q + df_make(__fdividef(r2.hi, b.hi));
+    return q + df_make(__fmul_rn(r2.hi, rb));
 }
 __device__ __forceinline__ df df_sqrt(df a)
 {
     if (!(a.hi > 0.f))
         return {sqrtf(a.hi), 0.f};
-    float const ri = rsqrtf(a.hi);
+    float const ri = rsqrt_approx(a.hi);
     float const y = __fmul_rn(a.hi, ri);
     df const e = a - two_prod(y, y);
     return fast_two_sum(y, __fmul_rn(__fmul_rn(e.hi, ri), 0.5f));

@@ -4,6 +4,7 @@
 #pragma once
 
 #include "agwn_internal.cuh"
+#include "approx.cuh"
 #include "tma.cuh"
 
 #include <type_traits>
@@ -650,22 +651,6 @@ __device__ __forceinline__ V atan_unit_lv(V t)
     p = lv_fma(p, s, lv_set<V>(-0.3333307334510578f));
     p = lv_fma(p, s, lv_set<V>(0.9999999847657755f));
     return lv_mul(t, p);
-}
-
-// The reciprocal and the reciprocal square root of the mixed kernel as single approximate instructions (inline PTX,
-// flushing subnormal inputs to zero), so that every inlined copy of the pair arithmetic rounds alike.  A flushed
-// input gives an infinite result, which the error bound turns into a NaN that sends the pair to FP64.
-__device__ __forceinline__ float rcp_approx(float x)
-{
-    float r;
-    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
-    return r;
-}
-__device__ __forceinline__ float rsqrt_approx(float x)
-{
-    float r;
-    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
-    return r;
 }
 
 // Per-vertex quantities of one boundary vertex relative to two queries (frame coordinates, one lane each):
