@@ -75,7 +75,9 @@ enum scratch_slot
     S_MISC2 = 8,
     S_MISC3 = 9,
     S_PARTIAL = 10, // the parametric integrator's per-group partial sums
-    S_COUNT = 11
+    S_ORDER0 = 11,  // the spatial order of the queries: sort keys, indices, digit counters (order.cu)
+    S_ORDER1 = 12,  // the queries in that order and their outputs
+    S_COUNT = 13
 };
 
 // A hierarchy over triangles in the frame of one ray direction (built by build_hier, lbvh.cu): internal nodes,
@@ -158,6 +160,15 @@ struct Context
     int integer_cells = 1;
     double mixed_min_pairs = double(1 << 20);
     bool mixed_certify = true;
+    // the spatial order of the queries (order.cu): the last decision and its key, and whether an evaluation on an
+    // ordered copy is running (no second ordering inside it)
+    const void* order_ptr = nullptr;
+    int64_t order_n = 0;
+    double order_dir[3] = {0, 0, 0};
+    bool order_incoherent = false;
+    float order_lo[2] = {0.f, 0.f};
+    float order_scale = 1.f;
+    bool ordering = false;
     int queries_per_thread = 2;
     int frac_block = 0; // 0: chosen per launch (frac.cu)
     int seg_tile = 512;

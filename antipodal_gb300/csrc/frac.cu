@@ -475,6 +475,31 @@ int mesh_batch(agwn_context* ctx, const agwn_bvh* bvh, const T* positions, int64
         return mesh_batch_pipelined<T>(*ctx, bvh, positions, n, out, x0, static_cast<const T*>(dseg), n_seg,
                                        want_frac);
     }
+    if constexpr (sizeof(T) == 8)
+    {
+        // mixed mode on device arrays: an incoherent query order runs on a spatially sorted copy (order.cu), where
+        // the mixed kernel certifies far more boundary groups; the values are the same bit for bit
+        if (want_frac && n_seg > 0 && ctx->frac_mode == AGWN_FRAC_MIXED && !ctx->ordering &&
+            n_seg < (int64_t(1) << 24) && double(n) * double(n_seg) >= ctx->mixed_min_pairs &&
+            is_device_pointer(positions) && is_device_pointer(out))
+        {
+            double const dir[3] = {x0[0], x0[1], x0[2]};
+            const int32_t* perm = nullptr;
+            AGWN_TRY(query_order(*ctx, positions, n, dir, true, &perm));
+            if (perm)
+            {
+                double* ps = nullptr;
+                AGWN_TRY(ctx->scratch_reserve(S_ORDER1, sizeof(double) * 4 * size_t(n), reinterpret_cast<void**>(&ps)));
+                double* const os = ps + 3 * size_t(n);
+                AGWN_TRY(gather_queries(*ctx, positions, perm, n, ps));
+                ctx->ordering = true;
+                int const rc = mesh_batch<T>(ctx, bvh, ps, n, os, x0, boundary, n_seg, want_frac);
+                ctx->ordering = false;
+                AGWN_TRY(rc);
+                return scatter_back<double>(*ctx, os, perm, n, out);
+            }
+        }
+    }
     if (n >= (int64_t(1) << 21) && want_frac && bvh && bvh->n_tri > 0 && is_device_pointer(positions) &&
         is_device_pointer(out))
     {

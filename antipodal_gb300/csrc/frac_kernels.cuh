@@ -672,16 +672,18 @@ constexpr int mixed_min_blocks()
 // With lambda = L / r, the segment subtends at most the angle lambda across the ray, den > 0, |num| / den <=
 // lambda / cos(lambda), and the first-order bound the kernel computes per pair is at most
 // lambda (1 / cos(lambda) + 1 / cos^2(lambda)) <= 2.02 lambda for lambda <= 0.1.  So r >= kappa L with
-// kappa = max(10, 3 / te_units) keeps every pair's bound below 0.75 of te_units: no pair goes to FP64, and the angle
-// lies in the first octant (|num| < den), where atan2 needs no unfolding.  With r also at least the near distance
+// kappa = max(10, 2.25 / te_units) keeps every pair's bound below 0.9 of te_units (the bound's own float rounding
+// is a few ulps): no pair goes to FP64, and the angle lies in the first octant (|num| < den), where atan2 needs no
+// unfolding.  With r also at least the near distance
 // of each vertex (sqrt of its near2), no vertex state is NaN.  A warp tests this once per group and query tile
 // against circles: each of its query slots' xy-circle and the group's, of centre (cx, cy) and reach = radius +
 // max(kappa L_max, near distance), with a relative and an absolute slack for the float arithmetic of the test.
 // Groups holding a chain start, the first group of a tile (its vertex before lies in the previous tile) and a
 // tile's last, partial group take the full path.  A certified group's terms are bit-identical to the full path's:
-// the same operations minus the selects that the certificate fixes.
-constexpr int kCertG = 16;
-constexpr int kCertMaxGroups = 128; // tiles of up to 2,048 entries
+// the same operations minus the selects that the certificate fixes.  Groups of 8 entries with kappa 10 certify 82%
+// of the pairs of a 212-segment loop with 256^3 grid queries (16 entries, kappa 11.9: 72%; 3% slower).
+constexpr int kCertG = 8;
+constexpr int kCertMaxGroups = 256; // tiles of up to 2,048 entries
 
 __device__ __forceinline__ float4 cert_group(SegM const* __restrict__ sb, int g, float kappa)
 {
@@ -775,7 +777,7 @@ __global__ void __launch_bounds__(256, mixed_min_blocks<K>())
     constexpr float kEpsBound = 4.0f * 5.9604645e-8f;
     float const te_units = term_err / kEpsBound;
     // kappa: the certificate's distance in longest segments (infinite with certify 0: no group certified)
-    float const kappa = certify ? fmaxf(10.f, 3.f / te_units) : INFINITY;
+    float const kappa = certify ? fmaxf(10.f, 2.25f / te_units) : INFINITY;
     // the certified groups of the tile in shared memory (every thread calls it; ends with a block barrier)
     auto groups_of = [&](SegM const* sb, int cnt)
     {

@@ -44,6 +44,20 @@ int integer_run(Context& ctx, const Bvh& bvh, const T* d_pos, int64_t n, int32_t
 // The hierarchy along dir_host and its cell grid (when enabled), built on ctx.stream unless cached.
 template <class T>
 int integer_prepare(Context& ctx, const Bvh& bvh, const T* dir_host);
+
+// Spatial order of the queries for the mixed kernels (order.cu).  For n >= kOrderMinQueries device-resident
+// queries whose order is incoherent across the direction dir (3 doubles, host), *perm receives a permutation (device
+// scratch S_ORDER0, valid until the next call) that sorts them along a 2D Morton curve across dir; otherwise (a
+// coherent order, fewer queries, or certification off) null.  With cacheable (the caller's own device array) the
+// decision is cached per (d_pos, n, dir); staged copies of host arrays are sampled on every call.
+constexpr int64_t kOrderMinQueries = int64_t(1) << 20;
+int query_order(Context& ctx, const double* d_pos, int64_t n, const double* dir, bool cacheable,
+                const int32_t** perm);
+// d_sorted[i] = d_pos[perm[i]] (three doubles each)
+int gather_queries(Context& ctx, const double* d_pos, const int32_t* perm, int64_t n, double* d_sorted);
+// d_out[perm[i]] = d_sorted[i] (double and int32_t)
+template <class T>
+int scatter_back(Context& ctx, const T* d_sorted, const int32_t* perm, int64_t n, T* d_out);
 } // namespace agwn
 
 struct agwn_bvh : agwn::Bvh

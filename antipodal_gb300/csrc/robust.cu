@@ -388,17 +388,54 @@ int robust_eval(agwn_context* ctx, const agwn_robust* r, const T* positions, int
     T* o = static_cast<T*>(dout);
     int32_t* c = static_cast<int32_t*>(dcnt);
     T* fr = static_cast<T*>(dfr);
-    switch (r->policy)
+    bool ordered = false;
+    if constexpr (std::is_same_v<T, double>)
     {
-    case 0:
-        AGWN_TRY((robust_run<T, P64>(*ctx, *r, p, n, o, c, fr)));
-        break;
-    case 1:
-        AGWN_TRY((robust_run<T, P128>(*ctx, *r, p, n, o, c, fr)));
-        break;
-    default:
-        AGWN_TRY((robust_run<T, PF>(*ctx, *r, p, n, o, c, fr)));
-        break;
+        // exact_float in mixed mode: an incoherent query order runs on a spatially sorted copy (order.cu), where the
+        // mixed kernel certifies far more boundary groups; the values are the same bit for bit
+        if (r->policy == 2 && ctx->robust_mode == AGWN_ROBUST_MIXED && !ctx->ordering && r->n_seg > 0 &&
+            r->n_seg < (int64_t(1) << 24) && double(n) * double(r->n_seg) >= ctx->mixed_min_pairs)
+        {
+            double const dir[3] = {-1.0, 0.0, 0.0}; // the evaluator's rays and fractional frame run along -x
+            const int32_t* perm = nullptr;
+            AGWN_TRY(query_order(*ctx, p, n, dir, dpos == positions, &perm));
+            if (perm)
+            {
+                size_t const m = size_t(n);
+                double* ps = nullptr;
+                AGWN_TRY(ctx->scratch_reserve(S_ORDER1, m * (sizeof(double) * (fr ? 5 : 4) + sizeof(int32_t)),
+                                              reinterpret_cast<void**>(&ps)));
+                double* const os = ps + 3 * m;
+                double* const fs = fr ? os + m : nullptr;
+                int32_t* const cs = reinterpret_cast<int32_t*>(os + (fr ? 2 : 1) * m);
+                AGWN_TRY(gather_queries(*ctx, p, perm, n, ps));
+                ctx->ordering = true;
+                int const rc = robust_run<T, PF>(*ctx, *r, ps, n, os, cs, fs);
+                ctx->ordering = false;
+                AGWN_TRY(rc);
+                AGWN_TRY(scatter_back<double>(*ctx, os, perm, n, o));
+                if (out_counts)
+                    AGWN_TRY(scatter_back<int32_t>(*ctx, cs, perm, n, c));
+                if (fs)
+                    AGWN_TRY(scatter_back<double>(*ctx, fs, perm, n, fr));
+                ordered = true;
+            }
+        }
+    }
+    if (!ordered)
+    {
+        switch (r->policy)
+        {
+        case 0:
+            AGWN_TRY((robust_run<T, P64>(*ctx, *r, p, n, o, c, fr)));
+            break;
+        case 1:
+            AGWN_TRY((robust_run<T, P128>(*ctx, *r, p, n, o, c, fr)));
+            break;
+        default:
+            AGWN_TRY((robust_run<T, PF>(*ctx, *r, p, n, o, c, fr)));
+            break;
+        }
     }
     if (h_out)
         AGWN_TRY_CUDA(cudaMemcpyAsync(out, dout, sizeof(T) * n, cudaMemcpyDeviceToHost, ctx->stream));

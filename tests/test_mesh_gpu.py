@@ -352,7 +352,7 @@ def _clustered_queries(rng, n_clusters, lo=-1.6, hi=1.6, spread=0.03):
 
 @pytest.mark.parametrize("n_seg,seg_tile,qpt", [(212, 512, 2), (600, 512, 2), (600, 128, 4), (300, 64, 8)])
 def test_mixed_certified_groups_equal_the_per_pair_path(gwn, oracle, n_seg, seg_tile, qpt):
-    """Boundary groups of 16 entries that lie far enough across the ray from all of a warp's queries (every pair's
+    """Boundary groups of 8 entries that lie far enough across the ray from all of a warp's queries (every pair's
     error bound below the FP64 threshold, every angle in the first octant) are evaluated without the per-pair bound
     and octant unfolding.  The operations left are the per-pair path's own, so certification on and off give the
     same results bit for bit: one tile or several, chain starts inside groups, every queries-per-thread variant."""
@@ -403,6 +403,39 @@ def test_mixed_certified_groups_range_guard(gwn, oracle):
         assert np.array_equal(outs[1], outs[0])
         assert np.all(np.isfinite(outs[1]))
         assert np.abs(outs[1] - oracle.frac_batch(q, x0, s)).max() <= TOL_MIXED
+
+
+def test_mixed_incoherent_queries_run_in_spatial_order(gwn, oracle):
+    """Queries in random order (warps of scattered queries certify almost no boundary group) run on a copy sorted
+    along a 2D Morton curve across the ray and are scattered back: the same values bit for bit as the per-pair path
+    on the given order, and most pairs certified.  Full GWN and fractional term on device arrays of 2^20 queries
+    and more."""
+    torch = pytest.importorskip("torch")
+    from antipodal_gb300 import _lib
+    verts, idx, bnd, _, x0 = synth.open_icosphere(seed=2, level=6, grid=0)
+    rng = np.random.default_rng(9)
+    q = rng.uniform(-1.3, 1.3, size=((1 << 20) + 4099, 3))
+    qd = torch.from_numpy(q).cuda()
+    res = {}
+    for cert in (1, 0):
+        with gwn.CudaDispatcher(precision="mixed", timing=True) as d:
+            d.set_option(_lib.OPT_MIXED_CERTIFY, cert)
+            isect = gwn.CudaIntersector(d, verts, idx)
+            full = torch.empty(len(q), dtype=torch.float64, device="cuda")
+            gwn.eval_gwnr_mesh_batch(d, isect, qd, full, x0, bnd)
+            d.stats(reset=True)
+            frac = torch.empty_like(full)
+            gwn.eval_gwnr_mesh_batch_fractional(d, qd, frac, x0, bnd)
+            st = d.stats(reset=True)
+            isect.close()
+            res[cert] = (full.cpu().numpy(), frac.cpu().numpy(), st["certified_pairs"] / max(1, st["pairs"]))
+    assert np.array_equal(res[1][0], res[0][0])
+    assert np.array_equal(res[1][1], res[0][1])
+    assert res[0][2] == 0.0
+    assert res[1][2] > 0.5, res[1][2]
+    sample = rng.choice(len(q), 2000, replace=False)
+    ref = oracle.full_naive(q[sample], x0, verts, idx, bnd)
+    assert np.abs(res[1][0][sample] - ref).max() <= TOL_MIXED
 
 
 @pytest.mark.parametrize("n_seg", [4096, 4097])

@@ -229,6 +229,39 @@ def test_robust_mixed_exact_float_chunked_equals_single_chunks(gwn, disp):
         r.close()
 
 
+def test_robust_mixed_exact_float_incoherent_order(gwn, disp):
+    """exact_float mixed over 2^20 or more queries in random order runs on a spatially sorted copy (the mixed
+    kernel then certifies far more boundary groups) and scatters the results back: values and counts equal those of
+    the per-pair path on the given order bit for bit."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(43)
+    v, i = synth.noisy_mesh("torus", 6000, 7, rng)
+    b = synth.boundary_segments(v, i)
+    lo, hi = v.min(0), v.max(0)
+    q = rng.uniform(lo - 0.1 * (hi - lo), hi + 0.1 * (hi - lo), size=((1 << 20) + 333, 3))
+    r = gwn.CudaRobustMeshGwn(disp, v, i, b, precision="exact_float")
+    try:
+        disp.set_robust_precision("mixed")
+        qd = torch.from_numpy(q).cuda()
+        outs = {}
+        for cert in (1, 0):
+            disp.set_option(_lib.OPT_MIXED_CERTIFY, cert)
+            o = torch.empty(len(q), dtype=torch.float64, device="cuda")
+            c = torch.empty(len(q), dtype=torch.int32, device="cuda")
+            r.evaluate(qd, o, c)
+            f = np.empty(len(q))
+            o2 = np.empty(len(q))
+            r.evaluate(qd.cpu().numpy(), o2, None, f)  # host arrays with the separate fractional output
+            outs[cert] = (o.cpu().numpy(), c.cpu().numpy(), o2, f)
+        for k in range(4):
+            assert np.array_equal(outs[1][k], outs[0][k]), k
+        assert np.array_equal(outs[1][0], outs[1][2])
+    finally:
+        disp.set_option(_lib.OPT_MIXED_CERTIFY, 1)
+        disp.set_robust_precision("exact")
+        r.close()
+
+
 @pytest.mark.parametrize("pol", ["int64_grid", "int128_grid", "exact_float"])
 def test_robust_counts_cells_equal_the_walk(gwn, pol):
     """The robust counts with candidate leaves from the cell grid (default) and from the hierarchy walk (option 0):
