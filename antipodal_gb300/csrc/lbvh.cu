@@ -933,8 +933,10 @@ int ray_hierarchy(Context& ctx, const Bvh& bvh, const T* dir_host)
 }
 } // namespace
 
-// The cell grid of the cached hierarchy (its leaves' float (u, v) corners), about two cells per leaf over the
-// widened boxes' extent.  Leaf boxes are widened by 4 * 2^-18 of the scene scale; a query takes the grid while its
+// The cell grid of the cached hierarchy (its leaves' float (u, v) corners), about 16 cells per leaf over the
+// widened boxes' extent (at most 2^22 cells).  Finer cells hold fewer leaves, so a query reads fewer list entries:
+// on a 76,496-triangle icosphere with 256^3 grid queries 2 cells per leaf read 5.06 entries per query (1.09 ms),
+// 16 read 3.49 (0.83 ms); 32 and 64 gained no more.  Leaf boxes are widened by 4 * 2^-18 of the scene scale; a query takes the grid while its
 // own tolerance (qmax + scene) * 2^-18 stays below 3.5 * 2^-18 of the scene scale (qmax <= 2.5 * scene), which
 // leaves room for the one-ulp difference between the corners and the walk's outward-rounded boxes.
 int build_cells(Context& ctx, const Hier& h, float scene_scale, CellGrid& g)
@@ -968,7 +970,7 @@ int build_cells(Context& ctx, const Hier& h, float scene_scale, CellGrid& g)
     double const W = double(v.umax) - double(v.umin), H = double(v.vmax) - double(v.vmin);
     if (!(W > 0) || !(H > 0) || !std::isfinite(W) || !std::isfinite(H))
         return AGWN_OK;
-    double const target = double(std::min<int64_t>(std::max<int64_t>(2 * n, 1024), int64_t(1) << 22));
+    double const target = double(std::min<int64_t>(std::max<int64_t>(16 * n, 1024), int64_t(1) << 22));
     double const side = std::sqrt(W * H / target);
     v.gu = int(std::min(4096.0, std::max(1.0, std::ceil(W / side))));
     v.gv = int(std::min(4096.0, std::max(1.0, std::ceil(H / side))));
