@@ -408,7 +408,7 @@ def run_ours(args):
             "chosen_over_plain": plain_step / step_ms,
             "accuracy": accuracy,
             "kernels_ms_alone": {"fractional": frac_ms, "integer": int_ms,
-                                 "note": "each kernel timed alone over all queries; the timed steps run both in 8 "
+                                 "note": "each kernel timed alone over all queries; the timed steps run both in 4 "
                                          "chunks on two streams, overlapped"},
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                          "frac": achieved / peak, "traffic": traffic,
