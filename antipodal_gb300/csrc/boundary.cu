@@ -186,6 +186,8 @@ int boundary_build(agwn_context* ctx, const T* vertices, int64_t nv, const int32
     AGWN_TRY(va.alloc(sizeof(int) * m));
     AGWN_TRY(vb.alloc(sizeof(int) * m));
     AGWN_TRY(hist.alloc(sizeof(unsigned) * 256 * size_t(n_rs_blocks)));
+    Buf hsum;
+    AGWN_TRY(hsum.alloc(sizeof(unsigned) * size_t(scan_sums_count(int64_t(256) * n_rs_blocks))));
     AGWN_TRY(net.alloc(sizeof(int) * m));
     AGWN_TRY(emit.alloc(sizeof(unsigned) * m));
     AGWN_TRY(pos.alloc(sizeof(unsigned) * m));
@@ -207,7 +209,7 @@ int boundary_build(agwn_context* ctx, const T* vertices, int64_t nv, const int32
             int const shift = 32 * half + sh;
             k_rs_hist<unsigned long long><<<n_rs_blocks, kRsBlock, 0, st>>>(kin, m, shift, hist.as<unsigned>(),
                                                                             n_rs_blocks);
-            k_rs_scan<<<1, 1024, 0, st>>>(hist.as<unsigned>(), int64_t(256) * n_rs_blocks);
+            scan_counters(st, hist.as<unsigned>(), int64_t(256) * n_rs_blocks, hsum.as<unsigned>());
             k_rs_scatter<unsigned long long, int><<<n_rs_blocks, kRsBlock, 0, st>>>(
                 kin, vin, m, shift, hist.as<unsigned>(), n_rs_blocks, kout, vout);
             std::swap(kin, kout);

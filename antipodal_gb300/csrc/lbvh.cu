@@ -847,6 +847,8 @@ int build_hier(Context& ctx, const T* tri_in, int64_t n_tri, const double* dir, 
         AGWN_TRY(vals1.alloc(sizeof(unsigned) * n_tri));
         int const n_rs_blocks = div_up(n_tri, kRsTile);
         AGWN_TRY(hist.alloc(sizeof(unsigned) * 256 * n_rs_blocks));
+        Tmp hsum;
+        AGWN_TRY(hsum.alloc(sizeof(unsigned) * scan_sums_count(int64_t(256) * n_rs_blocks)));
         AGWN_TRY(left.alloc(sizeof(int) * n_tri));
         AGWN_TRY(right.alloc(sizeof(int) * n_tri));
         AGWN_TRY(pnode.alloc(sizeof(int) * n_tri));
@@ -871,7 +873,7 @@ int build_hier(Context& ctx, const T* tri_in, int64_t n_tri, const double* dir, 
         {
             int const shift = 8 * pass;
             k_rs_hist<<<n_rs_blocks, kRsBlock, 0, st>>>(ka, n_tri, shift, hist.as<unsigned>(), n_rs_blocks);
-            k_rs_scan<<<1, 1024, 0, st>>>(hist.as<unsigned>(), int64_t(256) * n_rs_blocks);
+            scan_counters(st, hist.as<unsigned>(), int64_t(256) * n_rs_blocks, hsum.as<unsigned>());
             k_rs_scatter<<<n_rs_blocks, kRsBlock, 0, st>>>(ka, va, n_tri, shift, hist.as<unsigned>(), n_rs_blocks, kb,
                                                            vb);
             std::swap(ka, kb);
@@ -980,9 +982,11 @@ int build_cells(Context& ctx, const Hier& h, float scene_scale, CellGrid& g)
     AGWN_TRY(g.offsets.reserve(sizeof(unsigned) * (n_cells + 1)));
     unsigned* const off = static_cast<unsigned*>(g.offsets.ptr);
     AGWN_TRY_CUDA(cudaMemsetAsync(off, 0, sizeof(unsigned) * (n_cells + 1), st));
+    Tmp osum;
+    AGWN_TRY(osum.alloc(sizeof(unsigned) * scan_sums_count(n_cells + 1)));
     AGWN_TRY(ctx.launch_begin(AGWN_K_OTHER));
     k_cell_bin<<<gl, 256, 0, st>>>(leaf_uv, n, margin, v, off, total64, nullptr, nullptr);
-    k_rs_scan<<<1, 1024, 0, st>>>(off, n_cells + 1);
+    scan_counters(st, off, n_cells + 1, osum.as<unsigned>());
     AGWN_TRY(ctx.launch_end(AGWN_K_OTHER));
     unsigned long long total = 0;
     AGWN_TRY_CUDA(cudaMemcpyAsync(&total, total64, sizeof(total), cudaMemcpyDeviceToHost, st));

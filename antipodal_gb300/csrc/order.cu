@@ -139,95 +139,6 @@ __global__ void k_order_keys(const double* __restrict__ pos, int64_t n, Across a
     }
 }
 
-// Exclusive scan of the m digit counters of a sort pass in three steps: block sums of 4,096 counters, one block
-// scanning those sums (1,024 at a time, with a carry), and each block scanning its counters from its offset.
-constexpr int kScanCnt = 4096; // counters per block: 1,024 threads x 4
-
-__device__ __forceinline__ unsigned block_exclusive(unsigned v, unsigned* warp_tot, unsigned* total)
-{
-    int const lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    unsigned x = v;
-    for (int o = 1; o < 32; o <<= 1)
-    {
-        unsigned const y = __shfl_up_sync(0xffffffffu, x, o);
-        if (lane >= o)
-            x += y;
-    }
-    if (lane == 31)
-        warp_tot[warp] = x;
-    __syncthreads();
-    if (warp == 0)
-    {
-        unsigned w = warp_tot[lane];
-        unsigned z = w;
-        for (int o = 1; o < 32; o <<= 1)
-        {
-            unsigned const y = __shfl_up_sync(0xffffffffu, z, o);
-            if (lane >= o)
-                z += y;
-        }
-        warp_tot[lane] = z - w; // exclusive offsets of the warps
-        if (lane == 31)
-            *total = z;
-    }
-    __syncthreads();
-    unsigned const r = warp_tot[warp] + x - v;
-    __syncthreads();
-    return r;
-}
-
-__global__ void __launch_bounds__(1024) k_cnt_sums(const unsigned* __restrict__ c, int64_t m, unsigned* __restrict__ sums)
-{
-    __shared__ unsigned wt[32];
-    __shared__ unsigned tot;
-    int64_t const i0 = int64_t(blockIdx.x) * kScanCnt + 4 * threadIdx.x;
-    unsigned v = 0;
-    for (int k = 0; k < 4; ++k)
-        v += i0 + k < m ? c[i0 + k] : 0u;
-    block_exclusive(v, wt, &tot);
-    if (threadIdx.x == 0)
-        sums[blockIdx.x] = tot;
-}
-
-__global__ void __launch_bounds__(1024) k_cnt_top(unsigned* __restrict__ sums, int nb)
-{
-    __shared__ unsigned wt[32];
-    __shared__ unsigned tot;
-    unsigned carry = 0;
-    for (int b0 = 0; b0 < nb; b0 += 1024)
-    {
-        int const b = b0 + int(threadIdx.x);
-        unsigned const v = b < nb ? sums[b] : 0u;
-        unsigned const e = block_exclusive(v, wt, &tot);
-        if (b < nb)
-            sums[b] = carry + e;
-        carry += tot;
-        __syncthreads();
-    }
-}
-
-__global__ void __launch_bounds__(1024) k_cnt_apply(unsigned* __restrict__ c, int64_t m,
-                                                    const unsigned* __restrict__ sums)
-{
-    __shared__ unsigned wt[32];
-    __shared__ unsigned tot;
-    int64_t const i0 = int64_t(blockIdx.x) * kScanCnt + 4 * threadIdx.x;
-    unsigned v[4];
-    unsigned t = 0;
-    for (int k = 0; k < 4; ++k)
-    {
-        v[k] = i0 + k < m ? c[i0 + k] : 0u;
-        t += v[k];
-    }
-    unsigned run = sums[blockIdx.x] + block_exclusive(t, wt, &tot);
-    for (int k = 0; k < 4; ++k)
-        if (i0 + k < m)
-        {
-            c[i0 + k] = run;
-            run += v[k];
-        }
-}
-
 __global__ void k_gather_queries(const double* __restrict__ pos, const int32_t* __restrict__ perm, int64_t n,
                                  double* __restrict__ out)
 {
@@ -291,7 +202,7 @@ int query_order(Context& ctx, const double* d_pos, int64_t n, const double* dir,
     // keys and indices, ping-pong buffers of the sort, its digit counters and their block sums
     int const n_rs_blocks = div_up(n, kRsTile);
     int64_t const n_cnt = int64_t(256) * n_rs_blocks;
-    int const n_cb = div_up(n_cnt, kScanCnt);
+    int64_t const n_cb = scan_sums_count(n_cnt);
     size_t const off_hist = sizeof(uint32_t) * 4 * size_t(n);
     void* base = nullptr;
     AGWN_TRY(ctx.scratch_reserve(S_ORDER0, off_hist + sizeof(unsigned) * (size_t(n_cnt) + size_t(n_cb)), &base));
@@ -314,9 +225,7 @@ int query_order(Context& ctx, const double* d_pos, int64_t n, const double* dir,
         int const shift = 8 * pass;
         AGWN_TRY(ctx.launch_begin(AGWN_K_OTHER));
         k_rs_hist<<<n_rs_blocks, kRsBlock, 0, st>>>(kin, n, shift, hist, n_rs_blocks);
-        k_cnt_sums<<<n_cb, 1024, 0, st>>>(hist, n_cnt, csum);
-        k_cnt_top<<<1, 1024, 0, st>>>(csum, n_cb);
-        k_cnt_apply<<<n_cb, 1024, 0, st>>>(hist, n_cnt, csum);
+        scan_counters(st, hist, n_cnt, csum);
         k_rs_scatter<<<n_rs_blocks, kRsBlock, 0, st>>>(kin, vin, n, shift, hist, n_rs_blocks, kout, vout);
         AGWN_TRY(ctx.launch_end(AGWN_K_OTHER));
         std::swap(kin, kout);

@@ -61,6 +61,112 @@ __global__ void __launch_bounds__(1024) k_rs_scan(unsigned* __restrict__ hist, i
     }
 }
 
+// The same exclusive scan in three parallel steps, for many counters (a sort pass's digit counters over millions of
+// keys, a cell grid's offsets): block sums of 4,096 counters, one block scanning those sums (1,024 at a time, with a
+// carry), and each block scanning its counters from its offset.  scan_counters launches the three; sums:
+// scan_sums_count(m) unsigned of scratch.
+constexpr int kScanCnt = 4096; // counters per block: 1,024 threads x 4
+
+__device__ __forceinline__ unsigned block_exclusive(unsigned v, unsigned* warp_tot, unsigned* total)
+{
+    int const lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned x = v;
+    for (int o = 1; o < 32; o <<= 1)
+    {
+        unsigned const y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o)
+            x += y;
+    }
+    if (lane == 31)
+        warp_tot[warp] = x;
+    __syncthreads();
+    if (warp == 0)
+    {
+        unsigned w = warp_tot[lane];
+        unsigned z = w;
+        for (int o = 1; o < 32; o <<= 1)
+        {
+            unsigned const y = __shfl_up_sync(0xffffffffu, z, o);
+            if (lane >= o)
+                z += y;
+        }
+        warp_tot[lane] = z - w; // exclusive offsets of the warps
+        if (lane == 31)
+            *total = z;
+    }
+    __syncthreads();
+    unsigned const r = warp_tot[warp] + x - v;
+    __syncthreads();
+    return r;
+}
+
+__global__ void __launch_bounds__(1024) k_cnt_sums(const unsigned* __restrict__ c, int64_t m, unsigned* __restrict__ sums)
+{
+    __shared__ unsigned wt[32];
+    __shared__ unsigned tot;
+    int64_t const i0 = int64_t(blockIdx.x) * kScanCnt + 4 * threadIdx.x;
+    unsigned v = 0;
+    for (int k = 0; k < 4; ++k)
+        v += i0 + k < m ? c[i0 + k] : 0u;
+    block_exclusive(v, wt, &tot);
+    if (threadIdx.x == 0)
+        sums[blockIdx.x] = tot;
+}
+
+__global__ void __launch_bounds__(1024) k_cnt_top(unsigned* __restrict__ sums, int nb)
+{
+    __shared__ unsigned wt[32];
+    __shared__ unsigned tot;
+    unsigned carry = 0;
+    for (int b0 = 0; b0 < nb; b0 += 1024)
+    {
+        int const b = b0 + int(threadIdx.x);
+        unsigned const v = b < nb ? sums[b] : 0u;
+        unsigned const e = block_exclusive(v, wt, &tot);
+        if (b < nb)
+            sums[b] = carry + e;
+        carry += tot;
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(1024) k_cnt_apply(unsigned* __restrict__ c, int64_t m,
+                                                    const unsigned* __restrict__ sums)
+{
+    __shared__ unsigned wt[32];
+    __shared__ unsigned tot;
+    int64_t const i0 = int64_t(blockIdx.x) * kScanCnt + 4 * threadIdx.x;
+    unsigned v[4];
+    unsigned t = 0;
+    for (int k = 0; k < 4; ++k)
+    {
+        v[k] = i0 + k < m ? c[i0 + k] : 0u;
+        t += v[k];
+    }
+    unsigned run = sums[blockIdx.x] + block_exclusive(t, wt, &tot);
+    for (int k = 0; k < 4; ++k)
+        if (i0 + k < m)
+        {
+            c[i0 + k] = run;
+            run += v[k];
+        }
+}
+
+inline int64_t scan_sums_count(int64_t m)
+{
+    return (m + kScanCnt - 1) / kScanCnt;
+}
+
+inline void scan_counters(cudaStream_t st, unsigned* c, int64_t m, unsigned* sums)
+{
+    int const nb = int(scan_sums_count(m));
+    if (nb == 0)
+        return;
+    k_cnt_sums<<<nb, 1024, 0, st>>>(c, m, sums);
+    k_cnt_top<<<1, 1024, 0, st>>>(sums, nb);
+    k_cnt_apply<<<nb, 1024, 0, st>>>(c, m, sums);
+}
+
 template <class K, class V>
 __global__ void __launch_bounds__(kRsBlock) k_rs_scatter(const K* __restrict__ kin, const V* __restrict__ vin,
                                                          int64_t n, int shift, const unsigned* __restrict__ hist,
