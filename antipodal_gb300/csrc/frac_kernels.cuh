@@ -653,6 +653,27 @@ __device__ __forceinline__ V atan_unit_lv(V t)
     return lv_mul(t, p);
 }
 
+// atan(t) for 0 <= t <= 0.125: t (1 - s / 3 + s^2 / 5 - s^3 / 7), s = t^2, the Taylor series cut after t^7 (its
+// relative truncation error is below s^4 / 9 = 6.6e-9 at t = 0.125, under float's 6e-8).
+template <class V>
+__device__ __forceinline__ V atan_small_lv(V t)
+{
+    V const s = lv_mul(t, t);
+    V p = lv_set<V>(-0.14285714285714285f);
+    p = lv_fma(p, s, lv_set<V>(0.2f));
+    p = lv_fma(p, s, lv_set<V>(-0.3333333333333333f));
+    p = lv_fma(p, s, lv_set<V>(1.f));
+    return lv_mul(t, p);
+}
+// The mixed kernel's atan on [0, 1]: the short series up to t = 0.125 (which holds every pair of a certified
+// group), the degree-8 fit above.  Both of the kernel's paths evaluate a small t with atan_small_lv, so they round
+// alike.
+__device__ __forceinline__ float2 atan_mixed_lv(float2 t)
+{
+    float2 const a = atan_small_lv(t), b = atan_unit_lv(t);
+    return make_float2(t.x <= 0.125f ? a.x : b.x, t.y <= 0.125f ? a.y : b.y);
+}
+
 // Per-vertex quantities of one boundary vertex relative to two queries (frame coordinates, one lane each):
 // v = vertex - query and the half-angle form (n, d) of l + z, l = |v|; d is NaN at a near vertex.
 struct VState2
@@ -866,7 +887,9 @@ __global__ void __launch_bounds__(256, mixed_min_blocks<K>())
         // the common case) the body has no branches: a term taken to FP64 adds an exact zero to the TwoSum, so the
         // compiler schedules consecutive entries together.  With may_start true a chain start skips the pair term.
         // The arithmetic runs on packed pairs of queries; selects and comparisons per lane.
-        auto vertex = [&](SegM const& ent, VState2 (&cv)[KP])
+        // near: the NaN for a vertex within its near distance (a certified group has none, and its states come out
+        // the same without the test)
+        auto vertex = [&](SegM const& ent, VState2 (&cv)[KP], bool near)
         {
             float4 const A = ent.a, B = ent.b, C = ent.c;
             float2 const ax = lv_set<float2>(A.x), ay = lv_set<float2>(A.y), az = lv_set<float2>(A.z), cx = lv_set<float2>(C.x), cy = lv_set<float2>(C.y), cz = lv_set<float2>(C.z);
@@ -886,14 +909,14 @@ __global__ void __launch_bounds__(256, mixed_min_blocks<K>())
                 float2 const lpz = lv_add(l, c.z), lmz = lv_sub(l, c.z);
                 float const nan = __int_as_float(0x7fffffff);
                 c.n = make_float2(c.z.x >= 0.f ? lpz.x : r.x, c.z.y >= 0.f ? lpz.y : r.y);
-                c.d = make_float2(q.x < B.w ? nan : (c.z.x >= 0.f ? 1.f : lmz.x),
-                                  q.y < B.w ? nan : (c.z.y >= 0.f ? 1.f : lmz.y));
+                float2 const d = make_float2(c.z.x >= 0.f ? 1.f : lmz.x, c.z.y >= 0.f ? 1.f : lmz.y);
+                c.d = near ? make_float2(q.x < B.w ? nan : d.x, q.y < B.w ? nan : d.y) : d;
             }
         };
         // a certified pair term: the full path's operations with need = false, |num| <= den and den > 0
         auto fast = [&](SegM const& ent, VState2 (&pv)[KP], VState2 (&cv)[KP])
         {
-            vertex(ent, cv);
+            vertex(ent, cv, false);
             float4 const A = ent.a, B = ent.b;
             float2 const by = lv_set<float2>(B.y), nbx = lv_set<float2>(-B.x), w = lv_set<float2>(A.w);
 #pragma unroll
@@ -907,14 +930,14 @@ __global__ void __launch_bounds__(256, mixed_min_blocks<K>())
                 float2 const den_s = lv_fma(lv_fma(v0.x, v1.x, lv_mul(v0.y, v1.y)), D, nn);
                 float2 const an = make_float2(fabsf(num_s.x), fabsf(num_s.y));
                 float2 const inv = make_float2(rcp_approx(den_s.x), rcp_approx(den_s.y));
-                float2 const a = atan_unit_lv(lv_mul(an, inv));
+                float2 const a = atan_small_lv(lv_mul(an, inv)); // t <= 0.101 here
                 float2 const ang = make_float2(copysignf(a.x, num_s.x), copysignf(a.y, num_s.y));
                 two_sum_lv(acc[p], comp[p], lv_mul(w, ang));
             }
         };
         auto step = [&](SegM const& ent, VState2 (&pv)[KP], VState2 (&cv)[KP], bool may_start, int slot)
         {
-            vertex(ent, cv);
+            vertex(ent, cv, true);
             float4 const A = ent.a, B = ent.b, C = ent.c;
             int const sidx = __float_as_int(C.w);
             if (may_start && sidx < 0)
@@ -962,7 +985,7 @@ __global__ void __launch_bounds__(256, mixed_min_blocks<K>())
                 nb |= (need0 ? (1u << (slot * K + 2 * p)) : 0u) | (need1 ? (1u << (slot * K + 2 * p + 1)) : 0u);
                 // atan2(num_s, den_s): atan(t) in [0, pi/4], then the octant as |c1 - a| (pi/2 - a when |num| >
                 // |den|, else a) and |c2 - a| (pi - a when den < 0, else a), signed like num
-                float2 const a = atan_unit_lv(t);
+                float2 const a = atan_mixed_lv(t);
                 float2 const c1 = make_float2(sw0 ? 1.5707963267948966f : 0.f, sw1 ? 1.5707963267948966f : 0.f);
                 float2 const a1 = lv_sub(c1, a);
                 float2 const c2 = make_float2(den_s.x < 0.f ? 3.141592653589793f : 0.f,

@@ -130,3 +130,34 @@ def test_fit_in_float_meets_the_stated_bound():
     nz = t > 0
     rel = np.abs(r[nz] - exact[nz]) / exact[nz]
     assert rel.max() < 3.0e-7  # a few float ulps
+
+
+def small_series_coefficients():
+    """The coefficients of atan_small_lv (the short series of the certified groups), highest degree first."""
+    text = open(KERNELS).read()
+    body = text[text.index("V atan_small_lv(V t)"):]
+    body = body[:body.index("return")]
+    return [float(x) for x in re.findall(r"(-?\d+\.\d*(?:e-?\d+)?)f", body)]
+
+
+def test_small_series_is_the_taylor_series_and_meets_its_bound():
+    """atan_small_lv evaluates atan(t) = t (1 - s/3 + s^2/5 - s^3/7) for t <= 0.125 (every pair of a certified group
+    has t <= 0.101).  Its coefficients are the Taylor series' own, and evaluated in float32 Horner FMAs like the
+    device it stays within a few float ulps of FP64 atan there (the truncation itself is below 6.6e-9)."""
+    c = small_series_coefficients()
+    assert np.allclose(c, [-1 / 7, 1 / 5, -1 / 3, 1.0], rtol=1e-7, atol=0)
+    t = np.linspace(0.0, 0.125, 200_001).astype(np.float32)
+    s = (t * t).astype(np.float32)
+    p = np.float32(c[0])
+    for a in c[1:]:
+        p = (p.astype(np.float64) * s + np.float32(a)).astype(np.float32)
+    r = (t * p).astype(np.float32).astype(np.float64)
+    exact = np.arctan(t.astype(np.float64))
+    nz = t > 0
+    rel = np.abs(r[nz] - exact[nz]) / exact[nz]
+    assert rel.max() < 2.0e-7
+    # the truncation alone, in FP64
+    t64 = np.linspace(1e-6, 0.125, 10_001)
+    s64 = t64 * t64
+    trunc = np.abs(t64 * (1 - s64 / 3 + s64 ** 2 / 5 - s64 ** 3 / 7) - np.arctan(t64)) / np.arctan(t64)
+    assert trunc.max() < 6.6e-9
