@@ -892,7 +892,8 @@ __global__ void __launch_bounds__(256, mixed_min_blocks<K>())
         auto vertex = [&](SegM const& ent, VState2 (&cv)[KP], bool near)
         {
             float4 const A = ent.a, B = ent.b, C = ent.c;
-            float2 const ax = lv_set<float2>(A.x), ay = lv_set<float2>(A.y), az = lv_set<float2>(A.z), cx = lv_set<float2>(C.x), cy = lv_set<float2>(C.y), cz = lv_set<float2>(C.z);
+            float2 const ax = lv_set<float2>(A.x), ay = lv_set<float2>(A.y), az = lv_set<float2>(A.z);
+            float2 const cx = lv_set<float2>(C.x), cy = lv_set<float2>(C.y), cz = lv_set<float2>(C.z);
 #pragma unroll
             for (int p = 0; p < KP; ++p)
             {
@@ -1145,7 +1146,8 @@ __global__ void __launch_bounds__(256, mixed_min_blocks<K>())
             }
         }
         atomicAdd(reinterpret_cast<unsigned long long*>(counters), static_cast<unsigned long long>(fq.tail));
-        atomicAdd(reinterpret_cast<unsigned long long*>(counters + 3), static_cast<unsigned long long>(n_cert * 32 * K));
+        atomicAdd(reinterpret_cast<unsigned long long*>(counters + 3),
+                  static_cast<unsigned long long>(n_cert * 32 * K));
         atomicAdd(reinterpret_cast<unsigned long long*>(counters + 1), static_cast<unsigned long long>(tot));
     }
 }

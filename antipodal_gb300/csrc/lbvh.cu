@@ -938,9 +938,10 @@ int ray_hierarchy(Context& ctx, const Bvh& bvh, const T* dir_host)
 // The cell grid of the cached hierarchy (its leaves' float (u, v) corners), about 16 cells per leaf over the
 // widened boxes' extent (at most 2^22 cells).  Finer cells hold fewer leaves, so a query reads fewer list entries:
 // on a 76,496-triangle icosphere with 256^3 grid queries 2 cells per leaf read 5.06 entries per query (1.09 ms),
-// 16 read 3.49 (0.83 ms); 32 and 64 gained no more.  Leaf boxes are widened by 4 * 2^-18 of the scene scale; a query takes the grid while its
-// own tolerance (qmax + scene) * 2^-18 stays below 3.5 * 2^-18 of the scene scale (qmax <= 2.5 * scene), which
-// leaves room for the one-ulp difference between the corners and the walk's outward-rounded boxes.
+// 16 read 3.49 (0.83 ms); 32 and 64 gained no more.  Leaf boxes are widened by 4 * 2^-18 of the scene scale; a
+// query takes the grid while its own tolerance (qmax + scene) * 2^-18 stays below 3.5 * 2^-18 of the scene scale
+// (qmax <= 2.5 * scene), which leaves room for the one-ulp difference between the corners and the walk's
+// outward-rounded boxes.
 int build_cells(Context& ctx, const Hier& h, float scene_scale, CellGrid& g)
 {
     g.valid = false;

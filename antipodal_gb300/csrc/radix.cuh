@@ -100,7 +100,8 @@ __device__ __forceinline__ unsigned block_exclusive(unsigned v, unsigned* warp_t
     return r;
 }
 
-__global__ void __launch_bounds__(1024) k_cnt_sums(const unsigned* __restrict__ c, int64_t m, unsigned* __restrict__ sums)
+__global__ void __launch_bounds__(1024) k_cnt_sums(const unsigned* __restrict__ c, int64_t m,
+                                                   unsigned* __restrict__ sums)
 {
     __shared__ unsigned wt[32];
     __shared__ unsigned tot;
