@@ -116,8 +116,9 @@ class CudaDispatcher:
     accumulation and FP64 near / ill-conditioned / branch-cut pairs; double inputs), ``tau`` (mixed mode
     near-pair ratio), ``term_err`` (mixed mode per-pair FP32 error bound, radians),
     ``queries_per_thread``, ``block`` (0: automatic) and ``seg_tile`` (kernel shape), ``timing`` (CUDA-event
-    kernel timing), ``mixed_min_pairs`` (below this many (query, segment) pairs per call the mixed modes run the
-    exact kernels; None keeps the library default, 2^20).
+    kernel timing), ``mixed_min_pairs`` (below this many (query, segment) pairs per call, or on a boundary of
+    fewer than 32 segments, the mixed modes run the exact kernels; 0 always runs the mixed ones; None keeps the
+    library default, 2^14).
     Like PoolDispatcher it runs one job at a time.  ``parallel_for`` is not provided: arbitrary host callables
     have no device form here, and the library has no CPU fallback.
     """

@@ -158,7 +158,7 @@ struct Context
     const agwn_mlp* panel_mlp = nullptr; // the per-panel network of the double-float integrator (or none)
     float panel_beta = 0.02f;
     int integer_cells = 1;
-    double mixed_min_pairs = double(1 << 20);
+    double mixed_min_pairs = double(1 << 14);
     bool mixed_certify = true;
     // the spatial order of the queries (order.cu): the last decision and its key, and whether an evaluation on an
     // ordered copy is running (no second ordering inside it)
@@ -182,6 +182,19 @@ struct Context
     cudaEvent_t ev_end[kMaxPending] = {};
     int pending_class[kMaxPending] = {};
     int n_pending = 0;
+
+    // Whether a mixed-mode call of `pairs` (query, segment) pairs over a boundary of n_seg segments runs the mixed
+    // kernels: at least mixed_min_pairs pairs over at least kMixedMinSegments segments, or always with the minimum 0.
+    // The exact kernel's time follows the boundary's length (each thread's chain of FP64 terms), the mixed kernel's
+    // has a fixed part (the boundary's preparation) and, over long segments, many pairs within the near distance
+    // that go to FP64 anyway: on a GB300 the exact kernels were faster below 32 segments at every query count tried
+    // (2,000 to 200,000 random queries; 4 segments and 2e5 queries: 202 against 297 us), the mixed ones from 64
+    // segments at every count (64 segments and 2,000 queries: 293 against 537 us; 128: 198 against 1,065 us).
+    static constexpr int64_t kMixedMinSegments = 32;
+    bool use_mixed(double pairs, int64_t n_seg) const
+    {
+        return mixed_min_pairs == 0.0 || (pairs >= mixed_min_pairs && n_seg >= kMixedMinSegments);
+    }
 
     int scratch_reserve(int slot, size_t bytes, void** out);
     // Brackets a launch with timing events when AGWN_OPT_TIMING is on; always counts the launch.

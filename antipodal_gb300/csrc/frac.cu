@@ -84,10 +84,10 @@ struct FracPlan
     Frame* frame = nullptr;
 };
 
-// n_queries: the queries the plan will serve.  Below ctx.mixed_min_pairs (query, segment) pairs the mixed mode runs
-// the exact kernels: its one-block boundary preparation would cost more than the FP64 pairs it saves (a 4-segment
-// boundary with 1e5 queries: 0.21 ms mixed, 0.17 ms exact), and the exact form is the more accurate one.  So does
-// a boundary of 2^24 segments or more, beyond the mixed kernel's FP64 queue entries (24-bit segment indices).
+// n_queries: the queries the plan will serve.  On a boundary shorter than 32 segments, or below ctx.mixed_min_pairs
+// (query, segment) pairs, the mixed mode runs the exact kernels (Context::use_mixed: there they are the faster ones,
+// and the exact form is the more accurate one).  So does a boundary of 2^24 segments or more, beyond the mixed
+// kernel's FP64 queue entries (24-bit segment indices).
 // force_mixed: the mixed form whatever the context's fractional mode and the size (double only).
 template <class T>
 int fractional_prepare(Context& ctx, const T* x0_host, const T* d_seg_raw, int64_t n_seg, int64_t n_queries,
@@ -105,7 +105,7 @@ int fractional_prepare(Context& ctx, const T* x0_host, const T* d_seg_raw, int64
         return AGWN_OK;
     AGWN_CHECK_ARG(n_seg < (int64_t(1) << 31), "at most 2^31 - 1 boundary segments");
     p.mixed = (force_mixed || (ctx.frac_mode == AGWN_FRAC_MIXED && n_seg < (int64_t(1) << 24) &&
-                               double(n_queries) * double(n_seg) >= ctx.mixed_min_pairs)) &&
+                               ctx.use_mixed(double(n_queries) * double(n_seg), n_seg))) &&
               sizeof(T) == 8;
     if (!p.mixed)
     {
@@ -480,7 +480,7 @@ int mesh_batch(agwn_context* ctx, const agwn_bvh* bvh, const T* positions, int64
         // mixed mode on device arrays: an incoherent query order runs on a spatially sorted copy (order.cu), where
         // the mixed kernel certifies far more boundary groups; the values are the same bit for bit
         if (want_frac && n_seg > 0 && ctx->frac_mode == AGWN_FRAC_MIXED && !ctx->ordering &&
-            n_seg < (int64_t(1) << 24) && double(n) * double(n_seg) >= ctx->mixed_min_pairs &&
+            n_seg < (int64_t(1) << 24) && ctx->use_mixed(double(n) * double(n_seg), n_seg) &&
             is_device_pointer(positions) && is_device_pointer(out))
         {
             double const dir[3] = {x0[0], x0[1], x0[2]};

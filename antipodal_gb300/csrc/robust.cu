@@ -228,7 +228,8 @@ int robust_run(Context& ctx, const Robust& r, const T* d_pos, int64_t n, T* d_ou
         // mixed exact_float over many queries: counts and fractional term in chunks on two streams, so that one
         // chunk's counts (FP64 predicates) overlap another chunk's fractional term (FP32 pairs)
         if (!counts_ready && !d_frac && n >= (int64_t(1) << 21) && r.n_tri > 1 && ctx.integer_cells &&
-            ctx.robust_mode == AGWN_ROBUST_MIXED && r.n_seg > 0 && r.n_seg < (int64_t(1) << 24))
+            ctx.robust_mode == AGWN_ROBUST_MIXED && r.n_seg > 0 && r.n_seg < (int64_t(1) << 24) &&
+            ctx.use_mixed(double(n) * double(r.n_seg), r.n_seg))
         {
             if (!r.cells.valid)
                 AGWN_TRY(build_cells(ctx, r.hier, float(r.hier.scale), r.cells));
@@ -284,9 +285,9 @@ int robust_run(Context& ctx, const Robust& r, const T* d_pos, int64_t n, T* d_ou
     if constexpr (std::is_same_v<P, PF> && std::is_same_v<T, double>)
     {
         // mixed exact_float: the mesh functions' mixed kernel with the robust FP64 rule (frac.cu)
-        // (below ctx.mixed_min_pairs pairs the exact kernel is the faster one, as for the mesh functions)
+        // (on short boundaries and small calls the exact kernel is the faster one: Context::use_mixed)
         if (ctx.robust_mode == AGWN_ROBUST_MIXED && r.n_seg > 0 && r.n_seg < (int64_t(1) << 24) &&
-            double(n) * double(r.n_seg) >= ctx.mixed_min_pairs)
+            ctx.use_mixed(double(n) * double(r.n_seg), r.n_seg))
         {
             double* raw = nullptr;
             AGWN_TRY(ctx.scratch_reserve(S_MISC2, sizeof(double) * 7 * size_t(r.n_seg), reinterpret_cast<void**>(&raw)));
@@ -394,7 +395,7 @@ int robust_eval(agwn_context* ctx, const agwn_robust* r, const T* positions, int
         // exact_float in mixed mode: an incoherent query order runs on a spatially sorted copy (order.cu), where the
         // mixed kernel certifies far more boundary groups; the values are the same bit for bit
         if (r->policy == 2 && ctx->robust_mode == AGWN_ROBUST_MIXED && !ctx->ordering && r->n_seg > 0 &&
-            r->n_seg < (int64_t(1) << 24) && double(n) * double(r->n_seg) >= ctx->mixed_min_pairs)
+            r->n_seg < (int64_t(1) << 24) && ctx->use_mixed(double(n) * double(r->n_seg), r->n_seg))
         {
             double const dir[3] = {-1.0, 0.0, 0.0}; // the evaluator's rays and fractional frame run along -x
             const int32_t* perm = nullptr;

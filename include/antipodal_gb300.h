@@ -101,8 +101,10 @@ enum agwn_option
        direction) and cached with the hierarchy; 0 walks the hierarchy for every ray.  Counts are the same. */
     AGWN_OPT_INTEGER_CELLS = 10,
     /* Mixed modes (mesh, and the robust evaluator's exact_float): below this many (query, segment) pairs in one
-       call the exact FP64 kernels run instead, which are the faster ones there (the mixed form's boundary
-       preparation costs more than the FP64 pairs it saves).  Default 2^20; 0 always runs the mixed form. */
+       call, or on a boundary of fewer than 32 segments, the exact FP64 kernels run instead, which are the faster
+       ones there (the mixed form's boundary preparation costs more than the FP64 pairs it saves, and over long
+       segments most pairs fall within the near distance that sends them to FP64).  Default 2^14; 0 always runs
+       the mixed form. */
     AGWN_OPT_MIXED_MIN_PAIRS = 11,
     /* Mixed kernel: 1 (default) evaluates the boundary groups that a warp's queries certify (every pair far enough
        across the ray for its error bound to pass and its angle to lie in the first octant) without the per-pair

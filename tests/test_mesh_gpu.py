@@ -489,21 +489,22 @@ def test_integer_cells_equal_the_walk_and_the_oracle(gwn, oracle, dtype):
 
 
 def test_mixed_mode_runs_exact_kernels_below_its_minimum(gwn, oracle):
-    # below the minimum pair count (default 2^20 per call) the mixed mode runs the exact kernels: bit-identical to
-    # the exact mode; with the minimum at 0 it runs the mixed kernel (within the mixed tolerance)
+    # on a boundary of fewer than 32 segments (and below the minimum pair count, default 2^14 per call) the mixed
+    # mode runs the exact kernels: bit-identical to the exact mode; with the minimum at 0 it runs the mixed kernel
+    # (within the mixed tolerance)
     from antipodal_gb300 import _lib
     verts, idx, bnd, q, x0 = synth.rotated_open_cube(seed=3, n_queries=20_000)
     with gwn.CudaDispatcher() as d:
-        assert d.get_option(_lib.OPT_MIXED_MIN_PAIRS) == float(1 << 20)
+        assert d.get_option(_lib.OPT_MIXED_MIN_PAIRS) == float(1 << 14)
         isect = gwn.CudaIntersector(d, verts, idx)
         outs = {}
-        for prec, minp in (("exact", 1 << 20), ("mixed", 1 << 20), ("mixed", 0)):
+        for prec, minp in (("exact", 1 << 14), ("mixed", 1 << 14), ("mixed", 0)):
             d.set_precision(prec)
             d.set_option(_lib.OPT_MIXED_MIN_PAIRS, minp)
             o = np.empty(len(q))
             gwn.eval_gwnr_mesh_batch(d, isect, q, o, x0, bnd)
             outs[(prec, minp)] = o
         isect.close()
-    assert np.array_equal(outs[("mixed", 1 << 20)], outs[("exact", 1 << 20)])
-    assert np.abs(outs[("mixed", 0)] - outs[("exact", 1 << 20)]).max() <= TOL_MIXED
-    assert np.abs(outs[("exact", 1 << 20)] - oracle.full_naive(q, x0, verts, idx, bnd)).max() <= TOL_EXACT64
+    assert np.array_equal(outs[("mixed", 1 << 14)], outs[("exact", 1 << 14)])
+    assert np.abs(outs[("mixed", 0)] - outs[("exact", 1 << 14)]).max() <= TOL_MIXED
+    assert np.abs(outs[("exact", 1 << 14)] - oracle.full_naive(q, x0, verts, idx, bnd)).max() <= TOL_EXACT64
