@@ -438,6 +438,35 @@ def test_mixed_incoherent_queries_run_in_spatial_order(gwn, oracle):
     assert np.abs(res[1][0][sample] - ref).max() <= TOL_MIXED
 
 
+def test_mixed_query_order_decision_is_only_a_speed_matter(gwn):
+    """The order decision is kept per (array, size, direction).  Overwriting the same device array with queries in
+    another order keeps the old decision; either way the values equal those of a fresh context bit for bit."""
+    torch = pytest.importorskip("torch")
+    verts, idx, bnd, _, x0 = synth.open_icosphere(seed=5, level=5, grid=0)
+    n = (1 << 20) + 77
+    rng = np.random.default_rng(13)
+    q_rand = rng.uniform(-1.3, 1.3, size=(n, 3))
+    side = int(np.ceil(n ** (1 / 3)))
+    q_grid = synth.grid_queries(verts.min(0), verts.max(0), side, 1.2)[:n]
+    qd = torch.from_numpy(q_rand).cuda()
+    out = torch.empty(n, dtype=torch.float64, device="cuda")
+
+    def fresh(q):
+        with gwn.CudaDispatcher(precision="mixed") as d:
+            o = torch.empty(n, dtype=torch.float64, device="cuda")
+            gwn.eval_gwnr_mesh_batch_fractional(d, torch.from_numpy(q).cuda(), o, x0, bnd)
+            return o.cpu().numpy()
+
+    with gwn.CudaDispatcher(precision="mixed") as d:
+        gwn.eval_gwnr_mesh_batch_fractional(d, qd, out, x0, bnd)  # decided incoherent: sorted
+        first = out.cpu().numpy()
+        qd.copy_(torch.from_numpy(q_grid))  # the same array, now in grid order; the kept decision still sorts
+        gwn.eval_gwnr_mesh_batch_fractional(d, qd, out, x0, bnd)
+        second = out.cpu().numpy()
+    assert np.array_equal(first, fresh(q_rand))
+    assert np.array_equal(second, fresh(q_grid))
+
+
 @pytest.mark.parametrize("n_seg", [4096, 4097])
 def test_mixed_chain_limit(gwn, oracle, n_seg):
     # up to 4096 segments the boundary is chained; above, every segment is a chain of its own
