@@ -159,7 +159,7 @@ __device__ __forceinline__ double gk15_panel(const double* c, ev3<rd> p, ev3<rd>
 // ---- double-float form ----------------------------------------------------------------------------------------
 // The same integrand and panel rule in double-float arithmetic (df32.cuh, ~44 significant bits on the FP32 pipe):
 // the curve's control points relative to the query, the Bernstein basis and its derivative in closed form, the
-// normalisation and w - d_eta as above.  Not bit-identical to the reference (the value differs in the last ~1e-13
+// normalisation, and w - d_eta in the closed form below (the same quantity, fewer operations).  Not bit-identical to the reference (the value differs in the last ~1e-13
 // relative, and a panel whose |Ik - Ig| sits at the tolerance can be decided the other way); the tree rule, the
 // tolerances and the summation order are the plain integrator's.
 struct alignas(16) CurveDF
@@ -197,8 +197,16 @@ __device__ __forceinline__ df df_mulf(df a, float f)
     return fast_two_sum(p.hi, __fmaf_rn(a.lo, f, p.lo));
 }
 
-// w(t) - d_eta(t) with cp = the curve's control points minus the query.
-__device__ __forceinline__ df integrand_df(const df (&cp)[12], df3 x0, df t)
+// w(t) - d_eta(t) with cp = the curve's control points minus the query, in closed form.  The plain kernel evaluates
+// the reference's expression (integrand, gwn_parametric.hh:73-103): with G = r / |r|, G' its derivative, a = x0.G,
+// X = x0 - G a, X' = -(G (x0.G') + G' a), v = G - x0 a, v' = G' - x0 (x0.G'), d_eta = G.(X x X') / |X|^2 and
+// w = -x0.(v x v') / |v|^2.  Expanding (G x G = 0, G.(G x G') = 0, |G| = 1): G.(X x X') = a c and
+// x0.(v x v') = c with c = x0.(G x G'), |X|^2 = n - a^2 = |x0 x G|^2 (Lagrange's identity) and
+// |v|^2 = 1 + (n - 2) a^2 with n = |x0|^2.  So w - d_eta = -c / (1 + (n - 2) a^2) - a c / |x0 x G|^2, and for a
+// unit x0 (n = 1 to double precision) -c / (1 - a), free of the two terms' cancellation near a = -1.  Near a = 1
+// (the curve crossing the ray of x0 from the query) 1 - a, formed by subtraction, would keep only the square of the
+// angle's relative precision; there it is |x0 x G|^2 / (1 + a), whose cross product keeps the angle's own.
+__device__ __forceinline__ df integrand_df(const df (&cp)[12], df3 x0, df x0n, bool unit, df t)
 {
     df const u = df_make(1.f) - t;
     df const uu = u * u, tt = t * t, ut = u * t;
@@ -217,23 +225,27 @@ __device__ __forceinline__ df integrand_df(const df (&cp)[12], df3 x0, df t)
     df const s1 = dot(r, dr) * inv_s; // (2 r.dr) * (0.5 / s)
     df3 const G = r * inv_s;
     df3 const Gp = (dr - G * s1) * inv_s;
-    df const a = dot(x0, G), ap = dot(x0, Gp);
-    df3 const X = x0 - G * a;
-    df3 const Gap = G * ap, Gpa = Gp * a;
-    df3 const Xp{df_neg(Gap.x + Gpa.x), df_neg(Gap.y + Gpa.y), df_neg(Gap.z + Gpa.z)};
-    df const d_eta = dot(G, cross(X, Xp)) / dot(X, X);
-    // x1 = -x0, so x1 (x1 . G) = x0 (x0 . G)
-    df3 const v = G - x0 * a, vp = Gp - x0 * ap;
-    df const w = df_neg(dot(x0, cross(v, vp))) / dot(v, v);
-    return w - d_eta;
+    df const a = dot(x0, G);
+    df const c = dot(x0, cross(G, Gp));
+    df3 const xg = cross(x0, G);
+    df const xg2 = dot(xg, xg);
+    if (unit)
+    {
+        bool const ahead = a.hi >= 0.f;
+        df const num = ahead ? c * (df_make(1.f) + a) : c;
+        df const den = ahead ? xg2 : df_make(1.f) - a;
+        return df_neg(num / den);
+    }
+    return df_neg(c / (df_make(1.f) + (x0n - df_make(2.f)) * (a * a))) - (a * c) / xg2;
 }
 
-__device__ __forceinline__ double gk15_panel_df(const df (&cp)[12], df3 x0, int depth, uint32_t j, float* err)
+__device__ __forceinline__ double gk15_panel_df(const df (&cp)[12], df3 x0, df x0n, bool unit, int depth, uint32_t j,
+                                                float* err)
 {
     float const scale = ldexpf(1.f, -depth);
     float const h = 0.5f * scale;
     df const cc = two_sum(float(j) * scale, h); // both exact: the centre (j + 1/2) 2^-depth
-    df const f0 = integrand_df(cp, x0, cc);
+    df const f0 = integrand_df(cp, x0, x0n, unit, cc);
     // the Kronrod and Gauss sums accumulated node pair by node pair, in the order of the sums above (the same
     // values), so no node value stays live
     df ig = kGkWgdf[0] * f0;
@@ -242,7 +254,7 @@ __device__ __forceinline__ double gk15_panel_df(const df (&cp)[12], df3 x0, int 
     for (int k = 1; k <= 7; ++k)
     {
         df const dx = df_scale(kGkXdf[k], h);
-        df const s = integrand_df(cp, x0, cc - dx) + integrand_df(cp, x0, cc + dx);
+        df const s = integrand_df(cp, x0, x0n, unit, cc - dx) + integrand_df(cp, x0, x0n, unit, cc + dx);
         ik = ik + kGkWkdf[k] * s;
         if ((k & 1) == 0)
             ig = ig + kGkWgdf[k >> 1] * s;
@@ -336,6 +348,9 @@ __global__ void __launch_bounds__(kParamBlock, param_min_blocks<DF, PANEL>()) k_
     double* const slab = pair_vals + size_t(blockIdx.x) * kParamBlock * tile;
     ev3<rd> const x0{rd(x0x), rd(x0y), rd(x0z)};
     df3 const x0df{df_from(x0x), df_from(x0y), df_from(x0z)};
+    double const x0n = x0x * x0x + x0y * x0y + x0z * x0z;
+    bool const x0_unit = fabs(x0n - 1.0) <= 1e-15;
+    df const x0n_df = df_from(x0n);
     int64_t const n_blocks_q = (n + kParamBlock - 1) / kParamBlock;
     int const n_tiles = int((n_curves + tile - 1) / tile);
     int const tiles_per_group = (n_tiles + n_groups - 1) / n_groups;
@@ -499,7 +514,7 @@ __global__ void __launch_bounds__(kParamBlock, param_min_blocks<DF, PANEL>()) k_
                 if constexpr (DF)
                 {
                     float e32;
-                    v = gk15_panel_df(cp, x0df, d, j, &e32);
+                    v = gk15_panel_df(cp, x0df, x0n_df, x0_unit, d, j, &e32);
                     err = double(e32);
                 }
                 else
