@@ -202,10 +202,14 @@ __device__ __forceinline__ df df_mulf(df a, float f)
 // X = x0 - G a, X' = -(G (x0.G') + G' a), v = G - x0 a, v' = G' - x0 (x0.G'), d_eta = G.(X x X') / |X|^2 and
 // w = -x0.(v x v') / |v|^2.  Expanding (G x G = 0, G.(G x G') = 0, |G| = 1): G.(X x X') = a c and
 // x0.(v x v') = c with c = x0.(G x G'), |X|^2 = n - a^2 = |x0 x G|^2 (Lagrange's identity) and
-// |v|^2 = 1 + (n - 2) a^2 with n = |x0|^2.  So w - d_eta = -c / (1 + (n - 2) a^2) - a c / |x0 x G|^2, and for a
-// unit x0 (n = 1 to double precision) -c / (1 - a), free of the two terms' cancellation near a = -1.  Near a = 1
-// (the curve crossing the ray of x0 from the query) 1 - a, formed by subtraction, would keep only the square of the
-// angle's relative precision; there it is |x0 x G|^2 / (1 + a), whose cross product keeps the angle's own.
+// |v|^2 = 1 + (n - 2) a^2 with n = |x0|^2.  In terms of r itself (s = |r|, q = s^2, m = x0.r, G x G' = r x r' / q,
+// so c = T / q with T = x0.(r x r') = r'.(x0 x r)):
+//   w - d_eta = -T / (q + (n - 2) m^2) - m T / (s |x0 x r|^2),
+// and for a unit x0 (n = 1 to double precision) -T / (s (s - m)), free of the two terms' cancellation near
+// m = -s.  Near m = s (the curve crossing the ray of x0 from the query) s - m, formed by subtraction, would keep
+// only the square of the angle's relative precision; there it is |x0 x r|^2 / (s + m), whose cross product keeps
+// the angle's own.  For a unit x0: one square root and one quotient, against the expression's square root and three
+// quotients.
 __device__ __forceinline__ df integrand_df(const df (&cp)[12], df3 x0, df x0n, bool unit, df t)
 {
     df const u = df_make(1.f) - t;
@@ -220,23 +224,18 @@ __device__ __forceinline__ df integrand_df(const df (&cp)[12], df3 x0, df x0n, b
     dr.x = d0 * cp[0] + d1 * cp[3] + d2 * cp[6] + d3 * cp[9];
     dr.y = d0 * cp[1] + d1 * cp[4] + d2 * cp[7] + d3 * cp[10];
     dr.z = d0 * cp[2] + d1 * cp[5] + d2 * cp[8] + d3 * cp[11];
-    df const s = df_sqrt(dot(r, r));
-    df const inv_s = df_make(1.f) / s;
-    df const s1 = dot(r, dr) * inv_s; // (2 r.dr) * (0.5 / s)
-    df3 const G = r * inv_s;
-    df3 const Gp = (dr - G * s1) * inv_s;
-    df const a = dot(x0, G);
-    df const c = dot(x0, cross(G, Gp));
-    df3 const xg = cross(x0, G);
-    df const xg2 = dot(xg, xg);
+    df const q = dot(r, r);
+    df const s = df_sqrt(q);
+    df3 const xr = cross(x0, r);
+    df const T = dot(dr, xr), m = dot(x0, r);
     if (unit)
     {
-        bool const ahead = a.hi >= 0.f;
-        df const num = ahead ? c * (df_make(1.f) + a) : c;
-        df const den = ahead ? xg2 : df_make(1.f) - a;
+        bool const behind = m.hi < 0.f;
+        df const num = behind ? T : T * (s + m);
+        df const den = s * (behind ? s - m : dot(xr, xr));
         return df_neg(num / den);
     }
-    return df_neg(c / (df_make(1.f) + (x0n - df_make(2.f)) * (a * a))) - (a * c) / xg2;
+    return df_neg(T / (q + (x0n - df_make(2.f)) * (m * m))) - (m * T) / (s * dot(xr, xr));
 }
 
 __device__ __forceinline__ double gk15_panel_df(const df (&cp)[12], df3 x0, df x0n, bool unit, int depth, uint32_t j,
