@@ -28,9 +28,11 @@ namespace
 constexpr int kParamMaxDepth = 24; // deepest panel the integrator can reach (2^24 panels per curve)
 constexpr int kParamBlock = 128;
 constexpr int kParamTileMax = 1024; // curves staged per tile (96 KB of shared memory)
-// The double-float form stages 768 curves (72 KB, room for the per-panel network's weights beside them): measured on
-// 256 bicubic patches x 40K queries at tol 1e-10, 10% faster than 1024, and flat from 768 down to 128.
-constexpr int kParamTileDF = 768;
+// The double-float form stages 384 curves (36 KB, room for the per-panel network's weights beside them), so that
+// six blocks reside per SM, the number its 80 registers allow.  Measured on 256 bicubic patches at tol 1e-10:
+// 40K queries, 768 was 10% faster than 1024 and flat down to 128; 250K queries (one work item per query block),
+// 384 is 1.7% faster than 768 (three blocks per SM) and 256 1.4%.
+constexpr int kParamTileDF = 384;
 
 struct alignas(16) Bez
 {
