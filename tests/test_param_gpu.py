@@ -172,3 +172,23 @@ def test_param_double_float_form_agrees_with_plain(gwn, disp, tol):
     finally:
         disp.set_param_precision("exact")
     assert np.abs(got - g["param_lines_out"]).max() <= 1e-9
+
+
+@pytest.mark.parametrize("scale", [0.5, 2.0])
+def test_param_non_unit_x0(gwn, disp, oracle, scale):
+    """x0 is used as given, unnormalised, as in the reference.  The plain form stays bit-exact with the oracle; the
+    double-float form takes its general closed form (the short one holds for |x0| = 1 only) and stays within the
+    same bounds as for a unit x0."""
+    curves, q, x0 = patches(43, 4, 300)
+    x0 = x0 * scale
+    cfg = gwn.IntegrateConfig(0, 10, 1e-10)
+    exact = run(gwn, disp, q, x0, curves, cfg)
+    assert np.array_equal(exact, oracle.param_frac_bezier3(q, x0, curves, 0, 10, 1e-10))
+    disp.set_param_precision("mixed")
+    try:
+        mixed = run(gwn, disp, q, x0, curves, cfg)
+    finally:
+        disp.set_param_precision("exact")
+    d = np.abs(mixed - exact)
+    assert d.max() <= 1e-8, d.max()
+    assert np.median(d) <= 1e-12
