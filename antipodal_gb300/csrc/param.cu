@@ -160,10 +160,10 @@ __device__ __forceinline__ double gk15_panel(const double* c, ev3<rd> p, ev3<rd>
 
 // ---- double-float form ----------------------------------------------------------------------------------------
 // The same integrand and panel rule in double-float arithmetic (df32.cuh, ~44 significant bits on the FP32 pipe):
-// the curve's control points relative to the query, the Bernstein basis and its derivative in closed form, the
-// normalisation, and w - d_eta in the closed form below (the same quantity, fewer operations).  Not bit-identical to the reference (the value differs in the last ~1e-13
-// relative, and a panel whose |Ik - Ig| sits at the tolerance can be decided the other way); the tree rule, the
-// tolerances and the summation order are the plain integrator's.
+// the curve relative to the query in power form about t = 1/2 (power_about_half) and w - d_eta in the closed form
+// below -- the same quantities in fewer operations.  Not bit-identical to the reference (the value differs in the
+// last ~1e-13 relative, and a panel whose |Ik - Ig| sits at the tolerance can be decided the other way); the tree
+// rule, the tolerances and the summation order are the plain integrator's.
 struct alignas(16) CurveDF
 {
     df c[12];
