@@ -242,9 +242,10 @@ __device__ __forceinline__ df integrand_df(const df (&pc)[12], df3 x0, df x0n, b
 // Control points c0..c3 (minus the query) to power coefficients about t = 1/2, in place: with s03 = c0 + c3,
 // s12 = c1 + c2, d30 = c3 - c0 and d21 = c2 - c1, r(1/2) = (s03 + 3 s12) / 8, r'(1/2) = 3/4 (d30 + d21),
 // r''(1/2) / 2 = 3/2 (s03 - s12) and r''' / 6 = d30 - 3 d21.  Evaluated at |t - 1/2| <= 1/2 the power form rounds
-// about as the Bernstein form does (measured in FP32 on bicubic patch boundaries: median relative error of r 1.2x,
-// 1.9x for queries within 0.05 of a curve, and a lower maximum), and takes 12 double-float products, 3 products by
-// a float and 15 sums per node against the Bernstein form's 31, 5 and 21.
+// a little worse than the Bernstein form (in FP32 on bicubic patch boundaries, relative error of r: median 1.2x at
+// random pairs with a lower maximum, median 1.7x and p99 2.1x for queries 1e-4 to 1e-2 from a curve near their
+// closest point), and takes 12 double-float products, 3 products by a float and 15 sums per node against the
+// Bernstein form's 31, 5 and 21.
 __device__ __forceinline__ void power_about_half(df (&cp)[12])
 {
 #pragma unroll
